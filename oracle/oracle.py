@@ -1,0 +1,397 @@
+"""Test infrastructure only -- Python bindings for the oracle.
+
+``Oracle``      : the C restatement (oracle/hf_oracle.c, built by ``make -C oracle port``)
+                  driven from a case dict in the reference's JSON schema.
+``RefCart`` /
+``RefUns``      : the reference's own solver sources compiled in place
+                  (``make -C oracle ref`` -> oracle/_ref/), available only where the
+                  reference tree exists.
+
+Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg import this
+module.  The product never does.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import json
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PORT_LIB = os.path.join(HERE, "_build", "libhforacle.so")
+REF_CART_LIB = os.path.join(HERE, "_ref", "libhfref_cart.so")
+REF_UNS_LIB = os.path.join(HERE, "_ref", "libhfref_uns.so")
+
+MAXB = 16
+BC_KIND = {"Transmissive": 0, "Reflective": 1, "Dirichlet": 2, "Internal": 3}
+SIDES = ("bottom", "right", "top", "left")
+
+
+class _Mesh(C.Structure):
+    _fields_ = [
+        ("scheme", C.c_int), ("limiter", C.c_int), ("nblocks", C.c_int), ("ghost", C.c_int),
+        ("gamma", C.c_double), ("cfl", C.c_double), ("calls", C.c_int64),
+        ("t", C.c_double), ("t_end", C.c_double),
+        ("nx", C.c_int * MAXB), ("ny", C.c_int * MAXB),
+        ("xl", C.c_double * MAXB), ("xr", C.c_double * MAXB),
+        ("yb", C.c_double * MAXB), ("yt", C.c_double * MAXB),
+        ("bc_type", (C.c_int * 4) * MAXB), ("bc_block", (C.c_int * 4) * MAXB),
+        ("bc_state", ((C.c_double * 4) * 4) * MAXB),
+        ("U", C.c_void_p * MAXB), ("nthreads", C.c_int), ("hllc_errors", C.c_int64),
+    ]
+
+
+def build_port() -> str:
+    """Compile the C restatement (idempotent)."""
+    subprocess.run(["make", "-s", "-C", HERE, "port"], check=True)
+    return PORT_LIB
+
+
+_port = None
+
+
+def port_lib():
+    global _port
+    if _port is None:
+        if not os.path.exists(PORT_LIB):
+            build_port()
+        lib = C.CDLL(PORT_LIB)
+        d, p, i = C.c_double, C.c_void_p, C.c_int
+        lib.hfo_time_step.restype = d
+        lib.hfo_time_step.argtypes = [p]
+        lib.hfo_run.restype = i
+        lib.hfo_run.argtypes = [p, i, i, p]
+        lib.hfo_advance.argtypes = [p, d]
+        lib.hfo_apply_bcs.argtypes = [p]
+        lib.hfo_limiter.restype = d
+        lib.hfo_limiter.argtypes = [i, d]
+        lib.hfo_hllc.restype = i
+        lib.hfo_hllc.argtypes = [d, p, p, i, p]
+        lib.hfo_cons_to_prim.argtypes = [d, p, p]
+        lib.hfo_prim_to_cons.argtypes = [d, p, p]
+        lib.hfo_cons_flux.argtypes = [d, p, i, p]
+        lib.hfo_init_quadrant.argtypes = [p, i, d, d, p, p, p, p]
+        lib.hfo_init_constant.argtypes = [p, i, p]
+        lib.hfo_init_double.argtypes = [p, i, d, d, p, p, p]
+        lib.hfo_init_sphere.argtypes = [p, i, d, d, d, p, p]
+        lib.hfo_uns_geometry.argtypes = [i, p, p, p, p, p, p]
+        lib.hfo_uns_run.restype = i
+        lib.hfo_uns_run.argtypes = [d, d, p, i, p, p, p, p, p, p, p, p, i, p, i]
+        _port = lib
+    return _port
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def prim_to_cons(w, gamma=1.4):
+    w = np.ascontiguousarray(w, dtype=np.float64)
+    out = np.zeros(4)
+    port_lib().hfo_prim_to_cons(gamma, _ptr(w), _ptr(out))
+    return out
+
+
+class Oracle:
+    """The C restatement of the reference's Cartesian step, set up from a case dict
+    the way JSONParser does (parser.cpp:13-488)."""
+
+    def __init__(self, case: dict, nthreads: int = 1):
+        self.lib = port_lib()
+        self.case = case
+        m = _Mesh()
+        sch = case["scheme"]["type"]
+        m.scheme = 0 if sch == "Godunov" else 1
+        m.limiter = 0 if case["scheme"].get("limiter", "MinBee") == "MinBee" else 1
+        m.ghost = 1 if m.scheme == 0 else 2
+        gamma = float(case["model"]["gamma"])
+        m.gamma = gamma
+        m.cfl = float(case["simulation"]["cfl"])
+        m.t = float(case["simulation"]["t_start"])
+        m.t_end = float(case["simulation"]["t_end"])
+        m.nthreads = nthreads
+        blocks = case["mesh"]["blocks"]
+        m.nblocks = len(blocks)
+        self.U = []
+        for b, blk in enumerate(blocks):
+            e = blk["extents"]
+            m.nx[b], m.ny[b] = blk["x_cells"], blk["y_cells"]
+            m.xl[b], m.xr[b] = e["x_left"], e["x_right"]
+            m.yb[b], m.yt[b] = e["y_bottom"], e["y_top"]
+            for s, side in enumerate(SIDES):
+                bc = blk["boundaries"][side]
+                m.bc_type[b][s] = BC_KIND[bc["type"]]
+                if bc["type"] == "Internal":
+                    m.bc_block[b][s] = int(bc["block"])
+                if bc["type"] == "Dirichlet":
+                    st = np.array(bc["flow_state"], dtype=np.float64)
+                    if bc["variables"] == "Primitive":
+                        st = prim_to_cons(st, gamma)
+                    for v in range(4):
+                        m.bc_state[b][s][v] = st[v]
+            tx, ty = blk["x_cells"] + 2 * m.ghost, blk["y_cells"] + 2 * m.ghost
+            U = np.zeros((4, ty, tx))
+            self.U.append(U)
+            m.U[b] = U.ctypes.data
+        self.m = m
+        self._init_ic()
+
+    def _states(self, ic, keys):
+        out = []
+        for k in keys:
+            st = np.array(ic[k], dtype=np.float64)
+            out.append(st)
+        return out
+
+    def _init_ic(self):
+        ic = self.case["initial_condition"]
+        g = self.m.gamma
+        typ = ic["type"]
+        prim = ic.get("variables") == "Primitive"
+        lib = self.lib
+        mp = C.byref(self.m)
+        for b in range(self.m.nblocks):
+            if typ == "Constant":      # always converted (parser.cpp:317)
+                s = prim_to_cons(ic["init_state"], g)
+                lib.hfo_init_constant(mp, b, _ptr(s))
+            elif typ == "QuadRiemannProblem":
+                ne, nw, sw, se = self._states(ic, ["init_ne_state", "init_nw_state",
+                                                   "init_sw_state", "init_se_state"])
+                if prim:
+                    ne, nw, sw, se = (prim_to_cons(x, g) for x in (ne, nw, sw, se))
+                lib.hfo_init_quadrant(mp, b, float(ic["x_interface"]), float(ic["y_interface"]),
+                                      _ptr(ne), _ptr(nw), _ptr(sw), _ptr(se))
+            elif typ == "DoubleRiemannProblem":
+                l, mid, r = self._states(ic, ["init_left_state", "init_middle_state",
+                                              "init_right_state"])
+                if prim:
+                    l, mid, r = (prim_to_cons(x, g) for x in (l, mid, r))
+                lib.hfo_init_double(mp, b, float(ic["x_lm_interface"]), float(ic["x_mr_interface"]),
+                                    _ptr(l), _ptr(mid), _ptr(r))
+            elif typ == "SphericalRiemannProblem":   # always converted (parser.cpp:421-422)
+                si = prim_to_cons(ic["init_sphere_state"], g)
+                so = prim_to_cons(ic["init_ext_state"], g)
+                lib.hfo_init_sphere(mp, b, float(ic["radius"]), float(ic["x_origin"]),
+                                    float(ic["y_origin"]), _ptr(si), _ptr(so))
+            else:
+                raise ValueError(f"initial condition {typ!r} not supported")
+
+    # --- the reference's step pieces ---
+    def apply_bcs(self):
+        self.lib.hfo_apply_bcs(C.byref(self.m))
+
+    def time_step(self) -> float:
+        return self.lib.hfo_time_step(C.byref(self.m))
+
+    def advance(self, dt: float):
+        self.lib.hfo_advance(C.byref(self.m), dt)
+
+    def run(self, n: int, clamp_t_end: bool = False) -> np.ndarray:
+        dts = np.zeros(max(n, 1))
+        k = self.lib.hfo_run(C.byref(self.m), n, int(clamp_t_end), _ptr(dts))
+        return dts[:k]
+
+    @property
+    def t(self) -> float:
+        return self.m.t
+
+    @property
+    def calls(self) -> int:
+        return self.m.calls
+
+    @property
+    def hllc_errors(self) -> int:
+        return self.m.hllc_errors
+
+    def state(self, b: int = 0) -> np.ndarray:
+        return self.U[b].copy()
+
+    def set_state(self, b: int, U: np.ndarray):
+        self.U[b][...] = U
+
+
+# ----------------------------------------------------------------------------------
+# the reference itself (oracle/_ref), for pinning the restatement and making fixtures
+# ----------------------------------------------------------------------------------
+
+def ref_available() -> bool:
+    return os.path.exists(REF_CART_LIB) and os.path.exists(REF_UNS_LIB)
+
+
+_refc = None
+
+
+def ref_cart_lib():
+    global _refc
+    if _refc is None:
+        lib = C.CDLL(REF_CART_LIB)
+        p, i, d = C.c_void_p, C.c_int, C.c_double
+        lib.hfref_cart_create.restype = p
+        lib.hfref_cart_create.argtypes = [C.c_char_p]
+        lib.hfref_cart_destroy.argtypes = [p]
+        for f in ("hfref_cart_num_blocks", "hfref_cart_num_calls", "hfref_cart_num_steps"):
+            getattr(lib, f).restype = i
+            getattr(lib, f).argtypes = [p]
+        lib.hfref_cart_run.restype = i
+        lib.hfref_cart_run.argtypes = [p, i, i]
+        lib.hfref_cart_block_dims.argtypes = [p, i, p]
+        lib.hfref_cart_get_state.argtypes = [p, i, p]
+        lib.hfref_cart_set_state.argtypes = [p, i, p]
+        lib.hfref_cart_calls.argtypes = [p, p]
+        lib.hfref_cart_step_dts.argtypes = [p, p]
+        lib.hfref_cart_apply_bcs.argtypes = [p]
+        lib.hfref_cart_time.restype = d
+        lib.hfref_cart_time.argtypes = [p]
+        lib.hfref_hllc.argtypes = [d, p, p, i, p]
+        lib.hfref_limiter.restype = d
+        lib.hfref_limiter.argtypes = [i, d]
+        lib.hfref_cons_to_prim.argtypes = [d, p, p]
+        lib.hfref_cons_flux.argtypes = [d, p, i, p]
+        _refc = lib
+    return _refc
+
+
+class RefCart:
+    """The reference's Cartesian solver built from the same case JSON."""
+
+    def __init__(self, case: dict):
+        self.lib = ref_cart_lib()
+        self.h = C.c_void_p(self.lib.hfref_cart_create(json.dumps(case).encode()))
+
+    def __del__(self):
+        try:
+            self.lib.hfref_cart_destroy(self.h)
+        except Exception:
+            pass
+
+    def run(self, n: int, clamp_t_end: bool = False) -> int:
+        return self.lib.hfref_cart_run(self.h, n, int(clamp_t_end))
+
+    def apply_bcs(self):
+        self.lib.hfref_cart_apply_bcs(self.h)
+
+    def nblocks(self) -> int:
+        return self.lib.hfref_cart_num_blocks(self.h)
+
+    def state(self, b: int = 0) -> np.ndarray:
+        dims = (C.c_int * 3)()
+        self.lib.hfref_cart_block_dims(self.h, b, dims)
+        out = np.zeros((4, dims[1], dims[0]))
+        self.lib.hfref_cart_get_state(self.h, b, _ptr(out))
+        return out
+
+    def set_state(self, b: int, U: np.ndarray):
+        U = np.ascontiguousarray(U, dtype=np.float64)
+        self.lib.hfref_cart_set_state(self.h, b, _ptr(U))
+
+    def calls(self) -> np.ndarray:
+        n = self.lib.hfref_cart_num_calls(self.h)
+        out = np.zeros(max(n, 1))
+        self.lib.hfref_cart_calls(self.h, _ptr(out))
+        return out[:n]
+
+    def step_dts(self) -> np.ndarray:
+        n = self.lib.hfref_cart_num_steps(self.h)
+        out = np.zeros(max(n, 1))
+        self.lib.hfref_cart_step_dts(self.h, _ptr(out))
+        return out[:n]
+
+    def time(self) -> float:
+        return self.lib.hfref_cart_time(self.h)
+
+
+_refu = None
+
+
+def ref_uns_lib():
+    global _refu
+    if _refu is None:
+        lib = C.CDLL(REF_UNS_LIB)
+        p, i = C.c_void_p, C.c_int
+        lib.hfref_uns_create.restype = p
+        lib.hfref_uns_create.argtypes = [C.c_char_p, i, p, p, p]
+        lib.hfref_uns_destroy.argtypes = [p]
+        lib.hfref_uns_run.restype = i
+        lib.hfref_uns_run.argtypes = [p, i]
+        lib.hfref_uns_dts.argtypes = [p, p]
+        lib.hfref_uns_get_state.argtypes = [p, p]
+        lib.hfref_uns_set_state.argtypes = [p, p]
+        lib.hfref_uns_geometry.argtypes = [p, p, p, p, p]
+        _refu = lib
+    return _refu
+
+
+class RefUns:
+    """The reference's unstructured solver over a mesh given as arrays."""
+
+    def __init__(self, case: dict, nverts: np.ndarray, verts: np.ndarray, pair_nbr: np.ndarray):
+        self.lib = ref_uns_lib()
+        self.nverts = np.ascontiguousarray(nverts, dtype=np.int32)
+        self.verts = np.ascontiguousarray(verts, dtype=np.float64)
+        self.nbr = np.ascontiguousarray(pair_nbr, dtype=np.int32)
+        self.ncells = len(self.nverts)
+        self.npairs = int(self.nverts.sum())
+        self.h = C.c_void_p(self.lib.hfref_uns_create(json.dumps(case).encode(), self.ncells,
+                                                      _ptr(self.nverts), _ptr(self.verts),
+                                                      _ptr(self.nbr)))
+        self.nsteps = 0
+
+    def __del__(self):
+        try:
+            self.lib.hfref_uns_destroy(self.h)
+        except Exception:
+            pass
+
+    def run(self, n: int):
+        self.lib.hfref_uns_run(self.h, n)
+        self.nsteps += n
+
+    def dts(self) -> np.ndarray:
+        out = np.zeros(max(self.nsteps, 1))
+        self.lib.hfref_uns_dts(self.h, _ptr(out))
+        return out[: self.nsteps]
+
+    def state(self) -> np.ndarray:
+        out = np.zeros((4, self.ncells))
+        self.lib.hfref_uns_get_state(self.h, _ptr(out))
+        return out
+
+    def set_state(self, U: np.ndarray):
+        U = np.ascontiguousarray(U, dtype=np.float64)
+        self.lib.hfref_uns_set_state(self.h, _ptr(U))
+
+    def geometry(self):
+        ang = np.zeros(self.npairs)
+        ln = np.zeros(self.npairs)
+        area = np.zeros(self.ncells)
+        rin = np.zeros(self.ncells)
+        self.lib.hfref_uns_geometry(self.h, _ptr(ang), _ptr(ln), _ptr(area), _ptr(rin))
+        return ang, ln, area, rin
+
+
+def uns_geometry(nverts: np.ndarray, verts: np.ndarray):
+    """Edge angles/lengths and cell areas/incircle radii via the C restatement."""
+    nverts = np.ascontiguousarray(nverts, dtype=np.int32)
+    verts = np.ascontiguousarray(verts, dtype=np.float64)
+    npairs = int(nverts.sum())
+    ang, ln = np.zeros(npairs), np.zeros(npairs)
+    area, rin = np.zeros(len(nverts)), np.zeros(len(nverts))
+    port_lib().hfo_uns_geometry(len(nverts), _ptr(nverts), _ptr(verts), _ptr(ang), _ptr(ln),
+                                _ptr(area), _ptr(rin))
+    return ang, ln, area, rin
+
+
+def uns_run(gamma, cfl, calls, pair_start, pair_nbr, angle, length, area, rin, inlet, U, n,
+            nthreads=1):
+    """n steps of the restated unstructured Godunov solver; U ([4][ncells]) updated in place."""
+    c = C.c_int64(calls)
+    dts = np.zeros(max(n, 1))
+    ps = np.ascontiguousarray(pair_start, dtype=np.int32)
+    pn = np.ascontiguousarray(pair_nbr, dtype=np.int32)
+    inlet = np.ascontiguousarray(inlet, dtype=np.float64)
+    port_lib().hfo_uns_run(gamma, cfl, C.byref(c), U.shape[1], _ptr(ps), _ptr(pn), _ptr(angle),
+                           _ptr(length), _ptr(area), _ptr(rin), _ptr(inlet), _ptr(U), n,
+                           _ptr(dts), nthreads)
+    return dts[:n], c.value

@@ -1,0 +1,147 @@
+// Test infrastructure only: a fixed-step driver over the reference's own
+// unstructured solver sources (compiled in place by oracle/Makefile).
+//
+// The reference loads meshes only through LoadStructuredMesh
+// (src/fvm_2d_uns/mesh/mesh_structured/mesh_structured.cpp:23-122), which reads
+// quadrilaterals and matches neighbours in O(E^2).  This driver instead builds
+// Mesh(edges, cells, cell_edge_indices) directly (src/fvm_2d_uns/mesh/mesh/mesh.cpp:17-24)
+// with the same cell_edge_indices layout as mesh_structured.cpp:93-115:
+//   one entry per (cell, own edge) in cell order, [cell, neighbour-or-bc, pair index],
+// and the edge vector holding each cell's own Edge object in the same order.
+// The caller supplies the neighbour of each pair (a cell index, or the negative
+// BoundaryCondition code of src/fvm_2d_uns/scheme/boundary/boundary.h:12).
+// Everything else -- Godunov, HLLC, rotation, boundary states, TimeStep, ODE --
+// is the reference's own code, driven as Simulation::solve does
+// (src/fvm_2d_uns/simulation/simulation/simulation.cpp:61-120) for exactly N steps.
+#include <cstring>
+#include <functional>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include <nlohmann/json.hpp>
+
+#include "simulation/parser/parser.h"
+
+using json = nlohmann::json;
+using namespace HyperFlow;
+
+namespace {
+
+struct RefUns {
+    json config;
+    std::unique_ptr<JSONParser> parser;
+    std::shared_ptr<Model> model;
+    std::shared_ptr<Mesh> mesh;
+    std::shared_ptr<InitialCondition> initcon;
+    std::shared_ptr<RiemannSolver> riemann;
+    std::shared_ptr<Scheme> scheme;
+    std::shared_ptr<ODESolver> ode;
+    std::unique_ptr<TimeStep> time_step;
+    double t = 0.0;
+    std::vector<double> dts;
+};
+
+}  // namespace
+
+extern "C" {
+
+void* hfref_uns_create(const char* case_json, int ncells, const int* nverts,
+                       const double* verts, const int* pair_nbr) {
+    RefUns* r = new RefUns();
+    r->config = json::parse(case_json);
+    r->parser.reset(new JSONParser(r->config));
+    r->t = r->parser->get_t_start();
+    r->model = r->parser->generate_model();
+
+    CellVec1D cells;
+    cells.reserve(ncells);
+    size_t vo = 0;
+    for (int c = 0; c < ncells; ++c) {
+        Vec2D vs;
+        for (int k = 0; k < nverts[c]; ++k) {
+            Vec1D v = {verts[2 * (vo + k)], verts[2 * (vo + k) + 1]};
+            vs.push_back(v);
+        }
+        vo += nverts[c];
+        cells.push_back(Cell(vs));
+    }
+    std::vector<std::vector<int> > cei;
+    EdgeVec1D edges;
+    int pair = 0;
+    for (int c = 0; c < ncells; ++c) {
+        unsigned ne = cells[c].get_edges().size();
+        for (unsigned e = 0; e < ne; ++e) {
+            std::vector<int> idx = {c, pair_nbr[pair], pair};
+            cei.push_back(idx);
+            edges.push_back(cells[c].get_edges()[e]);
+            ++pair;
+        }
+    }
+    r->mesh = std::make_shared<Mesh>(edges, cells, cei);
+    r->initcon = r->parser->generate_initial_condition();
+    r->riemann = r->parser->generate_riemann_solver();
+    std::shared_ptr<TimeStep> unused = r->parser->generate_time_step();
+    r->scheme = r->parser->generate_spatial_scheme(r->model, r->riemann, unused, r->mesh);
+    r->ode = r->parser->generate_ode_solver();
+    r->mesh->initialise_field_values(r->initcon);
+    r->time_step.reset(new TimeStep(r->model, r->parser->get_cfl()));
+    return r;
+}
+
+void hfref_uns_destroy(void* h) { delete static_cast<RefUns*>(h); }
+
+int hfref_uns_run(void* h, int n) {
+    RefUns* r = static_cast<RefUns*>(h);
+    for (int s = 0; s < n; ++s) {
+        double dt = (*r->time_step)(r->mesh);
+        auto f = std::bind(&Scheme::operator(), r->scheme);
+        Vec2D upd = r->ode->operator()(f, r->mesh->get_cells_flow_values(), dt);
+        r->mesh->set_cells_flow_values(upd);
+        r->dts.push_back(dt);
+        r->t += dt;
+    }
+    return n;
+}
+
+void hfref_uns_dts(void* h, double* out) {
+    auto& d = static_cast<RefUns*>(h)->dts;
+    std::memcpy(out, d.data(), d.size() * sizeof(double));
+}
+
+// SoA [var][cell]
+void hfref_uns_get_state(void* h, double* out) {
+    auto& cells = static_cast<RefUns*>(h)->mesh->get_cells();
+    size_t n = cells.size();
+    for (size_t c = 0; c < n; ++c)
+        for (int k = 0; k < 4; ++k) out[k * n + c] = cells[c].get_flow_values()[k];
+}
+
+void hfref_uns_set_state(void* h, const double* in) {
+    auto& cells = static_cast<RefUns*>(h)->mesh->get_cells();
+    size_t n = cells.size();
+    for (size_t c = 0; c < n; ++c) {
+        Vec1D v(4);
+        for (int k = 0; k < 4; ++k) v[k] = in[k * n + c];
+        cells[c].set_flow_values(v);
+    }
+}
+
+// Geometry exactly as the reference computes it: per pair the outward normal
+// angle in degrees (edge.cpp:215-218) and length (edge.cpp:98-101); per cell the
+// signed area (polygon.cpp:172-186) and incircle radius (polygon.cpp:72-94).
+void hfref_uns_geometry(void* h, double* angle, double* length, double* area, double* rin) {
+    RefUns* r = static_cast<RefUns*>(h);
+    auto& edges = r->mesh->get_edges();
+    for (size_t e = 0; e < edges.size(); ++e) {
+        angle[e] = edges[e].get_outward_normal_angle();
+        length[e] = edges[e].get_length();
+    }
+    auto& cells = r->mesh->get_cells();
+    for (size_t c = 0; c < cells.size(); ++c) {
+        area[c] = cells[c].get_volume();
+        rin[c] = cells[c].radius_incircle();
+    }
+}
+
+}  // extern "C"
