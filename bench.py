@@ -1,0 +1,302 @@
+#!/usr/bin/env python
+"""Benchmark of the plain FP64 MUSCL-Hancock + HLLC time step on one GB300.
+
+Workload: the Mach 3 forward-facing step, 3 blocks at dx = dy = 1/1365 (819x273,
+819x1092, 3276x1092 = 4,695,327 cells), MinBee limiter, CFL 0.8, uniform inflow start.
+One step = ghost fill + CFL dt + the three block updates (each with its own predictor
+TimeStep call), exactly the reference's step.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line (rank 0).  `value` is device-resident throughput (state in HBM,
+CUDA events on the solver's stream around K steps); `e2e` is the same metric through the
+C ABI with host buffers (per step: upload every block from pinned host memory, one step,
+download every block).  With --gpus N under torchrun, every rank runs an independent
+replica (the path does not shard across GPUs) and `value` sums the replicas.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+BYTES_PER_CELL = 64          # 4 FP64 read + 4 FP64 written per cell update
+WORKLOAD = "mach3_forward_facing_step_3block_dx1_1365_muscl_hancock_minbee_hllc_fp64"
+
+
+def make_case(limiter: str = "MinBee"):
+    from hyperflow_gb300 import cases
+    return cases.forward_facing_step_case(1365, limiter=limiter, cfl=0.8, t_end=4.0)
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic():
+    """DRAM bytes per cell update of the stencil kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "mh_kernel_traffic.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            return json.load(f)
+    return None
+
+
+class Clocks:
+    """Samples nvidia-smi clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.lines = []
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in getattr(self, "lines", []):
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def cpu_run(case, steps: int, nthreads: int):
+    """The oracle (C restatement of the reference step) on host cores."""
+    from oracle.oracle import Oracle, build_port
+    build_port()
+    o = Oracle(case, nthreads=nthreads)
+    t0 = time.perf_counter()
+    o.run(steps)
+    return time.perf_counter() - t0
+
+
+def reference_arm(args, cells):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    case = make_case(args.limiter)
+    nth = os.cpu_count() or 1
+    from oracle.oracle import Oracle, build_port
+    build_port()
+    o = Oracle(case, nthreads=nth)
+    o.run(args.warmup)
+    t0 = time.perf_counter()
+    o.run(args.steps)
+    el = time.perf_counter() - t0
+    v = cells * args.steps / el / 1e6
+    print(json.dumps({
+        "metric": "Mcell-updates/s", "value": v, "unit": "Mcell-updates/s", "impl": "reference",
+        "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": el * 1e3 / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (the case's own initial condition)",
+        "config": {"workload": WORKLOAD, "cells": cells},
+        "cpu_baseline": {"value": v, "unit": "Mcell-updates/s", "cores": nth, "kind": "port",
+                         "sample": f"{args.steps} full steps of the workload after {args.warmup} warm-up steps"},
+        "e2e": {"value": v, "unit": "Mcell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--limiter", default="MinBee", choices=["MinBee", "VanLeer"])
+    ap.add_argument("--cpu-seconds", type=float, default=15.0, help="CPU-baseline sample budget")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    from hyperflow_gb300 import cases
+    case = make_case(args.limiter)
+    cells = cases.total_cells(case)
+
+    if args.impl == "reference":
+        reference_arm(args, cells)
+        return
+
+    import numpy as np
+    import torch
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    pg = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+        pg = dist
+
+    def barrier():
+        if pg is not None:
+            pg.barrier()
+        torch.cuda.synchronize()
+
+    from hyperflow_gb300 import CartSolver
+    s = CartSolver(case)
+    nb = s.nblocks
+    stream = torch.cuda.ExternalStream(s.stream())
+
+    # ---- device-resident timed region ----
+    s.run(args.warmup, graph=False)
+    s.sync()
+    s.profile(True)          # events around every step's stencil launches (same stream)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    barrier()
+    with Clocks(local) as clk:
+        e0.record(stream)
+        s.run(args.steps, graph=False)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    s.sync()
+    ms = e0.elapsed_time(e1)
+    stencil_ms, stencil_launches = s.kernel_time(0)
+    s.profile(False)
+    t_max = ms
+    if pg is not None:
+        tt = torch.tensor([ms], device="cuda")
+        pg.all_reduce(tt, op=pg.ReduceOp.MAX)
+        t_max = float(tt.item())
+    value = ws * cells * args.steps / (t_max / 1e3) / 1e6
+    hllc_fallbacks = s.hllc_errors()
+
+    # same run through the CUDA graph (one captured step replayed K times)
+    s.run(1, graph=True)
+    barrier()
+    g0 = torch.cuda.Event(enable_timing=True)
+    g1 = torch.cuda.Event(enable_timing=True)
+    g0.record(stream)
+    s.run(args.steps, graph=True)
+    g1.record(stream)
+    torch.cuda.synchronize()
+    graph_value = cells * args.steps / (g0.elapsed_time(g1) / 1e3) / 1e6
+
+    # ---- end to end through the C ABI with host buffers ----
+    host = []
+    h2d = 0
+    for b in range(nb):
+        d = s.block_dims(b)
+        t = torch.empty((4, d["total_y"], d["total_x"]), dtype=torch.float64).pin_memory()
+        a = t.numpy()
+        s.state(b, out=a)
+        host.append((t, a))
+        h2d += a.nbytes
+    e2e_steps = max(3, min(args.steps, 30))
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        for b in range(nb):
+            s.set_state(b, host[b][1])
+        s.step()
+        for b in range(nb):
+            s.state(b, out=host[b][1])
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    e2e_value = ws * cells * e2e_steps / e2e_s / 1e6
+
+    # ---- roofline of the stencil kernel ----
+    hbm, peak_kind = peaks()
+    achieved = BYTES_PER_CELL * cells * args.steps / (stencil_ms / 1e3) / 1e9
+    traffic = None
+    tr = ncu_traffic()
+    if tr and tr.get("workload") == WORKLOAD:
+        traffic = tr["dram_bytes_per_cell_update"] * cells / nb
+    roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+            "frac": achieved / hbm, "traffic": traffic, "peak_kind": peak_kind,
+            "algorithmic_bytes_per_launch": BYTES_PER_CELL * cells / nb,
+            "avg_launch_ms": stencil_ms / max(stencil_launches * nb, 1),
+            "kernel": "mh_kernel (fused MUSCL-Hancock + HLLC + forward Euler + CFL epilogue)"}
+
+    # ---- CPU baseline (rank 0, N=1): the oracle on all host cores, bounded sample ----
+    cpu = None
+    if rank == 0 and ws == 1:
+        nth = os.cpu_count() or 1
+        probe = cpu_run(case, 1, nth)
+        n_cpu = int(max(1, min(200, args.cpu_seconds / max(probe, 1e-3))))
+        el = cpu_run(case, n_cpu, nth)
+        cpu = {"value": cells * n_cpu / el / 1e6, "unit": "Mcell-updates/s", "cores": nth,
+               "kind": "port",
+               "sample": f"first {n_cpu} steps of the same workload (all {cells} cells)"}
+
+    launches_per_step = 3 + nb   # ghost fill, ghost CFL + dt, one stencil per block, finalize
+    if rank == 0:
+        line = {
+            "metric": "Mcell-updates/s", "value": value, "unit": "Mcell-updates/s",
+            "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (the case's own initial condition: uniform Mach 3 inflow)",
+            "config": {"workload": WORKLOAD, "cells": cells, "blocks": nb, "limiter": args.limiter,
+                       "cfl": 0.8, "l2": "state 2 x 300 MB > 129 MB L2, no flush needed",
+                       "parallelism": "replicas" if ws > 1 else "single GPU"},
+            "roofline": roof,
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_value, "unit": "Mcell-updates/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": h2d, "steps": e2e_steps},
+            "gpu_launches": launches_per_step * args.steps,
+            "clocks": clk.summary(),
+            "graph_value": graph_value,
+            "hllc_zero_flux_fallbacks": hllc_fallbacks,
+        }
+        print(json.dumps(line), flush=True)
+    s.close()
+    if pg is not None:
+        pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,77 @@
+"""Loads the in-tree CUDA library and declares the C-ABI signatures.
+
+There is no CPU fallback: if ``libhyperflow_gb300.so`` is missing, or a call needs
+a GPU and none is visible, the call raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "libhyperflow_gb300.so")
+
+HF_OK = 0
+STATUS = {0: "ok", 1: "bad argument", 2: "case file parse error", 3: "unsupported case",
+          4: "CUDA error", 5: "device error word raised", 6: "call out of order",
+          7: "no CUDA device"}
+
+LAYOUT_SOA = 0
+LAYOUT_AOS_XY = 1
+
+# every symbol include/hyperflow_gb300.h declares: name -> (restype, argtypes)
+_p, _i, _d, _sz, _i64 = C.c_void_p, C.c_int, C.c_double, C.c_size_t, C.c_int64
+SIGNATURES = {
+    "hf_create": (_i, [C.c_char_p, _sz, C.POINTER(_p)]),
+    "hf_destroy": (None, [_p]),
+    "hf_num_blocks": (_i, [_p, C.POINTER(_i)]),
+    "hf_block_dims": (_i, [_p, _i, C.POINTER(_i)]),
+    "hf_set_state": (_i, [_p, _i, _p, _i]),
+    "hf_get_state": (_i, [_p, _i, _p, _i]),
+    "hf_apply_bcs": (_i, [_p]),
+    "hf_time_step": (_i, [_p, C.POINTER(_d)]),
+    "hf_advance_block": (_i, [_p, _i, _d]),
+    "hf_advance": (_i, [_p, _d]),
+    "hf_step": (_i, [_p, C.POINTER(_d)]),
+    "hf_run": (_i, [_p, _i64, _i, _i, C.POINTER(_i64)]),
+    "hf_get_time": (_i, [_p, C.POINTER(_d), C.POINTER(_i64), C.POINTER(_d)]),
+    "hf_hllc_errors": (_i, [_p, C.POINTER(_i64)]),
+    "hf_sync": (_i, [_p]),
+    "hf_stream": (_i, [_p, C.POINTER(_p)]),
+    "hf_profile": (_i, [_p, _i]),
+    "hf_kernel_time": (_i, [_p, _i, C.POINTER(_d), C.POINTER(_i64)]),
+    "hf_status_string": (C.c_char_p, [_i]),
+    "hf_last_error_message": (C.c_char_p, [_p]),
+}
+
+_lib = None
+
+
+class HyperFlowError(RuntimeError):
+    def __init__(self, status: int, msg: str = ""):
+        self.status = status
+        super().__init__(f"{STATUS.get(status, status)}: {msg}" if msg else STATUS.get(status, str(status)))
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is missing: build it with "
+                               "`python -c 'import __graft_entry__ as g; g.build()'`")
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def check(status: int, ctx=None) -> None:
+    if status != HF_OK:
+        msg = ""
+        if ctx is not None:
+            m = lib().hf_last_error_message(ctx)
+            msg = m.decode() if m else ""
+        raise HyperFlowError(status, msg)

@@ -1,0 +1,685 @@
+// C ABI of the Cartesian GPU time step (declared in include/hyperflow_gb300.h).
+//
+// Host side: parses the reference's case file, builds the initial state exactly as
+// the reference does (setup only), owns the device buffers, the TMA descriptors and the
+// CUDA stream, and orders the kernels of one step:
+//     bc_fill -> ghost_cfl (dt) -> stencil(block 0) ... stencil(block B-1) -> finalize
+// which is the reference's apply_bcs -> calculate_time_step -> per-block ODE sequence
+// (src/fvm_2d_cart/simulation/simulation/simulation.cpp:85-120).
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include "../../include/hyperflow_gb300.h"
+#include "hf_cart.h"
+#include "hf_json.hpp"
+
+namespace {
+
+using hf::Json;
+
+typedef CUresult (*PFN_encodeTiled)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                    const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                    const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                    CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+PFN_encodeTiled get_encode() {
+    static PFN_encodeTiled fn = nullptr;
+    if (!fn) {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                             &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_encodeTiled>(p);
+    }
+    return fn;
+}
+
+struct BlockHost {
+    int nx, ny, tx, ty, pitch;
+    double xl, xr, yb, yt, dx, dy;
+    int bc_type[4];
+    int bc_block[4];
+    double bc_state[4][4];
+};
+
+// prim_to_cons, src/fvm_2d_cart/model/euler_ideal_gas/euler_ideal_gas.cpp:96-109
+void prim_to_cons(double gamma, const double* w, double* c) {
+    double rho = w[0], u = w[1], v = w[2], p = w[3];
+    c[0] = rho;
+    c[1] = rho * u;
+    c[2] = rho * v;
+    c[3] = p / (gamma - 1.0) + 0.5 * rho * (u * u + v * v);
+}
+
+std::vector<double> read_vec4(const Json& a) {
+    if (a.kind != Json::Array || a.size() != 4) throw std::runtime_error("state must have 4 entries");
+    std::vector<double> v(4);
+    for (int k = 0; k < 4; ++k) v[k] = a[k].number();
+    return v;
+}
+
+}  // namespace
+
+struct hf_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    int scheme = 0, limiter = 0, ghost = 1, nblocks = 0;
+    double gamma = 1.4, cfl = 0.5, t_start = 0.0, t_end = 0.0;
+    std::vector<BlockHost> blocks;
+    hf::MeshDev hmesh{};
+    hf::MeshDev* dmesh = nullptr;
+    hf::Ctrl* dctrl = nullptr;
+    CUtensorMap tmap[HF_MAXB][2];
+    std::vector<double*> allocs;
+    double* pinned = nullptr;   // staging for layout conversion
+    size_t pinned_n = 0;
+    int next_block = 0;         // next block hf_advance_block expects
+    long long host_step = 0;    // mirror of ctrl.step while the host drives the steps
+    // graphs of one step (index = clamp flag)
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    // profiling
+    bool profile = false;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev[2];
+    size_t ev_used[2] = {0, 0};
+    std::string err;
+};
+
+namespace {
+
+int fail(hf_ctx* c, int code, const std::string& msg) {
+    if (c) c->err = msg;
+    return code;
+}
+
+#define CK(call)                                                                        \
+    do {                                                                                \
+        cudaError_t e_ = (call);                                                        \
+        if (e_ != cudaSuccess)                                                          \
+            return fail(ctx, HF_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+// ---- initial conditions (setup only; same formulas as the reference) --------------
+// MeshBlock::calculate_centroids (mesh_block.cpp:239-257) + initialise_field_values
+// (215-224); the per-type field functions of quadrp.cpp:49-64, doublerp.cpp:42-55,
+// sphericalrp.cpp:62-72, constant.cpp:34-40; the parser's prim->cons conversions
+// (parser.cpp:311-428).
+void build_initial_state(const Json& ic, double gamma, const BlockHost& B, int g,
+                         std::vector<double>& soa) {
+    soa.assign((size_t)4 * B.ty * B.tx, 0.0);
+    const std::string type = ic["type"].string();
+    const bool prim = ic.has("variables") && ic["variables"].string() == "Primitive";
+    auto cons = [&](const Json& a, bool convert) {
+        std::vector<double> s = read_vec4(a), c(4);
+        if (!convert) return s;
+        prim_to_cons(gamma, s.data(), c.data());
+        return c;
+    };
+    std::vector<double> s0, s1, s2, s3;
+    double p0 = 0, p1 = 0, p2 = 0;
+    int kind;
+    if (type == "Constant") {
+        kind = 0;
+        s0 = cons(ic["init_state"], true);
+    } else if (type == "DoubleRiemannProblem") {
+        kind = 1;
+        p0 = ic["x_lm_interface"].number();
+        p1 = ic["x_mr_interface"].number();
+        s0 = cons(ic["init_left_state"], prim);
+        s1 = cons(ic["init_middle_state"], prim);
+        s2 = cons(ic["init_right_state"], prim);
+    } else if (type == "QuadRiemannProblem") {
+        kind = 2;
+        p0 = ic["x_interface"].number();
+        p1 = ic["y_interface"].number();
+        s0 = cons(ic["init_ne_state"], prim);
+        s1 = cons(ic["init_nw_state"], prim);
+        s2 = cons(ic["init_sw_state"], prim);
+        s3 = cons(ic["init_se_state"], prim);
+    } else if (type == "SphericalRiemannProblem") {
+        kind = 3;
+        p0 = ic["radius"].number();
+        p1 = ic["x_origin"].number();
+        p2 = ic["y_origin"].number();
+        s0 = cons(ic["init_sphere_state"], true);
+        s1 = cons(ic["init_ext_state"], true);
+    } else {
+        throw std::invalid_argument("initial condition '" + type + "' not supported");
+    }
+    const double sx = B.xl - (static_cast<double>(g) - 0.5) * B.dx;
+    const double sy = B.yb - (static_cast<double>(g) - 0.5) * B.dy;
+    for (int i = g; i < B.tx - g; ++i)
+        for (int j = g; j < B.ty - g; ++j) {
+            const double x = sx + static_cast<double>(i) * B.dx;
+            const double y = sy + static_cast<double>(j) * B.dy;
+            const double* s;
+            switch (kind) {
+                case 0: s = s0.data(); break;
+                case 1:
+                    if (x <= p0) s = s0.data();
+                    else if ((x > p0) && (x <= p1)) s = s1.data();
+                    else s = s2.data();
+                    break;
+                case 2:
+                    if ((x <= p0) && (y <= p1)) s = s2.data();          // SW
+                    else if ((x <= p0) && (y > p1)) s = s1.data();      // NW
+                    else if ((x > p0) && (y <= p1)) s = s3.data();      // SE
+                    else s = s0.data();                                  // NE
+                    break;
+                default:
+                    s = (((x - p1) * (x - p1) + (y - p2) * (y - p2)) <= (p0 * p0)) ? s0.data()
+                                                                                 : s1.data();
+            }
+            for (int v = 0; v < 4; ++v) soa[((size_t)v * B.ty + j) * B.tx + i] = s[v];
+        }
+}
+
+int parse_case(hf_ctx* ctx, const Json& cfg) {
+    const Json& model = cfg["model"];
+    if (model["model"].string() != "EulerIdealGas")
+        return fail(ctx, HF_ERR_UNSUPPORTED, "model must be EulerIdealGas");
+    ctx->gamma = model["gamma"].number();
+    const Json& sch = cfg["scheme"];
+    const std::string st = sch["type"].string();
+    if (st == "Godunov") {
+        ctx->scheme = 0;
+        ctx->ghost = 1;
+    } else if (st == "MUSCLHancock") {
+        ctx->scheme = 1;
+        ctx->ghost = 2;
+        const std::string lim = sch["limiter"].string();
+        if (lim == "MinBee") ctx->limiter = 0;
+        else if (lim == "VanLeer") ctx->limiter = 1;
+        else return fail(ctx, HF_ERR_UNSUPPORTED, "limiter '" + lim + "' not supported");
+    } else {
+        return fail(ctx, HF_ERR_UNSUPPORTED, "scheme '" + st + "' not supported");
+    }
+    if (sch["riemann"].string() != "HLLCEuler")
+        return fail(ctx, HF_ERR_UNSUPPORTED, "Riemann solver must be HLLCEuler");
+    if (sch["ode"].string() != "ForwardEuler")
+        return fail(ctx, HF_ERR_UNSUPPORTED, "ODE solver must be ForwardEuler");
+    const Json& sim = cfg["simulation"];
+    ctx->cfl = sim["cfl"].number();
+    ctx->t_start = sim["t_start"].number();
+    ctx->t_end = sim["t_end"].number();
+    const Json& blocks = cfg["mesh"]["blocks"];
+    ctx->nblocks = (int)blocks.size();
+    if (ctx->nblocks < 1 || ctx->nblocks > HF_MAXB)
+        return fail(ctx, HF_ERR_UNSUPPORTED, "between 1 and 16 mesh blocks are supported");
+    static const char* sides[4] = {"bottom", "right", "top", "left"};
+    for (int b = 0; b < ctx->nblocks; ++b) {
+        const Json& jb = blocks[b];
+        BlockHost B{};
+        const Json& ex = jb["extents"];
+        B.xl = ex["x_left"].number();
+        B.xr = ex["x_right"].number();
+        B.yb = ex["y_bottom"].number();
+        B.yt = ex["y_top"].number();
+        B.nx = (int)jb["x_cells"].number();
+        B.ny = (int)jb["y_cells"].number();
+        if (B.nx < 2 * ctx->ghost || B.ny < 2 * ctx->ghost)
+            return fail(ctx, HF_ERR_UNSUPPORTED, "a block needs at least 2*ghost cells per axis");
+        B.tx = B.nx + 2 * ctx->ghost;
+        B.ty = B.ny + 2 * ctx->ghost;
+        B.pitch = (B.tx + 31) / 32 * 32;
+        B.dx = (B.xr - B.xl) / B.nx;   // mesh_block.cpp:227-236
+        B.dy = (B.yt - B.yb) / B.ny;
+        for (int s = 0; s < 4; ++s) {
+            const Json& bc = jb["boundaries"][sides[s]];
+            const std::string kind = bc["type"].string();
+            if (kind == "Transmissive") B.bc_type[s] = hf::BC_TRANSMISSIVE;
+            else if (kind == "Reflective") B.bc_type[s] = hf::BC_REFLECTIVE;
+            else if (kind == "Dirichlet") {
+                B.bc_type[s] = hf::BC_DIRICHLET;
+                std::vector<double> st4 = read_vec4(bc["flow_state"]);
+                if (bc["variables"].string() == "Primitive") {
+                    double c4[4];
+                    prim_to_cons(ctx->gamma, st4.data(), c4);
+                    for (int v = 0; v < 4; ++v) B.bc_state[s][v] = c4[v];
+                } else {
+                    for (int v = 0; v < 4; ++v) B.bc_state[s][v] = st4[v];
+                }
+            } else if (kind == "Internal") {
+                B.bc_type[s] = hf::BC_INTERNAL;
+                B.bc_block[s] = (int)bc["block"].number();
+            } else {
+                return fail(ctx, HF_ERR_UNSUPPORTED, "boundary '" + kind + "' not recognised");
+            }
+        }
+        ctx->blocks.push_back(B);
+    }
+    // an Internal side copies whole rows/columns of its neighbour: the extents along the
+    // shared side must agree (the reference indexes the neighbour with the same index)
+    for (int b = 0; b < ctx->nblocks; ++b)
+        for (int s = 0; s < 4; ++s) {
+            const BlockHost& B = ctx->blocks[b];
+            if (B.bc_type[s] != hf::BC_INTERNAL) continue;
+            int e = B.bc_block[s];
+            if (e < 0 || e >= ctx->nblocks)
+                return fail(ctx, HF_ERR_ARG, "Internal boundary names a missing block");
+            const BlockHost& E = ctx->blocks[e];
+            bool along_x = (s == 0 || s == 2);
+            if (along_x ? (E.tx != B.tx) : (E.ty != B.ty))
+                return fail(ctx, HF_ERR_UNSUPPORTED, "Internal boundary between blocks of unequal extent");
+        }
+    return HF_OK;
+}
+
+int make_tmaps(hf_ctx* ctx) {
+    PFN_encodeTiled enc = get_encode();
+    if (!enc) return fail(ctx, HF_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
+    hf::StencilTiles t = hf::stencil_tiles(ctx->scheme);
+    for (int b = 0; b < ctx->nblocks; ++b) {
+        const BlockHost& B = ctx->blocks[b];
+        for (int k = 0; k < 2; ++k) {
+            cuuint64_t dims[3] = {(cuuint64_t)B.tx, (cuuint64_t)B.ty, 4};
+            cuuint64_t strides[2] = {(cuuint64_t)B.pitch * 8, (cuuint64_t)B.pitch * B.ty * 8};
+            cuuint32_t box[3] = {(cuuint32_t)(t.tx + 2 * ctx->ghost), (cuuint32_t)(t.ty + 2 * ctx->ghost), 4};
+            cuuint32_t es[3] = {1, 1, 1};
+            CUresult r = enc(&ctx->tmap[b][k], CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3,
+                             ctx->hmesh.b[b].buf[k], dims, strides, box, es,
+                             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                             CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+            if (r != CUDA_SUCCESS)
+                return fail(ctx, HF_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
+        }
+    }
+    return HF_OK;
+}
+
+long long read_step(hf_ctx* ctx) {
+    long long s = 0;
+    cudaStreamSynchronize(ctx->stream);
+    cudaMemcpy(&s, &ctx->dctrl->step, sizeof s, cudaMemcpyDeviceToHost);
+    return s;
+}
+
+double* staging(hf_ctx* ctx, size_t n) {
+    if (ctx->pinned_n < n) {
+        if (ctx->pinned) cudaFreeHost(ctx->pinned);
+        ctx->pinned = nullptr;
+        ctx->pinned_n = 0;
+        if (cudaMallocHost(&ctx->pinned, n * sizeof(double)) != cudaSuccess) return nullptr;
+        ctx->pinned_n = n;
+    }
+    return ctx->pinned;
+}
+
+void ev_record(hf_ctx* ctx, int kind, bool start) {
+    auto& v = ctx->ev[kind];
+    size_t& used = ctx->ev_used[kind];
+    if (start) {
+        if (used == v.size()) {
+            cudaEvent_t a, b;
+            cudaEventCreate(&a);
+            cudaEventCreate(&b);
+            v.push_back({a, b});
+        }
+        cudaEventRecord(v[used].first, ctx->stream);
+    } else {
+        cudaEventRecord(v[used].second, ctx->stream);
+        ++used;
+    }
+}
+
+// one step's kernels after the ghost fill: dt, then every block, then finalize
+int enqueue_step(hf_ctx* ctx, bool profiled) {
+    if (profiled) ev_record(ctx, 1, true);
+    CK(hf::launch_bc_fill(ctx->dctrl, ctx->dmesh, ctx->stream));
+    CK(hf::launch_ghost_cfl(ctx->dctrl, ctx->dmesh, ctx->hmesh.total_ghost, ctx->stream));
+    if (profiled) { ev_record(ctx, 1, false); ev_record(ctx, 0, true); }
+    for (int b = 0; b < ctx->nblocks; ++b)
+        CK(hf::launch_stencil(ctx->dctrl, ctx->dmesh, b, ctx->blocks[b].nx, ctx->blocks[b].ny,
+                              ctx->scheme, ctx->limiter, &ctx->tmap[b][0], &ctx->tmap[b][1],
+                              ctx->stream));
+    if (profiled) ev_record(ctx, 0, false);
+    CK(hf::launch_finalize(ctx->dctrl, ctx->stream));
+    return HF_OK;
+}
+
+int set_clamp(hf_ctx* ctx, int clamp) {
+    CK(cudaMemcpyAsync(&ctx->dctrl->clamp, &clamp, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+    return HF_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* hf_status_string(int s) {
+    switch (s) {
+        case HF_OK: return "ok";
+        case HF_ERR_ARG: return "bad argument";
+        case HF_ERR_PARSE: return "case file parse error";
+        case HF_ERR_UNSUPPORTED: return "unsupported case";
+        case HF_ERR_CUDA: return "CUDA error";
+        case HF_ERR_DEVICE: return "device error word raised";
+        case HF_ERR_STATE: return "call out of order";
+        case HF_ERR_NO_DEVICE: return "no CUDA device";
+        default: return "unknown status";
+    }
+}
+
+const char* hf_last_error_message(const hf_ctx* ctx) { return ctx ? ctx->err.c_str() : ""; }
+
+int hf_create(const char* case_json, size_t len, hf_ctx** out) {
+    if (!case_json || !out) return HF_ERR_ARG;
+    *out = nullptr;
+    std::unique_ptr<hf_ctx> holder(new hf_ctx());
+    hf_ctx* ctx = holder.get();
+    Json cfg;
+    try {
+        cfg = Json::parse(case_json, len);
+        int r = parse_case(ctx, cfg);
+        if (r != HF_OK) { *out = holder.release(); return r; }
+    } catch (const std::exception& e) {
+        ctx->err = e.what();
+        *out = holder.release();
+        return HF_ERR_PARSE;
+    }
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        ctx->err = "no CUDA device visible";
+        *out = holder.release();
+        return HF_ERR_NO_DEVICE;
+    }
+    *out = holder.release();
+    CK(cudaGetDevice(&ctx->device));
+    CK(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+    CK(hf::stencil_prepare());
+    // device state
+    hf::MeshDev& M = ctx->hmesh;
+    M.nblocks = ctx->nblocks;
+    M.ghost = ctx->ghost;
+    long long goff = 0;
+    for (int b = 0; b < ctx->nblocks; ++b) {
+        const BlockHost& B = ctx->blocks[b];
+        hf::BlockDev& D = M.b[b];
+        D.tx = B.tx; D.ty = B.ty; D.nx = B.nx; D.ny = B.ny; D.pitch = B.pitch;
+        for (int s = 0; s < 4; ++s) {
+            D.bc_type[s] = B.bc_type[s];
+            D.bc_block[s] = B.bc_block[s];
+            for (int v = 0; v < 4; ++v) D.bc_state[s][v] = B.bc_state[s][v];
+        }
+        size_t n = (size_t)4 * B.ty * B.pitch;
+        for (int k = 0; k < 2; ++k) {
+            double* p = nullptr;
+            CK(cudaMalloc(&p, n * sizeof(double)));
+            ctx->allocs.push_back(p);
+            CK(cudaMemsetAsync(p, 0, n * sizeof(double), ctx->stream));
+            D.buf[k] = p;
+        }
+        D.ghost_off = goff;
+        D.ghost_count = B.tx * B.ty - B.nx * B.ny;
+        goff += D.ghost_count;
+    }
+    M.total_ghost = goff;
+    CK(cudaMalloc(&ctx->dmesh, sizeof(hf::MeshDev)));
+    CK(cudaMemcpyAsync(ctx->dmesh, &M, sizeof M, cudaMemcpyHostToDevice, ctx->stream));
+    hf::Ctrl C{};
+    C.nblocks = ctx->nblocks;
+    C.scheme = ctx->scheme;
+    C.limiter = ctx->limiter;
+    C.ghost = ctx->ghost;
+    C.gamma = ctx->gamma;
+    C.g1 = ctx->gamma - 1.0;
+    C.cfl = ctx->cfl;
+    for (int b = 0; b < ctx->nblocks; ++b) {
+        C.dx[b] = ctx->blocks[b].dx;
+        C.dy[b] = ctx->blocks[b].dy;
+    }
+    C.t = ctx->t_start;
+    C.t_end = ctx->t_end;
+    CK(cudaMalloc(&ctx->dctrl, sizeof(hf::Ctrl)));
+    CK(cudaMemcpyAsync(ctx->dctrl, &C, sizeof C, cudaMemcpyHostToDevice, ctx->stream));
+    int r = make_tmaps(ctx);
+    if (r != HF_OK) return r;
+    // initial condition, uploaded into both buffers (ghosts zero until the first fill)
+    try {
+        for (int b = 0; b < ctx->nblocks; ++b) {
+            std::vector<double> soa;
+            build_initial_state(cfg["initial_condition"], ctx->gamma, ctx->blocks[b], ctx->ghost, soa);
+            r = hf_set_state(ctx, b, soa.data(), HF_LAYOUT_SOA);
+            if (r != HF_OK) return r;
+        }
+    } catch (const std::exception& e) {
+        return fail(ctx, HF_ERR_UNSUPPORTED, e.what());
+    }
+    CK(cudaStreamSynchronize(ctx->stream));
+    return HF_OK;
+}
+
+void hf_destroy(hf_ctx* ctx) {
+    if (!ctx) return;
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    for (int k = 0; k < 2; ++k) {
+        if (ctx->graph[k]) cudaGraphExecDestroy(ctx->graph[k]);
+        for (auto& pr : ctx->ev[k]) { cudaEventDestroy(pr.first); cudaEventDestroy(pr.second); }
+    }
+    for (double* p : ctx->allocs) cudaFree(p);
+    if (ctx->dmesh) cudaFree(ctx->dmesh);
+    if (ctx->dctrl) cudaFree(ctx->dctrl);
+    if (ctx->pinned) cudaFreeHost(ctx->pinned);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+int hf_num_blocks(const hf_ctx* ctx, int* n) {
+    if (!ctx || !n) return HF_ERR_ARG;
+    *n = ctx->nblocks;
+    return HF_OK;
+}
+
+int hf_block_dims(const hf_ctx* ctx, int b, int dims[5]) {
+    if (!ctx || !dims || b < 0 || b >= ctx->nblocks) return HF_ERR_ARG;
+    const BlockHost& B = ctx->blocks[b];
+    dims[0] = B.tx; dims[1] = B.ty; dims[2] = ctx->ghost; dims[3] = B.nx; dims[4] = B.ny;
+    return HF_OK;
+}
+
+int hf_set_state(hf_ctx* ctx, int b, const double* cons, int layout) {
+    if (!ctx || !cons || b < 0 || b >= ctx->nblocks) return HF_ERR_ARG;
+    if (layout != HF_LAYOUT_SOA && layout != HF_LAYOUT_AOS_XY) return HF_ERR_ARG;
+    if (ctx->next_block != 0) return fail(ctx, HF_ERR_STATE, "state upload in the middle of a step");
+    const BlockHost& B = ctx->blocks[b];
+    const hf::BlockDev& D = ctx->hmesh.b[b];
+    size_t n = (size_t)4 * B.ty * B.tx;
+    CK(cudaStreamSynchronize(ctx->stream));
+    const double* st = cons;   // SoA uploads go straight from the caller's buffer
+    if (layout == HF_LAYOUT_AOS_XY) {
+        double* tmp = staging(ctx, n);
+        if (!tmp) return fail(ctx, HF_ERR_CUDA, "pinned staging allocation failed");
+        for (int i = 0; i < B.tx; ++i)
+            for (int j = 0; j < B.ty; ++j)
+                for (int v = 0; v < 4; ++v)
+                    tmp[((size_t)v * B.ty + j) * B.tx + i] = cons[((size_t)i * B.ty + j) * 4 + v];
+        st = tmp;
+    }
+    long long step = read_step(ctx);
+    int p = (int)(step & 1);
+    for (int k = 0; k < 2; ++k)
+        CK(cudaMemcpy2DAsync(D.buf[k], (size_t)B.pitch * 8, st, (size_t)B.tx * 8, (size_t)B.tx * 8,
+                             (size_t)4 * B.ty, cudaMemcpyHostToDevice, ctx->stream));
+    // TimeStep terms of the uploaded interior
+    unsigned long long zero[2] = {0ull, 0ull};
+    CK(cudaMemcpyAsync(&ctx->dctrl->int_s[p][b][0], zero, sizeof zero, cudaMemcpyHostToDevice, ctx->stream));
+    CK(hf::launch_interior_cfl(ctx->dctrl, ctx->dmesh, b, B.nx, B.ny, p, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return HF_OK;
+}
+
+int hf_get_state(hf_ctx* ctx, int b, double* cons, int layout) {
+    if (!ctx || !cons || b < 0 || b >= ctx->nblocks) return HF_ERR_ARG;
+    if (layout != HF_LAYOUT_SOA && layout != HF_LAYOUT_AOS_XY) return HF_ERR_ARG;
+    const BlockHost& B = ctx->blocks[b];
+    const hf::BlockDev& D = ctx->hmesh.b[b];
+    long long step = read_step(ctx);
+    int p = (int)(step & 1);
+    // a block already advanced in the step in progress lives in the other buffer
+    if (ctx->next_block > b) p ^= 1;
+    size_t n = (size_t)4 * B.ty * B.tx;
+    double* st = layout == HF_LAYOUT_SOA ? cons : staging(ctx, n);
+    if (!st) return fail(ctx, HF_ERR_CUDA, "pinned staging allocation failed");
+    CK(cudaMemcpy2DAsync(st, (size_t)B.tx * 8, D.buf[p], (size_t)B.pitch * 8, (size_t)B.tx * 8,
+                         (size_t)4 * B.ty, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (layout == HF_LAYOUT_AOS_XY) {
+        for (int i = 0; i < B.tx; ++i)
+            for (int j = 0; j < B.ty; ++j)
+                for (int v = 0; v < 4; ++v)
+                    cons[((size_t)i * B.ty + j) * 4 + v] = st[((size_t)v * B.ty + j) * B.tx + i];
+    }
+    return HF_OK;
+}
+
+int hf_apply_bcs(hf_ctx* ctx) {
+    if (!ctx) return HF_ERR_ARG;
+    if (ctx->next_block != 0) return fail(ctx, HF_ERR_STATE, "apply_bcs in the middle of a step");
+    CK(hf::launch_bc_fill(ctx->dctrl, ctx->dmesh, ctx->stream));
+    return HF_OK;
+}
+
+int hf_time_step(hf_ctx* ctx, double* dt) {
+    if (!ctx) return HF_ERR_ARG;
+    int r = set_clamp(ctx, 0);
+    if (r != HF_OK) return r;
+    CK(hf::launch_ghost_cfl(ctx->dctrl, ctx->dmesh, ctx->hmesh.total_ghost, ctx->stream));
+    if (dt) {
+        CK(cudaMemcpyAsync(dt, &ctx->dctrl->dt_cfl, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+    }
+    return HF_OK;
+}
+
+int hf_advance_block(hf_ctx* ctx, int b, double dt) {
+    if (!ctx || b < 0 || b >= ctx->nblocks) return HF_ERR_ARG;
+    if (b != ctx->next_block) return fail(ctx, HF_ERR_STATE, "blocks must be advanced in order");
+    if (b == 0) CK(hf::launch_set_dt(ctx->dctrl, dt, ctx->stream));
+    CK(hf::launch_stencil(ctx->dctrl, ctx->dmesh, b, ctx->blocks[b].nx, ctx->blocks[b].ny,
+                          ctx->scheme, ctx->limiter, &ctx->tmap[b][0], &ctx->tmap[b][1], ctx->stream));
+    if (b == ctx->nblocks - 1) {
+        CK(hf::launch_finalize(ctx->dctrl, ctx->stream));
+        ctx->next_block = 0;
+    } else {
+        ctx->next_block = b + 1;
+    }
+    return HF_OK;
+}
+
+int hf_advance(hf_ctx* ctx, double dt) {
+    if (!ctx) return HF_ERR_ARG;
+    for (int b = 0; b < ctx->nblocks; ++b) {
+        int r = hf_advance_block(ctx, b, dt);
+        if (r != HF_OK) return r;
+    }
+    return HF_OK;
+}
+
+int hf_step(hf_ctx* ctx, double* dt) {
+    if (!ctx) return HF_ERR_ARG;
+    if (ctx->next_block != 0) return fail(ctx, HF_ERR_STATE, "step in the middle of a step");
+    int r = set_clamp(ctx, 0);
+    if (r != HF_OK) return r;
+    r = enqueue_step(ctx, ctx->profile);
+    if (r != HF_OK) return r;
+    if (dt) {
+        CK(cudaMemcpyAsync(dt, &ctx->dctrl->dt, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+    }
+    return HF_OK;
+}
+
+int hf_run(hf_ctx* ctx, int64_t n, int clamp_t_end, int use_graph, int64_t* steps_done) {
+    if (!ctx || n < 0) return HF_ERR_ARG;
+    if (ctx->next_block != 0) return fail(ctx, HF_ERR_STATE, "run in the middle of a step");
+    long long s0 = steps_done ? read_step(ctx) : 0;
+    int clamp = clamp_t_end ? 1 : 0;
+    int r = set_clamp(ctx, clamp);
+    if (r != HF_OK) return r;
+    if (use_graph && !ctx->profile) {
+        if (!ctx->graph[clamp]) {
+            cudaGraph_t g;
+            CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+            r = enqueue_step(ctx, false);
+            cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+            if (r != HF_OK) return r;
+            if (e != cudaSuccess) return fail(ctx, HF_ERR_CUDA, cudaGetErrorString(e));
+            CK(cudaGraphInstantiate(&ctx->graph[clamp], g, 0));
+            cudaGraphDestroy(g);
+        }
+        for (int64_t k = 0; k < n; ++k) CK(cudaGraphLaunch(ctx->graph[clamp], ctx->stream));
+    } else {
+        for (int64_t k = 0; k < n; ++k) {
+            r = enqueue_step(ctx, ctx->profile);
+            if (r != HF_OK) return r;
+        }
+    }
+    if (steps_done) *steps_done = read_step(ctx) - s0;
+    return HF_OK;
+}
+
+int hf_get_time(hf_ctx* ctx, double* t, int64_t* calls, double* last_dt) {
+    if (!ctx) return HF_ERR_ARG;
+    hf::Ctrl C;
+    CK(cudaStreamSynchronize(ctx->stream));
+    CK(cudaMemcpy(&C, ctx->dctrl, sizeof C, cudaMemcpyDeviceToHost));
+    if (t) *t = C.t;
+    if (calls) *calls = C.calls;
+    if (last_dt) *last_dt = C.dt;
+    return HF_OK;
+}
+
+int hf_hllc_errors(hf_ctx* ctx, int64_t* count) {
+    if (!ctx || !count) return HF_ERR_ARG;
+    long long v = 0;
+    CK(cudaStreamSynchronize(ctx->stream));
+    CK(cudaMemcpy(&v, &ctx->dctrl->hllc_errors, sizeof v, cudaMemcpyDeviceToHost));
+    *count = v;
+    return HF_OK;
+}
+
+int hf_sync(hf_ctx* ctx) {
+    if (!ctx) return HF_ERR_ARG;
+    CK(cudaStreamSynchronize(ctx->stream));
+    int e = 0;
+    CK(cudaMemcpy(&e, &ctx->dctrl->err, sizeof e, cudaMemcpyDeviceToHost));
+    if (e != 0) return fail(ctx, HF_ERR_DEVICE, "device error word " + std::to_string(e));
+    return HF_OK;
+}
+
+int hf_stream(hf_ctx* ctx, void** stream) {
+    if (!ctx || !stream) return HF_ERR_ARG;
+    *stream = (void*)ctx->stream;
+    return HF_OK;
+}
+
+int hf_profile(hf_ctx* ctx, int enable) {
+    if (!ctx) return HF_ERR_ARG;
+    CK(cudaStreamSynchronize(ctx->stream));
+    ctx->profile = enable != 0;
+    ctx->ev_used[0] = ctx->ev_used[1] = 0;
+    return HF_OK;
+}
+
+int hf_kernel_time(hf_ctx* ctx, int kind, double* ms, int64_t* launches) {
+    if (!ctx || kind < 0 || kind > 1) return HF_ERR_ARG;
+    CK(cudaStreamSynchronize(ctx->stream));
+    double tot = 0.0;
+    for (size_t i = 0; i < ctx->ev_used[kind]; ++i) {
+        float f = 0.f;
+        CK(cudaEventElapsedTime(&f, ctx->ev[kind][i].first, ctx->ev[kind][i].second));
+        tot += f;
+    }
+    if (ms) *ms = tot;
+    if (launches) *launches = (int64_t)ctx->ev_used[kind];
+    return HF_OK;
+}
+
+}  // extern "C"

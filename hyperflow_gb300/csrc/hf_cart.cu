@@ -1,0 +1,593 @@
+// Cartesian time-step kernels for sm_103a.
+//
+//   bc_fill       ghost/halo fill, Mesh::apply_bcs (src/fvm_2d_cart/mesh/mesh/mesh.cpp:31-39)
+//   ghost_cfl     TimeStep over ghost cells + the step dt (timestep.cpp:29-68)
+//   interior_cfl  TimeStep terms over interior cells (after a state upload)
+//   godunov       fused x/y HLLC + update, GodunovScheme (godunov.cpp:27-118) + ForwardEuler
+//   muscl_hancock fused slopes/limiter/predictor/HLLC/update, MUSCLHancockScheme
+//                 (muscl_hancock.cpp:41-376) + ForwardEuler, with the next step's TimeStep
+//                 terms reduced in the epilogue
+//
+// Layout: per block, SoA FP64 [var][total_y][pitch] (x contiguous), ghosts included, two
+// buffers alternating by step parity.  The stencil CTAs stage one tile plus its halo with a
+// single 3-D TMA load (box = tile + 2*ghost in x and y, all four variables) into shared
+// memory; halos come from the neighbouring tiles' cells in HBM, never from another CTA.
+#include <cstdio>
+
+#include "hf_cart.h"
+#include "hf_device.cuh"
+
+namespace hf {
+
+constexpr unsigned kWaitLimit = 1u << 22;   // bounded mbarrier polls before giving up
+
+// ------------------------------------------------------------------------------------
+// ghost fill (one CTA; sides strictly in the reference order)
+// ------------------------------------------------------------------------------------
+// transmissive_boundary.cpp:25-104, reflective_boundary.cpp:25-120,
+// dirichlet_boundary.cpp:25-104, internal_boundary.cpp:27-108.  Layer k = 0..g-1 counts
+// outward from the interior; source indices are the reference's, written per layer.
+__device__ void fill_side(const MeshDev* __restrict__ m, int b, int side, int p) {
+    const BlockDev& B = m->b[b];
+    const int g = m->ghost;
+    const int kind = B.bc_type[side];
+    const int e = B.bc_block[side];
+    const BlockDev& E = m->b[kind == BC_INTERNAL ? e : b];
+    const bool along_x = (side == SIDE_BOTTOM || side == SIDE_TOP);
+    const int n = along_x ? B.tx : B.ty;
+    const int neg_comp = along_x ? 2 : 1;
+    const size_t plane = (size_t)B.ty * B.pitch, eplane = (size_t)E.ty * E.pitch;
+    double* __restrict__ d0 = B.buf[p];
+    double* __restrict__ d1 = B.buf[p ^ 1];
+    const double* __restrict__ src = E.buf[p];
+    for (int pos = threadIdx.x; pos < n; pos += blockDim.x) {
+        for (int k = 0; k < g; ++k) {
+            int di, dj, si = 0, sj = 0;
+            switch (side) {
+                case SIDE_BOTTOM:
+                    di = pos; dj = g - 1 - k;
+                    si = pos; sj = kind == BC_INTERNAL ? E.ty - g - 1 - k : g + k;
+                    break;
+                case SIDE_TOP:
+                    di = pos; dj = B.ty - g + k;
+                    si = pos; sj = kind == BC_INTERNAL ? g + k : B.ty - g - 1 - k;
+                    break;
+                case SIDE_LEFT:
+                    dj = pos; di = g - 1 - k;
+                    sj = pos; si = kind == BC_INTERNAL ? E.tx - g - 1 - k : g + k;
+                    break;
+                default:  // right
+                    dj = pos; di = B.tx - g + k;
+                    sj = pos; si = kind == BC_INTERNAL ? g + k : B.tx - g - 1 - k;
+                    break;
+            }
+            const size_t dof = (size_t)dj * B.pitch + di;
+            const size_t sof = (size_t)sj * E.pitch + si;
+#pragma unroll
+            for (int v = 0; v < 4; ++v) {
+                double val;
+                if (kind == BC_DIRICHLET) {
+                    val = B.bc_state[side][v];
+                } else {
+                    val = src[v * eplane + sof];
+                    if (kind == BC_REFLECTIVE && v == neg_comp) val = -1.0 * val;
+                }
+                d0[v * plane + dof] = val;
+                d1[v * plane + dof] = val;
+            }
+        }
+    }
+}
+
+__global__ void __launch_bounds__(1024) bc_fill_kernel(Ctrl* __restrict__ c,
+                                                       const MeshDev* __restrict__ m) {
+    __shared__ int s_done;
+    const int p = (int)(c->step & 1);
+    if (threadIdx.x == 0) {
+        int done = c->clamp && (c->t == c->t_end);
+        c->done = done;
+        s_done = done;
+        if (!done) {
+            for (int b = 0; b < HF_MAXB; ++b) {
+                c->ghost_s[b][0] = c->ghost_s[b][1] = 0ull;
+                c->int_s[p ^ 1][b][0] = c->int_s[p ^ 1][b][1] = 0ull;
+            }
+            c->ticket = 0u;
+        }
+    }
+    __syncthreads();
+    if (s_done) return;
+    for (int b = 0; b < m->nblocks; ++b)
+        for (int side = 0; side < 4; ++side) {
+            fill_side(m, b, side, p);
+            __syncthreads();
+        }
+}
+
+// ------------------------------------------------------------------------------------
+// TimeStep over the ghost cells; the last CTA forms the step dt
+// ------------------------------------------------------------------------------------
+__device__ __forceinline__ void ghost_cell_ij(const BlockDev& B, int g, long long k, int& i, int& j) {
+    const long long row_cells = (long long)g * B.tx;
+    if (k < row_cells) {                      // bottom ghost rows
+        j = (int)(k / B.tx); i = (int)(k % B.tx);
+    } else if (k < 2 * row_cells) {           // top ghost rows
+        k -= row_cells;
+        j = B.ty - g + (int)(k / B.tx); i = (int)(k % B.tx);
+    } else {                                  // left/right ghost columns of interior rows
+        k -= 2 * row_cells;
+        j = g + (int)(k / (2 * g));
+        int c = (int)(k % (2 * g));
+        i = c < g ? c : B.tx - 2 * g + c;
+    }
+}
+
+constexpr int kRedThreads = 256;
+
+__global__ void __launch_bounds__(kRedThreads) ghost_cfl_kernel(Ctrl* __restrict__ c,
+                                                                const MeshDev* __restrict__ m) {
+    if (c->done) return;
+    const int p = (int)(c->step & 1);
+    const double g = c->gamma, g1 = c->g1;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (int b = 0; b < m->nblocks; ++b) {
+        const BlockDev& B = m->b[b];
+        const size_t plane = (size_t)B.ty * B.pitch;
+        const double* __restrict__ U = B.buf[p];
+        double mx = 0.0, my = 0.0;
+        for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < B.ghost_count;
+             k += stride) {
+            int i, j;
+            ghost_cell_ij(B, m->ghost, k, i, j);
+            size_t o = (size_t)j * B.pitch + i;
+            double sx, sy;
+            wave_terms(g, g1, U[o], U[plane + o], U[2 * plane + o], U[3 * plane + o], sx, sy);
+            mx = nmax(mx, sx);
+            my = nmax(my, sy);
+        }
+        block_max2_atomic<kRedThreads>(mx, my, &c->ghost_s[b][0], &c->ghost_s[b][1]);
+        __syncthreads();
+    }
+    // last CTA to finish forms the dt of this TimeStep call
+    __shared__ bool last;
+    __threadfence();
+    if (threadIdx.x == 0) last = (atomicAdd(&c->ticket, 1u) == gridDim.x - 1);
+    __syncthreads();
+    if (!last || threadIdx.x != 0) return;
+    __threadfence();
+    volatile Ctrl* vc = c;
+    Ctrl snap;
+    snap.nblocks = vc->nblocks;
+    snap.cfl = vc->cfl;
+    for (int b = 0; b < snap.nblocks; ++b) {
+        snap.dx[b] = vc->dx[b];
+        snap.dy[b] = vc->dy[b];
+        snap.ghost_s[b][0] = vc->ghost_s[b][0];
+        snap.ghost_s[b][1] = vc->ghost_s[b][1];
+        snap.int_s[p][b][0] = vc->int_s[p][b][0];
+        snap.int_s[p][b][1] = vc->int_s[p][b][1];
+    }
+    long long call = vc->calls;
+    double dt = cfl_dt(&snap, call, 0, p, p);
+    c->dt_cfl = dt;
+    if (c->clamp && c->t + dt > c->t_end) dt = c->t_end - c->t;   // simulation.cpp:88-90
+    c->dt = dt;
+    c->calls = call + 1;
+    c->ticket = 0u;
+}
+
+// TimeStep terms over one block's interior (after an upload of new state)
+__global__ void __launch_bounds__(kRedThreads) interior_cfl_kernel(Ctrl* __restrict__ c,
+                                                                   const MeshDev* __restrict__ m,
+                                                                   int b, int parity) {
+    const BlockDev& B = m->b[b];
+    const int g = m->ghost;
+    const size_t plane = (size_t)B.ty * B.pitch;
+    const double* __restrict__ U = B.buf[parity];
+    const double gm = c->gamma, g1 = c->g1;
+    double mx = 0.0, my = 0.0;
+    const long long n = (long long)B.nx * B.ny;
+    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n;
+         k += (long long)gridDim.x * blockDim.x) {
+        int i = (int)(k % B.nx) + g, j = (int)(k / B.nx) + g;
+        size_t o = (size_t)j * B.pitch + i;
+        double sx, sy;
+        wave_terms(gm, g1, U[o], U[plane + o], U[2 * plane + o], U[3 * plane + o], sx, sy);
+        mx = nmax(mx, sx);
+        my = nmax(my, sy);
+    }
+    block_max2_atomic<kRedThreads>(mx, my, &c->int_s[parity][b][0], &c->int_s[parity][b][1]);
+}
+
+__global__ void set_dt_kernel(Ctrl* c, double dt) { c->dt = dt; }
+
+// end of step: t += dt; the MUSCL-Hancock predictor calls advance the counter; flip parity
+__global__ void finalize_kernel(Ctrl* c) {
+    if (c->done) return;
+    c->t = c->t + c->dt;
+    if (c->scheme == 1) c->calls = c->calls + c->nblocks;
+    c->step = c->step + 1;
+}
+
+// ------------------------------------------------------------------------------------
+// shared helpers for the stencils
+// ------------------------------------------------------------------------------------
+// A face on a tile edge is formed by both tiles that share it, and partial tiles form
+// faces past the block.  Only the owner counts an HLLC zero-flux fallback, so the count
+// equals the reference's: face index gf (0..n along the normal) of row gr, local index lf.
+__device__ __forceinline__ bool owned_face(int gf, int lf, int T, int n, int gr, int nr) {
+    return gr < nr && gf <= n && (lf < T || gf == n);
+}
+// issue the tile's TMA load and wait for it (bounded); false if the wait gave up
+template <int NBYTES>
+__device__ __forceinline__ bool load_tile(double* sU, uint64_t* bar, const CUtensorMap* tm, int x0,
+                                          int y0, Ctrl* c) {
+    if (threadIdx.x == 0) {
+        mbar_init(bar, 1);
+        mbar_expect_tx(bar, NBYTES);
+        tma_load_3d(sU, tm, bar, x0, y0, 0);
+    }
+    __syncthreads();
+    bool ok = mbar_wait_bounded(bar, 0, kWaitLimit);
+    int bad = __syncthreads_or(!ok);
+    if (bad) {
+        if (threadIdx.x == 0) {
+            raise_error(c, HF_DEV_TIMEOUT);
+            mbar_wait_bounded(bar, 0, kWaitLimit);   // let an in-flight copy land before exit
+        }
+        __syncthreads();
+        return false;
+    }
+    return true;
+}
+
+// ------------------------------------------------------------------------------------
+// MUSCL-Hancock, fused
+// ------------------------------------------------------------------------------------
+template <int TX, int TY>
+struct MhLayout {
+    static constexpr int UX = TX + 4, UY = TY + 4;
+    static constexpr int AXN = (TX + 2) * TY, AYN = TX * (TY + 2);
+    static constexpr int AN = AXN > AYN ? AXN : AYN;
+    static constexpr int U_OFF = 0;
+    static constexpr int A_OFF = U_OFF + 4 * UY * UX;
+    static constexpr int F_OFF = A_OFF + 8 * AN;
+    static constexpr int G_OFF = F_OFF + 4 * TY * (TX + 1);
+    static constexpr int END = G_OFF + 4 * (TY + 1) * TX;
+    static constexpr size_t BYTES = (size_t)END * 8 + 16;   // + mbarrier
+    static constexpr int TMA_BYTES = 4 * UY * UX * 8;
+};
+
+template <int TX, int TY, int LIM, int NT>
+__global__ void __launch_bounds__(NT) mh_kernel(Ctrl* __restrict__ c, const MeshDev* __restrict__ m,
+                                                int b, const __grid_constant__ CUtensorMap tm0,
+                                                const __grid_constant__ CUtensorMap tm1) {
+    using L = MhLayout<TX, TY>;
+    extern __shared__ __align__(1024) double smem[];
+    double* sU = smem + L::U_OFF;
+    double* sA = smem + L::A_OFF;
+    double* sF = smem + L::F_OFF;
+    double* sG = smem + L::G_OFF;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + L::END);
+    if (c->done) return;
+
+    const BlockDev& B = m->b[b];
+    const int p = (int)(c->step & 1);
+    const int tiles_x = (B.nx + TX - 1) / TX;
+    const int x0 = (blockIdx.x % tiles_x) * TX, y0 = (blockIdx.x / tiles_x) * TY;
+
+    // scalars of this step while the tile is in flight
+    const double g = c->gamma, g1 = c->g1;
+    const double dt = c->dt;
+    // the predictor's own TimeStep call (muscl_hancock.cpp:246): blocks < b already advanced
+    const double dtp = cfl_dt(c, c->calls + b, b, p, p ^ 1);
+    const double dx = c->dx[b], dy = c->dy[b];
+    const double hdx = 0.5 * dtp / dx, hdy = 0.5 * dtp / dy;   // 248-249
+    const double one_dx = 1.0 / dx, one_dy = 1.0 / dy;          // 352-353
+    if (blockIdx.x == 0 && threadIdx.x == 0) c->dt_pred[b] = dtp;
+
+    if (!load_tile<L::TMA_BYTES>(sU, bar, p ? &tm1 : &tm0, x0, y0, c)) return;
+
+    int herr = 0;
+    // x phase: slopes, extrapolation, half-step predictor of the x face pair, cells -1..TX
+    for (int it = threadIdx.x; it < L::AXN; it += NT) {
+        const int lx = it % (TX + 2), ly = it / (TX + 2);
+        const int sx = lx + 1, sy = ly + 2;
+        double e0[4], e1[4];
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+            const double* row = sU + (v * L::UY + sy) * L::UX;
+            const double u0 = row[sx];
+            const double s = slope<LIM>(row[sx - 1], u0, row[sx + 1]);
+            e0[v] = u0 - 0.5 * s;
+            e1[v] = u0 + 0.5 * s;
+        }
+        Prim w0 = to_prim(g1, e0[0], e0[1], e0[2], e0[3]);
+        Prim w1 = to_prim(g1, e1[0], e1[1], e1[2], e1[3]);
+        double f0[4], f1[4];
+        flux<0>(w0, f0);
+        flux<0>(w1, f1);
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+            const double d = hdx * (f0[v] - f1[v]);
+            sA[(0 * 4 + v) * L::AN + it] = e0[v] + d;
+            sA[(1 * 4 + v) * L::AN + it] = e1[v] + d;
+        }
+    }
+    __syncthreads();
+    // x faces 0..TX of each tile row (face f is the left face of output cell f)
+    for (int it = threadIdx.x; it < (TX + 1) * TY; it += NT) {
+        const int fx = it % (TX + 1), fy = it / (TX + 1);
+        const int al = fy * (TX + 2) + fx;
+        double UL[4], UR[4], F[4];
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+            UL[v] = sA[(1 * 4 + v) * L::AN + al];
+            UR[v] = sA[(0 * 4 + v) * L::AN + al + 1];
+        }
+        const int bad = hllc_cons<0>(g, g1, UL, UR, F);
+        herr += bad && owned_face(x0 + fx, fx, TX, B.nx, y0 + fy, B.ny);
+#pragma unroll
+        for (int v = 0; v < 4; ++v) sF[(v * TY + fy) * (TX + 1) + fx] = F[v];
+    }
+    __syncthreads();
+    // y phase, cells -1..TY of each tile column
+    for (int it = threadIdx.x; it < L::AYN; it += NT) {
+        const int lx = it % TX, ly = it / TX;
+        const int sx = lx + 2, sy = ly + 1;
+        double e2[4], e3[4];
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+            const double* col = sU + (v * L::UY + sy) * L::UX + sx;
+            const double u0 = col[0];
+            const double s = slope<LIM>(col[-L::UX], u0, col[L::UX]);
+            e2[v] = u0 - 0.5 * s;
+            e3[v] = u0 + 0.5 * s;
+        }
+        Prim w2 = to_prim(g1, e2[0], e2[1], e2[2], e2[3]);
+        Prim w3 = to_prim(g1, e3[0], e3[1], e3[2], e3[3]);
+        double f2[4], f3[4];
+        flux<1>(w2, f2);
+        flux<1>(w3, f3);
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+            const double d = hdy * (f2[v] - f3[v]);
+            sA[(0 * 4 + v) * L::AN + it] = e2[v] + d;
+            sA[(1 * 4 + v) * L::AN + it] = e3[v] + d;
+        }
+    }
+    __syncthreads();
+    // y faces 0..TY of each tile column
+    for (int it = threadIdx.x; it < TX * (TY + 1); it += NT) {
+        const int gx = it % TX, gy = it / TX;
+        double UB[4], UT[4], F[4];
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+            UB[v] = sA[(1 * 4 + v) * L::AN + gy * TX + gx];
+            UT[v] = sA[(0 * 4 + v) * L::AN + (gy + 1) * TX + gx];
+        }
+        const int bad = hllc_cons<1>(g, g1, UB, UT, F);
+        herr += bad && owned_face(y0 + gy, gy, TY, B.ny, x0 + gx, B.nx);
+#pragma unroll
+        for (int v = 0; v < 4; ++v) sG[(v * (TY + 1) + gy) * TX + gx] = F[v];
+    }
+    __syncthreads();
+    // conservative update + forward Euler, and the next step's TimeStep terms
+    double* __restrict__ out = B.buf[p ^ 1];
+    const size_t plane = (size_t)B.ty * B.pitch;
+    double mx = 0.0, my = 0.0;
+    for (int it = threadIdx.x; it < TX * TY; it += NT) {
+        const int ox = it % TX, oy = it / TX;
+        const int gxx = x0 + ox, gyy = y0 + oy;
+        if (gxx < B.nx && gyy < B.ny) {
+            double un[4];
+            const size_t o = (size_t)(gyy + 2) * B.pitch + (gxx + 2);
+#pragma unroll
+            for (int v = 0; v < 4; ++v) {
+                const double Lv = (one_dx * (sF[(v * TY + oy) * (TX + 1) + ox] -
+                                             sF[(v * TY + oy) * (TX + 1) + ox + 1])) +
+                                  (one_dy * (sG[(v * (TY + 1) + oy) * TX + ox] -
+                                             sG[(v * (TY + 1) + oy + 1) * TX + ox]));
+                un[v] = dt * Lv + sU[(v * L::UY + oy + 2) * L::UX + ox + 2];
+                out[v * plane + o] = un[v];
+            }
+            double sx, sy;
+            wave_terms(g, g1, un[0], un[1], un[2], un[3], sx, sy);
+            mx = nmax(mx, sx);
+            my = nmax(my, sy);
+        }
+    }
+    block_max2_atomic<NT>(mx, my, &c->int_s[p ^ 1][b][0], &c->int_s[p ^ 1][b][1]);
+    if (herr) atomicAdd(reinterpret_cast<unsigned long long*>(&c->hllc_errors), (unsigned long long)herr);
+}
+
+// ------------------------------------------------------------------------------------
+// Godunov, fused: per-cell primitives/fluxes once, then x/y HLLC, then update
+// ------------------------------------------------------------------------------------
+template <int TX, int TY>
+struct GoLayout {
+    static constexpr int UX = TX + 2, UY = TY + 2, NC = UX * UY;
+    static constexpr int NQ = 12;   // u v p Et a fx0 fx1 fx2 fx3 fy0 fy2 fy3 (fy1 == fx2)
+    static constexpr int U_OFF = 0;
+    static constexpr int Q_OFF = U_OFF + 4 * NC;
+    static constexpr int F_OFF = Q_OFF + NQ * NC;
+    static constexpr int G_OFF = F_OFF + 4 * TY * (TX + 1);
+    static constexpr int END = G_OFF + 4 * (TY + 1) * TX;
+    static constexpr size_t BYTES = (size_t)END * 8 + 16;
+    static constexpr int TMA_BYTES = 4 * NC * 8;
+};
+
+template <int TX, int TY, int NT>
+__global__ void __launch_bounds__(NT) godunov_kernel(Ctrl* __restrict__ c,
+                                                     const MeshDev* __restrict__ m, int b,
+                                                     const __grid_constant__ CUtensorMap tm0,
+                                                     const __grid_constant__ CUtensorMap tm1) {
+    using L = GoLayout<TX, TY>;
+    extern __shared__ __align__(1024) double smem[];
+    double* sU = smem + L::U_OFF;
+    double* sQ = smem + L::Q_OFF;
+    double* sF = smem + L::F_OFF;
+    double* sG = smem + L::G_OFF;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + L::END);
+    if (c->done) return;
+
+    const BlockDev& B = m->b[b];
+    const int p = (int)(c->step & 1);
+    const int tiles_x = (B.nx + TX - 1) / TX;
+    const int x0 = (blockIdx.x % tiles_x) * TX, y0 = (blockIdx.x / tiles_x) * TY;
+    const double g = c->gamma, g1 = c->g1;
+    const double dt = c->dt;
+    const double one_dx = 1.0 / c->dx[b], one_dy = 1.0 / c->dy[b];   // godunov.cpp:97-98
+
+    if (!load_tile<L::TMA_BYTES>(sU, bar, p ? &tm1 : &tm0, x0, y0, c)) return;
+
+#define Q(k, cell) sQ[(k) * L::NC + (cell)]
+    for (int cell = threadIdx.x; cell < L::NC; cell += NT) {
+        Prim w = to_prim(g1, sU[cell], sU[L::NC + cell], sU[2 * L::NC + cell], sU[3 * L::NC + cell]);
+        double fx[4], fy[4];
+        flux<0>(w, fx);
+        flux<1>(w, fy);
+        Q(0, cell) = w.u; Q(1, cell) = w.v; Q(2, cell) = w.p; Q(3, cell) = w.Et;
+        Q(4, cell) = sound(g, w.r, w.p);
+        Q(5, cell) = fx[0]; Q(6, cell) = fx[1]; Q(7, cell) = fx[2]; Q(8, cell) = fx[3];
+        Q(9, cell) = fy[0]; Q(10, cell) = fy[2]; Q(11, cell) = fy[3];
+    }
+    __syncthreads();
+    int herr = 0;
+    auto load = [&](int cell, double* U, Prim& w, double& a, double* fx, double* fy) {
+#pragma unroll
+        for (int v = 0; v < 4; ++v) U[v] = sU[v * L::NC + cell];
+        w.r = U[0]; w.u = Q(0, cell); w.v = Q(1, cell); w.p = Q(2, cell); w.Et = Q(3, cell); w.q = 0.0;
+        a = Q(4, cell);
+        if (fx) { fx[0] = Q(5, cell); fx[1] = Q(6, cell); fx[2] = Q(7, cell); fx[3] = Q(8, cell); }
+        if (fy) { fy[0] = Q(9, cell); fy[1] = Q(7, cell); fy[2] = Q(10, cell); fy[3] = Q(11, cell); }
+    };
+    // x faces: face f of row r sits between tile cells (f-1, r) and (f, r)
+    for (int it = threadIdx.x; it < (TX + 1) * TY; it += NT) {
+        const int fx = it % (TX + 1), fy = it / (TX + 1);
+        const int cl = (fy + 1) * L::UX + fx, cr = cl + 1;
+        double UL[4], UR[4], FL[4], FR[4], F[4], aL, aR;
+        Prim wL, wR;
+        load(cl, UL, wL, aL, FL, nullptr);
+        load(cr, UR, wR, aR, FR, nullptr);
+        const int bad = hllc<0>(UL, wL, aL, FL, UR, wR, aR, FR, F);
+        herr += bad && owned_face(x0 + fx, fx, TX, B.nx, y0 + fy, B.ny);
+#pragma unroll
+        for (int v = 0; v < 4; ++v) sF[(v * TY + fy) * (TX + 1) + fx] = F[v];
+    }
+    for (int it = threadIdx.x; it < TX * (TY + 1); it += NT) {
+        const int gx = it % TX, gy = it / TX;
+        const int cb = gy * L::UX + gx + 1, ct = cb + L::UX;
+        double UB[4], UT[4], FB[4], FT[4], F[4], aB, aT;
+        Prim wB, wT;
+        load(cb, UB, wB, aB, nullptr, FB);
+        load(ct, UT, wT, aT, nullptr, FT);
+        const int bad = hllc<1>(UB, wB, aB, FB, UT, wT, aT, FT, F);
+        herr += bad && owned_face(y0 + gy, gy, TY, B.ny, x0 + gx, B.nx);
+#pragma unroll
+        for (int v = 0; v < 4; ++v) sG[(v * (TY + 1) + gy) * TX + gx] = F[v];
+    }
+#undef Q
+    __syncthreads();
+    double* __restrict__ out = B.buf[p ^ 1];
+    const size_t plane = (size_t)B.ty * B.pitch;
+    double mx = 0.0, my = 0.0;
+    for (int it = threadIdx.x; it < TX * TY; it += NT) {
+        const int ox = it % TX, oy = it / TX;
+        const int gxx = x0 + ox, gyy = y0 + oy;
+        if (gxx < B.nx && gyy < B.ny) {
+            double un[4];
+            const size_t o = (size_t)(gyy + 1) * B.pitch + (gxx + 1);
+#pragma unroll
+            for (int v = 0; v < 4; ++v) {
+                const double Lv = (one_dx * (sF[(v * TY + oy) * (TX + 1) + ox] -
+                                             sF[(v * TY + oy) * (TX + 1) + ox + 1])) +
+                                  (one_dy * (sG[(v * (TY + 1) + oy) * TX + ox] -
+                                             sG[(v * (TY + 1) + oy + 1) * TX + ox]));
+                un[v] = dt * Lv + sU[v * L::NC + (oy + 1) * L::UX + ox + 1];
+                out[v * plane + o] = un[v];
+            }
+            double sx, sy;
+            wave_terms(g, g1, un[0], un[1], un[2], un[3], sx, sy);
+            mx = nmax(mx, sx);
+            my = nmax(my, sy);
+        }
+    }
+    block_max2_atomic<NT>(mx, my, &c->int_s[p ^ 1][b][0], &c->int_s[p ^ 1][b][1]);
+    if (herr) atomicAdd(reinterpret_cast<unsigned long long*>(&c->hllc_errors), (unsigned long long)herr);
+}
+
+// ------------------------------------------------------------------------------------
+// launchers
+// ------------------------------------------------------------------------------------
+constexpr int kMhTX = 32, kMhTY = 16, kMhNT = 256;
+constexpr int kGoTX = 32, kGoTY = 16, kGoNT = 256;
+
+StencilTiles stencil_tiles(int scheme) {
+    return scheme == 0 ? StencilTiles{kGoTX, kGoTY} : StencilTiles{kMhTX, kMhTY};
+}
+
+cudaError_t stencil_prepare() {
+    cudaError_t e;
+    e = cudaFuncSetAttribute(mh_kernel<kMhTX, kMhTY, 0, kMhNT>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)MhLayout<kMhTX, kMhTY>::BYTES);
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(mh_kernel<kMhTX, kMhTY, 1, kMhNT>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)MhLayout<kMhTX, kMhTY>::BYTES);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(godunov_kernel<kGoTX, kGoTY, kGoNT>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)GoLayout<kGoTX, kGoTY>::BYTES);
+}
+
+cudaError_t launch_bc_fill(Ctrl* c, const MeshDev* m, cudaStream_t s) {
+    bc_fill_kernel<<<1, 1024, 0, s>>>(c, m);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_ghost_cfl(Ctrl* c, const MeshDev* m, long long total_ghost, cudaStream_t s) {
+    long long want = (total_ghost + kRedThreads - 1) / kRedThreads;
+    int grid = (int)(want < 1 ? 1 : (want > 4 * 152 ? 4 * 152 : want));
+    ghost_cfl_kernel<<<grid, kRedThreads, 0, s>>>(c, m);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_interior_cfl(Ctrl* c, const MeshDev* m, int b, int nx, int ny, int parity,
+                                cudaStream_t s) {
+    long long want = ((long long)nx * ny + kRedThreads - 1) / kRedThreads;
+    int grid = (int)(want < 1 ? 1 : (want > 8 * 152 ? 8 * 152 : want));
+    interior_cfl_kernel<<<grid, kRedThreads, 0, s>>>(c, m, b, parity);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_set_dt(Ctrl* c, double dt, cudaStream_t s) {
+    set_dt_kernel<<<1, 1, 0, s>>>(c, dt);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_finalize(Ctrl* c, cudaStream_t s) {
+    finalize_kernel<<<1, 1, 0, s>>>(c);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_stencil(Ctrl* c, const MeshDev* m, int b, int nx, int ny, int scheme, int limiter,
+                           const CUtensorMap* tm0, const CUtensorMap* tm1, cudaStream_t s) {
+    if (scheme == 0) {
+        int tiles = ((nx + kGoTX - 1) / kGoTX) * ((ny + kGoTY - 1) / kGoTY);
+        godunov_kernel<kGoTX, kGoTY, kGoNT>
+            <<<tiles, kGoNT, GoLayout<kGoTX, kGoTY>::BYTES, s>>>(c, m, b, *tm0, *tm1);
+    } else {
+        int tiles = ((nx + kMhTX - 1) / kMhTX) * ((ny + kMhTY - 1) / kMhTY);
+        if (limiter == 0)
+            mh_kernel<kMhTX, kMhTY, 0, kMhNT>
+                <<<tiles, kMhNT, MhLayout<kMhTX, kMhTY>::BYTES, s>>>(c, m, b, *tm0, *tm1);
+        else
+            mh_kernel<kMhTX, kMhTY, 1, kMhNT>
+                <<<tiles, kMhNT, MhLayout<kMhTX, kMhTY>::BYTES, s>>>(c, m, b, *tm0, *tm1);
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace hf

@@ -1,0 +1,51 @@
+// Internal interface between the C-ABI layer (hf_api.cpp) and the Cartesian kernels
+// (hf_cart.cu).  Not part of the public ABI.
+#pragma once
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include "hf_ctrl.h"
+
+namespace hf {
+
+enum { BC_TRANSMISSIVE = 0, BC_REFLECTIVE = 1, BC_DIRICHLET = 2, BC_INTERNAL = 3 };
+enum { SIDE_BOTTOM = 0, SIDE_RIGHT = 1, SIDE_TOP = 2, SIDE_LEFT = 3 };
+
+// One mesh block on the device: SoA FP64 [var][total_y][pitch], x contiguous, rows
+// padded to `pitch` doubles (a multiple of 32 = 256 bytes), two buffers that
+// alternate each step (the stencil reads one and writes the other).
+struct BlockDev {
+    int tx, ty, nx, ny, pitch;
+    double* buf[2];
+    int bc_type[4];
+    int bc_block[4];
+    double bc_state[4][4];
+    long long ghost_off;   // first index of this block in the all-blocks ghost-cell enumeration
+    int ghost_count;
+};
+
+struct MeshDev {
+    int nblocks, ghost;
+    long long total_ghost;
+    BlockDev b[HF_MAXB];
+};
+
+struct StencilTiles {
+    int tx, ty;   // output cells per CTA tile
+};
+
+// launchers (all asynchronous on `s`)
+cudaError_t launch_bc_fill(Ctrl* c, const MeshDev* m, cudaStream_t s);
+cudaError_t launch_ghost_cfl(Ctrl* c, const MeshDev* m, long long total_ghost, cudaStream_t s);
+cudaError_t launch_interior_cfl(Ctrl* c, const MeshDev* m, int b, int nx, int ny, int parity,
+                                cudaStream_t s);
+cudaError_t launch_set_dt(Ctrl* c, double dt, cudaStream_t s);
+cudaError_t launch_finalize(Ctrl* c, cudaStream_t s);
+cudaError_t launch_stencil(Ctrl* c, const MeshDev* m, int b, int nx, int ny, int scheme, int limiter,
+                           const CUtensorMap* tm0, const CUtensorMap* tm1, cudaStream_t s);
+// halo-tile box of the stencil for the scheme (TMA box = tile + 2*ghost per axis)
+StencilTiles stencil_tiles(int scheme);
+cudaError_t stencil_prepare();   // sets the large dynamic shared-memory opt-ins once
+
+}  // namespace hf

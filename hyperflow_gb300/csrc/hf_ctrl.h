@@ -1,0 +1,36 @@
+// The per-context control block shared by host and device code (plain data only).
+#pragma once
+
+#define HF_MAXB 16
+
+namespace hf {
+
+// the per-context control block, resident in device memory
+struct Ctrl {
+    // static (set once at context creation)
+    int nblocks, scheme, limiter, ghost;
+    double gamma, g1, cfl;                 // g1 = gamma - 1.0, as the reference recomputes it
+    double dx[HF_MAXB], dy[HF_MAXB];
+    // dynamic
+    double t, t_end;
+    double dt;                              // dt applied by the current step
+    double dt_cfl;                          // last step-call CFL dt before clamping
+    double dt_pred[HF_MAXB];                // MUSCL-Hancock predictor dt per block, last step
+    long long calls;                        // TimeStep calls made so far
+    long long step;                         // steps completed; parity selects the state buffer
+    int clamp;                              // device loop clamps dt to t_end and stops there
+    int done;                               // t == t_end reached (device loop)
+    unsigned long long ghost_s[HF_MAXB][2]; // max |u|+c, |v|+c over ghost cells (bit patterns)
+    unsigned long long int_s[2][HF_MAXB][2];// [parity][block] same over interior cells
+    unsigned int ticket;
+    int err;                                // first error code raised on the device
+    long long hllc_errors;                  // HLLC "should not get here" zero fluxes
+};
+
+enum : int {
+    HF_DEV_OK = 0,
+    HF_DEV_TIMEOUT = 1,   // a bounded wait gave up
+    HF_DEV_BOUNDS = 2,    // a checked index fell outside its buffer
+};
+
+}  // namespace hf

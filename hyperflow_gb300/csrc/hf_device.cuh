@@ -1,0 +1,305 @@
+// Device-side building blocks shared by every HyperFlow-GB300 kernel.
+//
+// Arithmetic parity: all kernels are compiled with --fmad=false, so a*b+c stays a
+// rounded multiply followed by a rounded add, exactly as the reference's C++ (ISO
+// mode, no contraction) evaluates it.  FP64 division and sqrt are IEEE correctly
+// rounded on the GPU, as they are in libm.  Every expression below keeps the
+// reference's operand order; identical sub-expressions the reference evaluates more
+// than once (cons_to_prim inside cons_flux_x, prim_total_energy inside calc_U_k, ...)
+// are evaluated once and reused, which changes no result because they are
+// deterministic functions of the same inputs.
+#pragma once
+
+#include <cstdint>
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include "hf_ctrl.h"
+
+namespace hf {
+
+__device__ __forceinline__ void raise_error(Ctrl* c, int code) { atomicCAS(&c->err, 0, code); }
+
+// ------------------------------------------------------------------------------
+// std::min / std::max exactly (NaN-order semantics of the C++ library)
+// ------------------------------------------------------------------------------
+__device__ __forceinline__ double smin(double a, double b) { return (b < a) ? b : a; }
+__device__ __forceinline__ double smax(double a, double b) { return (a < b) ? b : a; }
+__device__ __forceinline__ double sgn(double v) { return (double)((v > 0.0) - (v < 0.0)); }
+
+// ------------------------------------------------------------------------------
+// ideal-gas model, src/fvm_2d_cart/model/euler_ideal_gas/euler_ideal_gas.cpp
+// ------------------------------------------------------------------------------
+struct Prim {
+    double r, u, v, p;   // cons_to_prim (76-92)
+    double q;            // u*u + v*v, shared by cons_to_prim and prim_total_energy
+    double Et;           // prim_total_energy (40-46), recomputed from the primitives
+};
+
+__device__ __forceinline__ Prim to_prim(double g1, double r, double ru, double rv, double E) {
+    Prim w;
+    w.r = r;
+    w.u = ru / r;
+    w.v = rv / r;
+    w.q = w.u * w.u + w.v * w.v;
+    w.p = g1 * (E - 0.5 * r * w.q);
+    double e = w.p / (w.r * g1);           // prim_internal_energy (32-36)
+    w.Et = w.r * (0.5 * w.q + e);
+    return w;
+}
+
+// only the primitives (no energy): what TimeStep needs
+__device__ __forceinline__ void to_prim_short(double g1, double r, double ru, double rv, double E,
+                                              double& u, double& v, double& p) {
+    u = ru / r;
+    v = rv / r;
+    p = g1 * (E - 0.5 * r * (u * u + v * v));
+}
+
+// prim_speed_of_sound (60-64)
+__device__ __forceinline__ double sound(double g, double r, double p) { return sqrt(g * p / r); }
+
+// cons_flux_x / cons_flux_y (113-149): rho*u*u == (rho*u)*u etc.
+template <int DIR>
+__device__ __forceinline__ void flux(const Prim& w, double* f) {
+    if (DIR == 0) {
+        double ru = w.r * w.u;
+        f[0] = ru;
+        f[1] = ru * w.u + w.p;
+        f[2] = ru * w.v;
+        f[3] = w.u * (w.Et + w.p);
+    } else {
+        f[0] = w.r * w.v;
+        f[1] = w.r * w.u * w.v;
+        f[2] = f[0] * w.v + w.p;
+        f[3] = w.v * (w.Et + w.p);
+    }
+}
+
+// ------------------------------------------------------------------------------
+// HLLC, src/fvm_2d_cart/scheme/riemann/riemann_hllc/riemann_hllc.cpp:169-212
+// U*: calc_U_k (37-63); S*: calc_S_star (67-97); F*: calc_F_star (153-164).
+// Only the flux the branch returns is formed; the others would be discarded.
+// Returns 1 when the "should not get here" branch yields the zero flux.
+// ------------------------------------------------------------------------------
+template <int DIR>
+__device__ __forceinline__ void star_flux(const double* UK, const Prim& wK, double SK, double Ss,
+                                          const double* FK, double* F) {
+    double velK = DIR == 0 ? wK.u : wK.v;
+    double coef = wK.r * ((SK - velK) / (SK - Ss));
+    double us[4];
+    us[0] = coef;
+    if (DIR == 0) {
+        us[1] = coef * Ss;
+        us[2] = coef * wK.v;
+    } else {
+        us[1] = coef * wK.u;
+        us[2] = coef * Ss;
+    }
+    us[3] = coef * (wK.Et / wK.r + (Ss - velK) * (Ss + (wK.p / (wK.r * (SK - velK)))));
+#pragma unroll
+    for (int i = 0; i < 4; ++i) F[i] = FK[i] + SK * (us[i] - UK[i]);
+}
+
+template <int DIR>
+__device__ __forceinline__ int hllc(const double* UL, const Prim& wL, double aL, const double* FL,
+                                    const double* UR, const Prim& wR, double aR, const double* FR,
+                                    double* F) {
+    double velL = DIR == 0 ? wL.u : wL.v;
+    double velR = DIR == 0 ? wR.u : wR.v;
+    double SL = smin(velL - aL, velR - aR);
+    double SR = smax(velL + aL, velR + aR);
+    if (0.0 <= SL) {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) F[i] = FL[i];
+        return 0;
+    }
+    double num = wR.p - wL.p + wL.r * velL * (SL - velL) - wR.r * velR * (SR - velR);
+    double den = wL.r * (SL - velL) - wR.r * (SR - velR);
+    double Ss = num / den;
+    if (SL <= 0.0 && 0.0 <= Ss) {
+        star_flux<DIR>(UL, wL, SL, Ss, FL, F);
+        return 0;
+    }
+    if (Ss <= 0.0 && 0.0 <= SR) {
+        star_flux<DIR>(UR, wR, SR, Ss, FR, F);
+        return 0;
+    }
+    if (0.0 >= SR) {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) F[i] = FR[i];
+        return 0;
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) F[i] = 0.0;
+    return 1;
+}
+
+// HLLC from two conservative states (computes primitives, sound speeds, fluxes)
+template <int DIR>
+__device__ __forceinline__ int hllc_cons(double g, double g1, const double* UL, const double* UR,
+                                         double* F) {
+    Prim wL = to_prim(g1, UL[0], UL[1], UL[2], UL[3]);
+    Prim wR = to_prim(g1, UR[0], UR[1], UR[2], UR[3]);
+    // calc_wave_speeds_direct_min_max (127-150): sqrt(gamma * p / rho)
+    double aL = sound(g, wL.r, wL.p);
+    double aR = sound(g, wR.r, wR.p);
+    double FL[4], FR[4];
+    flux<DIR>(wL, FL);
+    flux<DIR>(wR, FR);
+    return hllc<DIR>(UL, wL, aL, FL, UR, wR, aR, FR, F);
+}
+
+// ------------------------------------------------------------------------------
+// slope limiters, src/fvm_2d_cart/scheme/limiter (omega 0, beta 1, tol 1e-6 from
+// parser.cpp:230-233) and the limited slope of muscl_hancock.cpp:67-206
+// ------------------------------------------------------------------------------
+constexpr double kTol = 1e-6;
+
+__device__ __forceinline__ double xi_right(double r) {
+    // Limiter::xi_right + denom_tol (limiter.cpp:26-53): 2*beta / (1 - omega + (1 + omega) r)
+    double den = 1.0 + r;   // (1.0 - 0.0) + (1.0 + 0.0) * r rounds to the same value
+    if (fabs(den) < kTol) den = (den == 0.0) ? kTol : kTol * sgn(den);
+    return 2.0 / den;
+}
+
+template <int LIM>
+__device__ __forceinline__ double limiter(double r) {
+    if (LIM == 0) {   // MinBeeLimiter::operator() minbee.cpp:29-38
+        if (r <= 0.0) return 0.0;
+        if ((0.0 < r) && (r <= 1.0)) return r;
+        return smin(1.0, xi_right(r));
+    } else {          // VanLeerLimiter::operator() vanleer.cpp:29-36
+        if (r <= 0.0) return 0.0;
+        return smin((2.0 * r) / (1.0 + r), xi_right(r));
+    }
+}
+
+// limited slope of one variable from the three cell averages (um, u0, up)
+template <int LIM>
+__device__ __forceinline__ double slope(double um, double u0, double up) {
+    double dl = u0 - um, dr = up - u0;
+    double dlc = dl, drc = dr;
+    if (fabs(dlc) <= kTol) dlc = (dlc == 0.0) ? kTol : kTol * sgn(dlc);
+    if (fabs(drc) <= kTol) drc = (drc == 0.0) ? kTol : kTol * sgn(drc);
+    double xi = limiter<LIM>(dlc / drc);
+    return xi * (0.5 * dl + 0.5 * dr);
+}
+
+// ------------------------------------------------------------------------------
+// TimeStep pieces (timestep.cpp:29-68)
+// ------------------------------------------------------------------------------
+// Per-cell wave-speed terms s_x = |u| + c and s_y = |v| + c.  The reference folds
+// dx / s over cells with std::min; fl(dx / s) is non-increasing in s, so that fold
+// equals fl(dx / max s) -- a max over s, which is exact in any order.  NaN terms are
+// skipped in both.
+__device__ __forceinline__ void wave_terms(double g, double g1, double r, double ru, double rv,
+                                           double E, double& sx, double& sy) {
+    double u, v, p;
+    to_prim_short(g1, r, ru, rv, E, u, v, p);
+    double c = sound(g, r, p);
+    sx = fabs(u) + c;
+    sy = fabs(v) + c;
+}
+
+// NaN-skipping max of non-negative values
+__device__ __forceinline__ double nmax(double m, double s) { return (s > m) ? s : m; }
+
+__device__ __forceinline__ unsigned long long dbits(double x) {
+    return (unsigned long long)__double_as_longlong(x);
+}
+__device__ __forceinline__ double bitsd(unsigned long long x) {
+    return __longlong_as_double((long long)x);
+}
+
+// dt of TimeStep call number `call` (0-based) over all blocks; blocks < new_upto take
+// their interior maximum from parity `pn` (already advanced this step), the others
+// from parity `po`.
+__device__ __forceinline__ double cfl_dt(const Ctrl* c, long long call, int new_upto, int po, int pn) {
+    double dtx = 1e16, dty = 1e16;
+    for (int b = 0; b < c->nblocks; ++b) {
+        int pp = b < new_upto ? pn : po;
+        double mx = smax(bitsd(c->ghost_s[b][0]), bitsd(c->int_s[pp][b][0]));
+        double my = smax(bitsd(c->ghost_s[b][1]), bitsd(c->int_s[pp][b][1]));
+        dtx = smin(dtx, c->dx[b] / mx);
+        dty = smin(dty, c->dy[b] / my);
+    }
+    double final_cfl = (call + 1 <= 10) ? 0.2 * c->cfl : c->cfl;
+    return final_cfl * smin(dtx, dty);
+}
+
+// block-wide max of two values, one atomicMax per CTA
+template <int NT>
+__device__ __forceinline__ void block_max2_atomic(double sx, double sy, unsigned long long* ax,
+                                                  unsigned long long* ay) {
+    __shared__ double red[2][NT / 32];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        sx = nmax(sx, __shfl_xor_sync(0xffffffffu, sx, o));
+        sy = nmax(sy, __shfl_xor_sync(0xffffffffu, sy, o));
+    }
+    int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (l == 0) { red[0][w] = sx; red[1][w] = sy; }
+    __syncthreads();
+    if (w == 0) {
+        sx = l < NT / 32 ? red[0][l] : 0.0;
+        sy = l < NT / 32 ? red[1][l] : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            sx = nmax(sx, __shfl_xor_sync(0xffffffffu, sx, o));
+            sy = nmax(sy, __shfl_xor_sync(0xffffffffu, sy, o));
+        }
+        if (l == 0) {
+            if (sx > 0.0) atomicMax(ax, dbits(sx));
+            if (sy > 0.0) atomicMax(ay, dbits(sy));
+        }
+    }
+}
+
+// ------------------------------------------------------------------------------
+// TMA + mbarrier (inline PTX, sm_90+ forms valid on sm_103a)
+// ------------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// bounded wait: gives up after `limit` polls (each poll itself suspends for a
+// hardware-chosen interval) and reports failure instead of hanging the GPU
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, uint32_t limit) {
+    for (uint32_t i = 0; i < limit; ++i)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, uint64_t* bar, int x,
+                                            int y, int z) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+        : "memory");
+}
+
+}  // namespace hf

@@ -1,0 +1,148 @@
+"""Python host mirror of the reference's Cartesian solver interface.
+
+``CartSolver`` exposes the reference's step pieces under their own names
+(src/fvm_2d_cart): ``apply_bcs`` (Mesh::apply_bcs, mesh.cpp:31-39),
+``calculate_time_step`` (Scheme::calculate_time_step -> TimeStep::operator(),
+timestep.cpp:29-68), ``advance_block`` / ``advance`` (ODESolver(Scheme(block)) +
+set_fields, simulation.cpp:106-110), and ``solve``-style loops (simulation.cpp:51-124)
+-- all executed by the CUDA kernels behind the C ABI of include/hyperflow_gb300.h.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import json
+
+import numpy as np
+
+from ._lib import LAYOUT_AOS_XY, LAYOUT_SOA, check, lib
+
+
+class CartSolver:
+    """One case file -> one device-resident simulation (FP64 SoA state in HBM)."""
+
+    def __init__(self, case):
+        text = case if isinstance(case, str) else json.dumps(case)
+        raw = text.encode()
+        L = lib()
+        h = C.c_void_p()
+        st = L.hf_create(raw, len(raw), C.byref(h))
+        self._h = h
+        if st != 0:
+            try:
+                check(st, h)
+            finally:
+                if h:
+                    L.hf_destroy(h)
+                self._h = None
+        n = C.c_int()
+        check(L.hf_num_blocks(self._h, C.byref(n)), self._h)
+        self.nblocks = n.value
+
+    # --- lifecycle ---
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().hf_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # --- geometry ---
+    def block_dims(self, b: int = 0) -> dict:
+        d = (C.c_int * 5)()
+        check(lib().hf_block_dims(self._h, b, d), self._h)
+        return {"total_x": d[0], "total_y": d[1], "ghost": d[2], "x_cells": d[3], "y_cells": d[4]}
+
+    def interior_cells(self) -> int:
+        return sum(self.block_dims(b)["x_cells"] * self.block_dims(b)["y_cells"]
+                   for b in range(self.nblocks))
+
+    # --- state ---
+    def state(self, b: int = 0, layout: str = "soa", out: np.ndarray | None = None) -> np.ndarray:
+        """SoA [var][y][x] (default) or MeshBlock order [x][y][var], ghosts included.
+        ``out`` (SoA, C-contiguous float64, e.g. pinned memory) receives the copy."""
+        d = self.block_dims(b)
+        if layout == "soa":
+            if out is None:
+                out = np.empty((4, d["total_y"], d["total_x"]))
+            assert out.shape == (4, d["total_y"], d["total_x"]) and out.flags.c_contiguous
+            check(lib().hf_get_state(self._h, b, out.ctypes.data, LAYOUT_SOA), self._h)
+        else:
+            out = np.empty((d["total_x"], d["total_y"], 4))
+            check(lib().hf_get_state(self._h, b, out.ctypes.data, LAYOUT_AOS_XY), self._h)
+        return out
+
+    def set_state(self, b: int, U: np.ndarray, layout: str = "soa"):
+        U = np.ascontiguousarray(U, dtype=np.float64)
+        lay = LAYOUT_SOA if layout == "soa" else LAYOUT_AOS_XY
+        check(lib().hf_set_state(self._h, b, U.ctypes.data, lay), self._h)
+
+    # --- the reference's step pieces ---
+    def apply_bcs(self):
+        check(lib().hf_apply_bcs(self._h), self._h)
+
+    def calculate_time_step(self) -> float:
+        dt = C.c_double()
+        check(lib().hf_time_step(self._h, C.byref(dt)), self._h)
+        return dt.value
+
+    def advance_block(self, b: int, dt: float):
+        check(lib().hf_advance_block(self._h, b, dt), self._h)
+
+    def advance(self, dt: float):
+        check(lib().hf_advance(self._h, dt), self._h)
+
+    def step(self) -> float:
+        dt = C.c_double()
+        check(lib().hf_step(self._h, C.byref(dt)), self._h)
+        return dt.value
+
+    def run(self, n: int, clamp_t_end: bool = False, graph: bool = True) -> int:
+        done = C.c_int64()
+        check(lib().hf_run(self._h, n, int(clamp_t_end), int(graph), C.byref(done)), self._h)
+        return done.value
+
+    def solve(self) -> int:
+        """Runs to t_end like Simulation::solve (without frame output); returns steps taken."""
+        total = 0
+        while True:
+            k = self.run(1000, clamp_t_end=True)
+            total += k
+            if k < 1000:
+                return total
+
+    def sync(self):
+        check(lib().hf_sync(self._h), self._h)
+
+    # --- introspection ---
+    def time(self):
+        t, c, d = C.c_double(), C.c_int64(), C.c_double()
+        check(lib().hf_get_time(self._h, C.byref(t), C.byref(c), C.byref(d)), self._h)
+        return t.value, c.value, d.value
+
+    def hllc_errors(self) -> int:
+        n = C.c_int64()
+        check(lib().hf_hllc_errors(self._h, C.byref(n)), self._h)
+        return n.value
+
+    def stream(self) -> int:
+        s = C.c_void_p()
+        check(lib().hf_stream(self._h, C.byref(s)), self._h)
+        return s.value or 0
+
+    def profile(self, enable: bool = True):
+        check(lib().hf_profile(self._h, int(enable)), self._h)
+
+    def kernel_time(self, kind: int = 0):
+        ms, n = C.c_double(), C.c_int64()
+        check(lib().hf_kernel_time(self._h, kind, C.byref(ms), C.byref(n)), self._h)
+        return ms.value, n.value

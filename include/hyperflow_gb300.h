@@ -1,0 +1,111 @@
+/* HyperFlow-GB300 -- C ABI of the GPU time step.
+ *
+ * This is the drop-in boundary for the reference solver's per-step update
+ * (qcrm/HyperFlow).  The reference's step is the triple
+ *     Mesh::apply_bcs()                     src/fvm_2d_cart/mesh/mesh/mesh.cpp:31-39
+ *     Scheme::calculate_time_step(mesh)     src/fvm_2d_cart/scheme/scheme/scheme.h:23
+ *     ODESolver::operator()(Scheme(block))  src/fvm_2d_cart/scheme/ode/ode/ode.h:22-24
+ * driven block by block by Simulation::solve (simulation.cpp:85-120).  Each entry point
+ * below replaces one of those calls (cited beside it) with device work on FP64 state
+ * resident in HBM; results match the reference bit for bit.
+ *
+ * Conventions: every call returns an HF_* status (never throws).  The caller owns host
+ * buffers; the context owns device memory and one CUDA stream.  A context is not
+ * thread-safe; distinct contexts are independent.
+ */
+#ifndef HYPERFLOW_GB300_H
+#define HYPERFLOW_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct hf_ctx hf_ctx;
+
+enum {
+    HF_OK = 0,
+    HF_ERR_ARG = 1,          /* bad argument (null pointer, index out of range, bad layout) */
+    HF_ERR_PARSE = 2,        /* case file is not valid JSON or misses a key the reference reads */
+    HF_ERR_UNSUPPORTED = 3,  /* a model/scheme/boundary the reference does not provide */
+    HF_ERR_CUDA = 4,         /* a CUDA runtime call failed (see hf_last_error_message) */
+    HF_ERR_DEVICE = 5,       /* a kernel raised its error word (bounded wait timed out, ...) */
+    HF_ERR_STATE = 6,        /* call out of order (e.g. advancing block 2 before block 1) */
+    HF_ERR_NO_DEVICE = 7     /* no CUDA device is visible */
+};
+
+/* state layouts for hf_set_state / hf_get_state */
+enum {
+    HF_LAYOUT_SOA = 0,       /* [var][y][x], x fastest, ghosts included (the device layout) */
+    HF_LAYOUT_AOS_XY = 1     /* [x][y][var], ghosts included: MeshBlock::fields order,
+                                src/fvm_2d_cart/mesh/mesh_block/mesh_block.cpp:35 */
+};
+
+/* Parses a case file (the JSON read by src/fvm_2d_cart/simulation/parser/parser.cpp:13-488,
+ * same keys and meaning), allocates device state, and initialises the interior from the
+ * initial condition exactly as Simulation::Simulation does (simulation.cpp:43).
+ * Replaces: JSONParser + generate_* + Simulation construction (src/fvm_2d_cart/main.cpp:33-86). */
+int hf_create(const char* case_json, size_t len, hf_ctx** out);
+void hf_destroy(hf_ctx* ctx);
+
+/* number of mesh blocks; dims = {total_x, total_y, ghost, x_cells, y_cells} of block b
+ * (MeshBlock::get_total_x_cells etc., mesh_block.cpp:70-97) */
+int hf_num_blocks(const hf_ctx* ctx, int* nblocks);
+int hf_block_dims(const hf_ctx* ctx, int block, int dims[5]);
+
+/* copy a block's conservative state (ghosts included) in / out.
+ * Replaces MeshBlock::set_fields / get_fields (mesh_block.cpp:155-164). */
+int hf_set_state(hf_ctx* ctx, int block, const double* cons, int layout);
+int hf_get_state(hf_ctx* ctx, int block, double* cons, int layout);
+
+/* Mesh::apply_bcs (mesh.cpp:31-39): ghost fill, blocks in order, bottom/right/top/left */
+int hf_apply_bcs(hf_ctx* ctx);
+
+/* TimeStep::operator() (src/fvm_2d_cart/scheme/timestep/timestep.cpp:29-68) as called by
+ * Scheme::calculate_time_step: CFL dt over all cells incl. ghosts; advances the call counter */
+int hf_time_step(hf_ctx* ctx, double* dt);
+
+/* ODESolver(Scheme(block b)) + set_fields for one block (simulation.cpp:106-110, fused
+ * forward Euler of forward_euler.cpp:15-33).  Blocks must be advanced in order 0..B-1 within
+ * a step; MUSCL-Hancock's predictor TimeStep call (muscl_hancock.cpp:246) happens on the
+ * device against the partly advanced mesh, as in the reference. */
+int hf_advance_block(hf_ctx* ctx, int block, double dt);
+/* all blocks in order with the same dt, then t += dt */
+int hf_advance(hf_ctx* ctx, double dt);
+
+/* one whole step with no clamps: apply_bcs, dt, advance; dt written if non-null */
+int hf_step(hf_ctx* ctx, double* dt);
+
+/* Simulation::solve's loop body (simulation.cpp:81-120, frame clamps excluded) run n times
+ * on the device with no host round trip per step: dt stays on the device.  clamp_t_end != 0
+ * applies the t_end clamp and stops at t_end like the reference.  use_graph != 0 replays a
+ * captured CUDA graph of one step.  steps_done (optional) = steps actually taken. */
+int hf_run(hf_ctx* ctx, int64_t n, int clamp_t_end, int use_graph, int64_t* steps_done);
+
+/* simulation time, TimeStep call count, and the dt applied by the last step */
+int hf_get_time(hf_ctx* ctx, double* t, int64_t* calls, double* last_dt);
+
+/* number of HLLC zero-flux fallbacks (riemann_hllc.cpp:207-211) seen so far */
+int hf_hllc_errors(hf_ctx* ctx, int64_t* count);
+
+/* waits for the context's stream; returns HF_ERR_DEVICE if a kernel raised its error word */
+int hf_sync(hf_ctx* ctx);
+
+/* the context's CUDA stream (a cudaStream_t), for callers that time or order work on it */
+int hf_stream(hf_ctx* ctx, void** stream);
+
+/* per-kernel timing: when enabled, every stencil launch is bracketed by CUDA events on the
+ * context's stream; hf_kernel_time returns the summed milliseconds and launch count since
+ * the last reset.  kind 0 = stencil (Godunov/MUSCL-Hancock), 1 = ghost fill + CFL. */
+int hf_profile(hf_ctx* ctx, int enable);
+int hf_kernel_time(hf_ctx* ctx, int kind, double* ms, int64_t* launches);
+
+const char* hf_status_string(int status);
+const char* hf_last_error_message(const hf_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,145 @@
+"""Generates the golden fixtures in this folder from the reference solver itself.
+
+Run where the reference tree exists (it builds oracle/_ref/ from the reference's own
+sources with ``make -C oracle ref``):
+
+    python tests/golden/make_golden.py
+
+Each fixture is an .npz holding the case JSON, the number of steps, the reference's
+step dt stream, every TimeStep call it made (step calls and MUSCL-Hancock predictor
+calls), and the final state of every block (SoA [var][y][x], ghosts included) -- or,
+for the full-size 256x256 Godunov workload, per-variable checksums and a seeded sample
+of cells instead of the whole state.  Unit fixtures hold HLLC fluxes and limiter values
+for random and edge-case inputs.
+"""
+from __future__ import annotations
+
+import json
+import math
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from hyperflow_gb300 import cases  # noqa: E402
+from oracle import oracle  # noqa: E402
+
+REF_CASES = "/root/reference/cases/fvm_2d_cart"
+
+# (ne, nw, sw, se) primitive states of two rarefactions moving apart at speed 2 / 3
+VACUUM2 = ([1.0, 2.0, 0.0, 0.4], [1.0, -2.0, 0.0, 0.4], [1.0, -2.0, 0.0, 0.4], [1.0, 2.0, 0.0, 0.4])
+VACUUM3 = ([1.0, 3.0, 0.0, 0.4], [1.0, -3.0, 0.0, 0.4], [1.0, -3.0, 0.0, 0.4], [1.0, 3.0, 0.0, 0.4])
+
+
+def cart_cases():
+    """(name, case, steps, clamp_t_end, full_state)"""
+    out = [
+        ("godunov_quad_48", cases.quadrant_case(48), 60, False, True),
+        ("godunov_quad_ragged_37x29", cases.quadrant_case(37, ny=29, split=(0.41, 0.63)), 50, False, True),
+        ("godunov_quad_reflective_40", cases.quadrant_case(40, bc="Reflective"), 60, False, True),
+        ("mh_minbee_quad_48", cases.quadrant_case(48, scheme="MUSCLHancock", limiter="MinBee"), 60, False, True),
+        ("mh_vanleer_quad_44x36", cases.quadrant_case(44, ny=36, scheme="MUSCLHancock", limiter="VanLeer"), 60, False, True),
+        ("mh_minbee_reflective_33x47", cases.quadrant_case(33, ny=47, scheme="MUSCLHancock", limiter="MinBee",
+                                                           bc="Reflective", split=(0.55, 0.35)), 50, False, True),
+        ("ffs_minbee_dx1_40", cases.forward_facing_step_case(40, limiter="MinBee"), 60, False, True),
+        ("ffs_vanleer_dx1_40", cases.forward_facing_step_case(40, limiter="VanLeer"), 60, False, True),
+        ("ffs_godunov_dx1_30", cases.forward_facing_step_case(30, scheme="Godunov"), 60, False, True),
+        # double rarefaction towards vacuum: the reference's HLLC "should not get here"
+        # zero-flux branch (riemann_hllc.cpp:207-211) fires hundreds of times per step
+        ("mh_minbee_vacuum_hllc_fallback", cases.quadrant_case(
+            32, ny=24, scheme="MUSCLHancock", limiter="MinBee", states=VACUUM2), 20, False, True),
+        ("mh_vanleer_vacuum_hllc_fallback", cases.quadrant_case(
+            30, ny=26, scheme="MUSCLHancock", limiter="VanLeer", states=VACUUM3), 20, False, True),
+        # the 256x256 Godunov workload at full length
+        ("godunov_quad_256_200", cases.quadrant_case(256), 200, False, False),
+    ]
+    for rel, steps in [("shock_tubes/toro/toro_shock_tube_01_godunov_hllc_100x5.json", 400),
+                       ("shock_tubes/toro/toro_shock_tube_01_muscl_hancock_vanleer_hllc_100x5.json", 400),
+                       ("sphericalrp/sphericalrp_godunov_hllc_50x50.json", 120),
+                       ("sphericalrp/sphericalrp_muscl_hancock_vanleer_hllc_50x50.json", 120)]:
+        with open(os.path.join(REF_CASES, rel)) as f:
+            case = json.load(f)
+        name = "refcase_" + os.path.splitext(os.path.basename(rel))[0]
+        out.append((name, case, steps, True, True))
+    return out
+
+
+def sample_idx(shape, n=2000, seed=7):
+    rng = np.random.default_rng(seed)
+    return np.stack([rng.integers(0, s, n) for s in shape[1:]], axis=0)
+
+
+def make_cart():
+    for name, case, steps, clamp, full in cart_cases():
+        ref = oracle.RefCart(case)
+        taken = ref.run(steps, clamp)
+        blocks = [ref.state(b) for b in range(ref.nblocks())]
+        data = {"case": json.dumps(case), "steps": taken, "clamp": int(clamp),
+                "step_dts": ref.step_dts(), "calls": ref.calls(), "t": ref.time(),
+                "nblocks": len(blocks)}
+        if full:
+            for b, U in enumerate(blocks):
+                data[f"U{b}"] = U
+        else:
+            U = blocks[0]
+            idx = sample_idx(U.shape)
+            data["sample_idx"] = idx
+            data["sample"] = U[:, idx[0], idx[1]]
+            data["sums"] = np.array([math.fsum(U[v].ravel()) for v in range(4)])
+            data["sumsq"] = np.array([math.fsum((U[v] * U[v]).ravel()) for v in range(4)])
+        np.savez_compressed(os.path.join(HERE, f"cart_{name}.npz"), **data)
+        print(name, taken, "steps")
+
+
+def unit_states(n=4000, seed=11):
+    """Random conservative states plus hand-picked edge cases (vacuum-like, supersonic,
+    zero velocity, equal states, NaN/inf)."""
+    rng = np.random.default_rng(seed)
+    rho = np.exp(rng.uniform(np.log(1e-3), np.log(10.0), n))
+    u = rng.uniform(-5, 5, n)
+    v = rng.uniform(-5, 5, n)
+    p = np.exp(rng.uniform(np.log(1e-4), np.log(100.0), n))
+    W = np.stack([rho, u, v, p], 1)
+    W[::17, 1] = 0.0
+    W[::23, 2] = 0.0
+    W[::29, 1] *= 40.0     # strongly supersonic
+    U = np.stack([oracle.prim_to_cons(w) for w in W])
+    return U
+
+
+def make_units():
+    lib = oracle.ref_cart_lib()
+    UL = unit_states(4000, 11)
+    UR = unit_states(4000, 12)
+    UR[::31] = UL[::31]                        # identical states
+    UL[5] = [np.nan, 0, 0, 1]                  # NaN density
+    UR[6] = [1.0, np.inf, 0.0, 1.0]            # infinite momentum
+    UL[7] = [1.0, 0.0, 0.0, -1.0]              # negative energy -> NaN sound speed
+    UL[8] = [0.0, 0.0, 0.0, 0.0]               # vacuum
+    F = np.zeros((2, len(UL), 4))
+    for d in range(2):
+        for k in range(len(UL)):
+            f = np.zeros(4)
+            a = np.ascontiguousarray(UL[k])
+            b = np.ascontiguousarray(UR[k])
+            lib.hfref_hllc(1.4, a.ctypes.data, b.ctypes.data, d, f.ctypes.data)
+            F[d, k] = f
+    rng = np.random.default_rng(3)
+    r = np.concatenate([rng.uniform(-3, 5, 3000), np.exp(rng.uniform(-20, 20, 500)),
+                        [0.0, -0.0, 1.0, 1.0 + 2**-52, 1.0 - 2**-53, -1.0, -1.0 + 1e-7,
+                         -1.0 - 1e-7, -0.9999999, np.inf, -np.inf, np.nan, 1e-300, -1e-300,
+                         2.0, 3.0, 0.5]])
+    lim = np.array([[lib.hfref_limiter(k, float(x)) for x in r] for k in range(2)])
+    np.savez_compressed(os.path.join(HERE, "unit_hllc_limiter.npz"), UL=UL, UR=UR, F=F, r=r, lim=lim)
+    print("units", len(UL), len(r))
+
+
+if __name__ == "__main__":
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref"], check=True)
+    make_units()
+    make_cart()

@@ -1,0 +1,154 @@
+"""GPU parity of the Cartesian time step through the C ABI: bit-exact against the
+reference's golden fixtures and against the oracle (the C restatement) on the same
+inputs, at fixture sizes and at the full benchmark sizes."""
+import math
+
+import numpy as np
+import pytest
+
+from conftest import golden_cart_names, load_golden
+
+pytestmark = pytest.mark.gpu
+
+
+def _solver(case):
+    from hyperflow_gb300 import CartSolver
+    return CartSolver(case)
+
+
+@pytest.mark.parametrize("name", golden_cart_names())
+def test_gpu_matches_reference_fixture(name):
+    g = load_golden(name)
+    s = _solver(g["case"])
+    taken = s.run(int(g["steps"]), clamp_t_end=bool(g["clamp"]))
+    assert taken == int(g["steps"])
+    t, calls, _ = s.time()
+    assert t == float(g["t"])
+    assert calls == len(g["calls"])
+    if "U0" in g:
+        for b in range(int(g["nblocks"])):
+            np.testing.assert_array_equal(s.state(b), g[f"U{b}"])
+    else:
+        U = s.state(0)
+        idx = g["sample_idx"]
+        np.testing.assert_array_equal(U[:, idx[0], idx[1]], g["sample"])
+        assert [math.fsum(U[v].ravel()) for v in range(4)] == list(g["sums"])
+        assert [math.fsum((U[v] * U[v]).ravel()) for v in range(4)] == list(g["sumsq"])
+
+
+@pytest.mark.parametrize("name", ["godunov_quad_48", "mh_minbee_quad_48", "ffs_vanleer_dx1_40",
+                                  "mh_minbee_vacuum_hllc_fallback"])
+def test_gpu_dt_stream_step_by_step(name, port_lib):
+    """hf_step returns each step's dt: the whole stream equals the reference's."""
+    g = load_golden(name)
+    s = _solver(g["case"])
+    dts = [s.step() for _ in range(int(g["steps"]))]
+    np.testing.assert_array_equal(np.array(dts), g["step_dts"])
+
+
+def test_gpu_hllc_fallback_count_matches_oracle(port_lib):
+    from oracle.oracle import Oracle
+    g = load_golden("mh_vanleer_vacuum_hllc_fallback")
+    o = Oracle(g["case"], nthreads=4)
+    o.run(int(g["steps"]))
+    s = _solver(g["case"])
+    s.run(int(g["steps"]))
+    assert o.hllc_errors > 0
+    assert s.hllc_errors() == o.hllc_errors
+
+
+def test_gpu_piecewise_api_equals_device_loop():
+    """apply_bcs / calculate_time_step / advance_block driven from the host (the
+    reference's Simulation::solve sequence) equals hf_run's device loop, with and
+    without the CUDA graph."""
+    from hyperflow_gb300 import cases
+    case = cases.forward_facing_step_case(40, limiter="MinBee")
+    a, b, c = _solver(case), _solver(case), _solver(case)
+    for _ in range(25):
+        a.apply_bcs()
+        dt = a.calculate_time_step()
+        for blk in range(a.nblocks):
+            a.advance_block(blk, dt)
+    b.run(25, graph=True)
+    c.run(25, graph=False)
+    for blk in range(3):
+        np.testing.assert_array_equal(a.state(blk), b.state(blk))
+        np.testing.assert_array_equal(a.state(blk), c.state(blk))
+    assert a.time()[:2] == b.time()[:2] == c.time()[:2]
+
+
+def test_gpu_state_layouts_round_trip():
+    from hyperflow_gb300 import cases
+    s = _solver(cases.quadrant_case(20, ny=13, scheme="MUSCLHancock", limiter="MinBee"))
+    s.run(3)
+    soa = s.state(0)
+    aos = s.state(0, layout="aos")
+    np.testing.assert_array_equal(np.transpose(aos, (2, 1, 0)), soa)
+    s.set_state(0, aos, layout="aos")
+    np.testing.assert_array_equal(s.state(0), soa)
+
+
+def test_gpu_set_state_then_step_matches_oracle(port_lib):
+    """An uploaded arbitrary state (a drop-in caller's fields) steps exactly like the
+    reference: the interior TimeStep terms are recomputed from the upload."""
+    from hyperflow_gb300 import cases
+    from oracle.oracle import Oracle
+    case = cases.quadrant_case(36, ny=28, scheme="MUSCLHancock", limiter="VanLeer")
+    rng = np.random.default_rng(5)
+    o = Oracle(case)
+    U = o.state(0)
+    g = 2
+    U[0, g:-g, g:-g] *= rng.uniform(0.8, 1.2, U[0, g:-g, g:-g].shape)
+    U[3, g:-g, g:-g] *= rng.uniform(0.9, 1.1, U[3, g:-g, g:-g].shape)
+    o.set_state(0, U)
+    s = _solver(case)
+    s.set_state(0, U)
+    o.run(15)
+    s.run(15)
+    np.testing.assert_array_equal(s.state(0), o.state(0))
+
+
+@pytest.mark.parametrize("which", ["godunov_256", "mh_minbee_ffs_full", "mh_vanleer_4096"])
+def test_gpu_full_size_matches_oracle(which, port_lib):
+    """The full benchmark sizes, a few steps, against the oracle on all host cores."""
+    import os
+    from hyperflow_gb300 import cases
+    from oracle.oracle import Oracle
+    if which == "godunov_256":
+        case, steps = cases.quadrant_case(256), 200
+    elif which == "mh_minbee_ffs_full":
+        case, steps = cases.forward_facing_step_case(1365, limiter="MinBee"), 4
+    else:
+        case, steps = cases.quadrant_case(4096, scheme="MUSCLHancock", limiter="VanLeer"), 2
+    o = Oracle(case, nthreads=os.cpu_count() or 4)
+    o.run(steps)
+    s = _solver(case)
+    s.run(steps)
+    for b in range(s.nblocks):
+        np.testing.assert_array_equal(s.state(b), o.state(b))
+    assert s.time()[1] == o.calls
+
+
+def test_gpu_reflective_box_conserves_mass():
+    """Closed reflective box: total mass is conserved to round-off over many steps
+    (a size-independent property at a large size)."""
+    from hyperflow_gb300 import cases
+    case = cases.quadrant_case(1024, scheme="MUSCLHancock", limiter="MinBee", bc="Reflective")
+    s = _solver(case)
+    g = 2
+    m0 = math.fsum(s.state(0)[0, g:-g, g:-g].ravel())
+    s.run(100)
+    m1 = math.fsum(s.state(0)[0, g:-g, g:-g].ravel())
+    assert abs(m1 - m0) <= 1e-12 * abs(m0)
+
+
+def test_gpu_transpose_symmetry():
+    """x<->y mirrored initial data gives the transposed solution (to rounding: the
+    reference's x and y fluxes group products differently, e.g. (rho*u)*v)."""
+    from hyperflow_gb300 import cases
+    st = ([1.0, 0.0, 0.0, 1.0], [0.5, 0.3, 0.1, 0.4], [0.2, 0.2, 0.2, 0.1], [0.5, 0.1, 0.3, 0.4])
+    a = _solver(cases.quadrant_case(128, scheme="MUSCLHancock", limiter="VanLeer", states=st))
+    a.run(60)
+    Ua = a.state(0)
+    sym = np.stack([Ua[0].T, Ua[2].T, Ua[1].T, Ua[3].T])
+    np.testing.assert_allclose(Ua, sym, rtol=1e-10, atol=1e-12)
