@@ -31,9 +31,17 @@ BYTES_PER_CELL = 64          # 4 FP64 read + 4 FP64 written per cell update
 WORKLOAD = "mach3_forward_facing_step_3block_dx1_1365_muscl_hancock_minbee_hllc_fp64"
 
 
-def make_case(limiter: str = "MinBee"):
+def make_case(limiter: str = "MinBee", workload: str = "ffs", n: int = 4096):
     from hyperflow_gb300 import cases
+    if workload == "square":
+        return cases.quadrant_case(n, scheme="MUSCLHancock", limiter=limiter, cfl=0.8)
     return cases.forward_facing_step_case(1365, limiter=limiter, cfl=0.8, t_end=4.0)
+
+
+def workload_name(args):
+    if args.workload == "square":
+        return f"quadrant_riemann_{args.n}x{args.n}_muscl_hancock_{args.limiter.lower()}_hllc_fp64"
+    return WORKLOAD
 
 
 def peaks():
@@ -128,7 +136,7 @@ def reference_arm(args, cells):
     ws, rank, _ = dist_env()
     if rank != 0:
         return
-    case = make_case(args.limiter)
+    case = make_case(args.limiter, args.workload, args.n)
     nth = os.cpu_count() or 1
     from oracle.oracle import Oracle, build_port
     build_port()
@@ -143,7 +151,7 @@ def reference_arm(args, cells):
         "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": el * 1e3 / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (the case's own initial condition)",
-        "config": {"workload": WORKLOAD, "cells": cells},
+        "config": {"workload": workload_name(args), "cells": cells},
         "cpu_baseline": {"value": v, "unit": "Mcell-updates/s", "cores": nth, "kind": "port",
                          "sample": f"{args.steps} full steps of the workload after {args.warmup} warm-up steps"},
         "e2e": {"value": v, "unit": "Mcell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -158,11 +166,16 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--limiter", default="MinBee", choices=["MinBee", "VanLeer"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="CPU-baseline sample budget")
+    ap.add_argument("--workload", default="ffs", choices=["ffs", "square"],
+                    help="ffs: the 3-block forward-facing step (default); square: one n x n block")
+    ap.add_argument("--n", type=int, default=4096, help="side of the square workload")
+    ap.add_argument("--quick", action="store_true",
+                    help="device-resident timing only (no graph pass, e2e or CPU baseline)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
     from hyperflow_gb300 import cases
-    case = make_case(args.limiter)
+    case = make_case(args.limiter, args.workload, args.n)
     cells = cases.total_cells(case)
 
     if args.impl == "reference":
@@ -214,6 +227,15 @@ def main():
     value = ws * cells * args.steps / (t_max / 1e3) / 1e6
     hllc_fallbacks = s.hllc_errors()
 
+    if args.quick:
+        if rank == 0:
+            print(json.dumps({"metric": "Mcell-updates/s", "value": value, "unit": "Mcell-updates/s",
+                              "steps": args.steps, "ms_per_step": t_max / args.steps,
+                              "config": {"workload": workload_name(args), "cells": cells},
+                              "stencil_ms_per_step": stencil_ms / args.steps}), flush=True)
+        s.close()
+        return
+
     # same run through the CUDA graph (one captured step replayed K times)
     s.run(1, graph=True)
     barrier()
@@ -253,7 +275,7 @@ def main():
     achieved = BYTES_PER_CELL * cells * args.steps / (stencil_ms / 1e3) / 1e9
     traffic = None
     tr = ncu_traffic()
-    if tr and tr.get("workload") == WORKLOAD:
+    if tr and tr.get("workload") == workload_name(args):
         traffic = tr["dram_bytes_per_cell_update"] * cells / nb
     roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
             "frac": achieved / hbm, "traffic": traffic, "peak_kind": peak_kind,
@@ -280,7 +302,7 @@ def main():
             "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (the case's own initial condition: uniform Mach 3 inflow)",
-            "config": {"workload": WORKLOAD, "cells": cells, "blocks": nb, "limiter": args.limiter,
+            "config": {"workload": workload_name(args), "cells": cells, "blocks": nb, "limiter": args.limiter,
                        "cfl": 0.8, "l2": "state 2 x 300 MB > 129 MB L2, no flush needed",
                        "parallelism": "replicas" if ws > 1 else "single GPU"},
             "roofline": roof,

@@ -41,6 +41,21 @@ SIGNATURES = {
     "hf_profile": (_i, [_p, _i]),
     "hf_kernel_time": (_i, [_p, _i, C.POINTER(_d), C.POINTER(_i64)]),
     "hf_status_string": (C.c_char_p, [_i]),
+    # unstructured (include/hyperflow_gb300_uns.h)
+    "hf_uns_create": (_i, [C.c_char_p, _sz, C.POINTER(_p)]),
+    "hf_uns_create_mesh": (_i, [C.c_char_p, _sz, C.c_char_p, _sz, C.POINTER(_p)]),
+    "hf_uns_destroy": (None, [_p]),
+    "hf_uns_last_error_message": (C.c_char_p, [_p]),
+    "hf_uns_sizes": (_i, [_p, C.POINTER(_i64), C.POINTER(_i64)]),
+    "hf_uns_mesh_arrays": (_i, [_p, _p, _p, _p, _p, _p, _p]),
+    "hf_uns_set_state": (_i, [_p, _p]),
+    "hf_uns_get_state": (_i, [_p, _p]),
+    "hf_uns_time_step": (_i, [_p, C.POINTER(_d)]),
+    "hf_uns_advance": (_i, [_p, _d]),
+    "hf_uns_run": (_i, [_p, _i64, _i, _i, C.POINTER(_i64)]),
+    "hf_uns_get_time": (_i, [_p, C.POINTER(_d), C.POINTER(_i64), C.POINTER(_d)]),
+    "hf_uns_hllc_errors": (_i, [_p, C.POINTER(_i64)]),
+    "hf_uns_stream": (_i, [_p, C.POINTER(_p)]),
     "hf_last_error_message": (C.c_char_p, [_p]),
 }
 
@@ -68,10 +83,10 @@ def lib() -> C.CDLL:
     return _lib
 
 
-def check(status: int, ctx=None) -> None:
+def check(status: int, ctx=None, msgfn: str = "hf_last_error_message") -> None:
     if status != HF_OK:
         msg = ""
         if ctx is not None:
-            m = lib().hf_last_error_message(ctx)
+            m = getattr(lib(), msgfn)(ctx)
             msg = m.decode() if m else ""
         raise HyperFlowError(status, msg)

@@ -1,0 +1,643 @@
+// Unstructured (triangle / quadrilateral) Godunov + HLLC time step for sm_103a, and its
+// C ABI (declared in include/hyperflow_gb300_uns.h).
+//
+// Reference: src/fvm_2d_uns -- GodunovScheme::operator() (scheme/godunov/godunov.cpp:31-77)
+// walks every (cell, edge) pair in order; for each it rotates the cell state and the
+// neighbour state (a cell, or a boundary state from scheme/boundary/boundary.cpp:29-69)
+// into the edge's outward-normal frame (model/euler_ideal_gas/euler_ideal_gas.cpp:152-165),
+// runs HLLC in x, rotates the flux back, scales by the edge length and accumulates on the
+// cell; then L = -acc/area and forward Euler.  TimeStep (scheme/timestep/timestep.cpp:29-62)
+// uses the incircle radius.
+//
+// Device layout: cells SoA FP64 [4][ncells] (two buffers alternating by step parity); the
+// (cell, edge) pairs in CSR order by cell -- exactly the reference's cell_edge_indices
+// order -- with per-pair neighbour index (or negative boundary code), length and the
+// cos/sin of the rotation angles precomputed on the host with the same libm calls the
+// reference makes every step.  One thread owns one cell and accumulates its pairs in
+// order, so the sum matches the reference bit for bit.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <memory>
+#include <sstream>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/hyperflow_gb300_uns.h"
+#include "hf_device.cuh"
+#include "hf_json.hpp"
+
+namespace hf {
+
+struct UnsCtrl {
+    double gamma, g1, cfl;
+    double t, t_end, dt;
+    long long calls, step;
+    int clamp, done;
+    unsigned long long min_dt[2];   // [parity] min over cells of r_in / (|V| + c), bit pattern
+    int err;
+    long long hllc_errors;
+};
+
+struct UnsMesh {
+    int ncells;
+    const int* __restrict__ pair_start;   // ncells + 1
+    const int* __restrict__ nbr;          // per pair: cell index, or -1 reflective, -2 transmissive, -3 inlet
+    const double* __restrict__ geo;       // per pair: [5][npairs] cos a, sin a, cos(-a), sin(-a), length
+    const double* __restrict__ inv_area;  // per cell 1.0 / signed area
+    const double* __restrict__ rin;       // per cell incircle radius (quads: shortest edge)
+    double* U[2];
+    double inlet[4];
+    long long npairs;
+};
+
+// rotate_flow_values (euler_ideal_gas.cpp:152-165) with precomputed cos/sin
+__device__ __forceinline__ void rot(double c, double s, const double* f, double* o) {
+    o[0] = f[0];
+    o[1] = c * f[1] + s * f[2];
+    o[2] = -1.0 * s * f[1] + c * f[2];
+    o[3] = f[3];
+}
+
+// TimeStep term r_in / (|V| + c) of one cell (uns timestep.cpp:51-58)
+__device__ __forceinline__ double uns_dt_term(double g, double g1, double rin, const double* u) {
+    double uu, vv, p;
+    to_prim_short(g1, u[0], u[1], u[2], u[3], uu, vv, p);
+    double c = sound(g, u[0], p);
+    return rin / (fabs(sqrt(uu * uu + vv * vv)) + c);
+}
+
+// NaN-skipping min of non-negative values
+__device__ __forceinline__ double nmin(double m, double s) { return (s < m) ? s : m; }
+
+template <int NT>
+__device__ __forceinline__ void block_min_atomic(double v, unsigned long long* acc) {
+    __shared__ double red[NT / 32];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = nmin(v, __shfl_xor_sync(0xffffffffu, v, o));
+    int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (l == 0) red[w] = v;
+    __syncthreads();
+    if (w == 0) {
+        v = l < NT / 32 ? red[l] : 1e16;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v = nmin(v, __shfl_xor_sync(0xffffffffu, v, o));
+        if (l == 0 && v < 1e16) atomicMin(acc, dbits(v));
+    }
+}
+
+constexpr int kUnsNT = 256;
+
+__global__ void __launch_bounds__(kUnsNT) uns_cfl_kernel(UnsCtrl* __restrict__ c, UnsMesh m, int parity) {
+    double mn = 1e16;
+    const double* U = m.U[parity];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m.ncells; i += gridDim.x * blockDim.x) {
+        double u[4] = {U[i], U[m.ncells + i], U[2 * (size_t)m.ncells + i], U[3 * (size_t)m.ncells + i]};
+        mn = nmin(mn, uns_dt_term(c->gamma, c->g1, m.rin[i], u));
+    }
+    block_min_atomic<kUnsNT>(mn, &c->min_dt[parity]);
+}
+
+// start of a device-loop step: stop at t_end, form dt (TimeStep call), reset the accumulator
+__global__ void uns_prep_kernel(UnsCtrl* c) {
+    int p = (int)(c->step & 1);
+    if (c->clamp && c->t == c->t_end) { c->done = 1; return; }
+    c->done = 0;
+    double dtr = smin(1e16, bitsd(c->min_dt[p]));
+    double final_cfl = (c->calls + 1 <= 10) ? 0.2 * c->cfl : c->cfl;
+    double dt = final_cfl * dtr;
+    if (c->clamp && c->t + dt > c->t_end) dt = c->t_end - c->t;   // simulation.cpp:85-88
+    c->dt = dt;
+    c->calls = c->calls + 1;
+    c->min_dt[p ^ 1] = dbits(1e16);
+}
+
+__global__ void uns_set_dt_kernel(UnsCtrl* c, double dt) {
+    c->done = 0;
+    c->dt = dt;
+    c->min_dt[(c->step & 1) ^ 1] = dbits(1e16);
+}
+
+__global__ void uns_finalize_kernel(UnsCtrl* c) {
+    if (c->done) return;
+    c->t = c->t + c->dt;
+    c->step = c->step + 1;
+}
+
+__global__ void __launch_bounds__(kUnsNT) uns_step_kernel(UnsCtrl* __restrict__ c, UnsMesh m) {
+    if (c->done) return;
+    const int p = (int)(c->step & 1);
+    const double g = c->gamma, g1 = c->g1, dt = c->dt;
+    const size_t N = (size_t)m.ncells;
+    const double* __restrict__ U = m.U[p];
+    double* __restrict__ Un = m.U[p ^ 1];
+    double mn = 1e16;
+    int herr = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m.ncells; i += gridDim.x * blockDim.x) {
+        double cv[4] = {U[i], U[N + i], U[2 * N + i], U[3 * N + i]};
+        double acc[4] = {0.0, 0.0, 0.0, 0.0};
+        const int e0 = m.pair_start[i], e1 = m.pair_start[i + 1];
+        for (int e = e0; e < e1; ++e) {
+            const double ca = m.geo[e], sa = m.geo[m.npairs + e];
+            const double cn = m.geo[2 * m.npairs + e], sn = m.geo[3 * m.npairs + e];
+            const double len = m.geo[4 * m.npairs + e];
+            const int k = m.nbr[e];
+            double rc[4], rn[4];
+            rot(ca, sa, cv, rc);
+            if (k >= 0) {
+                double nb[4] = {U[k], U[N + k], U[2 * N + k], U[3 * N + k]};
+                rot(ca, sa, nb, rn);
+            } else if (k == -1) {   // reflective: rotate, negate normal momentum, rotate back
+                double r1[4], nb[4];
+                r1[0] = rc[0]; r1[1] = rc[1] * -1.0; r1[2] = rc[2]; r1[3] = rc[3];
+                rot(cn, sn, r1, nb);
+                rot(ca, sa, nb, rn);
+            } else if (k == -2) {   // transmissive: the cell's own state
+                rot(ca, sa, cv, rn);
+            } else {                // inlet
+                rot(ca, sa, m.inlet, rn);
+            }
+            double rf[4], f[4];
+            herr += hllc_cons<0>(g, g1, rc, rn, rf);
+            rot(cn, sn, rf, f);
+#pragma unroll
+            for (int v = 0; v < 4; ++v) acc[v] = acc[v] + len * f[v];
+        }
+        const double inv = m.inv_area[i];
+        double un[4];
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+            const double L = -1.0 * (inv * acc[v]);
+            un[v] = dt * L + cv[v];
+            Un[v * N + i] = un[v];
+        }
+        mn = nmin(mn, uns_dt_term(g, g1, m.rin[i], un));
+    }
+    block_min_atomic<kUnsNT>(mn, &c->min_dt[p ^ 1]);
+    if (herr) atomicAdd(reinterpret_cast<unsigned long long*>(&c->hllc_errors), (unsigned long long)herr);
+}
+
+}  // namespace hf
+
+// =====================================================================================
+// host side
+// =====================================================================================
+using hf::Json;
+
+struct hf_uns {
+    cudaStream_t stream = nullptr;
+    double gamma = 1.4, cfl = 0.5, t_start = 0.0, t_end = 0.0;
+    double inlet[4] = {0, 0, 0, 0};
+    int ncells = 0;
+    std::vector<int> nverts;
+    std::vector<double> verts;          // per cell vertex, x y
+    std::vector<int> codes;             // per pair boundary code from the mesh file
+    std::vector<int> pair_start, nbr;
+    std::vector<double> angle, length, area, rin;
+    std::vector<double> init;           // initial SoA state
+    hf::UnsMesh dm{};
+    hf::UnsCtrl* dctrl = nullptr;
+    std::vector<void*> allocs;
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    std::string err;
+};
+
+namespace {
+
+int ufail(hf_uns* u, int code, const std::string& m) {
+    if (u) u->err = m;
+    return code;
+}
+
+#define UCK(call)                                                                              \
+    do {                                                                                       \
+        cudaError_t e_ = (call);                                                               \
+        if (e_ != cudaSuccess)                                                                 \
+            return ufail(u, HF_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));  \
+    } while (0)
+
+void prim_to_cons(double gamma, const double* w, double* c) {
+    double rho = w[0], uu = w[1], v = w[2], p = w[3];
+    c[0] = rho;
+    c[1] = rho * uu;
+    c[2] = rho * v;
+    c[3] = p / (gamma - 1.0) + 0.5 * rho * (uu * uu + v * v);
+}
+
+// the mesh text format of generate_block_mesh.py:217-246, cells of 3 or 4 vertices
+int parse_mesh(hf_uns* u, const std::string& text) {
+    std::istringstream in(text);
+    std::string line;
+    if (!std::getline(in, line) || line.compare(0, 5, "CELLS") != 0)
+        return ufail(u, HF_ERR_PARSE, "mesh: expected CELLS header");
+    if (!std::getline(in, line)) return ufail(u, HF_ERR_PARSE, "mesh: missing cell count");
+    long n = std::strtol(line.c_str(), nullptr, 0);
+    u->nverts.reserve(n);
+    u->verts.reserve((size_t)n * 8);
+    while (std::getline(in, line)) {
+        if (line.compare(0, 5, "EDGES") == 0) break;
+        const char* s = line.c_str();
+        char* end = nullptr;
+        double v[8];
+        int k = 0;
+        while (k < 8) {
+            double x = std::strtod(s, &end);
+            if (end == s) break;
+            v[k++] = x;
+            s = end;
+        }
+        if (k != 6 && k != 8) return ufail(u, HF_ERR_PARSE, "mesh: a cell needs 3 or 4 vertices");
+        u->nverts.push_back(k / 2);
+        for (int i = 0; i < k; ++i) u->verts.push_back(v[i]);
+    }
+    if ((long)u->nverts.size() != n) return ufail(u, HF_ERR_PARSE, "mesh: cell count mismatch");
+    if (!std::getline(in, line)) return ufail(u, HF_ERR_PARSE, "mesh: missing edge count");
+    long ne = std::strtol(line.c_str(), nullptr, 0);
+    while (std::getline(in, line)) {
+        if (line.empty()) continue;
+        u->codes.push_back((int)std::strtol(line.c_str(), nullptr, 0));
+    }
+    if ((long)u->codes.size() != ne) return ufail(u, HF_ERR_PARSE, "mesh: edge count mismatch");
+    u->ncells = (int)n;
+    return HF_OK;
+}
+
+struct EdgeKey {
+    uint64_t a, b, c, d;
+    bool operator==(const EdgeKey& o) const { return a == o.a && b == o.b && c == o.c && d == o.d; }
+};
+struct EdgeHash {
+    size_t operator()(const EdgeKey& k) const {
+        uint64_t h = k.a * 0x9E3779B97F4A7C15ull;
+        h ^= k.b + 0x7F4A7C159E3779B9ull + (h << 6) + (h >> 2);
+        h ^= k.c + 0x94D049BB133111EBull + (h << 6) + (h >> 2);
+        h ^= k.d + 0xBF58476D1CE4E5B9ull + (h << 6) + (h >> 2);
+        return (size_t)h;
+    }
+};
+uint64_t bitsof(double x) {
+    if (x == 0.0) x = 0.0;   // -0.0 and +0.0 name the same point
+    uint64_t b;
+    std::memcpy(&b, &x, 8);
+    return b;
+}
+
+// Neighbour search of mesh_structured.cpp:92-114 (a pair's neighbour is the cell holding
+// the same edge reversed; unmatched pairs keep their boundary code), by hashing the
+// exact endpoint coordinates instead of the O(E^2) scan.  For meshes whose shared
+// vertices are written identically -- every mesh the generators produce -- this is the
+// same match the reference finds with its 1e-12 tolerance.
+void build_pairs(hf_uns* u) {
+    int n = u->ncells;
+    u->pair_start.assign(n + 1, 0);
+    for (int c = 0; c < n; ++c) u->pair_start[c + 1] = u->pair_start[c] + u->nverts[c];
+    std::unordered_map<EdgeKey, int, EdgeHash> table;
+    table.reserve((size_t)u->pair_start[n] * 2);
+    std::vector<size_t> voff(n + 1, 0);
+    for (int c = 0; c < n; ++c) voff[c + 1] = voff[c] + u->nverts[c];
+    for (int c = 0; c < n; ++c) {
+        const double* V = &u->verts[2 * voff[c]];
+        int nv = u->nverts[c];
+        for (int k = 0; k < nv; ++k) {
+            int k1 = (k == nv - 1) ? 0 : k + 1;
+            table[EdgeKey{bitsof(V[2 * k]), bitsof(V[2 * k + 1]), bitsof(V[2 * k1]), bitsof(V[2 * k1 + 1])}] = c;
+        }
+    }
+    u->nbr.resize(u->pair_start[n]);
+    for (int c = 0; c < n; ++c) {
+        const double* V = &u->verts[2 * voff[c]];
+        int nv = u->nverts[c];
+        for (int k = 0; k < nv; ++k) {
+            int k1 = (k == nv - 1) ? 0 : k + 1;
+            auto it = table.find(EdgeKey{bitsof(V[2 * k1]), bitsof(V[2 * k1 + 1]), bitsof(V[2 * k]), bitsof(V[2 * k + 1])});
+            int pr = u->pair_start[c] + k;
+            u->nbr[pr] = it != table.end() ? it->second : u->codes[pr];
+        }
+    }
+}
+
+// geometry exactly as the reference: Edge (edge.cpp:165-218), Polygon (polygon.cpp:72-212)
+void build_geometry(hf_uns* u) {
+    int n = u->ncells;
+    size_t np = u->pair_start[n];
+    u->angle.resize(np);
+    u->length.resize(np);
+    u->area.resize(n);
+    u->rin.resize(n);
+    size_t vo = 0;
+    for (int c = 0; c < n; ++c) {
+        int nv = u->nverts[c];
+        const double* V = &u->verts[2 * vo];
+        double el[4];
+        for (int k = 0; k < nv; ++k) {
+            int k1 = (k == nv - 1) ? 0 : k + 1;
+            double p0 = V[2 * k1] - V[2 * k], p1 = V[2 * k1 + 1] - V[2 * k + 1];
+            double n0 = p1, n1 = -1.0 * p0;
+            double nl = std::sqrt(n0 * n0 + n1 * n1);
+            n0 /= nl;
+            n1 /= nl;
+            size_t pr = u->pair_start[c] + k;
+            u->angle[pr] = std::atan2(n1, n0) * 180.0 / M_PI;
+            double d = 0.0;
+            d += p0 * p0;
+            d += p1 * p1;
+            u->length[pr] = std::sqrt(d);
+            el[k] = u->length[pr];
+        }
+        double vol = 0.0;
+        for (int k = 0; k < nv; ++k) {
+            int k1 = (k == nv - 1) ? 0 : k + 1;
+            vol += (V[2 * k] * V[2 * k1 + 1] - V[2 * k1] * V[2 * k + 1]);
+        }
+        vol *= 0.5;
+        u->area[c] = vol;
+        if (nv == 3) {
+            double a = el[0], b = el[1], cc = el[2];
+            double s = (a + b + cc) / 2.0;
+            double num = s * (s - a) * (s - b) * (s - cc);
+            u->rin[c] = std::sqrt(num) / s;
+        } else {
+            double sh = 1e16;
+            for (int k = 0; k < nv; ++k) sh = (sh < el[k]) ? sh : el[k];
+            u->rin[c] = sh;
+        }
+        vo += nv;
+    }
+}
+
+template <class T>
+int upload(hf_uns* u, T** dst, const std::vector<T>& src) {
+    UCK(cudaMalloc(dst, src.size() * sizeof(T) + 16));
+    u->allocs.push_back(*dst);
+    UCK(cudaMemcpy(*dst, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice));
+    return HF_OK;
+}
+
+int read_step(hf_uns* u, long long* s) {
+    UCK(cudaStreamSynchronize(u->stream));
+    UCK(cudaMemcpy(s, &u->dctrl->step, sizeof *s, cudaMemcpyDeviceToHost));
+    return HF_OK;
+}
+
+int finish_create(hf_uns* u, const Json& cfg) {
+    const Json& ic = cfg["initial_condition"];
+    const std::string type = ic["type"].string();
+    double w[4], c4[4];
+    if (type != "Constant") return ufail(u, HF_ERR_UNSUPPORTED, "unstructured IC must be Constant");
+    for (int k = 0; k < 4; ++k) w[k] = ic["init_state"][k].number();
+    prim_to_cons(u->gamma, w, c4);   // parser.cpp always converts the constant state
+    build_pairs(u);
+    build_geometry(u);
+    int n = u->ncells;
+    u->init.assign((size_t)4 * n, 0.0);
+    for (int v = 0; v < 4; ++v)
+        for (int c = 0; c < n; ++c) u->init[(size_t)v * n + c] = c4[v];
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+        return ufail(u, HF_ERR_NO_DEVICE, "no CUDA device visible");
+    UCK(cudaStreamCreateWithFlags(&u->stream, cudaStreamNonBlocking));
+    size_t np = u->pair_start[n];
+    std::vector<double> geo(5 * np), inv(n);
+    for (size_t e = 0; e < np; ++e) {
+        double a = u->angle[e] * (M_PI / 180.0);
+        double an = (-1.0 * u->angle[e]) * (M_PI / 180.0);
+        geo[e] = std::cos(a);
+        geo[np + e] = std::sin(a);
+        geo[2 * np + e] = std::cos(an);
+        geo[3 * np + e] = std::sin(an);
+        geo[4 * np + e] = u->length[e];
+    }
+    for (int c = 0; c < n; ++c) inv[c] = 1.0 / u->area[c];
+    int r;
+    int* ps; int* nb; double* g; double* ia; double* ri;
+    if ((r = upload(u, &ps, u->pair_start)) || (r = upload(u, &nb, u->nbr)) || (r = upload(u, &g, geo)) ||
+        (r = upload(u, &ia, inv)) || (r = upload(u, &ri, u->rin)))
+        return r;
+    u->dm.ncells = n;
+    u->dm.pair_start = ps;
+    u->dm.nbr = nb;
+    u->dm.geo = g;
+    u->dm.inv_area = ia;
+    u->dm.rin = ri;
+    u->dm.npairs = (long long)np;
+    for (int k = 0; k < 4; ++k) u->dm.inlet[k] = u->inlet[k];
+    for (int k = 0; k < 2; ++k) {
+        double* p;
+        UCK(cudaMalloc(&p, (size_t)4 * n * sizeof(double)));
+        u->allocs.push_back(p);
+        u->dm.U[k] = p;
+    }
+    hf::UnsCtrl C{};
+    C.gamma = u->gamma;
+    C.g1 = u->gamma - 1.0;
+    C.cfl = u->cfl;
+    C.t = u->t_start;
+    C.t_end = u->t_end;
+    UCK(cudaMalloc(&u->dctrl, sizeof C));
+    UCK(cudaMemcpy(u->dctrl, &C, sizeof C, cudaMemcpyHostToDevice));
+    return hf_uns_set_state(u, u->init.data());
+}
+
+int enqueue_uns_step(hf_uns* u, bool prep) {
+    int grid = (u->ncells + hf::kUnsNT - 1) / hf::kUnsNT;
+    if (prep) hf::uns_prep_kernel<<<1, 1, 0, u->stream>>>(u->dctrl);
+    hf::uns_step_kernel<<<grid, hf::kUnsNT, 0, u->stream>>>(u->dctrl, u->dm);
+    hf::uns_finalize_kernel<<<1, 1, 0, u->stream>>>(u->dctrl);
+    UCK(cudaGetLastError());
+    return HF_OK;
+}
+
+int create_common(const char* case_json, size_t len, const std::string* mesh_text, hf_uns** out) {
+    if (!case_json || !out) return HF_ERR_ARG;
+    hf_uns* u = new hf_uns();
+    *out = u;
+    try {
+        Json cfg = Json::parse(case_json, len);
+        if (cfg["model"]["model"].string() != "EulerIdealGas")
+            return ufail(u, HF_ERR_UNSUPPORTED, "model must be EulerIdealGas");
+        u->gamma = cfg["model"]["gamma"].number();
+        if (cfg["scheme"]["type"].string() != "Godunov")
+            return ufail(u, HF_ERR_UNSUPPORTED, "the unstructured solver is Godunov only");
+        if (cfg["scheme"]["riemann"].string() != "HLLCEuler")
+            return ufail(u, HF_ERR_UNSUPPORTED, "Riemann solver must be HLLCEuler");
+        u->cfl = cfg["simulation"]["cfl"].number();
+        u->t_start = cfg["simulation"]["t_start"].number();
+        u->t_end = cfg["simulation"]["t_end"].number();
+        double w[4];
+        for (int k = 0; k < 4; ++k) w[k] = cfg["mesh"]["boundaries"]["inlet"][k].number();
+        prim_to_cons(u->gamma, w, u->inlet);   // parser.cpp:211-217
+        const std::string mt = cfg["mesh"]["type"].string();
+        if (mt != "hyperflow_structured" && mt != "hyperflow_unstructured")
+            return ufail(u, HF_ERR_UNSUPPORTED, "mesh type '" + mt + "' not supported");
+        std::string text;
+        if (mesh_text) {
+            text = *mesh_text;
+        } else {
+            std::ifstream f(cfg["mesh"]["file"].string());
+            if (!f) return ufail(u, HF_ERR_ARG, "unable to open mesh file " + cfg["mesh"]["file"].string());
+            std::stringstream ss;
+            ss << f.rdbuf();
+            text = ss.str();
+        }
+        int r = parse_mesh(u, text);
+        if (r != HF_OK) return r;
+        return finish_create(u, cfg);
+    } catch (const std::exception& e) {
+        return ufail(u, HF_ERR_PARSE, e.what());
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+int hf_uns_create(const char* case_json, size_t len, hf_uns** out) {
+    return create_common(case_json, len, nullptr, out);
+}
+
+int hf_uns_create_mesh(const char* case_json, size_t len, const char* mesh_text, size_t mesh_len,
+                       hf_uns** out) {
+    if (!mesh_text) return HF_ERR_ARG;
+    std::string t(mesh_text, mesh_len);
+    return create_common(case_json, len, &t, out);
+}
+
+void hf_uns_destroy(hf_uns* u) {
+    if (!u) return;
+    if (u->stream) cudaStreamSynchronize(u->stream);
+    for (int k = 0; k < 2; ++k)
+        if (u->graph[k]) cudaGraphExecDestroy(u->graph[k]);
+    for (void* p : u->allocs) cudaFree(p);
+    if (u->dctrl) cudaFree(u->dctrl);
+    if (u->stream) cudaStreamDestroy(u->stream);
+    delete u;
+}
+
+const char* hf_uns_last_error_message(const hf_uns* u) { return u ? u->err.c_str() : ""; }
+
+int hf_uns_sizes(const hf_uns* u, int64_t* ncells, int64_t* npairs) {
+    if (!u) return HF_ERR_ARG;
+    if (ncells) *ncells = u->ncells;
+    if (npairs) *npairs = u->pair_start.empty() ? 0 : u->pair_start.back();
+    return HF_OK;
+}
+
+int hf_uns_mesh_arrays(const hf_uns* u, int32_t* pair_start, int32_t* nbr, double* angle,
+                       double* length, double* area, double* rin) {
+    if (!u) return HF_ERR_ARG;
+    size_t n = u->ncells, np = u->pair_start.empty() ? 0 : u->pair_start.back();
+    if (pair_start) std::memcpy(pair_start, u->pair_start.data(), (n + 1) * sizeof(int));
+    if (nbr) std::memcpy(nbr, u->nbr.data(), np * sizeof(int));
+    if (angle) std::memcpy(angle, u->angle.data(), np * sizeof(double));
+    if (length) std::memcpy(length, u->length.data(), np * sizeof(double));
+    if (area) std::memcpy(area, u->area.data(), n * sizeof(double));
+    if (rin) std::memcpy(rin, u->rin.data(), n * sizeof(double));
+    return HF_OK;
+}
+
+int hf_uns_set_state(hf_uns* u, const double* cons) {
+    if (!u || !cons || !u->dctrl) return HF_ERR_ARG;
+    long long s;
+    int r = read_step(u, &s);
+    if (r) return r;
+    int p = (int)(s & 1);
+    size_t bytes = (size_t)4 * u->ncells * sizeof(double);
+    UCK(cudaMemcpyAsync(u->dm.U[p], cons, bytes, cudaMemcpyHostToDevice, u->stream));
+    unsigned long long init = 0;
+    double big = 1e16;
+    std::memcpy(&init, &big, 8);
+    UCK(cudaMemcpyAsync(&u->dctrl->min_dt[p], &init, 8, cudaMemcpyHostToDevice, u->stream));
+    int grid = (u->ncells + hf::kUnsNT - 1) / hf::kUnsNT;
+    if (grid > 8 * 152) grid = 8 * 152;
+    hf::uns_cfl_kernel<<<grid, hf::kUnsNT, 0, u->stream>>>(u->dctrl, u->dm, p);
+    UCK(cudaGetLastError());
+    UCK(cudaStreamSynchronize(u->stream));
+    return HF_OK;
+}
+
+int hf_uns_get_state(hf_uns* u, double* cons) {
+    if (!u || !cons || !u->dctrl) return HF_ERR_ARG;
+    long long s;
+    int r = read_step(u, &s);
+    if (r) return r;
+    UCK(cudaMemcpy(cons, u->dm.U[s & 1], (size_t)4 * u->ncells * sizeof(double), cudaMemcpyDeviceToHost));
+    return HF_OK;
+}
+
+int hf_uns_time_step(hf_uns* u, double* dt) {
+    if (!u || !u->dctrl) return HF_ERR_ARG;
+    int clamp = 0;
+    UCK(cudaMemcpyAsync(&u->dctrl->clamp, &clamp, sizeof clamp, cudaMemcpyHostToDevice, u->stream));
+    hf::uns_prep_kernel<<<1, 1, 0, u->stream>>>(u->dctrl);
+    UCK(cudaGetLastError());
+    if (dt) {
+        UCK(cudaMemcpyAsync(dt, &u->dctrl->dt, sizeof(double), cudaMemcpyDeviceToHost, u->stream));
+        UCK(cudaStreamSynchronize(u->stream));
+    }
+    return HF_OK;
+}
+
+int hf_uns_advance(hf_uns* u, double dt) {
+    if (!u || !u->dctrl) return HF_ERR_ARG;
+    hf::uns_set_dt_kernel<<<1, 1, 0, u->stream>>>(u->dctrl, dt);
+    return enqueue_uns_step(u, false);
+}
+
+int hf_uns_run(hf_uns* u, int64_t n, int clamp_t_end, int use_graph, int64_t* steps_done) {
+    if (!u || !u->dctrl || n < 0) return HF_ERR_ARG;
+    long long s0 = 0;
+    int r = read_step(u, &s0);
+    if (r) return r;
+    int clamp = clamp_t_end ? 1 : 0;
+    UCK(cudaMemcpyAsync(&u->dctrl->clamp, &clamp, sizeof clamp, cudaMemcpyHostToDevice, u->stream));
+    if (use_graph) {
+        if (!u->graph[clamp]) {
+            cudaGraph_t g;
+            UCK(cudaStreamBeginCapture(u->stream, cudaStreamCaptureModeThreadLocal));
+            r = enqueue_uns_step(u, true);
+            cudaError_t e = cudaStreamEndCapture(u->stream, &g);
+            if (r) return r;
+            if (e != cudaSuccess) return ufail(u, HF_ERR_CUDA, cudaGetErrorString(e));
+            UCK(cudaGraphInstantiate(&u->graph[clamp], g, 0));
+            cudaGraphDestroy(g);
+        }
+        for (int64_t k = 0; k < n; ++k) UCK(cudaGraphLaunch(u->graph[clamp], u->stream));
+    } else {
+        for (int64_t k = 0; k < n; ++k)
+            if ((r = enqueue_uns_step(u, true))) return r;
+    }
+    long long s1;
+    if ((r = read_step(u, &s1))) return r;
+    if (steps_done) *steps_done = s1 - s0;
+    return HF_OK;
+}
+
+int hf_uns_get_time(hf_uns* u, double* t, int64_t* calls, double* last_dt) {
+    if (!u || !u->dctrl) return HF_ERR_ARG;
+    hf::UnsCtrl C;
+    UCK(cudaStreamSynchronize(u->stream));
+    UCK(cudaMemcpy(&C, u->dctrl, sizeof C, cudaMemcpyDeviceToHost));
+    if (t) *t = C.t;
+    if (calls) *calls = C.calls;
+    if (last_dt) *last_dt = C.dt;
+    return HF_OK;
+}
+
+int hf_uns_hllc_errors(hf_uns* u, int64_t* count) {
+    if (!u || !u->dctrl || !count) return HF_ERR_ARG;
+    long long v;
+    UCK(cudaStreamSynchronize(u->stream));
+    UCK(cudaMemcpy(&v, &u->dctrl->hllc_errors, sizeof v, cudaMemcpyDeviceToHost));
+    *count = v;
+    return HF_OK;
+}
+
+int hf_uns_stream(hf_uns* u, void** stream) {
+    if (!u || !stream) return HF_ERR_ARG;
+    *stream = (void*)u->stream;
+    return HF_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,100 @@
+"""Python host mirror of the reference's unstructured solver (src/fvm_2d_uns).
+
+``UnsSolver`` runs the reference's unstructured step -- TimeStep (timestep.cpp:29-62),
+GodunovScheme + forward Euler (godunov.cpp:31-77) -- on the GPU through the C ABI of
+include/hyperflow_gb300_uns.h.  Meshes use the reference's text format, extended to
+triangles (see meshgen.py).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import json
+
+import numpy as np
+
+from ._lib import check, lib
+
+_MSG = "hf_uns_last_error_message"
+
+
+class UnsSolver:
+    def __init__(self, case, mesh_text: str | None = None):
+        text = case if isinstance(case, str) else json.dumps(case)
+        raw = text.encode()
+        L = lib()
+        h = C.c_void_p()
+        if mesh_text is None:
+            st = L.hf_uns_create(raw, len(raw), C.byref(h))
+        else:
+            mt = mesh_text.encode()
+            st = L.hf_uns_create_mesh(raw, len(raw), mt, len(mt), C.byref(h))
+        self._h = h
+        if st != 0:
+            try:
+                check(st, h, _MSG)
+            finally:
+                if h:
+                    L.hf_uns_destroy(h)
+                self._h = None
+        nc, npair = C.c_int64(), C.c_int64()
+        check(L.hf_uns_sizes(self._h, C.byref(nc), C.byref(npair)), self._h, _MSG)
+        self.ncells, self.npairs = nc.value, npair.value
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().hf_uns_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def mesh_arrays(self):
+        ps = np.empty(self.ncells + 1, np.int32)
+        nbr = np.empty(self.npairs, np.int32)
+        ang, ln = np.empty(self.npairs), np.empty(self.npairs)
+        area, rin = np.empty(self.ncells), np.empty(self.ncells)
+        check(lib().hf_uns_mesh_arrays(self._h, ps.ctypes.data, nbr.ctypes.data, ang.ctypes.data,
+                                       ln.ctypes.data, area.ctypes.data, rin.ctypes.data), self._h, _MSG)
+        return {"pair_start": ps, "nbr": nbr, "angle": ang, "length": ln, "area": area, "rin": rin}
+
+    def state(self, out: np.ndarray | None = None) -> np.ndarray:
+        if out is None:
+            out = np.empty((4, self.ncells))
+        check(lib().hf_uns_get_state(self._h, out.ctypes.data), self._h, _MSG)
+        return out
+
+    def set_state(self, U: np.ndarray):
+        U = np.ascontiguousarray(U, dtype=np.float64)
+        assert U.shape == (4, self.ncells)
+        check(lib().hf_uns_set_state(self._h, U.ctypes.data), self._h, _MSG)
+
+    def calculate_time_step(self) -> float:
+        dt = C.c_double()
+        check(lib().hf_uns_time_step(self._h, C.byref(dt)), self._h, _MSG)
+        return dt.value
+
+    def advance(self, dt: float):
+        check(lib().hf_uns_advance(self._h, dt), self._h, _MSG)
+
+    def run(self, n: int, clamp_t_end: bool = False, graph: bool = True) -> int:
+        done = C.c_int64()
+        check(lib().hf_uns_run(self._h, n, int(clamp_t_end), int(graph), C.byref(done)), self._h, _MSG)
+        return done.value
+
+    def time(self):
+        t, c, d = C.c_double(), C.c_int64(), C.c_double()
+        check(lib().hf_uns_get_time(self._h, C.byref(t), C.byref(c), C.byref(d)), self._h, _MSG)
+        return t.value, c.value, d.value
+
+    def hllc_errors(self) -> int:
+        n = C.c_int64()
+        check(lib().hf_uns_hllc_errors(self._h, C.byref(n)), self._h, _MSG)
+        return n.value
+
+    def stream(self) -> int:
+        s = C.c_void_p()
+        check(lib().hf_uns_stream(self._h, C.byref(s)), self._h, _MSG)
+        return s.value or 0

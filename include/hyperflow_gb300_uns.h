@@ -1,0 +1,65 @@
+/* HyperFlow-GB300 -- C ABI of the unstructured (triangle / quadrilateral) GPU time step.
+ *
+ * Drop-in for the reference's unstructured solver step (qcrm/HyperFlow, src/fvm_2d_uns):
+ *     TimeStep::operator()(mesh)            src/fvm_2d_uns/scheme/timestep/timestep.cpp:29-62
+ *     ODESolver(GodunovScheme::operator())  src/fvm_2d_uns/scheme/godunov/godunov.cpp:31-77,
+ *                                           src/fvm_2d_uns/scheme/ode/forward_euler/forward_euler.cpp
+ * as driven by Simulation::solve (src/fvm_2d_uns/simulation/simulation/simulation.cpp:61-120).
+ * Status codes are the HF_* codes of hyperflow_gb300.h.  Cell states are SoA [4][ncells]
+ * (rho, rho*u, rho*v, E) in the mesh file's cell order.
+ */
+#ifndef HYPERFLOW_GB300_UNS_H
+#define HYPERFLOW_GB300_UNS_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#include "hyperflow_gb300.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct hf_uns hf_uns;
+
+/* Parses the unstructured case file (keys of src/fvm_2d_uns/simulation/parser/parser.cpp:
+ * model, mesh.{type,file,boundaries.inlet}, initial_condition, scheme, simulation) and loads
+ * mesh.file.  Replaces JSONParser::generate_mesh + LoadStructuredMesh
+ * (src/fvm_2d_uns/mesh/mesh_structured/mesh_structured.cpp:23-122): same text format, cells
+ * of 3 or 4 vertices, neighbours found by hashing edge endpoints instead of the O(E^2) scan.
+ * On failure *out may still be set (for hf_uns_last_error_message); destroy it. */
+int hf_uns_create(const char* case_json, size_t len, hf_uns** out);
+/* same, with the mesh text passed in memory instead of read from mesh.file */
+int hf_uns_create_mesh(const char* case_json, size_t len, const char* mesh_text, size_t mesh_len,
+                       hf_uns** out);
+void hf_uns_destroy(hf_uns* u);
+const char* hf_uns_last_error_message(const hf_uns* u);
+
+/* cell and (cell, edge)-pair counts (Mesh::get_cells / get_cell_edge_indices, mesh.cpp) */
+int hf_uns_sizes(const hf_uns* u, int64_t* ncells, int64_t* npairs);
+/* host copies of the loaded mesh: CSR pair starts, neighbour per pair (cell index or the
+ * negative BoundaryCondition code of src/fvm_2d_uns/scheme/boundary/boundary.h:12), and
+ * the reference's geometry (Edge outward-normal angle in degrees and length, edge.cpp:98-218;
+ * Polygon signed area and incircle radius, polygon.cpp:72-186).  Null outputs are skipped. */
+int hf_uns_mesh_arrays(const hf_uns* u, int32_t* pair_start, int32_t* nbr, double* angle,
+                       double* length, double* area, double* rin);
+
+/* Mesh::set_cells_flow_values / get_cells_flow_values (src/fvm_2d_uns/mesh/mesh/mesh.cpp:153-168) */
+int hf_uns_set_state(hf_uns* u, const double* cons);
+int hf_uns_get_state(hf_uns* u, double* cons);
+
+/* TimeStep::operator() (uns timestep.cpp:29-62): advances the call counter */
+int hf_uns_time_step(hf_uns* u, double* dt);
+/* ODESolver(Scheme()) + set_cells_flow_values with the given dt (simulation.cpp:103-105) */
+int hf_uns_advance(hf_uns* u, double dt);
+/* n steps of the loop body on the device (dt stays on the device); clamp_t_end stops at t_end */
+int hf_uns_run(hf_uns* u, int64_t n, int clamp_t_end, int use_graph, int64_t* steps_done);
+
+int hf_uns_get_time(hf_uns* u, double* t, int64_t* calls, double* last_dt);
+int hf_uns_hllc_errors(hf_uns* u, int64_t* count);
+int hf_uns_stream(hf_uns* u, void** stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -139,7 +139,51 @@ def make_units():
     print("units", len(UL), len(r))
 
 
+def quad_channel(nx=24, ny=10, seed=4):
+    """A quadrilateral channel mesh in the reference's quad format: jittered interior
+    vertices, inlet on the left, transmissive right, reflective top and bottom."""
+    rng = np.random.default_rng(seed)
+    xs = np.linspace(0.0, 2.4, nx + 1)
+    ys = np.linspace(0.0, 1.0, ny + 1)
+    X, Y = np.meshgrid(xs, ys, indexing="ij")
+    inner = (slice(1, nx), slice(1, ny))
+    X[inner] += rng.uniform(-0.2, 0.2, X[inner].shape) * (xs[1] - xs[0])
+    Y[inner] += rng.uniform(-0.2, 0.2, Y[inner].shape) * (ys[1] - ys[0])
+    verts, codes = [], []
+    for i in range(nx):
+        for j in range(ny):
+            v = [(X[i, j], Y[i, j]), (X[i + 1, j], Y[i + 1, j]), (X[i + 1, j + 1], Y[i + 1, j + 1]),
+                 (X[i, j + 1], Y[i, j + 1])]
+            verts.append(v)
+            # edges: bottom, right, top, left
+            codes.append([-1 if j == 0 else 0, -2 if i == nx - 1 else 0, -1 if j == ny - 1 else 0,
+                          -3 if i == 0 else 0])
+    return np.array(verts, dtype=np.float64), np.array(codes, dtype=np.int32)
+
+
+def make_uns():
+    from hyperflow_gb300 import meshgen
+    sets = [("tri_hole_3k", *meshgen.jittered_hole_mesh(3000, seed=3), 40, 0.5),
+            ("quad_channel_240", *quad_channel(), 60, 0.5)]
+    for name, verts, codes, steps, cfl in sets:
+        nbr = meshgen.match_neighbours(verts, codes)
+        case = meshgen.channel_case("mesh.hmsh", cfl=cfl)
+        nverts = np.full(len(verts), verts.shape[1], np.int32)
+        ref = oracle.RefUns(case, nverts, verts.reshape(-1, 2), nbr)
+        ang, ln, area, rin = ref.geometry()
+        ref.run(steps)
+        np.savez_compressed(os.path.join(HERE, f"uns_{name}.npz"), case=json.dumps(case),
+                            verts=verts, codes=codes, nbr=nbr, steps=steps, dts=ref.dts(),
+                            U=ref.state(), angle=ang, length=ln, area=area, rin=rin)
+        print("uns", name, len(verts), "cells", steps, "steps")
+
+
 if __name__ == "__main__":
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref"], check=True)
-    make_units()
-    make_cart()
+    which = sys.argv[1:] or ["units", "cart", "uns"]
+    if "units" in which:
+        make_units()
+    if "cart" in which:
+        make_cart()
+    if "uns" in which:
+        make_uns()

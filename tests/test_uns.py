@@ -1,0 +1,123 @@
+"""Unstructured Godunov + HLLC step (src/fvm_2d_uns): oracle against the reference's
+fixtures (CPU), and the CUDA path against both (GPU), bit for bit."""
+import glob
+import json
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+
+def uns_names():
+    return sorted(os.path.basename(p)[4:-4] for p in glob.glob(os.path.join(GOLDEN, "uns_*.npz")))
+
+
+def load(name):
+    d = np.load(os.path.join(GOLDEN, f"uns_{name}.npz"))
+    g = {k: d[k] for k in d.files}
+    g["case"] = json.loads(str(g["case"]))
+    return g
+
+
+def _inlet(case):
+    from oracle.oracle import prim_to_cons
+    return prim_to_cons(case["mesh"]["boundaries"]["inlet"])
+
+
+@pytest.mark.parametrize("name", uns_names())
+def test_uns_oracle_matches_reference_fixture(name, port_lib):
+    from oracle import oracle
+    from hyperflow_gb300 import meshgen
+    g = load(name)
+    V, codes = g["verts"], g["codes"]
+    nbr = meshgen.match_neighbours(V, codes)
+    np.testing.assert_array_equal(nbr, g["nbr"])
+    nverts = np.full(len(V), V.shape[1], np.int32)
+    ang, ln, area, rin = oracle.uns_geometry(nverts, V.reshape(-1, 2))
+    for a, b in ((ang, "angle"), (ln, "length"), (area, "area"), (rin, "rin")):
+        np.testing.assert_array_equal(a, g[b])
+    U = np.zeros((4, len(V)))
+    U[:] = oracle.prim_to_cons(g["case"]["initial_condition"]["init_state"])[:, None]
+    ps = np.concatenate([[0], np.cumsum(nverts)]).astype(np.int32)
+    dts, calls = oracle.uns_run(1.4, g["case"]["simulation"]["cfl"], 0, ps, nbr, ang, ln, area, rin,
+                                _inlet(g["case"]), U, int(g["steps"]), nthreads=4)
+    np.testing.assert_array_equal(dts, g["dts"])
+    np.testing.assert_array_equal(U, g["U"])
+
+
+def test_mesh_text_round_trip():
+    from hyperflow_gb300 import meshgen
+    V, codes = meshgen.jittered_hole_mesh(500, seed=9)
+    text = meshgen.hmsh_text(V, codes)
+    lines = text.splitlines()
+    assert lines[0] == "CELLS" and int(lines[1]) == len(V)
+    back = np.array([[float(x) for x in l.split()] for l in lines[2:2 + len(V)]]).reshape(V.shape)
+    np.testing.assert_array_equal(back, V)
+
+
+def test_generator_is_canonical():
+    from hyperflow_gb300 import meshgen
+    a = meshgen.jittered_hole_mesh(2000, seed=5)
+    b = meshgen.jittered_hole_mesh(2000, seed=5)
+    np.testing.assert_array_equal(a[0], b[0])
+    np.testing.assert_array_equal(a[1], b[1])
+    V = a[0]
+    cross = (V[:, 1, 0] - V[:, 0, 0]) * (V[:, 2, 1] - V[:, 0, 1]) - \
+            (V[:, 1, 1] - V[:, 0, 1]) * (V[:, 2, 0] - V[:, 0, 0])
+    assert (cross > 0).all()                       # counter-clockwise
+    assert set(np.unique(a[1])) == {0, -1, -2, -3}  # interior, wall, outflow, inlet
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", uns_names())
+def test_uns_gpu_matches_reference_fixture(name):
+    from hyperflow_gb300 import UnsSolver, meshgen
+    g = load(name)
+    s = UnsSolver(g["case"], mesh_text=meshgen.hmsh_text(g["verts"], g["codes"]))
+    m = s.mesh_arrays()
+    np.testing.assert_array_equal(m["nbr"], g["nbr"])
+    for k in ("angle", "length", "area", "rin"):
+        np.testing.assert_array_equal(m[k], g[k])
+    dts = []
+    for _ in range(int(g["steps"])):
+        dts.append(s.calculate_time_step())
+        s.advance(dts[-1])
+    np.testing.assert_array_equal(np.array(dts), g["dts"])
+    np.testing.assert_array_equal(s.state(), g["U"])
+
+
+@pytest.mark.gpu
+def test_uns_gpu_device_loop_equals_piecewise():
+    from hyperflow_gb300 import UnsSolver, meshgen
+    g = load("tri_hole_3k")
+    text = meshgen.hmsh_text(g["verts"], g["codes"])
+    a, b = UnsSolver(g["case"], mesh_text=text), UnsSolver(g["case"], mesh_text=text)
+    a.run(int(g["steps"]), graph=True)
+    np.testing.assert_array_equal(a.state(), g["U"])
+    b.run(int(g["steps"]), graph=False)
+    np.testing.assert_array_equal(b.state(), g["U"])
+    assert a.time()[1] == int(g["steps"])
+
+
+@pytest.mark.gpu
+def test_uns_gpu_full_size_matches_oracle(tmp_path):
+    """The ~1M-triangle circular-hole channel (Mach 2, CFL 0.5), read from a mesh file
+    as the reference reads it, against the oracle on all host cores."""
+    from hyperflow_gb300 import UnsSolver, meshgen
+    from oracle import oracle
+    V, codes = meshgen.jittered_hole_mesh(1_000_000, seed=0)
+    path = tmp_path / "channel.hmsh"
+    meshgen.write_hmsh(str(path), V, codes)
+    case = meshgen.channel_case(str(path), cfl=0.5)
+    s = UnsSolver(case)
+    assert 950_000 < s.ncells < 1_050_000
+    m = s.mesh_arrays()
+    steps = 20
+    s.run(steps)
+    U = np.zeros((4, s.ncells))
+    U[:] = oracle.prim_to_cons(case["initial_condition"]["init_state"])[:, None]
+    dts, _ = oracle.uns_run(1.4, 0.5, 0, m["pair_start"], m["nbr"], m["angle"], m["length"], m["area"],
+                            m["rin"], _inlet(case), U, steps, nthreads=os.cpu_count() or 4)
+    np.testing.assert_array_equal(s.state(), U)
