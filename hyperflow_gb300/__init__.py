@@ -4,4 +4,5 @@ behind a C ABI (include/hyperflow_gb300.h)."""
 from ._lib import HyperFlowError, lib  # noqa: F401
 from .solver import CartSolver  # noqa: F401
 from .uns import UnsSolver  # noqa: F401
+from .batch import BatchSolver  # noqa: F401
 from . import cases  # noqa: F401

@@ -57,6 +57,23 @@ SIGNATURES = {
     "hf_uns_hllc_errors": (_i, [_p, C.POINTER(_i64)]),
     "hf_uns_stream": (_i, [_p, C.POINTER(_p)]),
     "hf_last_error_message": (C.c_char_p, [_p]),
+    # batched (include/hyperflow_gb300_batch.h)
+    "hf_batch_create": (_i, [C.c_char_p, _sz, C.POINTER(_p)]),
+    "hf_batch_destroy": (None, [_p]),
+    "hf_batch_last_error_message": (C.c_char_p, [_p]),
+    "hf_batch_sizes": (_i, [_p, C.POINTER(_i), C.POINTER(_i64)]),
+    "hf_batch_instance_side": (_i, [_p, _i, C.POINTER(_i)]),
+    "hf_batch_num_configs": (_i, [C.POINTER(_i)]),
+    "hf_batch_config_info": (_i, [_i, C.POINTER(_i), C.POINTER(_i), C.POINTER(_i), C.POINTER(_i)]),
+    "hf_batch_set_config": (_i, [_p, _i]),
+    "hf_batch_autotune": (_i, [_p, _i, C.POINTER(_i), _p]),
+    "hf_batch_run": (_i, [_p, _i64, _i]),
+    "hf_batch_sync": (_i, [_p]),
+    "hf_batch_get_state": (_i, [_p, _i, _p]),
+    "hf_batch_set_state": (_i, [_p, _i, _p]),
+    "hf_batch_instance_time": (_i, [_p, _i, C.POINTER(_d), C.POINTER(_d)]),
+    "hf_batch_counters": (_i, [_p, C.POINTER(_i64), C.POINTER(_i64), C.POINTER(_i64)]),
+    "hf_batch_stream": (_i, [_p, C.POINTER(_p)]),
 }
 
 _lib = None

@@ -115,6 +115,27 @@ def forward_facing_step_case(cells_per_unit: int = 1365, limiter: str = "MinBee"
     }
 
 
+def batch_manifest(count: int = 512, seed: int = 0, side_min: int = 64, side_max: int = 1024,
+                   limiter: str = "MinBee", cfl: float = 0.8) -> dict:
+    """The batched workload: `count` independent square four-quadrant Riemann problems on
+    [0,1]^2, sides log-uniform in [side_min, side_max] (rounded), split point uniform in
+    [0.3,0.7]^2, and per quadrant rho ~ U[0.1,2], p ~ U[0.1,10], u, v ~ U[-1,1]
+    (primitive), transmissive on every side, MUSCL-Hancock + HLLC.  Seeded."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(count):
+        n = int(round(math.exp(rng.uniform(math.log(side_min), math.log(side_max)))))
+        split = (float(rng.uniform(0.3, 0.7)), float(rng.uniform(0.3, 0.7)))
+        states = []
+        for _q in range(4):
+            states.append([float(rng.uniform(0.1, 2.0)), float(rng.uniform(-1.0, 1.0)),
+                           float(rng.uniform(-1.0, 1.0)), float(rng.uniform(0.1, 10.0))])
+        out.append(quadrant_case(n, scheme="MUSCLHancock", limiter=limiter, cfl=cfl, split=split,
+                                 states=states))
+    return {"cases": out}
+
+
 def to_json(case: dict) -> str:
     return json.dumps(case, indent=1)
 
@@ -123,5 +144,5 @@ def total_cells(case: dict) -> int:
     return sum(b["x_cells"] * b["y_cells"] for b in case["mesh"]["blocks"])
 
 
-__all__ = ["quadrant_case", "forward_facing_step_case", "to_json", "total_cells",
+__all__ = ["quadrant_case", "forward_facing_step_case", "batch_manifest", "to_json", "total_cells",
            "QUAD_NE", "QUAD_NW", "QUAD_SW", "QUAD_SE", "GAMMA", "math"]

@@ -106,13 +106,15 @@ int fail(hf_ctx* c, int code, const std::string& msg) {
             return fail(ctx, HF_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
     } while (0)
 
+}  // namespace
+
 // ---- initial conditions (setup only; same formulas as the reference) --------------
 // MeshBlock::calculate_centroids (mesh_block.cpp:239-257) + initialise_field_values
 // (215-224); the per-type field functions of quadrp.cpp:49-64, doublerp.cpp:42-55,
 // sphericalrp.cpp:62-72, constant.cpp:34-40; the parser's prim->cons conversions
 // (parser.cpp:311-428).
-void build_initial_state(const Json& ic, double gamma, const BlockHost& B, int g,
-                         std::vector<double>& soa) {
+void hf::build_initial_state(const Json& ic, double gamma, const BlockGeom& B, int g,
+                             std::vector<double>& soa) {
     soa.assign((size_t)4 * B.ty * B.tx, 0.0);
     const std::string type = ic["type"].string();
     const bool prim = ic.has("variables") && ic["variables"].string() == "Primitive";
@@ -180,6 +182,8 @@ void build_initial_state(const Json& ic, double gamma, const BlockHost& B, int g
             for (int v = 0; v < 4; ++v) soa[((size_t)v * B.ty + j) * B.tx + i] = s[v];
         }
 }
+
+namespace {
 
 int parse_case(hf_ctx* ctx, const Json& cfg) {
     const Json& model = cfg["model"];
@@ -445,7 +449,9 @@ int hf_create(const char* case_json, size_t len, hf_ctx** out) {
     try {
         for (int b = 0; b < ctx->nblocks; ++b) {
             std::vector<double> soa;
-            build_initial_state(cfg["initial_condition"], ctx->gamma, ctx->blocks[b], ctx->ghost, soa);
+            hf::BlockGeom G{ctx->blocks[b].tx, ctx->blocks[b].ty, ctx->blocks[b].xl, ctx->blocks[b].yb,
+                            ctx->blocks[b].dx, ctx->blocks[b].dy};
+            hf::build_initial_state(cfg["initial_condition"], ctx->gamma, G, ctx->ghost, soa);
             r = hf_set_state(ctx, b, soa.data(), HF_LAYOUT_SOA);
             if (r != HF_OK) return r;
         }

@@ -16,6 +16,7 @@
 
 #include "hf_cart.h"
 #include "hf_device.cuh"
+#include "hf_mh_tile.cuh"
 
 namespace hf {
 
@@ -212,12 +213,6 @@ __global__ void finalize_kernel(Ctrl* c) {
 // ------------------------------------------------------------------------------------
 // shared helpers for the stencils
 // ------------------------------------------------------------------------------------
-// A face on a tile edge is formed by both tiles that share it, and partial tiles form
-// faces past the block.  Only the owner counts an HLLC zero-flux fallback, so the count
-// equals the reference's: face index gf (0..n along the normal) of row gr, local index lf.
-__device__ __forceinline__ bool owned_face(int gf, int lf, int T, int n, int gr, int nr) {
-    return gr < nr && gf <= n && (lf < T || gf == n);
-}
 // issue the tile's TMA load and wait for it (bounded); false if the wait gave up
 template <int NBYTES>
 __device__ __forceinline__ bool load_tile(double* sU, uint64_t* bar, const CUtensorMap* tm, int x0,
@@ -246,16 +241,14 @@ __device__ __forceinline__ bool load_tile(double* sU, uint64_t* bar, const CUten
 // ------------------------------------------------------------------------------------
 template <int TX, int TY>
 struct MhLayout {
-    static constexpr int UX = TX + 4, UY = TY + 4;
-    static constexpr int AXN = (TX + 2) * TY, AYN = TX * (TY + 2);
-    static constexpr int AN = AXN > AYN ? AXN : AYN;
+    using T = MhTile<TX, TY>;
     static constexpr int U_OFF = 0;
-    static constexpr int A_OFF = U_OFF + 4 * UY * UX;
-    static constexpr int F_OFF = A_OFF + 8 * AN;
-    static constexpr int G_OFF = F_OFF + 4 * TY * (TX + 1);
-    static constexpr int END = G_OFF + 4 * (TY + 1) * TX;
+    static constexpr int A_OFF = U_OFF + T::U_SIZE;
+    static constexpr int F_OFF = A_OFF + T::A_SIZE;
+    static constexpr int G_OFF = F_OFF + T::F_SIZE;
+    static constexpr int END = G_OFF + T::G_SIZE;
     static constexpr size_t BYTES = (size_t)END * 8 + 16;   // + mbarrier
-    static constexpr int TMA_BYTES = 4 * UY * UX * 8;
+    static constexpr int TMA_BYTES = T::U_SIZE * 8;
 };
 
 template <int TX, int TY, int LIM, int NT>
@@ -288,90 +281,7 @@ __global__ void __launch_bounds__(NT) mh_kernel(Ctrl* __restrict__ c, const Mesh
 
     if (!load_tile<L::TMA_BYTES>(sU, bar, p ? &tm1 : &tm0, x0, y0, c)) return;
 
-    int herr = 0;
-    // x phase: slopes, extrapolation, half-step predictor of the x face pair, cells -1..TX
-    for (int it = threadIdx.x; it < L::AXN; it += NT) {
-        const int lx = it % (TX + 2), ly = it / (TX + 2);
-        const int sx = lx + 1, sy = ly + 2;
-        double e0[4], e1[4];
-#pragma unroll
-        for (int v = 0; v < 4; ++v) {
-            const double* row = sU + (v * L::UY + sy) * L::UX;
-            const double u0 = row[sx];
-            const double s = slope<LIM>(row[sx - 1], u0, row[sx + 1]);
-            e0[v] = u0 - 0.5 * s;
-            e1[v] = u0 + 0.5 * s;
-        }
-        Prim w0 = to_prim(g1, e0[0], e0[1], e0[2], e0[3]);
-        Prim w1 = to_prim(g1, e1[0], e1[1], e1[2], e1[3]);
-        double f0[4], f1[4];
-        flux<0>(w0, f0);
-        flux<0>(w1, f1);
-#pragma unroll
-        for (int v = 0; v < 4; ++v) {
-            const double d = hdx * (f0[v] - f1[v]);
-            sA[(0 * 4 + v) * L::AN + it] = e0[v] + d;
-            sA[(1 * 4 + v) * L::AN + it] = e1[v] + d;
-        }
-    }
-    __syncthreads();
-    // x faces 0..TX of each tile row (face f is the left face of output cell f)
-    for (int it = threadIdx.x; it < (TX + 1) * TY; it += NT) {
-        const int fx = it % (TX + 1), fy = it / (TX + 1);
-        const int al = fy * (TX + 2) + fx;
-        double UL[4], UR[4], F[4];
-#pragma unroll
-        for (int v = 0; v < 4; ++v) {
-            UL[v] = sA[(1 * 4 + v) * L::AN + al];
-            UR[v] = sA[(0 * 4 + v) * L::AN + al + 1];
-        }
-        const int bad = hllc_cons<0>(g, g1, UL, UR, F);
-        herr += bad && owned_face(x0 + fx, fx, TX, B.nx, y0 + fy, B.ny);
-#pragma unroll
-        for (int v = 0; v < 4; ++v) sF[(v * TY + fy) * (TX + 1) + fx] = F[v];
-    }
-    __syncthreads();
-    // y phase, cells -1..TY of each tile column
-    for (int it = threadIdx.x; it < L::AYN; it += NT) {
-        const int lx = it % TX, ly = it / TX;
-        const int sx = lx + 2, sy = ly + 1;
-        double e2[4], e3[4];
-#pragma unroll
-        for (int v = 0; v < 4; ++v) {
-            const double* col = sU + (v * L::UY + sy) * L::UX + sx;
-            const double u0 = col[0];
-            const double s = slope<LIM>(col[-L::UX], u0, col[L::UX]);
-            e2[v] = u0 - 0.5 * s;
-            e3[v] = u0 + 0.5 * s;
-        }
-        Prim w2 = to_prim(g1, e2[0], e2[1], e2[2], e2[3]);
-        Prim w3 = to_prim(g1, e3[0], e3[1], e3[2], e3[3]);
-        double f2[4], f3[4];
-        flux<1>(w2, f2);
-        flux<1>(w3, f3);
-#pragma unroll
-        for (int v = 0; v < 4; ++v) {
-            const double d = hdy * (f2[v] - f3[v]);
-            sA[(0 * 4 + v) * L::AN + it] = e2[v] + d;
-            sA[(1 * 4 + v) * L::AN + it] = e3[v] + d;
-        }
-    }
-    __syncthreads();
-    // y faces 0..TY of each tile column
-    for (int it = threadIdx.x; it < TX * (TY + 1); it += NT) {
-        const int gx = it % TX, gy = it / TX;
-        double UB[4], UT[4], F[4];
-#pragma unroll
-        for (int v = 0; v < 4; ++v) {
-            UB[v] = sA[(1 * 4 + v) * L::AN + gy * TX + gx];
-            UT[v] = sA[(0 * 4 + v) * L::AN + (gy + 1) * TX + gx];
-        }
-        const int bad = hllc_cons<1>(g, g1, UB, UT, F);
-        herr += bad && owned_face(y0 + gy, gy, TY, B.ny, x0 + gx, B.nx);
-#pragma unroll
-        for (int v = 0; v < 4; ++v) sG[(v * (TY + 1) + gy) * TX + gx] = F[v];
-    }
-    __syncthreads();
+    const int herr = mh_tile_fluxes<TX, TY, NT, LIM>(sU, sA, sF, sG, g, g1, hdx, hdy, x0, y0, B.nx, B.ny);
     // conservative update + forward Euler, and the next step's TimeStep terms
     double* __restrict__ out = B.buf[p ^ 1];
     const size_t plane = (size_t)B.ty * B.pitch;
@@ -384,11 +294,7 @@ __global__ void __launch_bounds__(NT) mh_kernel(Ctrl* __restrict__ c, const Mesh
             const size_t o = (size_t)(gyy + 2) * B.pitch + (gxx + 2);
 #pragma unroll
             for (int v = 0; v < 4; ++v) {
-                const double Lv = (one_dx * (sF[(v * TY + oy) * (TX + 1) + ox] -
-                                             sF[(v * TY + oy) * (TX + 1) + ox + 1])) +
-                                  (one_dy * (sG[(v * (TY + 1) + oy) * TX + ox] -
-                                             sG[(v * (TY + 1) + oy + 1) * TX + ox]));
-                un[v] = dt * Lv + sU[(v * L::UY + oy + 2) * L::UX + ox + 2];
+                un[v] = mh_update<TX, TY>(sU, sF, sG, v, ox, oy, dt, one_dx, one_dy);
                 out[v * plane + o] = un[v];
             }
             double sx, sy;

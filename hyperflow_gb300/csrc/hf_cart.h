@@ -5,7 +5,10 @@
 #include <cuda.h>
 #include <cuda_runtime.h>
 
+#include <vector>
+
 #include "hf_ctrl.h"
+#include "hf_json.hpp"
 
 namespace hf {
 
@@ -47,5 +50,18 @@ cudaError_t launch_stencil(Ctrl* c, const MeshDev* m, int b, int nx, int ny, int
 // halo-tile box of the stencil for the scheme (TMA box = tile + 2*ghost per axis)
 StencilTiles stencil_tiles(int scheme);
 cudaError_t stencil_prepare();   // sets the large dynamic shared-memory opt-ins once
+
+// geometry of one block as the initial condition needs it
+struct BlockGeom {
+    int tx, ty;          // total cells incl. ghosts
+    double xl, yb;       // lower-left corner of the interior
+    double dx, dy;
+};
+// The case's initial condition on one block's interior (MeshBlock::calculate_centroids +
+// initialise_field_values, mesh_block.cpp:215-257; the IC classes of
+// src/fvm_2d_cart/simulation/initcon; the parser's prim->cons conversions).  SoA
+// [4][ty][tx] with zero ghosts.  Throws std::invalid_argument for an unknown IC type.
+void build_initial_state(const Json& ic, double gamma, const BlockGeom& B, int ghost,
+                         std::vector<double>& soa);
 
 }  // namespace hf

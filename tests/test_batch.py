@@ -1,0 +1,98 @@
+"""Batched MUSCL-Hancock (one persistent cooperative launch per run of steps): every case
+must equal the reference step run on that case alone -- here the oracle, bit for bit --
+for every launch configuration, with and without the CUDA graph."""
+import numpy as np
+import pytest
+
+
+def test_manifest_matches_the_workload_spec():
+    from hyperflow_gb300 import cases
+    m = cases.batch_manifest(512, seed=0)
+    assert len(m["cases"]) == 512
+    sides = np.array([c["mesh"]["blocks"][0]["x_cells"] for c in m["cases"]])
+    assert sides.min() >= 64 and sides.max() <= 1024
+    # log-uniform: the median side is near sqrt(64 * 1024) = 256
+    assert 200 < np.median(sides) < 330
+    for c in m["cases"][:50]:
+        ic = c["initial_condition"]
+        assert 0.3 <= ic["x_interface"] <= 0.7 and 0.3 <= ic["y_interface"] <= 0.7
+        for k in ("init_ne_state", "init_nw_state", "init_sw_state", "init_se_state"):
+            r, u, v, p = ic[k]
+            assert 0.1 <= r <= 2 and -1 <= u <= 1 and -1 <= v <= 1 and 0.1 <= p <= 10
+        assert all(b["type"] == "Transmissive" for b in c["mesh"]["blocks"][0]["boundaries"].values())
+    assert cases.batch_manifest(8, seed=3) == cases.batch_manifest(8, seed=3)
+
+
+def _oracle_interior(case, steps):
+    from oracle.oracle import Oracle
+    o = Oracle(case, nthreads=4)
+    o.run(steps)
+    return o.state(0)[:, 2:-2, 2:-2], o.t
+
+
+@pytest.mark.gpu
+def test_batch_every_config_matches_oracle(port_lib):
+    from hyperflow_gb300 import BatchSolver, cases
+    from hyperflow_gb300.batch import configs
+    m = cases.batch_manifest(10, seed=7, side_min=64, side_max=100)
+    steps = 25
+    ref = [_oracle_interior(c, steps) for c in m["cases"]]
+    for k in range(len(configs())):
+        b = BatchSolver(m)
+        b.set_config(k)
+        b.run(steps, graph=False)
+        b.sync()
+        for i in range(b.ninstances):
+            np.testing.assert_array_equal(b.state(i), ref[i][0], err_msg=f"config {k} case {i}")
+            assert b.instance_time(i)[0] == ref[i][1]
+        assert b.counters()["calls"] == 2 * steps
+
+
+@pytest.mark.gpu
+def test_batch_graph_and_chunks_equal_single_launch(port_lib):
+    from hyperflow_gb300 import BatchSolver, cases
+    m = cases.batch_manifest(6, seed=11, side_min=64, side_max=90, limiter="VanLeer")
+    a, b = BatchSolver(m), BatchSolver(m)
+    a.run(30, graph=False)
+    for _ in range(3):
+        b.run(10, graph=True)       # one captured 10-step launch, replayed
+    b.sync()
+    for i in range(a.ninstances):
+        np.testing.assert_array_equal(a.state(i), b.state(i))
+    ref, _ = _oracle_interior(m["cases"][0], 30)
+    np.testing.assert_array_equal(a.state(0), ref)
+
+
+@pytest.mark.gpu
+def test_batch_autotune_restores_state(port_lib):
+    from hyperflow_gb300 import BatchSolver, cases
+    m = cases.batch_manifest(8, seed=2, side_min=64, side_max=128)
+    b = BatchSolver(m)
+    b.run(3, graph=False)
+    before = [b.state(i) for i in range(b.ninstances)]
+    best, ms = b.autotune(steps_per_trial=2)
+    assert 0 <= best < len(ms) and (ms > 0).all()
+    for i in range(b.ninstances):
+        np.testing.assert_array_equal(b.state(i), before[i])
+    b.run(5, graph=True)
+    b.sync()
+    ref, _ = _oracle_interior(m["cases"][1], 8)
+    np.testing.assert_array_equal(b.state(1), ref)
+
+
+@pytest.mark.gpu
+def test_batch_full_workload_sample_matches_oracle(port_lib):
+    """The 512-case workload (sides 64..1024), 3 steps; a seeded sample of cases plus the
+    smallest and largest checked against the oracle."""
+    from hyperflow_gb300 import BatchSolver, cases
+    m = cases.batch_manifest(512, seed=0)
+    b = BatchSolver(m)
+    assert b.ninstances == 512
+    b.run(3, graph=True)
+    b.sync()
+    sides = np.array(b.sides)
+    rng = np.random.default_rng(1)
+    pick = set(rng.choice(512, 12, replace=False).tolist()) | {int(sides.argmin()), int(sides.argmax())}
+    for i in sorted(pick):
+        ref, t = _oracle_interior(m["cases"][i], 3)
+        np.testing.assert_array_equal(b.state(i), ref, err_msg=f"case {i} side {sides[i]}")
