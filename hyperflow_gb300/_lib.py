@@ -14,7 +14,7 @@ LIB_PATH = os.path.join(PKG, "libhyperflow_gb300.so")
 HF_OK = 0
 STATUS = {0: "ok", 1: "bad argument", 2: "case file parse error", 3: "unsupported case",
           4: "CUDA error", 5: "device error word raised", 6: "call out of order",
-          7: "no CUDA device"}
+          7: "no CUDA device", 8: "problem exceeds the fixed-size working area"}
 
 LAYOUT_SOA = 0
 LAYOUT_AOS_XY = 1
@@ -41,6 +41,7 @@ SIGNATURES = {
     "hf_profile": (_i, [_p, _i]),
     "hf_kernel_time": (_i, [_p, _i, C.POINTER(_d), C.POINTER(_i64)]),
     "hf_status_string": (C.c_char_p, [_i]),
+    "hf_time_step_noalloc": (_i, [_p, _i, _i, _i, _d, _d, _d, _d, _i64, _p, _p]),
     # unstructured (include/hyperflow_gb300_uns.h)
     "hf_uns_create": (_i, [C.c_char_p, _sz, C.POINTER(_p)]),
     "hf_uns_create_mesh": (_i, [C.c_char_p, _sz, C.c_char_p, _sz, C.POINTER(_p)]),

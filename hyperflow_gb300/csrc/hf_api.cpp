@@ -367,6 +367,7 @@ const char* hf_status_string(int s) {
         case HF_ERR_DEVICE: return "device error word raised";
         case HF_ERR_STATE: return "call out of order";
         case HF_ERR_NO_DEVICE: return "no CUDA device";
+        case HF_ERR_TOO_LARGE: return "problem exceeds the fixed-size working area";
         default: return "unknown status";
     }
 }

@@ -33,7 +33,8 @@ enum {
     HF_ERR_CUDA = 4,         /* a CUDA runtime call failed (see hf_last_error_message) */
     HF_ERR_DEVICE = 5,       /* a kernel raised its error word (bounded wait timed out, ...) */
     HF_ERR_STATE = 6,        /* call out of order (e.g. advancing block 2 before block 1) */
-    HF_ERR_NO_DEVICE = 7     /* no CUDA device is visible */
+    HF_ERR_NO_DEVICE = 7,    /* no CUDA device is visible */
+    HF_ERR_TOO_LARGE = 8     /* the problem exceeds a fixed-size working area */
 };
 
 /* state layouts for hf_set_state / hf_get_state */
@@ -101,6 +102,20 @@ int hf_stream(hf_ctx* ctx, void** stream);
  * the last reset.  kind 0 = stencil (Godunov/MUSCL-Hancock), 1 = ghost fill + CFL. */
 int hf_profile(hf_ctx* ctx, int enable);
 int hf_kernel_time(hf_ctx* ctx, int kind, double* ms, int64_t* launches);
+
+/* The CFL time step of one block for callers that cannot allocate device memory (a
+ * pool-managed application, a no-allocation time loop).  No counterpart in the reference:
+ * it computes what TimeStep::operator() computes, over all total_x * total_y cells of one
+ * block given as SoA FP64 [4][total_y][pitch] in device memory, for TimeStep call number
+ * call_index (0-based; the first 10 calls use 0.2 * cfl), and writes dt to the device word
+ * d_dt on `stream` (a cudaStream_t; 0 = default stream).  It allocates nothing: its only
+ * working memory is a 64 KiB static device array, so it handles at most 16,777,216 cells
+ * (larger blocks return HF_ERR_TOO_LARGE).  Calls that overlap on the GPU share that array
+ * and race.  The first call on each device looks up the array's address; make it before
+ * any stream capture. */
+int hf_time_step_noalloc(const double* d_cons, int total_x, int total_y, int pitch, double dx,
+                         double dy, double gamma, double cfl, int64_t call_index, double* d_dt,
+                         void* stream);
 
 const char* hf_status_string(int status);
 const char* hf_last_error_message(const hf_ctx* ctx);
