@@ -303,7 +303,7 @@ def main():
             "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (the case's own initial condition: uniform Mach 3 inflow)",
             "config": {"workload": workload_name(args), "cells": cells, "blocks": nb, "limiter": args.limiter,
-                       "cfl": 0.8, "l2": "state 2 x 300 MB > 129 MB L2, no flush needed",
+                       "cfl": 0.8, "l2": "state 2 x 151 MB buffers > 129 MB L2, no flush needed",
                        "parallelism": "replicas" if ws > 1 else "single GPU"},
             "roofline": roof,
             "cpu_baseline": cpu,

@@ -75,6 +75,25 @@ SIGNATURES = {
     "hf_batch_instance_time": (_i, [_p, _i, C.POINTER(_d), C.POINTER(_d)]),
     "hf_batch_counters": (_i, [_p, C.POINTER(_i64), C.POINTER(_i64), C.POINTER(_i64)]),
     "hf_batch_stream": (_i, [_p, C.POINTER(_p)]),
+    # learned coarse solver (include/hyperflow_gb300_learned.h)
+    "hf_lc_create": (_i, [_i, _d, _d, _d, _i, C.POINTER(_p)]),
+    "hf_lc_destroy": (None, [_p]),
+    "hf_lc_last_error_message": (C.c_char_p, [_p]),
+    "hf_lc_num_params": (_i, [C.POINTER(_i)]),
+    "hf_lc_set_params": (_i, [_p, _p]),
+    "hf_lc_get_params": (_i, [_p, _p]),
+    "hf_lc_set_bound": (_i, [_p, _d]),
+    "hf_lc_set_state": (_i, [_p, _p]),
+    "hf_lc_get_state": (_i, [_p, _p]),
+    "hf_lc_set_time": (_i, [_p, _d]),
+    "hf_lc_get_time": (_i, [_p, C.POINTER(_d)]),
+    "hf_lc_cfl_dt": (_i, [_p, C.POINTER(_d)]),
+    "hf_lc_step": (_i, [_p, _d, _i, C.POINTER(_i64)]),
+    "hf_lc_run_to": (_i, [_p, _d, _i, C.POINTER(_i64), C.POINTER(_i64)]),
+    "hf_lc_train_step": (_i, [_p, _p, _p, _p, _d, _d, C.POINTER(_d)]),
+    "hf_lc_mlp_forward": (_i, [_p, _p, _i, _p]),
+    "hf_lc_mlp_backward": (_i, [_p, _p, _p, _i, _p]),
+    "hf_lc_stream": (_i, [_p, C.POINTER(_p)]),
 }
 
 _lib = None

@@ -115,6 +115,28 @@ def forward_facing_step_case(cells_per_unit: int = 1365, limiter: str = "MinBee"
     }
 
 
+def shock_bubble_case(n: int = 2048, scheme: str = "MUSCLHancock", limiter: str = "MinBee",
+                      cfl: float = 0.8, t_end: float = 0.25, mach: float = 1.22,
+                      bubble_density: float = 0.138, radius: float = 0.2, bubble=(0.4, 0.5),
+                      shock_x: float = 0.12) -> dict:
+    """A Mach 1.22 shock moving in +x through still air (rho 1, p 1) onto a circular bubble of
+    density 0.138 and radius 0.2, on [0,1]^2 with transmissive sides (new
+    initial_condition type "ShockBubble"; post-shock state from Rankine-Hugoniot)."""
+    b = _bc("Transmissive")
+    return {
+        "model": {"model": "EulerIdealGas", "gamma": GAMMA},
+        "mesh": {"blocks": [_block(0.0, 1.0, 0.0, 1.0, n, n, b, b, b, b)]},
+        "domain": _domain(0.0, 1.0, 0.0, 1.0),
+        "initial_condition": {
+            "type": "ShockBubble", "variables": "Primitive", "shock_x": shock_x, "mach": mach,
+            "bubble_x": bubble[0], "bubble_y": bubble[1], "bubble_radius": radius,
+            "bubble_density": bubble_density, "ambient_state": [1.0, 0.0, 0.0, 1.0],
+        },
+        "scheme": _scheme(scheme, limiter),
+        "simulation": _simulation(cfl, t_end),
+    }
+
+
 def batch_manifest(count: int = 512, seed: int = 0, side_min: int = 64, side_max: int = 1024,
                    limiter: str = "MinBee", cfl: float = 0.8) -> dict:
     """The batched workload: `count` independent square four-quadrant Riemann problems on
@@ -144,5 +166,5 @@ def total_cells(case: dict) -> int:
     return sum(b["x_cells"] * b["y_cells"] for b in case["mesh"]["blocks"])
 
 
-__all__ = ["quadrant_case", "forward_facing_step_case", "batch_manifest", "to_json", "total_cells",
+__all__ = ["quadrant_case", "forward_facing_step_case", "shock_bubble_case", "batch_manifest", "to_json", "total_cells",
            "QUAD_NE", "QUAD_NW", "QUAD_SW", "QUAD_SE", "GAMMA", "math"]

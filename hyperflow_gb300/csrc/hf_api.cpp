@@ -108,6 +108,39 @@ int fail(hf_ctx* c, int code, const std::string& msg) {
 
 }  // namespace
 
+// Shock-bubble states (no counterpart in the reference).  Keys: shock_x, mach,
+// bubble_x, bubble_y, bubble_radius, bubble_density, ambient_state (primitive rho,u,v,p).
+// The post-shock state follows the Rankine-Hugoniot relations for a shock of Mach number M
+// moving into the ambient gas: p2 = p1 (1 + 2g/(g+1) (M^2 - 1)),
+// rho2 = rho1 (g+1) M^2 / ((g-1) M^2 + 2), u2 = u1 + M c1 (1 - rho1/rho2), c1 = sqrt(g p1/rho1).
+// Outputs: positions (shock_x, bubble_x, bubble_y, radius) and conservative states
+// (post-shock, bubble, ambient).
+namespace {
+void shock_bubble_states(const hf::Json& ic, double g, double& shock_x, double& bx, double& by,
+                         double& r, std::vector<double>& post, std::vector<double>& bub,
+                         std::vector<double>& amb) {
+    shock_x = ic["shock_x"].number();
+    const double M = ic["mach"].number();
+    bx = ic["bubble_x"].number();
+    by = ic["bubble_y"].number();
+    r = ic["bubble_radius"].number();
+    const double rb = ic["bubble_density"].number();
+    std::vector<double> a = read_vec4(ic["ambient_state"]);
+    const double rho1 = a[0], u1 = a[1], v1 = a[2], p1 = a[3];
+    const double c1 = std::sqrt(g * p1 / rho1);
+    const double p2 = p1 * (1.0 + 2.0 * g / (g + 1.0) * (M * M - 1.0));
+    const double rho2 = rho1 * ((g + 1.0) * M * M / ((g - 1.0) * M * M + 2.0));
+    const double u2 = u1 + M * c1 * (1.0 - rho1 / rho2);
+    const double wpost[4] = {rho2, u2, v1, p2}, wbub[4] = {rb, u1, v1, p1}, wamb[4] = {rho1, u1, v1, p1};
+    post.assign(4, 0.0);
+    bub.assign(4, 0.0);
+    amb.assign(4, 0.0);
+    prim_to_cons(g, wpost, post.data());
+    prim_to_cons(g, wbub, bub.data());
+    prim_to_cons(g, wamb, amb.data());
+}
+}  // namespace
+
 // ---- initial conditions (setup only; same formulas as the reference) --------------
 // MeshBlock::calculate_centroids (mesh_block.cpp:239-257) + initialise_field_values
 // (215-224); the per-type field functions of quadrp.cpp:49-64, doublerp.cpp:42-55,
@@ -125,7 +158,7 @@ void hf::build_initial_state(const Json& ic, double gamma, const BlockGeom& B, i
         return c;
     };
     std::vector<double> s0, s1, s2, s3;
-    double p0 = 0, p1 = 0, p2 = 0;
+    double p0 = 0, p1 = 0, p2 = 0, p3 = 0;
     int kind;
     if (type == "Constant") {
         kind = 0;
@@ -152,6 +185,11 @@ void hf::build_initial_state(const Json& ic, double gamma, const BlockGeom& B, i
         p2 = ic["y_origin"].number();
         s0 = cons(ic["init_sphere_state"], true);
         s1 = cons(ic["init_ext_state"], true);
+    } else if (type == "ShockBubble") {
+        // a planar shock of Mach number `mach` moving in +x into the ambient state, and a
+        // circular bubble of another density at the ambient pressure and velocity
+        kind = 4;
+        shock_bubble_states(ic, gamma, p0, p1, p2, p3, s0, s1, s2);
     } else {
         throw std::invalid_argument("initial condition '" + type + "' not supported");
     }
@@ -175,9 +213,14 @@ void hf::build_initial_state(const Json& ic, double gamma, const BlockGeom& B, i
                     else if ((x > p0) && (y <= p1)) s = s3.data();      // SE
                     else s = s0.data();                                  // NE
                     break;
-                default:
+                case 3:
                     s = (((x - p1) * (x - p1) + (y - p2) * (y - p2)) <= (p0 * p0)) ? s0.data()
                                                                                  : s1.data();
+                    break;
+                default:   // shock-bubble: post-shock left of the shock, then bubble, then ambient
+                    if (x <= p0) s = s0.data();
+                    else if (((x - p1) * (x - p1) + (y - p2) * (y - p2)) <= (p3 * p3)) s = s1.data();
+                    else s = s2.data();
             }
             for (int v = 0; v < 4; ++v) soa[((size_t)v * B.ty + j) * B.tx + i] = s[v];
         }

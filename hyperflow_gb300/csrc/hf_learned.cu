@@ -1,0 +1,832 @@
+// Learned coarse solver: an FP32 MUSCL-Hancock + HLLC step on a coarse grid plus a per-face
+// flux correction predicted by a small MLP, trained on box-filtered fine-grid FP64 runs of
+// the plain solver.  C ABI in include/hyperflow_gb300_learned.h.  No counterpart in the
+// reference; the plain part follows the reference's MUSCL-Hancock step
+// (src/fvm_2d_cart/scheme/muscl_hancock/muscl_hancock.cpp:41-376) in FP32 on one block with
+// transmissive sides (ghost cells read as mirrored interior cells).
+//
+// Per face (x faces between cells (i,j),(i+1,j); y faces between (i,j),(i,j+1)):
+//   features: a 4x4 window of cells -- 4 along the face normal (offsets -1..2 from the
+//     lower cell) by 4 along the face (offsets -1..2) -- each as (rho/rho_ref - 1,
+//     u_n/c_ref, u_t/c_ref, p/p_ref - 1) with rho_ref, p_ref the mean of the two face
+//     cells and c_ref = sqrt(gamma p_ref / rho_ref): 64 inputs, rounded to BF16;
+//   MLP: 64 -> 64 (GELU) -> 64 (GELU) -> 4, BF16 weights and activations on the tensor
+//     cores (mma.sync m16n8k16, FP32 accumulation), FP32 biases;
+//   correction: dF = rho_ref c_ref * (o0, o1 c_ref, o2 c_ref, o3 c_ref^2) in the face frame
+//     (normal, tangential), rotated back to (x, y);
+//   guard: a cell whose corrected update has rho <= 0, p <= 0, or a density / energy change
+//     beyond `bound` times the plain update's, rejects the corrections on all its faces (they
+//     fall back to the plain flux); a cell still violating after that takes its plain update.
+// Training: one-step loss L = mean_cells sum_v w_v (U^{n+1}_v - T_v)^2 against the filtered
+// fine solution T; dL/dF flows only through the linear conservative update.  Backward and
+// Adam are hand-written FP32 kernels (weight gradients on the CUDA cores).
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include <cuda_bf16.h>
+
+#include "../../include/hyperflow_gb300_learned.h"
+#include "hf_device.cuh"
+
+namespace hf {
+namespace lc {
+
+constexpr int H = 64;          // hidden width
+constexpr int NIN = 64;        // inputs
+constexpr int NOUT = 4;
+// packed parameter layout (floats): W1[64][64] b1[64] W2[64][64] b2[64] W3[4][64] b3[4]
+constexpr int OFF_W1 = 0, OFF_B1 = OFF_W1 + H * NIN, OFF_W2 = OFF_B1 + H, OFF_B2 = OFF_W2 + H * H,
+              OFF_W3 = OFF_B2 + H, OFF_B3 = OFF_W3 + NOUT * H, NPARAM = OFF_B3 + NOUT;
+
+__device__ __forceinline__ float gelu(float z) {
+    const float k = 0.7978845608028654f;   // sqrt(2/pi)
+    return 0.5f * z * (1.0f + tanhf(k * (z + 0.044715f * z * z * z)));
+}
+__device__ __forceinline__ float gelu_grad(float z) {
+    const float k = 0.7978845608028654f;
+    const float u = k * (z + 0.044715f * z * z * z);
+    const float t = tanhf(u);
+    return 0.5f * (1.0f + t) + 0.5f * z * (1.0f - t * t) * k * (1.0f + 3.0f * 0.044715f * z * z);
+}
+
+__device__ __forceinline__ int mir(int x, int n) {
+    x = x < 0 ? -1 - x : (x >= n ? 2 * n - 1 - x : x);
+    return x < 0 ? 0 : (x >= n ? n - 1 : x);
+}
+
+// ---------------------------------------------------------------------------------
+// FP32 model + HLLC + limiter (the reference's formulas, single precision)
+// ---------------------------------------------------------------------------------
+struct PrimF { float r, u, v, p, E; };
+__device__ __forceinline__ PrimF prim(float g1, const float* c) {
+    PrimF w;
+    w.r = c[0];
+    w.u = c[1] / c[0];
+    w.v = c[2] / c[0];
+    const float q = w.u * w.u + w.v * w.v;
+    w.p = g1 * (c[3] - 0.5f * c[0] * q);
+    w.E = w.r * (0.5f * q + w.p / (w.r * g1));
+    return w;
+}
+template <int DIR>
+__device__ __forceinline__ void fluxf(const PrimF& w, float* f) {
+    if (DIR == 0) { float ru = w.r * w.u; f[0] = ru; f[1] = ru * w.u + w.p; f[2] = ru * w.v; f[3] = w.u * (w.E + w.p); }
+    else { f[0] = w.r * w.v; f[1] = w.r * w.u * w.v; f[2] = f[0] * w.v + w.p; f[3] = w.v * (w.E + w.p); }
+}
+template <int DIR>
+__device__ void hllcf(float g, float g1, const float* UL, const float* UR, float* F) {
+    PrimF wL = prim(g1, UL), wR = prim(g1, UR);
+    const float aL = sqrtf(g * wL.p / wL.r), aR = sqrtf(g * wR.p / wR.r);
+    const float vL = DIR == 0 ? wL.u : wL.v, vR = DIR == 0 ? wR.u : wR.v;
+    const float SL = fminf(vL - aL, vR - aR), SR = fmaxf(vL + aL, vR + aR);
+    float FL[4], FR[4];
+    fluxf<DIR>(wL, FL);
+    fluxf<DIR>(wR, FR);
+    if (0.0f <= SL) { for (int i = 0; i < 4; ++i) F[i] = FL[i]; return; }
+    if (SR <= 0.0f) { for (int i = 0; i < 4; ++i) F[i] = FR[i]; return; }
+    const float Ss = (wR.p - wL.p + wL.r * vL * (SL - vL) - wR.r * vR * (SR - vR)) /
+                     (wL.r * (SL - vL) - wR.r * (SR - vR));
+    const bool left = 0.0f <= Ss;
+    const PrimF& w = left ? wL : wR;
+    const float SK = left ? SL : SR, vK = left ? vL : vR;
+    const float* UK = left ? UL : UR;
+    const float* FK = left ? FL : FR;
+    const float coef = w.r * ((SK - vK) / (SK - Ss));
+    float us[4];
+    us[0] = coef;
+    us[1] = DIR == 0 ? coef * Ss : coef * w.u;
+    us[2] = DIR == 0 ? coef * w.v : coef * Ss;
+    us[3] = coef * (w.E / w.r + (Ss - vK) * (Ss + w.p / (w.r * (SK - vK))));
+    for (int i = 0; i < 4; ++i) F[i] = FK[i] + SK * (us[i] - UK[i]);
+}
+__device__ __forceinline__ float limf(int lim, float r) {
+    if (r <= 0.0f) return 0.0f;
+    const float xr = 2.0f / (1.0f + r);
+    if (lim == 0) return r <= 1.0f ? r : fminf(1.0f, xr);
+    return fminf(2.0f * r / (1.0f + r), xr);
+}
+__device__ __forceinline__ float slopef(int lim, float um, float u0, float up) {
+    float dl = u0 - um, dr = up - u0;
+    float dlc = fabsf(dl) <= 1e-6f ? (dl == 0.0f ? 1e-6f : copysignf(1e-6f, dl)) : dl;
+    float drc = fabsf(dr) <= 1e-6f ? (dr == 0.0f ? 1e-6f : copysignf(1e-6f, dr)) : dr;
+    return limf(lim, dlc / drc) * (0.5f * dl + 0.5f * dr);
+}
+
+struct Grid {
+    int n;
+    float dx, g, g1;
+    int lim;
+};
+
+__device__ __forceinline__ void load_cell(const float* __restrict__ U, int n, int i, int j, float* c) {
+    const size_t o = (size_t)mir(j, n) * n + mir(i, n), pl = (size_t)n * n;
+    c[0] = U[o]; c[1] = U[pl + o]; c[2] = U[2 * pl + o]; c[3] = U[3 * pl + o];
+}
+
+// evolved face pair of cell (i, j) in direction DIR: e0 (lower face), e1 (upper face)
+template <int DIR>
+__device__ void evolved_pair(const float* __restrict__ U, const Grid& G, float hdt_dx, int i, int j,
+                             float* e0, float* e1) {
+    float cm[4], c0[4], cp[4];
+    load_cell(U, G.n, i - (DIR == 0), j - (DIR == 1), cm);
+    load_cell(U, G.n, i, j, c0);
+    load_cell(U, G.n, i + (DIR == 0), j + (DIR == 1), cp);
+    for (int v = 0; v < 4; ++v) {
+        const float s = slopef(G.lim, cm[v], c0[v], cp[v]);
+        e0[v] = c0[v] - 0.5f * s;
+        e1[v] = c0[v] + 0.5f * s;
+    }
+    PrimF w0 = prim(G.g1, e0), w1 = prim(G.g1, e1);
+    float f0[4], f1[4];
+    fluxf<DIR>(w0, f0);
+    fluxf<DIR>(w1, f1);
+    for (int v = 0; v < 4; ++v) {
+        const float d = hdt_dx * (f0[v] - f1[v]);
+        e0[v] += d;
+        e1[v] += d;
+    }
+}
+
+// face index f: x faces first (f = j*(n+1) + i, face between cells i-1 and i, i in 0..n),
+// then y faces (f = NX + j*n + i, between cells (i, j-1) and (i, j), j in 0..n)
+__device__ __forceinline__ void face_of(int f, int n, int& dir, int& i, int& j) {
+    const int nxf = (n + 1) * n;
+    if (f < nxf) { dir = 0; j = f / (n + 1); i = f % (n + 1); }
+    else { f -= nxf; dir = 1; j = f / n; i = f % n; }
+}
+
+// plain MUSCL-Hancock HLLC flux of every face (FP32)
+__global__ void plain_flux_kernel(const float* __restrict__ U, Grid G, float dt, float* __restrict__ F) {
+    const int nf = 2 * (G.n + 1) * G.n;
+    const float hdt = 0.5f * dt / G.dx;
+    for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < nf; f += gridDim.x * blockDim.x) {
+        int dir, i, j;
+        face_of(f, G.n, dir, i, j);
+        float a0[4], a1[4], b0[4], b1[4], out[4];
+        if (dir == 0) {
+            evolved_pair<0>(U, G, hdt, i - 1, j, a0, a1);
+            evolved_pair<0>(U, G, hdt, i, j, b0, b1);
+            hllcf<0>(G.g, G.g1, a1, b0, out);
+        } else {
+            evolved_pair<1>(U, G, hdt, i, j - 1, a0, a1);
+            evolved_pair<1>(U, G, hdt, i, j, b0, b1);
+            hllcf<1>(G.g, G.g1, a1, b0, out);
+        }
+        for (int v = 0; v < 4; ++v) F[(size_t)v * nf + f] = out[v];
+    }
+}
+
+// features (BF16 [nf][64]) and the correction scale of every face
+__global__ void features_kernel(const float* __restrict__ U, Grid G, __nv_bfloat16* __restrict__ X,
+                                float* __restrict__ scale /* [nf][2]: rho_ref, c_ref */) {
+    const int nf = 2 * (G.n + 1) * G.n;
+    for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < nf; f += gridDim.x * blockDim.x) {
+        int dir, i, j;
+        face_of(f, G.n, dir, i, j);
+        // lower cell (il, jl), normal unit (dn_i, dn_j), tangent (dt_i, dt_j)
+        const int il = dir == 0 ? i - 1 : i, jl = dir == 0 ? j : j - 1;
+        const int ni = dir == 0, nj = dir == 1, ti = dir == 1, tj = dir == 0;
+        float cl[4], cr[4];
+        load_cell(U, G.n, il, jl, cl);
+        load_cell(U, G.n, il + ni, jl + nj, cr);
+        PrimF wl = prim(G.g1, cl), wr = prim(G.g1, cr);
+        const float rr = 0.5f * (wl.r + wr.r), pr = 0.5f * (wl.p + wr.p);
+        const float cref = sqrtf(fmaxf(G.g * pr / rr, 1e-12f));
+        scale[2 * (size_t)f] = rr;
+        scale[2 * (size_t)f + 1] = cref;
+        __nv_bfloat16* x = X + (size_t)f * NIN;
+        int k = 0;
+        for (int a = -1; a <= 2; ++a)
+            for (int b = -1; b <= 2; ++b) {
+                float c[4];
+                load_cell(U, G.n, il + a * ni + b * ti, jl + a * nj + b * tj, c);
+                PrimF w = prim(G.g1, c);
+                const float un = dir == 0 ? w.u : w.v, ut = dir == 0 ? w.v : w.u;
+                x[k++] = __float2bfloat16_rn(w.r / rr - 1.0f);
+                x[k++] = __float2bfloat16_rn(un / cref);
+                x[k++] = __float2bfloat16_rn(ut / cref);
+                x[k++] = __float2bfloat16_rn(w.p / pr - 1.0f);
+            }
+    }
+}
+
+// ---------------------------------------------------------------------------------
+// MLP forward on the tensor cores: mma.sync m16n8k16 BF16 x BF16 -> FP32
+// ---------------------------------------------------------------------------------
+__device__ __forceinline__ void mma_bf16(float* c, const uint32_t* a, uint32_t b0, uint32_t b1) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
+        "{%8,%9}, {%0,%1,%2,%3};"
+        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+__device__ __forceinline__ uint32_t pack2(float lo, float hi) {
+    __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<uint32_t*>(&v);
+}
+
+constexpr int kMlpWarps = 8;
+
+// Y[nf][4] = MLP(X).  When Z1/Z2 are given (training), the hidden pre-activations are saved.
+__global__ void __launch_bounds__(kMlpWarps * 32)
+mlp_forward_kernel(const __nv_bfloat16* __restrict__ X, int nf, const __nv_bfloat16* __restrict__ Wb,
+                   const float* __restrict__ P, float* __restrict__ Y, float* __restrict__ Z1,
+                   float* __restrict__ Z2) {
+    __shared__ __align__(16) __nv_bfloat16 sW1[H * NIN], sW2[H * H], sW3[8 * H];
+    __shared__ float sb1[H], sb2[H], sb3[8];
+    for (int k = threadIdx.x; k < H * NIN; k += blockDim.x) { sW1[k] = Wb[k]; sW2[k] = Wb[H * NIN + k]; }
+    for (int k = threadIdx.x; k < 8 * H; k += blockDim.x)
+        sW3[k] = k < NOUT * H ? Wb[H * NIN + H * H + k] : __float2bfloat16_rn(0.0f);
+    for (int k = threadIdx.x; k < H; k += blockDim.x) { sb1[k] = P[OFF_B1 + k]; sb2[k] = P[OFF_B2 + k]; }
+    if (threadIdx.x < 8) sb3[threadIdx.x] = threadIdx.x < NOUT ? P[OFF_B3 + threadIdx.x] : 0.0f;
+    __syncthreads();
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int g = lane >> 2, t = lane & 3;
+    for (int base = (blockIdx.x * kMlpWarps + w) * 16; base < nf; base += gridDim.x * kMlpWarps * 16) {
+        const int r0 = base + g, r1 = base + g + 8;
+        const bool v0 = r0 < nf, v1 = r1 < nf;
+        uint32_t a[4][4];
+        const uint32_t* x0 = reinterpret_cast<const uint32_t*>(X + (size_t)r0 * NIN);
+        const uint32_t* x1 = reinterpret_cast<const uint32_t*>(X + (size_t)r1 * NIN);
+#pragma unroll
+        for (int kt = 0; kt < 4; ++kt) {
+            a[kt][0] = v0 ? x0[kt * 8 + t] : 0u;
+            a[kt][1] = v1 ? x1[kt * 8 + t] : 0u;
+            a[kt][2] = v0 ? x0[kt * 8 + 4 + t] : 0u;
+            a[kt][3] = v1 ? x1[kt * 8 + 4 + t] : 0u;
+        }
+        // two hidden layers
+#pragma unroll
+        for (int layer = 0; layer < 2; ++layer) {
+            const __nv_bfloat16* sW = layer == 0 ? sW1 : sW2;
+            const float* sb = layer == 0 ? sb1 : sb2;
+            float* Zs = layer == 0 ? Z1 : Z2;
+            float c[8][4];
+#pragma unroll
+            for (int nt = 0; nt < 8; ++nt) {
+                c[nt][0] = c[nt][1] = c[nt][2] = c[nt][3] = 0.0f;
+                const uint32_t* wrow = reinterpret_cast<const uint32_t*>(sW + (nt * 8 + g) * 64);
+#pragma unroll
+                for (int kt = 0; kt < 4; ++kt) mma_bf16(c[nt], a[kt], wrow[kt * 8 + t], wrow[kt * 8 + 4 + t]);
+            }
+            float h[8][4];
+#pragma unroll
+            for (int nt = 0; nt < 8; ++nt) {
+                const int col = nt * 8 + 2 * t;
+                const float z0 = c[nt][0] + sb[col], z1 = c[nt][1] + sb[col + 1];
+                const float z2 = c[nt][2] + sb[col], z3 = c[nt][3] + sb[col + 1];
+                if (Zs) {
+                    if (v0) { Zs[(size_t)r0 * H + col] = z0; Zs[(size_t)r0 * H + col + 1] = z1; }
+                    if (v1) { Zs[(size_t)r1 * H + col] = z2; Zs[(size_t)r1 * H + col + 1] = z3; }
+                }
+                h[nt][0] = gelu(z0); h[nt][1] = gelu(z1); h[nt][2] = gelu(z2); h[nt][3] = gelu(z3);
+            }
+#pragma unroll
+            for (int kt = 0; kt < 4; ++kt) {
+                a[kt][0] = pack2(h[2 * kt][0], h[2 * kt][1]);
+                a[kt][1] = pack2(h[2 * kt][2], h[2 * kt][3]);
+                a[kt][2] = pack2(h[2 * kt + 1][0], h[2 * kt + 1][1]);
+                a[kt][3] = pack2(h[2 * kt + 1][2], h[2 * kt + 1][3]);
+            }
+        }
+        float c[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        const uint32_t* wrow = reinterpret_cast<const uint32_t*>(sW3 + g * 64);
+#pragma unroll
+        for (int kt = 0; kt < 4; ++kt) mma_bf16(c, a[kt], wrow[kt * 8 + t], wrow[kt * 8 + 4 + t]);
+        if (t < 2) {
+            const int col = 2 * t;
+            if (v0) { Y[(size_t)r0 * 4 + col] = c[0] + sb3[col]; Y[(size_t)r0 * 4 + col + 1] = c[1] + sb3[col + 1]; }
+            if (v1) { Y[(size_t)r1 * 4 + col] = c[2] + sb3[col]; Y[(size_t)r1 * 4 + col + 1] = c[3] + sb3[col + 1]; }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------------
+// MLP backward (FP32 on the CUDA cores, the forward's BF16 weights and activations)
+// ---------------------------------------------------------------------------------
+constexpr int kBwdFaces = 16;   // 38 KB of static shared memory per CTA
+__global__ void __launch_bounds__(256)
+mlp_backward_kernel(const __nv_bfloat16* __restrict__ X, int nf, const __nv_bfloat16* __restrict__ Wb,
+                    const float* __restrict__ Z1, const float* __restrict__ Z2,
+                    const float* __restrict__ dY, float* __restrict__ grad) {
+    __shared__ float sW2[H * H], sW3[NOUT * H];
+    __shared__ float sx[kBwdFaces][NIN], sh1[kBwdFaces][H], sh2[kBwdFaces][H];
+    __shared__ float sdz1[kBwdFaces][H], sdz2[kBwdFaces][H], sdy[kBwdFaces][NOUT];
+    for (int k = threadIdx.x; k < H * H; k += blockDim.x) sW2[k] = __bfloat162float(Wb[H * NIN + k]);
+    for (int k = threadIdx.x; k < NOUT * H; k += blockDim.x) sW3[k] = __bfloat162float(Wb[H * NIN + H * H + k]);
+    // per-thread gradient accumulators: thread owns 16 entries of each weight matrix
+    float gW1[16], gW2[16], gb1 = 0.f, gb2 = 0.f, gW3 = 0.f, gb3 = 0.f;
+    for (int q = 0; q < 16; ++q) gW1[q] = gW2[q] = 0.f;
+    const int tid = threadIdx.x;
+    __syncthreads();
+    for (int base = blockIdx.x * kBwdFaces; base < nf; base += gridDim.x * kBwdFaces) {
+        // stage inputs, activations (as the forward rounded them) and output gradients
+        for (int k = tid; k < kBwdFaces * H; k += 256) {
+            const int f = k / H, c = k % H, r = base + f;
+            const bool ok = r < nf;
+            sx[f][c] = ok ? __bfloat162float(X[(size_t)r * NIN + c]) : 0.f;
+            const float z1 = ok ? Z1[(size_t)r * H + c] : 0.f, z2 = ok ? Z2[(size_t)r * H + c] : 0.f;
+            sh1[f][c] = __bfloat162float(__float2bfloat16_rn(gelu(z1)));
+            sh2[f][c] = __bfloat162float(__float2bfloat16_rn(gelu(z2)));
+            sdz1[f][c] = gelu_grad(z1);     // temporarily the derivative factors
+            sdz2[f][c] = gelu_grad(z2);
+        }
+        for (int k = tid; k < kBwdFaces * NOUT; k += 256) {
+            const int f = k / NOUT, o = k % NOUT, r = base + f;
+            sdy[f][o] = r < nf ? dY[(size_t)r * NOUT + o] : 0.f;
+        }
+        __syncthreads();
+        // dz2 = (dY W3) * gelu'(z2)
+        for (int k = tid; k < kBwdFaces * H; k += 256) {
+            const int f = k / H, c = k % H;
+            float s = 0.f;
+            for (int o = 0; o < NOUT; ++o) s += sdy[f][o] * sW3[o * H + c];
+            sdz2[f][c] *= s;
+        }
+        __syncthreads();
+        // dz1 = (dz2 W2) * gelu'(z1)
+        for (int k = tid; k < kBwdFaces * H; k += 256) {
+            const int f = k / H, c = k % H;
+            float s = 0.f;
+            for (int o = 0; o < H; ++o) s += sdz2[f][o] * sW2[o * H + c];
+            sdz1[f][c] *= s;
+        }
+        __syncthreads();
+        // weight gradients: thread tid owns rows (tid / 4), columns (tid % 4) * 16 .. + 15
+        const int row = tid >> 2, c0 = (tid & 3) * 16;
+        for (int f = 0; f < kBwdFaces; ++f) {
+            const float d1 = sdz1[f][row], d2 = sdz2[f][row];
+            for (int q = 0; q < 16; ++q) {
+                gW1[q] += d1 * sx[f][c0 + q];
+                gW2[q] += d2 * sh1[f][c0 + q];
+            }
+        }
+        if ((tid & 3) == 0)
+            for (int f = 0; f < kBwdFaces; ++f) { gb1 += sdz1[f][row]; gb2 += sdz2[f][row]; }
+        // W3 (4 x 64) and b3: threads 0..255 own one W3 entry each
+        {
+            const int o = tid / H, c = tid % H;
+            for (int f = 0; f < kBwdFaces; ++f) gW3 += sdy[f][o] * sh2[f][c];
+            if (tid < NOUT)
+                for (int f = 0; f < kBwdFaces; ++f) gb3 += sdy[f][tid];
+        }
+        __syncthreads();
+    }
+    const int row = tid >> 2, c0 = (tid & 3) * 16;
+    for (int q = 0; q < 16; ++q) {
+        atomicAdd(&grad[OFF_W1 + row * NIN + c0 + q], gW1[q]);
+        atomicAdd(&grad[OFF_W2 + row * H + c0 + q], gW2[q]);
+    }
+    if ((tid & 3) == 0) { atomicAdd(&grad[OFF_B1 + row], gb1); atomicAdd(&grad[OFF_B2 + row], gb2); }
+    atomicAdd(&grad[OFF_W3 + tid], gW3);
+    if (tid < NOUT) atomicAdd(&grad[OFF_B3 + tid], gb3);
+}
+
+// Adam on the FP32 master parameters; refreshes the BF16 weight copy
+__global__ void adam_kernel(float* __restrict__ P, const float* __restrict__ G, float* __restrict__ m,
+                            float* __restrict__ v, __nv_bfloat16* __restrict__ Wb, float lr, float b1,
+                            float b2, float eps, float c1, float c2) {
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < NPARAM; k += gridDim.x * blockDim.x) {
+        const float g = G[k];
+        const float mk = b1 * m[k] + (1.f - b1) * g, vk = b2 * v[k] + (1.f - b2) * g * g;
+        m[k] = mk;
+        v[k] = vk;
+        P[k] -= lr * (mk / c1) / (sqrtf(vk / c2) + eps);
+    }
+}
+
+__global__ void to_bf16_kernel(const float* __restrict__ P, __nv_bfloat16* __restrict__ Wb) {
+    // BF16 copies of W1, W2, W3 (contiguous: [W1 | W2 | W3])
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < H * NIN + H * H + NOUT * H; k += gridDim.x * blockDim.x) {
+        int src = k < H * NIN ? OFF_W1 + k : (k < H * NIN + H * H ? OFF_W2 + (k - H * NIN) : OFF_W3 + (k - H * NIN - H * H));
+        Wb[k] = __float2bfloat16_rn(P[src]);
+    }
+}
+
+// ---------------------------------------------------------------------------------
+// corrections, guarded update, loss gradient
+// ---------------------------------------------------------------------------------
+// dF (physical, [4][nf]) from the MLP outputs
+__global__ void correction_kernel(const float* __restrict__ Y, const float* __restrict__ scale, int n,
+                                  float* __restrict__ dF) {
+    const int nf = 2 * (n + 1) * n;
+    for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < nf; f += gridDim.x * blockDim.x) {
+        const float r = scale[2 * (size_t)f], c = scale[2 * (size_t)f + 1];
+        const float m = r * c;
+        const float o0 = Y[4 * (size_t)f], o1 = Y[4 * (size_t)f + 1], o2 = Y[4 * (size_t)f + 2], o3 = Y[4 * (size_t)f + 3];
+        const bool xface = f < (n + 1) * n;
+        dF[f] = m * o0;
+        dF[(size_t)nf + f] = m * c * (xface ? o1 : o2);          // x momentum: normal on x faces
+        dF[2 * (size_t)nf + f] = m * c * (xface ? o2 : o1);      // y momentum
+        dF[3 * (size_t)nf + f] = m * c * c * o3;
+    }
+}
+
+__device__ __forceinline__ int xf(int n, int i, int j) { return j * (n + 1) + i; }            // left face of (i,j)
+__device__ __forceinline__ int yf(int n, int i, int j) { return (n + 1) * n + j * n + i; }    // bottom face
+
+// update of cell (i,j) with fluxes F (+ dF on faces whose mask bit is set)
+__device__ __forceinline__ void cell_update(const float* __restrict__ U, const float* __restrict__ F,
+                                            const float* __restrict__ dF, const unsigned char* __restrict__ ok,
+                                            int n, float r, int i, int j, float* out) {
+    const int nf = 2 * (n + 1) * n;
+    const int fl = xf(n, i, j), fr = xf(n, i + 1, j), fb = yf(n, i, j), ft = yf(n, i, j + 1);
+    const size_t o = (size_t)j * n + i, pl = (size_t)n * n;
+    for (int v = 0; v < 4; ++v) {
+        float Fl = F[(size_t)v * nf + fl], Fr = F[(size_t)v * nf + fr];
+        float Gb = F[(size_t)v * nf + fb], Gt = F[(size_t)v * nf + ft];
+        if (dF) {
+            if (!ok || ok[fl]) Fl += dF[(size_t)v * nf + fl];
+            if (!ok || ok[fr]) Fr += dF[(size_t)v * nf + fr];
+            if (!ok || ok[fb]) Gb += dF[(size_t)v * nf + fb];
+            if (!ok || ok[ft]) Gt += dF[(size_t)v * nf + ft];
+        }
+        out[v] = U[v * pl + o] + r * ((Fl - Fr) + (Gb - Gt));
+    }
+}
+
+__device__ __forceinline__ bool cell_bad(float g1, const float* un, const float* up, const float* u0, float bound) {
+    PrimF w = prim(g1, un);
+    if (!(w.r > 0.0f) || !(w.p > 0.0f)) return true;
+    const float dr = fabsf(un[0] - up[0]), de = fabsf(un[3] - up[3]);
+    const float sr = fabsf(up[0] - u0[0]) + 1e-6f * fabsf(u0[0]), se = fabsf(up[3] - u0[3]) + 1e-6f * fabsf(u0[3]);
+    return dr > bound * sr || de > bound * se;
+}
+
+// pass 1: mark faces whose correction is rejected (any adjacent cell violates)
+__global__ void guard_kernel(const float* __restrict__ U, const float* __restrict__ F, const float* __restrict__ dF,
+                             Grid G, float r, float bound, unsigned char* __restrict__ ok,
+                             unsigned long long* __restrict__ rejected) {
+    const int n = G.n;
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n * n; c += gridDim.x * blockDim.x) {
+        const int i = c % n, j = c / n;
+        float un[4], up[4], u0[4];
+        cell_update(U, F, dF, nullptr, n, r, i, j, un);
+        cell_update(U, F, nullptr, nullptr, n, r, i, j, up);
+        for (int v = 0; v < 4; ++v) u0[v] = U[(size_t)v * n * n + (size_t)j * n + i];
+        if (cell_bad(G.g1, un, up, u0, bound)) {
+            ok[xf(n, i, j)] = 0; ok[xf(n, i + 1, j)] = 0; ok[yf(n, i, j)] = 0; ok[yf(n, i, j + 1)] = 0;
+            atomicAdd(rejected, 1ull);
+        }
+    }
+}
+
+// pass 2: the update (corrections where accepted); a cell still violating takes its plain update
+__global__ void update_kernel(const float* __restrict__ U, const float* __restrict__ F, const float* __restrict__ dF,
+                              const unsigned char* __restrict__ ok, Grid G, float r, float bound,
+                              float* __restrict__ Un, float* __restrict__ maxs) {
+    const int n = G.n;
+    float m = 0.0f;
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n * n; c += gridDim.x * blockDim.x) {
+        const int i = c % n, j = c / n;
+        float un[4], up[4], u0[4];
+        cell_update(U, F, nullptr, nullptr, n, r, i, j, up);
+        if (dF) {
+            cell_update(U, F, dF, ok, n, r, i, j, un);
+            for (int v = 0; v < 4; ++v) u0[v] = U[(size_t)v * n * n + (size_t)j * n + i];
+            if (ok && cell_bad(G.g1, un, up, u0, bound))
+                for (int v = 0; v < 4; ++v) un[v] = up[v];
+        } else {
+            for (int v = 0; v < 4; ++v) un[v] = up[v];
+        }
+        for (int v = 0; v < 4; ++v) Un[(size_t)v * n * n + (size_t)j * n + i] = un[v];
+        PrimF w = prim(G.g1, un);
+        const float cs = sqrtf(G.g * w.p / w.r);
+        const float s = fmaxf(fabsf(w.u), fabsf(w.v)) + cs;
+        if (s > m) m = s;
+    }
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0 && m > 0.0f) atomicMax(reinterpret_cast<int*>(maxs), __float_as_int(m));
+}
+
+// dL/dY for L = (1/N) sum_cells sum_v w_v (U^{n+1}_v - T_v)^2, U^{n+1} with every correction
+__global__ void loss_grad_kernel(const float* __restrict__ Un, const float* __restrict__ T, const float* __restrict__ scale,
+                                 int n, float r, const float* __restrict__ wv, float* __restrict__ dY,
+                                 double* __restrict__ loss) {
+    const int nf = 2 * (n + 1) * n;
+    const float invN = 1.0f / ((float)n * n);
+    double ls = 0.0;
+    for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < nf; f += gridDim.x * blockDim.x) {
+        int dir, i, j;
+        face_of(f, n, dir, i, j);
+        // cells below (lower) and above (upper) the face; outside cells do not exist
+        const int il = dir == 0 ? i - 1 : i, jl = dir == 0 ? j : j - 1;
+        const int iu = i, ju = j;
+        float gF[4];
+        for (int v = 0; v < 4; ++v) {
+            float gl = 0.f, gu = 0.f;
+            if (il >= 0 && jl >= 0) {
+                const size_t o = (size_t)v * n * n + (size_t)jl * n + il;
+                gl = 2.0f * wv[v] * (Un[o] - T[o]) * invN;
+            }
+            if (iu < n && ju < n) {
+                const size_t o = (size_t)v * n * n + (size_t)ju * n + iu;
+                gu = 2.0f * wv[v] * (Un[o] - T[o]) * invN;
+            }
+            // U_lower gets -r*F, U_upper gets +r*F
+            gF[v] = r * (gu - gl);
+        }
+        const float rr = scale[2 * (size_t)f], c = scale[2 * (size_t)f + 1], m = rr * c;
+        const bool xface = dir == 0;
+        dY[4 * (size_t)f] = m * gF[0];
+        dY[4 * (size_t)f + 1] = m * c * (xface ? gF[1] : gF[2]);
+        dY[4 * (size_t)f + 2] = m * c * (xface ? gF[2] : gF[1]);
+        dY[4 * (size_t)f + 3] = m * c * c * gF[3];
+    }
+    // the loss itself, over cells
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n * n; c += gridDim.x * blockDim.x)
+        for (int v = 0; v < 4; ++v) {
+            const float d = Un[(size_t)v * n * n + c] - T[(size_t)v * n * n + c];
+            ls += (double)(wv[v] * d * d * invN);
+        }
+    for (int o = 16; o > 0; o >>= 1) ls += __shfl_xor_sync(0xffffffffu, ls, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(loss, ls);
+}
+
+}  // namespace lc
+}  // namespace hf
+
+// =====================================================================================
+// host side
+// =====================================================================================
+using namespace hf::lc;
+
+struct hf_lc {
+    int n = 0, lim = 0;
+    double dx = 0, gamma = 1.4, cfl = 0.8, bound = 0.5;
+    cudaStream_t stream = nullptr;
+    float *U[2] = {nullptr, nullptr}, *F = nullptr, *dF = nullptr, *scale = nullptr, *Y = nullptr;
+    float *Z1 = nullptr, *Z2 = nullptr, *dY = nullptr, *T = nullptr, *wv = nullptr;
+    __nv_bfloat16 *X = nullptr, *Wb = nullptr;
+    float *P = nullptr, *grad = nullptr, *m1 = nullptr, *m2 = nullptr, *maxs = nullptr;
+    unsigned char* ok = nullptr;
+    unsigned long long* rejected = nullptr;
+    double* loss = nullptr;
+    int cur = 0;
+    long long adam_t = 0;
+    double t = 0.0;
+    std::vector<void*> allocs;
+    std::string err;
+};
+
+namespace {
+
+int lfail(hf_lc* L, int code, const std::string& m) {
+    if (L) L->err = m;
+    return code;
+}
+#define LCK(call)                                                                             \
+    do {                                                                                      \
+        cudaError_t e_ = (call);                                                              \
+        if (e_ != cudaSuccess)                                                                \
+            return lfail(L, HF_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+template <class T>
+int alloc(hf_lc* L, T** p, size_t n) {
+    LCK(cudaMalloc(p, n * sizeof(T) + 64));
+    L->allocs.push_back(*p);
+    LCK(cudaMemset(*p, 0, n * sizeof(T) + 64));
+    return HF_OK;
+}
+
+hf::lc::Grid grid(const hf_lc* L) {
+    hf::lc::Grid G;
+    G.n = L->n;
+    G.dx = (float)L->dx;
+    G.g = (float)L->gamma;
+    G.g1 = (float)(L->gamma - 1.0);
+    G.lim = L->lim;
+    return G;
+}
+
+int nfaces(const hf_lc* L) { return 2 * (L->n + 1) * L->n; }
+int blocks_for(long long n, int t) { long long b = (n + t - 1) / t; return (int)(b > 4096 ? 4096 : (b < 1 ? 1 : b)); }
+
+// plain fluxes, and (use_mlp) features -> MLP -> corrections for state U[cur]
+int fluxes(hf_lc* L, float dt, bool use_mlp, bool save_acts) {
+    hf::lc::Grid G = grid(L);
+    const int nf = nfaces(L);
+    plain_flux_kernel<<<blocks_for(nf, 256), 256, 0, L->stream>>>(L->U[L->cur], G, dt, L->F);
+    if (use_mlp) {
+        features_kernel<<<blocks_for(nf, 256), 256, 0, L->stream>>>(L->U[L->cur], G, L->X, L->scale);
+        mlp_forward_kernel<<<blocks_for(nf, kMlpWarps * 16), kMlpWarps * 32, 0, L->stream>>>(
+            L->X, nf, L->Wb, L->P, L->Y, save_acts ? L->Z1 : nullptr, save_acts ? L->Z2 : nullptr);
+        correction_kernel<<<blocks_for(nf, 256), 256, 0, L->stream>>>(L->Y, L->scale, L->n, L->dF);
+    }
+    LCK(cudaGetLastError());
+    return HF_OK;
+}
+
+double max_speed(hf_lc* L) {
+    float m = 0.f;
+    cudaMemcpy(&m, L->maxs, sizeof m, cudaMemcpyDeviceToHost);
+    return m;
+}
+
+}  // namespace
+
+extern "C" {
+
+int hf_lc_create(int n, double dx, double gamma, double cfl, int limiter, hf_lc** out) {
+    if (!out || n < 4 || n > 8192 || dx <= 0) return HF_ERR_ARG;
+    hf_lc* L = new hf_lc();
+    *out = L;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return lfail(L, HF_ERR_NO_DEVICE, "no CUDA device");
+    L->n = n; L->dx = dx; L->gamma = gamma; L->cfl = cfl; L->lim = limiter;
+    LCK(cudaStreamCreateWithFlags(&L->stream, cudaStreamNonBlocking));
+    const size_t cells = (size_t)n * n, nf = nfaces(L);
+    int r;
+    if ((r = alloc(L, &L->U[0], 4 * cells)) || (r = alloc(L, &L->U[1], 4 * cells)) || (r = alloc(L, &L->F, 4 * nf)) ||
+        (r = alloc(L, &L->dF, 4 * nf)) || (r = alloc(L, &L->scale, 2 * nf)) || (r = alloc(L, &L->Y, 4 * nf)) ||
+        (r = alloc(L, &L->Z1, (size_t)H * nf)) || (r = alloc(L, &L->Z2, (size_t)H * nf)) || (r = alloc(L, &L->dY, 4 * nf)) ||
+        (r = alloc(L, &L->T, 4 * cells)) || (r = alloc(L, &L->wv, 4)) || (r = alloc(L, &L->X, (size_t)NIN * nf)) ||
+        (r = alloc(L, &L->Wb, (size_t)(H * NIN + H * H + NOUT * H))) || (r = alloc(L, &L->P, (size_t)NPARAM)) ||
+        (r = alloc(L, &L->grad, (size_t)NPARAM)) || (r = alloc(L, &L->m1, (size_t)NPARAM)) ||
+        (r = alloc(L, &L->m2, (size_t)NPARAM)) || (r = alloc(L, &L->maxs, 4)) || (r = alloc(L, &L->ok, nf)) ||
+        (r = alloc(L, &L->rejected, 1)) || (r = alloc(L, &L->loss, 1)))
+        return r;
+    return HF_OK;
+}
+
+void hf_lc_destroy(hf_lc* L) {
+    if (!L) return;
+    if (L->stream) cudaStreamSynchronize(L->stream);
+    for (void* p : L->allocs) cudaFree(p);
+    if (L->stream) cudaStreamDestroy(L->stream);
+    delete L;
+}
+
+const char* hf_lc_last_error_message(const hf_lc* L) { return L ? L->err.c_str() : ""; }
+int hf_lc_num_params(int* n) { if (!n) return HF_ERR_ARG; *n = NPARAM; return HF_OK; }
+
+int hf_lc_set_params(hf_lc* L, const float* params) {
+    if (!L || !params) return HF_ERR_ARG;
+    LCK(cudaMemcpy(L->P, params, NPARAM * sizeof(float), cudaMemcpyHostToDevice));
+    to_bf16_kernel<<<16, 256, 0, L->stream>>>(L->P, L->Wb);
+    LCK(cudaMemsetAsync(L->m1, 0, NPARAM * sizeof(float), L->stream));
+    LCK(cudaMemsetAsync(L->m2, 0, NPARAM * sizeof(float), L->stream));
+    L->adam_t = 0;
+    LCK(cudaStreamSynchronize(L->stream));
+    return HF_OK;
+}
+
+int hf_lc_get_params(hf_lc* L, float* params) {
+    if (!L || !params) return HF_ERR_ARG;
+    LCK(cudaStreamSynchronize(L->stream));
+    LCK(cudaMemcpy(params, L->P, NPARAM * sizeof(float), cudaMemcpyDeviceToHost));
+    return HF_OK;
+}
+
+int hf_lc_set_state(hf_lc* L, const float* U) {
+    if (!L || !U) return HF_ERR_ARG;
+    LCK(cudaStreamSynchronize(L->stream));
+    LCK(cudaMemcpy(L->U[L->cur], U, (size_t)4 * L->n * L->n * sizeof(float), cudaMemcpyHostToDevice));
+    return HF_OK;
+}
+
+int hf_lc_get_state(hf_lc* L, float* U) {
+    if (!L || !U) return HF_ERR_ARG;
+    LCK(cudaStreamSynchronize(L->stream));
+    LCK(cudaMemcpy(U, L->U[L->cur], (size_t)4 * L->n * L->n * sizeof(float), cudaMemcpyDeviceToHost));
+    return HF_OK;
+}
+
+int hf_lc_cfl_dt(hf_lc* L, double* dt) {
+    if (!L || !dt) return HF_ERR_ARG;
+    // max wave speed of the current state (an update with zero fluxes writes U unchanged)
+    hf::lc::Grid G = grid(L);
+    LCK(cudaMemsetAsync(L->maxs, 0, 4, L->stream));
+    LCK(cudaMemsetAsync(L->F, 0, (size_t)4 * nfaces(L) * sizeof(float), L->stream));
+    update_kernel<<<blocks_for((long long)L->n * L->n, 256), 256, 0, L->stream>>>(
+        L->U[L->cur], L->F, nullptr, nullptr, G, 0.0f, 0.0f, L->U[L->cur ^ 1], L->maxs);
+    LCK(cudaGetLastError());
+    LCK(cudaStreamSynchronize(L->stream));
+    *dt = L->cfl * L->dx / max_speed(L);
+    return HF_OK;
+}
+
+// one coarse step with the given dt; use_mlp adds the guarded correction
+int hf_lc_step(hf_lc* L, double dt, int use_mlp, int64_t* rejected_cells) {
+    if (!L || dt <= 0) return HF_ERR_ARG;
+    hf::lc::Grid G = grid(L);
+    int r = fluxes(L, (float)dt, use_mlp != 0, false);
+    if (r) return r;
+    const float rr = (float)(dt / L->dx);
+    const int nf = nfaces(L);
+    LCK(cudaMemsetAsync(L->maxs, 0, 4, L->stream));
+    if (use_mlp) {
+        LCK(cudaMemsetAsync(L->ok, 1, nf, L->stream));
+        LCK(cudaMemsetAsync(L->rejected, 0, 8, L->stream));
+        guard_kernel<<<blocks_for((long long)L->n * L->n, 256), 256, 0, L->stream>>>(
+            L->U[L->cur], L->F, L->dF, G, rr, (float)L->bound, L->ok, L->rejected);
+    }
+    update_kernel<<<blocks_for((long long)L->n * L->n, 256), 256, 0, L->stream>>>(
+        L->U[L->cur], L->F, use_mlp ? L->dF : nullptr, use_mlp ? L->ok : nullptr, G, rr, (float)L->bound,
+        L->U[L->cur ^ 1], L->maxs);
+    LCK(cudaGetLastError());
+    L->cur ^= 1;
+    L->t += dt;
+    if (rejected_cells) {
+        unsigned long long v = 0;
+        if (use_mlp) LCK(cudaMemcpyAsync(&v, L->rejected, 8, cudaMemcpyDeviceToHost, L->stream));
+        LCK(cudaStreamSynchronize(L->stream));
+        *rejected_cells = (int64_t)v;
+    }
+    return HF_OK;
+}
+
+// runs until t_end with CFL dt (host loop, one sync per step for dt); returns steps
+int hf_lc_run_to(hf_lc* L, double t_end, int use_mlp, int64_t* steps, int64_t* rejected_cells) {
+    if (!L) return HF_ERR_ARG;
+    int64_t k = 0, rej = 0;
+    while (L->t < t_end) {
+        double dt;
+        int r = hf_lc_cfl_dt(L, &dt);
+        if (r) return r;
+        if (L->t + dt > t_end) dt = t_end - L->t;
+        int64_t rc = 0;
+        r = hf_lc_step(L, dt, use_mlp, use_mlp ? &rc : nullptr);
+        if (r) return r;
+        rej += rc;
+        ++k;
+    }
+    LCK(cudaStreamSynchronize(L->stream));
+    if (steps) *steps = k;
+    if (rejected_cells) *rejected_cells = rej;
+    return HF_OK;
+}
+
+int hf_lc_set_time(hf_lc* L, double t) { if (!L) return HF_ERR_ARG; L->t = t; return HF_OK; }
+int hf_lc_get_time(hf_lc* L, double* t) { if (!L || !t) return HF_ERR_ARG; *t = L->t; return HF_OK; }
+int hf_lc_set_bound(hf_lc* L, double bound) { if (!L || bound <= 0) return HF_ERR_ARG; L->bound = bound; return HF_OK; }
+
+// One training iteration on the pair (U0, T) with step dt: forward (plain + MLP, no guard),
+// loss and dL/dY, backward, Adam.  U0/T are host arrays [4][n][n]; w = 4 variable weights.
+int hf_lc_train_step(hf_lc* L, const float* U0, const float* T, const float* w, double dt, double lr,
+                     double* loss) {
+    if (!L || !U0 || !T || !w || dt <= 0) return HF_ERR_ARG;
+    const size_t bytes = (size_t)4 * L->n * L->n * sizeof(float);
+    const int nf = nfaces(L);
+    hf::lc::Grid G = grid(L);
+    LCK(cudaMemcpyAsync(L->U[L->cur], U0, bytes, cudaMemcpyHostToDevice, L->stream));
+    LCK(cudaMemcpyAsync(L->T, T, bytes, cudaMemcpyHostToDevice, L->stream));
+    LCK(cudaMemcpyAsync(L->wv, w, 4 * sizeof(float), cudaMemcpyHostToDevice, L->stream));
+    int r = fluxes(L, (float)dt, true, true);
+    if (r) return r;
+    const float rr = (float)(dt / L->dx);
+    update_kernel<<<blocks_for((long long)L->n * L->n, 256), 256, 0, L->stream>>>(
+        L->U[L->cur], L->F, L->dF, nullptr, G, rr, 0.0f, L->U[L->cur ^ 1], L->maxs);
+    LCK(cudaMemsetAsync(L->loss, 0, 8, L->stream));
+    loss_grad_kernel<<<blocks_for(nf, 256), 256, 0, L->stream>>>(L->U[L->cur ^ 1], L->T, L->scale, L->n, rr, L->wv,
+                                                                  L->dY, L->loss);
+    LCK(cudaMemsetAsync(L->grad, 0, NPARAM * sizeof(float), L->stream));
+    mlp_backward_kernel<<<blocks_for(nf, kBwdFaces) > 1024 ? 1024 : blocks_for(nf, kBwdFaces), 256, 0, L->stream>>>(
+        L->X, nf, L->Wb, L->Z1, L->Z2, L->dY, L->grad);
+    L->adam_t += 1;
+    const float b1 = 0.9f, b2 = 0.999f;
+    const float c1 = 1.f - powf(b1, (float)L->adam_t), c2 = 1.f - powf(b2, (float)L->adam_t);
+    adam_kernel<<<16, 256, 0, L->stream>>>(L->P, L->grad, L->m1, L->m2, L->Wb, (float)lr, b1, b2, 1e-8f, c1, c2);
+    to_bf16_kernel<<<16, 256, 0, L->stream>>>(L->P, L->Wb);
+    LCK(cudaGetLastError());
+    if (loss) {
+        LCK(cudaMemcpyAsync(loss, L->loss, 8, cudaMemcpyDeviceToHost, L->stream));
+    }
+    LCK(cudaStreamSynchronize(L->stream));
+    return HF_OK;
+}
+
+// ---- test entry points: the MLP alone on given inputs ----
+int hf_lc_mlp_forward(hf_lc* L, const uint16_t* x_bf16, int nf, float* y) {
+    if (!L || !x_bf16 || !y || nf < 1 || nf > nfaces(L)) return HF_ERR_ARG;
+    LCK(cudaMemcpy(L->X, x_bf16, (size_t)nf * NIN * 2, cudaMemcpyHostToDevice));
+    mlp_forward_kernel<<<blocks_for(nf, kMlpWarps * 16), kMlpWarps * 32, 0, L->stream>>>(L->X, nf, L->Wb, L->P, L->Y,
+                                                                                         L->Z1, L->Z2);
+    LCK(cudaGetLastError());
+    LCK(cudaStreamSynchronize(L->stream));
+    LCK(cudaMemcpy(y, L->Y, (size_t)nf * 4 * sizeof(float), cudaMemcpyDeviceToHost));
+    return HF_OK;
+}
+
+int hf_lc_mlp_backward(hf_lc* L, const uint16_t* x_bf16, const float* dy, int nf, float* grad) {
+    if (!L || !x_bf16 || !dy || !grad || nf < 1 || nf > nfaces(L)) return HF_ERR_ARG;
+    LCK(cudaMemcpy(L->X, x_bf16, (size_t)nf * NIN * 2, cudaMemcpyHostToDevice));
+    mlp_forward_kernel<<<blocks_for(nf, kMlpWarps * 16), kMlpWarps * 32, 0, L->stream>>>(L->X, nf, L->Wb, L->P, L->Y,
+                                                                                         L->Z1, L->Z2);
+    LCK(cudaMemcpyAsync(L->dY, dy, (size_t)nf * 4 * sizeof(float), cudaMemcpyHostToDevice, L->stream));
+    LCK(cudaMemsetAsync(L->grad, 0, NPARAM * sizeof(float), L->stream));
+    mlp_backward_kernel<<<blocks_for(nf, kBwdFaces) > 1024 ? 1024 : blocks_for(nf, kBwdFaces), 256, 0, L->stream>>>(
+        L->X, nf, L->Wb, L->Z1, L->Z2, L->dY, L->grad);
+    LCK(cudaGetLastError());
+    LCK(cudaStreamSynchronize(L->stream));
+    LCK(cudaMemcpy(grad, L->grad, NPARAM * sizeof(float), cudaMemcpyDeviceToHost));
+    return HF_OK;
+}
+
+int hf_lc_stream(hf_lc* L, void** s) { if (!L || !s) return HF_ERR_ARG; *s = (void*)L->stream; return HF_OK; }
+
+}  // extern "C"

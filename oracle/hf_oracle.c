@@ -239,6 +239,21 @@ void hfo_init_sphere(hfo_mesh *m, int b, double radius, double xo, double yo,
     init_ic(m, b, sph_fn, &c);
 }
 
+typedef struct { double sx, bx, by, r; const double *post, *bub, *amb; } sb_ctx;
+static void sb_fn(const void *p, double x, double y, double *o) {
+    const sb_ctx *c = (const sb_ctx *)p;
+    const double *s;
+    if (x <= c->sx) s = c->post;
+    else if (((x - c->bx) * (x - c->bx) + (y - c->by) * (y - c->by)) <= (c->r * c->r)) s = c->bub;
+    else s = c->amb;
+    memcpy(o, s, 4 * sizeof(double));
+}
+void hfo_init_shock_bubble(hfo_mesh *m, int b, double shock_x, double bx, double by, double r,
+                           const double *post, const double *bubble, const double *ambient) {
+    sb_ctx c = {shock_x, bx, by, r, post, bubble, ambient};
+    init_ic(m, b, sb_fn, &c);
+}
+
 /* ---------------- boundaries: src/fvm_2d_cart/scheme/boundary ------------------------ */
 
 static inline void copy_cell(hfo_mesh *m, int bd, int id, int jd, int bs, int is, int js) {

@@ -61,6 +61,10 @@ void hfo_init_double(hfo_mesh *m, int b, double xlm, double xmr, const double *l
                      const double *mid, const double *r);
 void hfo_init_sphere(hfo_mesh *m, int b, double radius, double xo, double yo,
                      const double *in, const double *out);
+/* shock-bubble (no reference counterpart): post-shock state for x <= shock_x, else the
+ * bubble state inside the circle, else the ambient state */
+void hfo_init_shock_bubble(hfo_mesh *m, int b, double shock_x, double bx, double by, double r,
+                           const double *post, const double *bubble, const double *ambient);
 
 /* the step pieces */
 void hfo_apply_bcs(hfo_mesh *m);

@@ -76,6 +76,7 @@ def port_lib():
         lib.hfo_init_constant.argtypes = [p, i, p]
         lib.hfo_init_double.argtypes = [p, i, d, d, p, p, p]
         lib.hfo_init_sphere.argtypes = [p, i, d, d, d, p, p]
+        lib.hfo_init_shock_bubble.argtypes = [p, i, d, d, d, d, p, p, p]
         lib.hfo_uns_geometry.argtypes = [i, p, p, p, p, p, p]
         lib.hfo_uns_run.restype = i
         lib.hfo_uns_run.argtypes = [d, d, p, i, p, p, p, p, p, p, p, p, i, p, i]
@@ -92,6 +93,22 @@ def prim_to_cons(w, gamma=1.4):
     out = np.zeros(4)
     port_lib().hfo_prim_to_cons(gamma, _ptr(w), _ptr(out))
     return out
+
+
+def shock_bubble_states(ic, g):
+    """Rankine-Hugoniot post-shock state for a shock of Mach M moving into the ambient gas,
+    the bubble state and the ambient state, all conservative."""
+    import math
+    rho1, u1, v1, p1 = (float(x) for x in ic["ambient_state"])
+    M = float(ic["mach"])
+    c1 = math.sqrt(g * p1 / rho1)
+    p2 = p1 * (1.0 + 2.0 * g / (g + 1.0) * (M * M - 1.0))
+    rho2 = rho1 * ((g + 1.0) * M * M / ((g - 1.0) * M * M + 2.0))
+    u2 = u1 + M * c1 * (1.0 - rho1 / rho2)
+    post = prim_to_cons([rho2, u2, v1, p2], g)
+    bub = prim_to_cons([float(ic["bubble_density"]), u1, v1, p1], g)
+    amb = prim_to_cons([rho1, u1, v1, p1], g)
+    return post, bub, amb
 
 
 class Oracle:
@@ -175,6 +192,11 @@ class Oracle:
                 so = prim_to_cons(ic["init_ext_state"], g)
                 lib.hfo_init_sphere(mp, b, float(ic["radius"]), float(ic["x_origin"]),
                                     float(ic["y_origin"]), _ptr(si), _ptr(so))
+            elif typ == "ShockBubble":
+                post, bub, amb = shock_bubble_states(ic, g)
+                lib.hfo_init_shock_bubble(mp, b, float(ic["shock_x"]), float(ic["bubble_x"]),
+                                          float(ic["bubble_y"]), float(ic["bubble_radius"]),
+                                          _ptr(post), _ptr(bub), _ptr(amb))
             else:
                 raise ValueError(f"initial condition {typ!r} not supported")
 
