@@ -137,6 +137,23 @@ def shock_bubble_case(n: int = 2048, scheme: str = "MUSCLHancock", limiter: str 
     }
 
 
+def random_quadrant_case(n: int, seed: int, limiter: str = "MinBee", cfl: float = 0.8,
+                         t_end: float | None = None) -> dict:
+    """One four-quadrant Riemann problem drawn like the batched workload's cases (split in
+    [0.3,0.7]^2, rho in [0.1,2], p in [0.1,10], u, v in [-1,1]); t_end defaults to the time
+    the fastest initial wave needs to cross a quarter of the domain."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    split = (float(rng.uniform(0.3, 0.7)), float(rng.uniform(0.3, 0.7)))
+    states = [[float(rng.uniform(0.1, 2.0)), float(rng.uniform(-1.0, 1.0)),
+               float(rng.uniform(-1.0, 1.0)), float(rng.uniform(0.1, 10.0))] for _ in range(4)]
+    if t_end is None:
+        smax = max(max(abs(u), abs(v)) + math.sqrt(GAMMA * p / r) for r, u, v, p in states)
+        t_end = 0.25 / smax
+    return quadrant_case(n, scheme="MUSCLHancock", limiter=limiter, cfl=cfl, split=split,
+                         states=states, t_end=t_end)
+
+
 def batch_manifest(count: int = 512, seed: int = 0, side_min: int = 64, side_max: int = 1024,
                    limiter: str = "MinBee", cfl: float = 0.8) -> dict:
     """The batched workload: `count` independent square four-quadrant Riemann problems on
@@ -166,5 +183,6 @@ def total_cells(case: dict) -> int:
     return sum(b["x_cells"] * b["y_cells"] for b in case["mesh"]["blocks"])
 
 
-__all__ = ["quadrant_case", "forward_facing_step_case", "shock_bubble_case", "batch_manifest", "to_json", "total_cells",
+__all__ = ["quadrant_case", "forward_facing_step_case", "shock_bubble_case", "random_quadrant_case",
+           "batch_manifest", "to_json", "total_cells",
            "QUAD_NE", "QUAD_NW", "QUAD_SW", "QUAD_SE", "GAMMA", "math"]

@@ -566,6 +566,7 @@ struct hf_lc {
     unsigned long long* rejected = nullptr;
     double* loss = nullptr;
     int cur = 0;
+    long long steps = 0;       // steps since time 0 (TimeStep's start-up multiplier)
     long long adam_t = 0;
     double t = 0.0;
     std::vector<void*> allocs;
@@ -731,6 +732,7 @@ int hf_lc_step(hf_lc* L, double dt, int use_mlp, int64_t* rejected_cells) {
     LCK(cudaGetLastError());
     L->cur ^= 1;
     L->t += dt;
+    L->steps += 1;
     if (rejected_cells) {
         unsigned long long v = 0;
         if (use_mlp) LCK(cudaMemcpyAsync(&v, L->rejected, 8, cudaMemcpyDeviceToHost, L->stream));
@@ -748,6 +750,9 @@ int hf_lc_run_to(hf_lc* L, double t_end, int use_mlp, int64_t* steps, int64_t* r
         double dt;
         int r = hf_lc_cfl_dt(L, &dt);
         if (r) return r;
+        // the reference's TimeStep uses 0.2 x CFL for its first 10 calls; a MUSCL-Hancock
+        // step makes two (step and predictor), so the first 5 steps are reduced
+        if (L->steps < 5) dt *= 0.2;
         if (L->t + dt > t_end) dt = t_end - L->t;
         int64_t rc = 0;
         r = hf_lc_step(L, dt, use_mlp, use_mlp ? &rc : nullptr);
@@ -761,7 +766,12 @@ int hf_lc_run_to(hf_lc* L, double t_end, int use_mlp, int64_t* steps, int64_t* r
     return HF_OK;
 }
 
-int hf_lc_set_time(hf_lc* L, double t) { if (!L) return HF_ERR_ARG; L->t = t; return HF_OK; }
+int hf_lc_set_time(hf_lc* L, double t) {
+    if (!L) return HF_ERR_ARG;
+    L->t = t;
+    if (t == 0.0) L->steps = 0;
+    return HF_OK;
+}
 int hf_lc_get_time(hf_lc* L, double* t) { if (!L || !t) return HF_ERR_ARG; *t = L->t; return HF_OK; }
 int hf_lc_set_bound(hf_lc* L, double bound) { if (!L || bound <= 0) return HF_ERR_ARG; L->bound = bound; return HF_OK; }
 

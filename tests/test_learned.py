@@ -1,0 +1,143 @@
+"""Learned coarse solver: the MLP kernels against the CPU oracle (oracle/mlp_oracle.py),
+the FP32 plain step against the FP64 step, the guard, and a training run that must beat
+the plain coarse step it corrects."""
+import numpy as np
+import pytest
+
+
+def test_bf16_rounding_matches_torch():
+    import torch
+    from oracle import mlp_oracle as M
+    x = np.random.default_rng(0).standard_normal(10000).astype(np.float32) * 10
+    x[:4] = [0.0, -0.0, 1e-40, 3.0e38]
+    want = torch.from_numpy(x).to(torch.bfloat16).view(torch.int16).numpy().view(np.uint16)
+    np.testing.assert_array_equal(M.bf16_bits(x), want)
+
+
+def test_box_filter_conserves_totals():
+    from hyperflow_gb300.learned import box_filter
+    U = np.random.default_rng(1).uniform(0.1, 2.0, (4, 64, 64))
+    F = box_filter(U, 4)
+    assert F.shape == (4, 16, 16)
+    np.testing.assert_allclose(F.sum(axis=(1, 2)) * 16, U.sum(axis=(1, 2)), rtol=1e-13)
+
+
+def test_mlp_oracle_gradient_is_the_derivative():
+    """Central differences confirm the oracle's backward formulas on the unrounded network
+    (BF16 rounding of activations is piecewise constant, so the kernels' backward -- like
+    any BF16 training -- passes it straight through)."""
+    from oracle import mlp_oracle as M
+    from hyperflow_gb300.learned import init_params
+    rng = np.random.default_rng(2)
+    p = init_params(3, out_scale=1.0).astype(np.float64)
+    x = M.bf16_bits(rng.standard_normal((8, 64)).astype(np.float32))
+    dy = rng.standard_normal((8, 4))
+    g = M.backward(p, x, dy, rounding=False)
+    for k in (M.OFF_B3 + 1, M.OFF_W3 + 70, M.OFF_B2 + 5, M.OFF_W2 + 300, M.OFF_B1 + 7, M.OFF_W1 + 1234):
+        e = np.zeros_like(p)
+        e[k] = 1e-5
+        fp = (M.forward(p + e, x, rounding=False)[0] * dy).sum()
+        fm = (M.forward(p - e, x, rounding=False)[0] * dy).sum()
+        assert abs((fp - fm) / 2e-5 - g[k]) < 1e-6 * (1 + abs(g[k]))
+
+
+def _rand_case(rng, nf=1000):
+    from oracle import mlp_oracle as M
+    from hyperflow_gb300.learned import init_params
+    p = init_params(int(rng.integers(100)), out_scale=1.0)
+    p[M.OFF_B1:M.OFF_W2] = rng.uniform(-0.5, 0.5, 64)
+    p[M.OFF_B3:] = rng.uniform(-0.1, 0.1, 4)
+    x = M.bf16_bits(rng.standard_normal((nf, 64)).astype(np.float32))
+    return p, x
+
+
+@pytest.mark.gpu
+def test_mlp_forward_on_tensor_cores_matches_oracle():
+    from oracle import mlp_oracle as M
+    from hyperflow_gb300.learned import LearnedSolver
+    rng = np.random.default_rng(4)
+    ls = LearnedSolver(64, 1 / 64)
+    for nf in (1000, 17, 2 * 65 * 64):          # partial tiles and a full grid's faces
+        p, x = _rand_case(rng, nf)
+        ls.set_params(p)
+        y = ls.mlp_forward(x)
+        ref, _ = M.forward(p, x)
+        # FP32 accumulation order and tanhf vs tanh: BF16-level agreement
+        np.testing.assert_allclose(y, ref, rtol=2e-2, atol=2e-3)
+        assert np.abs(y - ref).mean() < 1e-3
+
+
+@pytest.mark.gpu
+def test_mlp_backward_matches_oracle():
+    from oracle import mlp_oracle as M
+    from hyperflow_gb300.learned import LearnedSolver
+    rng = np.random.default_rng(5)
+    ls = LearnedSolver(64, 1 / 64)
+    p, x = _rand_case(rng, 777)
+    ls.set_params(p)
+    dy = rng.standard_normal((777, 4)).astype(np.float32)
+    g = ls.mlp_backward(x, dy)
+    ref = M.backward(p, x, dy)
+    for a, b in ((M.OFF_W1, M.OFF_B1), (M.OFF_B1, M.OFF_W2), (M.OFF_W2, M.OFF_B2), (M.OFF_B2, M.OFF_W3),
+                 (M.OFF_W3, M.OFF_B3), (M.OFF_B3, M.NPARAM)):
+        err = np.linalg.norm(g[a:b] - ref[a:b]) / (np.linalg.norm(ref[a:b]) + 1e-12)
+        assert err < 2e-2, (a, b, err)
+
+
+@pytest.mark.gpu
+def test_fp32_plain_step_tracks_fp64_step():
+    """The learned solver's plain FP32 path is the reference scheme in single precision."""
+    from hyperflow_gb300 import CartSolver, cases
+    from hyperflow_gb300.learned import LearnedSolver
+    case = cases.quadrant_case(96, scheme="MUSCLHancock", limiter="MinBee")
+    s = CartSolver(case)
+    U0 = s.state(0)[:, 2:-2, 2:-2]
+    ls = LearnedSolver(96, 1 / 96)
+    ls.set_state(U0.astype(np.float32))
+    for _ in range(20):
+        dt = s.step()
+        ls.step(dt, use_mlp=False)
+    U = s.state(0)[:, 2:-2, 2:-2]
+    V = ls.state().astype(np.float64)
+    assert np.abs(V - U).max() / np.abs(U).max() < 2e-4
+
+
+@pytest.mark.gpu
+def test_guard_keeps_positivity_and_rejects():
+    from oracle import mlp_oracle as M
+    from hyperflow_gb300 import CartSolver, cases
+    from hyperflow_gb300.learned import LearnedSolver, init_params
+    case = cases.shock_bubble_case(128)
+    s = CartSolver(case)
+    U0 = s.state(0)[:, 2:-2, 2:-2].astype(np.float32)
+    ls = LearnedSolver(128, 1 / 128)
+    p = init_params(0)
+    p[M.OFF_B3:] = [5.0, -5.0, 5.0, -50.0]          # absurd corrections
+    ls.set_params(p)
+    ls.set_state(U0)
+    rejected = 0
+    for _ in range(10):
+        rejected += ls.step(ls.cfl_dt(), use_mlp=True)
+    U = ls.state().astype(np.float64)
+    rho = U[0]
+    pres = 0.4 * (U[3] - 0.5 * (U[1] ** 2 + U[2] ** 2) / rho)
+    assert rejected > 0 and (rho > 0).all() and (pres > 0).all()
+
+
+@pytest.mark.gpu
+def test_training_beats_the_plain_coarse_step():
+    """Trained on filtered 256^2 FP64 runs (4x coarser grid: 64^2), the corrected one-step
+    error on held-out pairs is below the plain coarse step's -- what the network gains."""
+    from hyperflow_gb300 import cases
+    from hyperflow_gb300.learned import LearnedSolver, fine_pairs, init_params, one_step_loss, train
+    tr = fine_pairs(cases.shock_bubble_case(256, t_end=1.0), 0.12, stride=2)
+    tr += fine_pairs(cases.quadrant_case(256, scheme="MUSCLHancock", limiter="MinBee"), 0.06, stride=2)
+    held = fine_pairs(cases.shock_bubble_case(256, bubble=(0.45, 0.55), radius=0.18, t_end=1.0), 0.1, stride=3)
+    ls = LearnedSolver(64, 1 / 64)
+    ls.set_params(init_params(0))
+    losses, w = train(ls, tr, iters=600, lr=2e-3)
+    plain = one_step_loss(ls, held, w, use_mlp=False)
+    learned = one_step_loss(ls, held, w, use_mlp=True)
+    assert np.isfinite(losses).all()
+    assert losses[-50:].mean() < losses[:50].mean()
+    assert learned < 0.9 * plain, (learned, plain)
