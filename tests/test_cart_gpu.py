@@ -158,3 +158,17 @@ def test_gpu_transpose_symmetry():
     # rounding asymmetry grows through limiter switches (~1e-8 after 60 steps); an x/y
     # mix-up in a kernel would show at O(1)
     np.testing.assert_allclose(Ua, sym, rtol=1e-6, atol=1e-9)
+
+
+def test_gpu_shock_bubble_matches_oracle(port_lib):
+    """The shock-bubble initial condition (no reference counterpart) on the GPU path and in
+    the oracle, 512^2 MUSCL-Hancock, bit for bit."""
+    from hyperflow_gb300 import cases
+    from oracle.oracle import Oracle
+    case = cases.shock_bubble_case(512)
+    o = Oracle(case, nthreads=8)
+    s = _solver(case)
+    np.testing.assert_array_equal(s.state(0), o.state(0))
+    o.run(40)
+    s.run(40)
+    np.testing.assert_array_equal(s.state(0), o.state(0))
