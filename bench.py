@@ -294,7 +294,8 @@ def main():
                "kind": "port",
                "sample": f"first {n_cpu} steps of the same workload (all {cells} cells)"}
 
-    launches_per_step = 3 + nb   # ghost fill, ghost CFL + dt, one stencil per block, finalize
+    # step start, one ghost-fill launch per block side, ghost CFL + dt, one stencil per block, finalize
+    launches_per_step = 3 + 5 * nb
     if rank == 0:
         line = {
             "metric": "Mcell-updates/s", "value": value, "unit": "Mcell-updates/s",

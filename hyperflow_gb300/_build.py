@@ -17,8 +17,9 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(PKG, "csrc")
 OBJ = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libhyperflow_gb300.so")
+HOSTMATH_LIB = os.path.join(PKG, "libhf_hostmath.so")
 
-SOURCES = ["hf_cart.cu", "hf_api.cpp", "hf_uns.cu", "hf_noalloc.cu", "hf_batch.cu", "hf_learned.cu"]
+SOURCES = ["hf_cart.cu", "hf_api.cpp", "hf_uns.cu", "hf_noalloc.cu", "hf_batch.cu", "hf_learned.cu", "hf_diag.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--fmad=false", "-Xcompiler", "-fPIC",
               "-Xcompiler", "-ffp-contract=off", "-I" + os.path.join(PKG, "..", "include")]
@@ -52,6 +53,11 @@ def build(verbose: bool = False, extra: list[str] | None = None) -> str:
         objs = list(ex.map(lambda s: _compile(s, extra or []), srcs))
     cmd = [nvcc(), *ARCH, "-shared", "-o", LIB, *objs]
     r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+    # the kernels' arithmetic built for the host (CPU tests of the device math)
+    hm = _compile("hf_hostmath.cu", extra or [])
+    r = subprocess.run([nvcc(), *ARCH, "-shared", "-o", HOSTMATH_LIB, hm], capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
     if verbose:

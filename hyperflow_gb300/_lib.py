@@ -40,6 +40,13 @@ SIGNATURES = {
     "hf_stream": (_i, [_p, C.POINTER(_p)]),
     "hf_profile": (_i, [_p, _i]),
     "hf_kernel_time": (_i, [_p, _i, C.POINTER(_d), C.POINTER(_i64)]),
+    "hf_frames_enable": (_i, [_p, _i]),
+    "hf_frame_len": (_i, [_p, C.POINTER(_i64)]),
+    "hf_frames_pending": (_i, [_p, C.POINTER(_i64)]),
+    "hf_frame_pop": (_i, [_p, _p, C.POINTER(_d), C.POINTER(_i64)]),
+    "hf_checkpoint_size": (_i, [_p, C.POINTER(_sz)]),
+    "hf_checkpoint_save": (_i, [_p, _p, _sz]),
+    "hf_checkpoint_load": (_i, [_p, _p, _sz]),
     "hf_status_string": (C.c_char_p, [_i]),
     "hf_time_step_noalloc": (_i, [_p, _i, _i, _i, _d, _d, _d, _d, _i64, _p, _p]),
     # unstructured (include/hyperflow_gb300_uns.h)
@@ -57,6 +64,7 @@ SIGNATURES = {
     "hf_uns_get_time": (_i, [_p, C.POINTER(_d), C.POINTER(_i64), C.POINTER(_d)]),
     "hf_uns_hllc_errors": (_i, [_p, C.POINTER(_i64)]),
     "hf_uns_stream": (_i, [_p, C.POINTER(_p)]),
+    "hf_uns_set_edge_mode": (_i, [_p, _i]),
     "hf_last_error_message": (C.c_char_p, [_p]),
     # batched (include/hyperflow_gb300_batch.h)
     "hf_batch_create": (_i, [C.c_char_p, _sz, C.POINTER(_p)]),
@@ -94,6 +102,8 @@ SIGNATURES = {
     "hf_lc_mlp_forward": (_i, [_p, _p, _i, _p]),
     "hf_lc_mlp_backward": (_i, [_p, _p, _p, _i, _p]),
     "hf_lc_stream": (_i, [_p, C.POINTER(_p)]),
+    # self-tests (include/hyperflow_gb300_diag.h)
+    "hf_diag_div_check": (_i, [C.c_uint64, _i64, _i, C.POINTER(_i64), _p]),
 }
 
 _lib = None

@@ -81,6 +81,13 @@ struct hf_ctx {
     std::vector<double*> allocs;
     double* pinned = nullptr;   // staging for layout conversion
     size_t pinned_n = 0;
+    int side_len[2 * HF_MAXB] = {};   // total_x, total_y per block (ghost-fill launch sizes)
+    // frame output: simulation.animation of the case and the device frame ring
+    bool has_anim = false;
+    double anim_duration = 0.0, anim_fps = 0.0;
+    hf::FrameRing ring{};
+    int ring_slots = 0;
+    long long drained = 0;      // host count of frames popped from the ring
     int next_block = 0;         // next block hf_advance_block expects
     long long host_step = 0;    // mirror of ctrl.step while the host drives the steps
     // graphs of one step (index = clamp flag)
@@ -256,6 +263,11 @@ int parse_case(hf_ctx* ctx, const Json& cfg) {
     ctx->cfl = sim["cfl"].number();
     ctx->t_start = sim["t_start"].number();
     ctx->t_end = sim["t_end"].number();
+    if (sim.has("animation")) {
+        ctx->has_anim = true;
+        ctx->anim_duration = sim["animation"]["duration"].number();
+        ctx->anim_fps = sim["animation"]["fps"].number();
+    }
     const Json& blocks = cfg["mesh"]["blocks"];
     ctx->nblocks = (int)blocks.size();
     if (ctx->nblocks < 1 || ctx->nblocks > HF_MAXB)
@@ -379,7 +391,7 @@ void ev_record(hf_ctx* ctx, int kind, bool start) {
 // one step's kernels after the ghost fill: dt, then every block, then finalize
 int enqueue_step(hf_ctx* ctx, bool profiled) {
     if (profiled) ev_record(ctx, 1, true);
-    CK(hf::launch_bc_fill(ctx->dctrl, ctx->dmesh, ctx->stream));
+    CK(hf::launch_bc_fill(ctx->dctrl, ctx->dmesh, ctx->side_len, ctx->nblocks, ctx->stream));
     CK(hf::launch_ghost_cfl(ctx->dctrl, ctx->dmesh, ctx->hmesh.total_ghost, ctx->stream));
     if (profiled) { ev_record(ctx, 1, false); ev_record(ctx, 0, true); }
     for (int b = 0; b < ctx->nblocks; ++b)
@@ -387,6 +399,7 @@ int enqueue_step(hf_ctx* ctx, bool profiled) {
                               ctx->scheme, ctx->limiter, &ctx->tmap[b][0], &ctx->tmap[b][1],
                               ctx->stream));
     if (profiled) ev_record(ctx, 0, false);
+    if (ctx->ring_slots > 0) CK(hf::launch_frame_copy(ctx->dctrl, ctx->dmesh, ctx->ring, ctx->stream));
     CK(hf::launch_finalize(ctx->dctrl, ctx->stream));
     return HF_OK;
 }
@@ -464,6 +477,8 @@ int hf_create(const char* case_json, size_t len, hf_ctx** out) {
             CK(cudaMemsetAsync(p, 0, n * sizeof(double), ctx->stream));
             D.buf[k] = p;
         }
+        ctx->side_len[2 * b] = B.tx;
+        ctx->side_len[2 * b + 1] = B.ty;
         D.ghost_off = goff;
         D.ghost_count = B.tx * B.ty - B.nx * B.ny;
         goff += D.ghost_count;
@@ -514,6 +529,7 @@ void hf_destroy(hf_ctx* ctx) {
         for (auto& pr : ctx->ev[k]) { cudaEventDestroy(pr.first); cudaEventDestroy(pr.second); }
     }
     for (double* p : ctx->allocs) cudaFree(p);
+    if (ctx->ring.base) cudaFree(ctx->ring.base);
     if (ctx->dmesh) cudaFree(ctx->dmesh);
     if (ctx->dctrl) cudaFree(ctx->dctrl);
     if (ctx->pinned) cudaFreeHost(ctx->pinned);
@@ -592,7 +608,7 @@ int hf_get_state(hf_ctx* ctx, int b, double* cons, int layout) {
 int hf_apply_bcs(hf_ctx* ctx) {
     if (!ctx) return HF_ERR_ARG;
     if (ctx->next_block != 0) return fail(ctx, HF_ERR_STATE, "apply_bcs in the middle of a step");
-    CK(hf::launch_bc_fill(ctx->dctrl, ctx->dmesh, ctx->stream));
+    CK(hf::launch_bc_fill(ctx->dctrl, ctx->dmesh, ctx->side_len, ctx->nblocks, ctx->stream));
     return HF_OK;
 }
 
@@ -715,6 +731,186 @@ int hf_profile(hf_ctx* ctx, int enable) {
     CK(cudaStreamSynchronize(ctx->stream));
     ctx->profile = enable != 0;
     ctx->ev_used[0] = ctx->ev_used[1] = 0;
+    return HF_OK;
+}
+
+// ---- frame output (Simulation::solve's cadence, simulation.cpp:57-122) ----
+
+int hf_frames_enable(hf_ctx* ctx, int ring_slots) {
+    if (!ctx || ring_slots < 0 || ring_slots == 1 || ring_slots > HF_MAXRING) return HF_ERR_ARG;
+    if (ring_slots > 0 && !ctx->has_anim)
+        return fail(ctx, HF_ERR_ARG, "the case has no simulation.animation {duration, fps}");
+    if (ctx->next_block != 0) return fail(ctx, HF_ERR_STATE, "frames_enable in the middle of a step");
+    CK(cudaStreamSynchronize(ctx->stream));
+    for (int k = 0; k < 2; ++k)
+        if (ctx->graph[k]) { cudaGraphExecDestroy(ctx->graph[k]); ctx->graph[k] = nullptr; }
+    if (ctx->ring.base) { CK(cudaFree(ctx->ring.base)); ctx->ring.base = nullptr; }
+    ctx->ring_slots = 0;
+    long long len = 0;
+    for (int b = 0; b < ctx->nblocks; ++b) {
+        ctx->ring.off[b] = len;
+        len += 4LL * ctx->blocks[b].nx * ctx->blocks[b].ny;
+    }
+    ctx->ring.slot_len = len;
+    if (ring_slots > 0) {
+        CK(cudaMalloc(&ctx->ring.base, (size_t)ring_slots * len * sizeof(double)));
+        ctx->ring_slots = ring_slots;
+    }
+    // the interval exactly as simulation.cpp:57 forms it
+    const double interval = ring_slots > 0 ? ctx->t_end / (ctx->anim_duration * ctx->anim_fps) : 0.0;
+    hf::Ctrl C;
+    CK(cudaMemcpy(&C, ctx->dctrl, sizeof C, cudaMemcpyDeviceToHost));
+    C.frames = ring_slots > 0 ? 1 : 0;
+    C.ring_slots = ring_slots;
+    C.frame_interval = interval;
+    C.captured = C.drained = 0;
+    ctx->drained = 0;
+    CK(cudaMemcpy(ctx->dctrl, &C, sizeof C, cudaMemcpyHostToDevice));
+    return HF_OK;
+}
+
+int hf_frame_len(const hf_ctx* ctx, int64_t* n) {
+    if (!ctx || !n) return HF_ERR_ARG;
+    long long len = 0;
+    for (int b = 0; b < ctx->nblocks; ++b) len += 4LL * ctx->blocks[b].nx * ctx->blocks[b].ny;
+    *n = len;
+    return HF_OK;
+}
+
+int hf_frames_pending(hf_ctx* ctx, int64_t* n) {
+    if (!ctx || !n) return HF_ERR_ARG;
+    long long cap = 0;
+    CK(cudaStreamSynchronize(ctx->stream));
+    CK(cudaMemcpy(&cap, &ctx->dctrl->captured, sizeof cap, cudaMemcpyDeviceToHost));
+    *n = ctx->ring_slots > 0 ? cap - ctx->drained : 0;
+    return HF_OK;
+}
+
+int hf_frame_pop(hf_ctx* ctx, double* cons, double* t, int64_t* index) {
+    if (!ctx) return HF_ERR_ARG;
+    if (ctx->ring_slots == 0) return fail(ctx, HF_ERR_STATE, "frames are not enabled");
+    hf::Ctrl C;
+    CK(cudaStreamSynchronize(ctx->stream));
+    CK(cudaMemcpy(&C, ctx->dctrl, sizeof C, cudaMemcpyDeviceToHost));
+    if (C.captured == ctx->drained) return fail(ctx, HF_ERR_STATE, "no frame pending");
+    const long long slot = ctx->drained % ctx->ring_slots;
+    if (cons)
+        CK(cudaMemcpy(cons, ctx->ring.base + slot * ctx->ring.slot_len,
+                      (size_t)ctx->ring.slot_len * sizeof(double), cudaMemcpyDeviceToHost));
+    if (t) *t = C.ring_t[slot];
+    if (index) *index = C.ring_idx[slot];
+    ctx->drained += 1;
+    long long d = ctx->drained;
+    CK(cudaMemcpy(&ctx->dctrl->drained, &d, sizeof d, cudaMemcpyHostToDevice));
+    return HF_OK;
+}
+
+// ---- checkpoint / restart ----
+
+namespace {
+struct CkptHeader {
+    char magic[8];
+    uint32_t version, ctrl_bytes;
+    int32_t nblocks, scheme, limiter, ghost;
+    double gamma, cfl, t_end;
+    int32_t tx[HF_MAXB], ty[HF_MAXB], pitch[HF_MAXB];
+    uint64_t state_bytes;
+};
+const char kCkptMagic[8] = {'H', 'F', 'C', 'K', 'P', 'T', '0', '1'};
+
+CkptHeader ckpt_header(const hf_ctx* ctx) {
+    CkptHeader h;
+    std::memset(&h, 0, sizeof h);
+    std::memcpy(h.magic, kCkptMagic, 8);
+    h.version = 1;
+    h.ctrl_bytes = (uint32_t)sizeof(hf::Ctrl);
+    h.nblocks = ctx->nblocks;
+    h.scheme = ctx->scheme;
+    h.limiter = ctx->limiter;
+    h.ghost = ctx->ghost;
+    h.gamma = ctx->gamma;
+    h.cfl = ctx->cfl;
+    h.t_end = ctx->t_end;
+    uint64_t n = 0;
+    for (int b = 0; b < ctx->nblocks; ++b) {
+        h.tx[b] = ctx->blocks[b].tx;
+        h.ty[b] = ctx->blocks[b].ty;
+        h.pitch[b] = ctx->blocks[b].pitch;
+        n += 2ull * 4 * ctx->blocks[b].ty * ctx->blocks[b].pitch * sizeof(double);
+    }
+    h.state_bytes = n;
+    return h;
+}
+}  // namespace
+
+int hf_checkpoint_size(const hf_ctx* ctx, size_t* bytes) {
+    if (!ctx || !bytes) return HF_ERR_ARG;
+    CkptHeader h = ckpt_header(ctx);
+    *bytes = sizeof h + sizeof(hf::Ctrl) + (size_t)h.state_bytes;
+    return HF_OK;
+}
+
+int hf_checkpoint_save(hf_ctx* ctx, void* buf, size_t bytes) {
+    if (!ctx || !buf) return HF_ERR_ARG;
+    size_t need = 0;
+    hf_checkpoint_size(ctx, &need);
+    if (bytes < need) return fail(ctx, HF_ERR_ARG, "checkpoint buffer too small");
+    if (ctx->next_block != 0) return fail(ctx, HF_ERR_STATE, "checkpoint in the middle of a step");
+    CkptHeader h = ckpt_header(ctx);
+    hf::Ctrl C;
+    CK(cudaStreamSynchronize(ctx->stream));
+    CK(cudaMemcpy(&C, ctx->dctrl, sizeof C, cudaMemcpyDeviceToHost));
+    if (ctx->ring_slots > 0 && C.captured != ctx->drained)
+        return fail(ctx, HF_ERR_STATE, "pop the pending frames before a checkpoint");
+    char* p = static_cast<char*>(buf);
+    std::memcpy(p, &h, sizeof h);
+    p += sizeof h;
+    std::memcpy(p, &C, sizeof C);
+    p += sizeof C;
+    for (int b = 0; b < ctx->nblocks; ++b)
+        for (int k = 0; k < 2; ++k) {
+            size_t n = (size_t)4 * ctx->blocks[b].ty * ctx->blocks[b].pitch * sizeof(double);
+            CK(cudaMemcpy(p, ctx->hmesh.b[b].buf[k], n, cudaMemcpyDeviceToHost));
+            p += n;
+        }
+    return HF_OK;
+}
+
+int hf_checkpoint_load(hf_ctx* ctx, const void* buf, size_t bytes) {
+    if (!ctx || !buf) return HF_ERR_ARG;
+    if (ctx->next_block != 0) return fail(ctx, HF_ERR_STATE, "restore in the middle of a step");
+    size_t need = 0;
+    hf_checkpoint_size(ctx, &need);
+    if (bytes < need) return fail(ctx, HF_ERR_ARG, "checkpoint too short for this case");
+    CkptHeader want = ckpt_header(ctx), got;
+    std::memcpy(&got, buf, sizeof got);
+    if (std::memcmp(got.magic, kCkptMagic, 8) != 0 || got.version != want.version)
+        return fail(ctx, HF_ERR_PARSE, "not a checkpoint of this format version");
+    if (std::memcmp(&got, &want, sizeof got) != 0)
+        return fail(ctx, HF_ERR_ARG, "checkpoint was taken from a different case or build");
+    const char* p = static_cast<const char*>(buf) + sizeof got;
+    hf::Ctrl C, cur;
+    std::memcpy(&C, p, sizeof C);
+    p += sizeof C;
+    CK(cudaStreamSynchronize(ctx->stream));
+    CK(cudaMemcpy(&cur, ctx->dctrl, sizeof cur, cudaMemcpyDeviceToHost));
+    // the ring belongs to this context: keep its configuration, start it empty
+    C.frames = cur.frames;
+    C.ring_slots = cur.ring_slots;
+    C.frame_interval = cur.frame_interval;
+    C.captured = C.drained = 0;
+    C.clamp = 0;
+    C.done = 0;
+    C.err = 0;
+    ctx->drained = 0;
+    for (int b = 0; b < ctx->nblocks; ++b)
+        for (int k = 0; k < 2; ++k) {
+            size_t n = (size_t)4 * ctx->blocks[b].ty * ctx->blocks[b].pitch * sizeof(double);
+            CK(cudaMemcpy(ctx->hmesh.b[b].buf[k], p, n, cudaMemcpyHostToDevice));
+            p += n;
+        }
+    CK(cudaMemcpy(ctx->dctrl, &C, sizeof C, cudaMemcpyHostToDevice));
+    ctx->host_step = C.step;
     return HF_OK;
 }
 

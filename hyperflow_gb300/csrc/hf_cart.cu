@@ -41,7 +41,7 @@ __device__ void fill_side(const MeshDev* __restrict__ m, int b, int side, int p)
     double* __restrict__ d0 = B.buf[p];
     double* __restrict__ d1 = B.buf[p ^ 1];
     const double* __restrict__ src = E.buf[p];
-    for (int pos = threadIdx.x; pos < n; pos += blockDim.x) {
+    for (int pos = blockIdx.x * blockDim.x + threadIdx.x; pos < n; pos += gridDim.x * blockDim.x) {
         for (int k = 0; k < g; ++k) {
             int di, dj, si = 0, sj = 0;
             switch (side) {
@@ -80,29 +80,28 @@ __device__ void fill_side(const MeshDev* __restrict__ m, int b, int side, int p)
     }
 }
 
-__global__ void __launch_bounds__(1024) bc_fill_kernel(Ctrl* __restrict__ c,
-                                                       const MeshDev* __restrict__ m) {
-    __shared__ int s_done;
+// start of a step: stop at t_end (device loop), clear this step's accumulators
+__global__ void step_begin_kernel(Ctrl* __restrict__ c) {
     const int p = (int)(c->step & 1);
-    if (threadIdx.x == 0) {
-        int done = c->clamp && (c->t == c->t_end);
-        c->done = done;
-        s_done = done;
-        if (!done) {
-            for (int b = 0; b < HF_MAXB; ++b) {
-                c->ghost_s[b][0] = c->ghost_s[b][1] = 0ull;
-                c->int_s[p ^ 1][b][0] = c->int_s[p ^ 1][b][1] = 0ull;
-            }
-            c->ticket = 0u;
-        }
+    int done = c->clamp && (c->t == c->t_end);
+    // a step takes at most two frames: pause the loop while the ring lacks room for them
+    if (c->clamp && c->frames && c->captured - c->drained > c->ring_slots - 2) done = 1;
+    c->done = done;
+    c->snap_pre = c->snap_post = 0;
+    if (done) return;
+    for (int b = 0; b < HF_MAXB; ++b) {
+        c->ghost_s[b][0] = c->ghost_s[b][1] = 0ull;
+        c->int_s[p ^ 1][b][0] = c->int_s[p ^ 1][b][1] = 0ull;
     }
-    __syncthreads();
-    if (s_done) return;
-    for (int b = 0; b < m->nblocks; ++b)
-        for (int side = 0; side < 4; ++side) {
-            fill_side(m, b, side, p);
-            __syncthreads();
-        }
+    c->ticket = 0u;
+}
+
+// one side of one block; the sides run as consecutive launches in the reference order, so
+// a side sees every value the sides before it wrote
+__global__ void __launch_bounds__(256) bc_side_kernel(const Ctrl* __restrict__ c,
+                                                      const MeshDev* __restrict__ m, int b, int side) {
+    if (c->done) return;
+    fill_side(m, b, side, (int)(c->step & 1));
 }
 
 // ------------------------------------------------------------------------------------
@@ -171,7 +170,18 @@ __global__ void __launch_bounds__(kRedThreads) ghost_cfl_kernel(Ctrl* __restrict
     long long call = vc->calls;
     double dt = cfl_dt(&snap, call, 0, p, p);
     c->dt_cfl = dt;
-    if (c->clamp && c->t + dt > c->t_end) dt = c->t_end - c->t;   // simulation.cpp:88-90
+    const double t = c->t;
+    if (c->clamp && t + dt > c->t_end) dt = c->t_end - t;        // simulation.cpp:88-90
+    if (c->clamp && c->frames) {
+        const double cur = c->frame_next;
+        c->snap_pre = (cur == 0.0);                              // simulation.cpp:93-96
+        if ((t + dt > cur) && (cur > 0.0)) dt = cur - t;         // simulation.cpp:98-102
+        if (fabs(t - cur) < 1e-12) {                             // simulation.cpp:106-113
+            c->snap_post = 1;
+            c->frame_next = cur + c->frame_interval;
+        }
+        c->snap_t = t;
+    }
     c->dt = dt;
     c->calls = call + 1;
     c->ticket = 0u;
@@ -202,9 +212,51 @@ __global__ void __launch_bounds__(kRedThreads) interior_cfl_kernel(Ctrl* __restr
 
 __global__ void set_dt_kernel(Ctrl* c, double dt) { c->dt = dt; }
 
-// end of step: t += dt; the MUSCL-Hancock predictor calls advance the counter; flip parity
+// Frames of this step into the device ring: the interior of every block, SoA per block,
+// packed ([b][var][y][x]); the state before the update is still in buffer `step & 1` and the
+// updated one in the other buffer until finalize flips the parity.
+__global__ void __launch_bounds__(256) frame_copy_kernel(const Ctrl* __restrict__ c,
+                                                         const MeshDev* __restrict__ m,
+                                                         FrameRing ring) {
+    if (c->done) return;
+    const int pre = c->snap_pre, post = c->snap_post;
+    if (!pre && !post) return;
+    const int p = (int)(c->step & 1);
+    const long long R = c->ring_slots;
+    const long long slot_pre = c->captured % R, slot_post = (c->captured + pre) % R;
+    const int g = m->ghost;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (int which = 0; which < 2; ++which) {
+        if (which == 0 ? !pre : !post) continue;
+        double* __restrict__ dst = ring.base + (which == 0 ? slot_pre : slot_post) * ring.slot_len;
+        for (int b = 0; b < m->nblocks; ++b) {
+            const BlockDev& B = m->b[b];
+            const double* __restrict__ src = B.buf[which == 0 ? p : p ^ 1];
+            const long long plane = (long long)B.nx * B.ny, n = 4 * plane;
+            double* __restrict__ d = dst + ring.off[b];
+            for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride) {
+                const long long v = k / plane, r = k - v * plane;
+                const int j = (int)(r / B.nx), i = (int)(r - (long long)j * B.nx);
+                d[k] = src[(size_t)v * B.ty * B.pitch + (size_t)(j + g) * B.pitch + (i + g)];
+            }
+        }
+    }
+}
+
+// end of step: t += dt; the MUSCL-Hancock predictor calls advance the counter; record this
+// step's frames; flip parity
 __global__ void finalize_kernel(Ctrl* c) {
     if (c->done) return;
+    if (c->clamp && c->frames) {
+        for (int which = 0; which < 2; ++which) {
+            if (which == 0 ? !c->snap_pre : !c->snap_post) continue;
+            const long long slot = c->captured % c->ring_slots;
+            c->ring_t[slot] = c->snap_t;
+            c->ring_idx[slot] = c->frame_idx;
+            c->frame_idx = c->frame_idx + 1;
+            c->captured = c->captured + 1;
+        }
+    }
     c->t = c->t + c->dt;
     if (c->scheme == 1) c->calls = c->calls + c->nblocks;
     c->step = c->step + 1;
@@ -448,8 +500,14 @@ cudaError_t stencil_prepare() {
                                 (int)GoLayout<kGoTX, kGoTY>::BYTES);
 }
 
-cudaError_t launch_bc_fill(Ctrl* c, const MeshDev* m, cudaStream_t s) {
-    bc_fill_kernel<<<1, 1024, 0, s>>>(c, m);
+cudaError_t launch_bc_fill(Ctrl* c, const MeshDev* m, const int* side_len, int nblocks, cudaStream_t s) {
+    step_begin_kernel<<<1, 1, 0, s>>>(c);
+    for (int b = 0; b < nblocks; ++b)
+        for (int side = 0; side < 4; ++side) {
+            const int n = side_len[2 * b + (side == SIDE_BOTTOM || side == SIDE_TOP ? 0 : 1)];
+            int grid = (n + 255) / 256;
+            bc_side_kernel<<<grid < 1 ? 1 : grid, 256, 0, s>>>(c, m, b, side);
+        }
     return cudaGetLastError();
 }
 
@@ -470,6 +528,11 @@ cudaError_t launch_interior_cfl(Ctrl* c, const MeshDev* m, int b, int nx, int ny
 
 cudaError_t launch_set_dt(Ctrl* c, double dt, cudaStream_t s) {
     set_dt_kernel<<<1, 1, 0, s>>>(c, dt);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_frame_copy(Ctrl* c, const MeshDev* m, const FrameRing& ring, cudaStream_t s) {
+    frame_copy_kernel<<<4 * 152, 256, 0, s>>>(c, m, ring);
     return cudaGetLastError();
 }
 

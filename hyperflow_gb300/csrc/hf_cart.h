@@ -34,17 +34,28 @@ struct MeshDev {
     BlockDev b[HF_MAXB];
 };
 
+// the device frame ring: slots of slot_len doubles; block b's interior at off[b] in a slot
+struct FrameRing {
+    double* base;
+    long long slot_len;
+    long long off[HF_MAXB];
+};
+
 struct StencilTiles {
     int tx, ty;   // output cells per CTA tile
 };
 
 // launchers (all asynchronous on `s`)
-cudaError_t launch_bc_fill(Ctrl* c, const MeshDev* m, cudaStream_t s);
+// ghost fill: one launch per (block, side) in the reference order; side_len[2b] = total_x,
+// side_len[2b+1] = total_y of block b
+cudaError_t launch_bc_fill(Ctrl* c, const MeshDev* m, const int* side_len, int nblocks, cudaStream_t s);
 cudaError_t launch_ghost_cfl(Ctrl* c, const MeshDev* m, long long total_ghost, cudaStream_t s);
 cudaError_t launch_interior_cfl(Ctrl* c, const MeshDev* m, int b, int nx, int ny, int parity,
                                 cudaStream_t s);
 cudaError_t launch_set_dt(Ctrl* c, double dt, cudaStream_t s);
 cudaError_t launch_finalize(Ctrl* c, cudaStream_t s);
+// this step's frames (if any) into the ring; between the stencils and launch_finalize
+cudaError_t launch_frame_copy(Ctrl* c, const MeshDev* m, const FrameRing& ring, cudaStream_t s);
 cudaError_t launch_stencil(Ctrl* c, const MeshDev* m, int b, int nx, int ny, int scheme, int limiter,
                            const CUtensorMap* tm0, const CUtensorMap* tm1, cudaStream_t s);
 // halo-tile box of the stencil for the scheme (TMA box = tile + 2*ghost per axis)

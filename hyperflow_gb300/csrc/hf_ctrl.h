@@ -2,6 +2,7 @@
 #pragma once
 
 #define HF_MAXB 16
+#define HF_MAXRING 32
 
 namespace hf {
 
@@ -25,6 +26,17 @@ struct Ctrl {
     unsigned int ticket;
     int err;                                // first error code raised on the device
     long long hllc_errors;                  // HLLC "should not get here" zero fluxes
+    // frame output with Simulation::solve's cadence (device loop only, i.e. clamp set)
+    int frames;                             // frame clamp and capture on
+    int ring_slots;                         // depth of the device frame ring
+    int snap_pre, snap_post;                // this step takes a frame before / after its update
+    double frame_next;                      // the time of the next frame (cur_frame_out)
+    double frame_interval;                  // t_end / (duration * fps)
+    double snap_t;                          // time label of this step's frames
+    long long frame_idx;                    // frames taken so far, the final one excluded
+    long long captured, drained;            // frames put into / taken out of the ring
+    double ring_t[HF_MAXRING];              // time label per ring slot
+    long long ring_idx[HF_MAXRING];         // frame index per ring slot
 };
 
 enum : int {

@@ -2,8 +2,9 @@
 //
 // Arithmetic parity: all kernels are compiled with --fmad=false, so a*b+c stays a
 // rounded multiply followed by a rounded add, exactly as the reference's C++ (ISO
-// mode, no contraction) evaluates it.  FP64 division and sqrt are IEEE correctly
-// rounded on the GPU, as they are in libm.  Every expression below keeps the
+// mode, no contraction) evaluates it.  Divisions and square roots are correctly rounded
+// (div_rn / sqrt_rn of hf_intdiv.cuh compute them on the integer pipes, bit-identical to
+// the IEEE operations of the hardware and of libm).  Every expression below keeps the
 // reference's operand order; identical sub-expressions the reference evaluates more
 // than once (cons_to_prim inside cons_flux_x, prim_total_energy inside calc_U_k, ...)
 // are evaluated once and reused, which changes no result because they are
@@ -15,6 +16,7 @@
 #include <cuda_runtime.h>
 
 #include "hf_ctrl.h"
+#include "hf_intdiv.cuh"
 
 namespace hf {
 
@@ -23,9 +25,9 @@ __device__ __forceinline__ void raise_error(Ctrl* c, int code) { atomicCAS(&c->e
 // ------------------------------------------------------------------------------
 // std::min / std::max exactly (NaN-order semantics of the C++ library)
 // ------------------------------------------------------------------------------
-__device__ __forceinline__ double smin(double a, double b) { return (b < a) ? b : a; }
-__device__ __forceinline__ double smax(double a, double b) { return (a < b) ? b : a; }
-__device__ __forceinline__ double sgn(double v) { return (double)((v > 0.0) - (v < 0.0)); }
+HF_HD double smin(double a, double b) { return lt(b, a) ? b : a; }
+HF_HD double smax(double a, double b) { return lt(a, b) ? b : a; }
+HF_HD double sgn(double v) { return (double)((v > 0.0) - (v < 0.0)); }
 
 // ------------------------------------------------------------------------------
 // ideal-gas model, src/fvm_2d_cart/model/euler_ideal_gas/euler_ideal_gas.cpp
@@ -36,32 +38,32 @@ struct Prim {
     double Et;           // prim_total_energy (40-46), recomputed from the primitives
 };
 
-__device__ __forceinline__ Prim to_prim(double g1, double r, double ru, double rv, double E) {
+HF_HD Prim to_prim(double g1, double r, double ru, double rv, double E) {
     Prim w;
     w.r = r;
-    w.u = ru / r;
-    w.v = rv / r;
+    w.u = div_rn(ru, r);
+    w.v = div_rn(rv, r);
     w.q = w.u * w.u + w.v * w.v;
     w.p = g1 * (E - 0.5 * r * w.q);
-    double e = w.p / (w.r * g1);           // prim_internal_energy (32-36)
+    double e = div_rn(w.p, w.r * g1);      // prim_internal_energy (32-36)
     w.Et = w.r * (0.5 * w.q + e);
     return w;
 }
 
 // only the primitives (no energy): what TimeStep needs
-__device__ __forceinline__ void to_prim_short(double g1, double r, double ru, double rv, double E,
+HF_HD void to_prim_short(double g1, double r, double ru, double rv, double E,
                                               double& u, double& v, double& p) {
-    u = ru / r;
-    v = rv / r;
+    u = div_rn(ru, r);
+    v = div_rn(rv, r);
     p = g1 * (E - 0.5 * r * (u * u + v * v));
 }
 
 // prim_speed_of_sound (60-64)
-__device__ __forceinline__ double sound(double g, double r, double p) { return sqrt(g * p / r); }
+HF_HD double sound(double g, double r, double p) { return sqrt_rn(div_rn(g * p, r)); }
 
 // cons_flux_x / cons_flux_y (113-149): rho*u*u == (rho*u)*u etc.
 template <int DIR>
-__device__ __forceinline__ void flux(const Prim& w, double* f) {
+HF_HD void flux(const Prim& w, double* f) {
     if (DIR == 0) {
         double ru = w.r * w.u;
         f[0] = ru;
@@ -83,10 +85,10 @@ __device__ __forceinline__ void flux(const Prim& w, double* f) {
 // Returns 1 when the "should not get here" branch yields the zero flux.
 // ------------------------------------------------------------------------------
 template <int DIR>
-__device__ __forceinline__ void star_flux(const double* UK, const Prim& wK, double SK, double Ss,
+HF_HD void star_flux(const double* UK, const Prim& wK, double SK, double Ss,
                                           const double* FK, double* F) {
     double velK = DIR == 0 ? wK.u : wK.v;
-    double coef = wK.r * ((SK - velK) / (SK - Ss));
+    double coef = wK.r * div_rn(SK - velK, SK - Ss);
     double us[4];
     us[0] = coef;
     if (DIR == 0) {
@@ -96,36 +98,36 @@ __device__ __forceinline__ void star_flux(const double* UK, const Prim& wK, doub
         us[1] = coef * wK.u;
         us[2] = coef * Ss;
     }
-    us[3] = coef * (wK.Et / wK.r + (Ss - velK) * (Ss + (wK.p / (wK.r * (SK - velK)))));
+    us[3] = coef * (div_rn(wK.Et, wK.r) + (Ss - velK) * (Ss + div_rn(wK.p, wK.r * (SK - velK))));
 #pragma unroll
     for (int i = 0; i < 4; ++i) F[i] = FK[i] + SK * (us[i] - UK[i]);
 }
 
 template <int DIR>
-__device__ __forceinline__ int hllc(const double* UL, const Prim& wL, double aL, const double* FL,
+HF_HD int hllc(const double* UL, const Prim& wL, double aL, const double* FL,
                                     const double* UR, const Prim& wR, double aR, const double* FR,
                                     double* F) {
     double velL = DIR == 0 ? wL.u : wL.v;
     double velR = DIR == 0 ? wR.u : wR.v;
     double SL = smin(velL - aL, velR - aR);
     double SR = smax(velL + aL, velR + aR);
-    if (0.0 <= SL) {
+    if (ge0(SL)) {
 #pragma unroll
         for (int i = 0; i < 4; ++i) F[i] = FL[i];
         return 0;
     }
     double num = wR.p - wL.p + wL.r * velL * (SL - velL) - wR.r * velR * (SR - velR);
     double den = wL.r * (SL - velL) - wR.r * (SR - velR);
-    double Ss = num / den;
-    if (SL <= 0.0 && 0.0 <= Ss) {
+    double Ss = div_rn(num, den);
+    if (le0(SL) && ge0(Ss)) {
         star_flux<DIR>(UL, wL, SL, Ss, FL, F);
         return 0;
     }
-    if (Ss <= 0.0 && 0.0 <= SR) {
+    if (le0(Ss) && ge0(SR)) {
         star_flux<DIR>(UR, wR, SR, Ss, FR, F);
         return 0;
     }
-    if (0.0 >= SR) {
+    if (le0(SR)) {
 #pragma unroll
         for (int i = 0; i < 4; ++i) F[i] = FR[i];
         return 0;
@@ -137,7 +139,7 @@ __device__ __forceinline__ int hllc(const double* UL, const Prim& wL, double aL,
 
 // HLLC from two conservative states (computes primitives, sound speeds, fluxes)
 template <int DIR>
-__device__ __forceinline__ int hllc_cons(double g, double g1, const double* UL, const double* UR,
+HF_HD int hllc_cons(double g, double g1, const double* UL, const double* UR,
                                          double* F) {
     Prim wL = to_prim(g1, UL[0], UL[1], UL[2], UL[3]);
     Prim wR = to_prim(g1, UR[0], UR[1], UR[2], UR[3]);
@@ -156,33 +158,36 @@ __device__ __forceinline__ int hllc_cons(double g, double g1, const double* UL, 
 // ------------------------------------------------------------------------------
 constexpr double kTol = 1e-6;
 
-__device__ __forceinline__ double xi_right(double r) {
+HF_HD double xi_right(double r) {
     // Limiter::xi_right + denom_tol (limiter.cpp:26-53): 2*beta / (1 - omega + (1 + omega) r)
     double den = 1.0 + r;   // (1.0 - 0.0) + (1.0 + 0.0) * r rounds to the same value
-    if (fabs(den) < kTol) den = (den == 0.0) ? kTol : kTol * sgn(den);
-    return 2.0 / den;
+    if ((f64_bits(den) & kAbs) < f64_bits(kTol)) den = (den == 0.0) ? kTol : kTol * sgn(den);
+    return div_rn(2.0, den);
 }
 
 template <int LIM>
-__device__ __forceinline__ double limiter(double r) {
+HF_HD double limiter(double r) {
     if (LIM == 0) {   // MinBeeLimiter::operator() minbee.cpp:29-38
-        if (r <= 0.0) return 0.0;
-        if ((0.0 < r) && (r <= 1.0)) return r;
-        return smin(1.0, xi_right(r));
+        if (le0(r)) return 0.0;
+        // here r > 0 or NaN; (0 < r && r <= 1) is the unsigned bit compare with 1.0
+        if (f64_bits(r) <= 0x3FF0000000000000ull) return r;
+        // r > 1: 1 + r > 2, so denom_tol leaves it and 2/(1+r) <= 1 = min(1, 2/(1+r));
+        // r NaN: min(1.0, NaN) is 1.0
+        return is_nan(r) ? 1.0 : div_rn(2.0, 1.0 + r);
     } else {          // VanLeerLimiter::operator() vanleer.cpp:29-36
-        if (r <= 0.0) return 0.0;
-        return smin((2.0 * r) / (1.0 + r), xi_right(r));
+        if (le0(r)) return 0.0;
+        return smin(div_rn(2.0 * r, 1.0 + r), xi_right(r));
     }
 }
 
 // limited slope of one variable from the three cell averages (um, u0, up)
 template <int LIM>
-__device__ __forceinline__ double slope(double um, double u0, double up) {
+HF_HD double slope(double um, double u0, double up) {
     double dl = u0 - um, dr = up - u0;
     double dlc = dl, drc = dr;
-    if (fabs(dlc) <= kTol) dlc = (dlc == 0.0) ? kTol : kTol * sgn(dlc);
-    if (fabs(drc) <= kTol) drc = (drc == 0.0) ? kTol : kTol * sgn(drc);
-    double xi = limiter<LIM>(dlc / drc);
+    if (abs_le(dlc, kTol)) dlc = (dlc == 0.0) ? kTol : kTol * sgn(dlc);
+    if (abs_le(drc, kTol)) drc = (drc == 0.0) ? kTol : kTol * sgn(drc);
+    double xi = limiter<LIM>(div_rn(dlc, drc));
     return xi * (0.5 * dl + 0.5 * dr);
 }
 
@@ -193,7 +198,7 @@ __device__ __forceinline__ double slope(double um, double u0, double up) {
 // dx / s over cells with std::min; fl(dx / s) is non-increasing in s, so that fold
 // equals fl(dx / max s) -- a max over s, which is exact in any order.  NaN terms are
 // skipped in both.
-__device__ __forceinline__ void wave_terms(double g, double g1, double r, double ru, double rv,
+HF_HD void wave_terms(double g, double g1, double r, double ru, double rv,
                                            double E, double& sx, double& sy) {
     double u, v, p;
     to_prim_short(g1, r, ru, rv, E, u, v, p);
@@ -203,7 +208,11 @@ __device__ __forceinline__ void wave_terms(double g, double g1, double r, double
 }
 
 // NaN-skipping max of non-negative values
-__device__ __forceinline__ double nmax(double m, double s) { return (s > m) ? s : m; }
+HF_HD double nmax(double m, double s) {
+    // s > m for m >= +0 (never NaN): the unsigned bit order, NaN excluded
+    const uint64_t us = f64_bits(s);
+    return (us <= kInf && us > f64_bits(m)) ? s : m;
+}
 
 __device__ __forceinline__ unsigned long long dbits(double x) {
     return (unsigned long long)__double_as_longlong(x);

@@ -51,6 +51,14 @@ struct UnsMesh {
     double* U[2];
     double inlet[4];
     long long npairs;
+    // edge-based mode: per pair, the unique interior edge it belongs to and whether the pair
+    // owns it (+1) or takes the owner's flux negated (-1); -1 for boundary pairs
+    const int* __restrict__ pair_edge;
+    const signed char* __restrict__ pair_sign;
+    const int* __restrict__ edge_pair;      // per unique edge: the owning pair
+    const int* __restrict__ edge_cell;      // per unique edge: the owning cell
+    double* edge_flux;                      // [4][nedges]: length x rotated-back HLLC flux
+    int nedges;
 };
 
 // rotate_flow_values (euler_ideal_gas.cpp:152-165) with precomputed cos/sin
@@ -66,7 +74,7 @@ __device__ __forceinline__ double uns_dt_term(double g, double g1, double rin, c
     double uu, vv, p;
     to_prim_short(g1, u[0], u[1], u[2], u[3], uu, vv, p);
     double c = sound(g, u[0], p);
-    return rin / (fabs(sqrt(uu * uu + vv * vv)) + c);
+    return div_rn(rin, fabs(sqrt_rn(uu * uu + vv * vv)) + c);
 }
 
 // NaN-skipping min of non-negative values
@@ -89,6 +97,54 @@ __device__ __forceinline__ void block_min_atomic(double v, unsigned long long* a
 }
 
 constexpr int kUnsNT = 256;
+
+// length x rotated-back HLLC flux of the pair (owner cell c, neighbour cell k)
+__device__ __forceinline__ int pair_flux(const UnsMesh& m, const double* __restrict__ U, size_t N, double g,
+                                         double g1, int e, const double* cv, double* f) {
+    const double ca = m.geo[e], sa = m.geo[m.npairs + e];
+    const double cn = m.geo[2 * m.npairs + e], sn = m.geo[3 * m.npairs + e];
+    const double len = m.geo[4 * m.npairs + e];
+    const int k = m.nbr[e];
+    double rc[4], rn[4];
+    rot(ca, sa, cv, rc);
+    if (k >= 0) {
+        double nb[4] = {U[k], U[N + k], U[2 * N + k], U[3 * N + k]};
+        rot(ca, sa, nb, rn);
+    } else if (k == -1) {   // reflective: rotate, negate normal momentum, rotate back
+        double r1[4], nb[4];
+        r1[0] = rc[0]; r1[1] = rc[1] * -1.0; r1[2] = rc[2]; r1[3] = rc[3];
+        rot(cn, sn, r1, nb);
+        rot(ca, sa, nb, rn);
+    } else if (k == -2) {   // transmissive: the cell's own state
+        rot(ca, sa, cv, rn);
+    } else {                // inlet
+        rot(ca, sa, m.inlet, rn);
+    }
+    double rf[4], fr[4];
+    const int bad = hllc_cons<0>(g, g1, rc, rn, rf);
+    rot(cn, sn, rf, fr);
+#pragma unroll
+    for (int v = 0; v < 4; ++v) f[v] = len * fr[v];
+    return bad;
+}
+
+// edge-based mode, pass 1: one flux per unique interior edge, from its owner's side
+__global__ void __launch_bounds__(kUnsNT) uns_edge_flux_kernel(UnsCtrl* __restrict__ c, UnsMesh m) {
+    if (c->done) return;
+    const int p = (int)(c->step & 1);
+    const double g = c->gamma, g1 = c->g1;
+    const size_t N = (size_t)m.ncells;
+    const double* __restrict__ U = m.U[p];
+    int herr = 0;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < m.nedges; e += gridDim.x * blockDim.x) {
+        const int i = m.edge_cell[e];
+        double cv[4] = {U[i], U[N + i], U[2 * N + i], U[3 * N + i]}, f[4];
+        herr += pair_flux(m, U, N, g, g1, m.edge_pair[e], cv, f);
+#pragma unroll
+        for (int v = 0; v < 4; ++v) m.edge_flux[(size_t)v * m.nedges + e] = f[v];
+    }
+    if (herr) atomicAdd(reinterpret_cast<unsigned long long*>(&c->hllc_errors), (unsigned long long)herr);
+}
 
 __global__ void __launch_bounds__(kUnsNT) uns_cfl_kernel(UnsCtrl* __restrict__ c, UnsMesh m, int parity) {
     double mn = 1e16;
@@ -140,30 +196,17 @@ __global__ void __launch_bounds__(kUnsNT) uns_step_kernel(UnsCtrl* __restrict__ 
         double acc[4] = {0.0, 0.0, 0.0, 0.0};
         const int e0 = m.pair_start[i], e1 = m.pair_start[i + 1];
         for (int e = e0; e < e1; ++e) {
-            const double ca = m.geo[e], sa = m.geo[m.npairs + e];
-            const double cn = m.geo[2 * m.npairs + e], sn = m.geo[3 * m.npairs + e];
-            const double len = m.geo[4 * m.npairs + e];
-            const int k = m.nbr[e];
-            double rc[4], rn[4];
-            rot(ca, sa, cv, rc);
-            if (k >= 0) {
-                double nb[4] = {U[k], U[N + k], U[2 * N + k], U[3 * N + k]};
-                rot(ca, sa, nb, rn);
-            } else if (k == -1) {   // reflective: rotate, negate normal momentum, rotate back
-                double r1[4], nb[4];
-                r1[0] = rc[0]; r1[1] = rc[1] * -1.0; r1[2] = rc[2]; r1[3] = rc[3];
-                rot(cn, sn, r1, nb);
-                rot(ca, sa, nb, rn);
-            } else if (k == -2) {   // transmissive: the cell's own state
-                rot(ca, sa, cv, rn);
-            } else {                // inlet
-                rot(ca, sa, m.inlet, rn);
-            }
-            double rf[4], f[4];
-            herr += hllc_cons<0>(g, g1, rc, rn, rf);
-            rot(cn, sn, rf, f);
+            double f[4];
+            const int ed = m.pair_edge ? m.pair_edge[e] : -1;
+            if (ed >= 0) {          // edge-based mode: the owner's flux, negated on the other side
+                const double sg = (double)m.pair_sign[e];
 #pragma unroll
-            for (int v = 0; v < 4; ++v) acc[v] = acc[v] + len * f[v];
+                for (int v = 0; v < 4; ++v) f[v] = sg * m.edge_flux[(size_t)v * m.nedges + ed];
+            } else {
+                herr += pair_flux(m, U, N, g, g1, e, cv, f);
+            }
+#pragma unroll
+            for (int v = 0; v < 4; ++v) acc[v] = acc[v] + f[v];
         }
         const double inv = m.inv_area[i];
         double un[4];
@@ -201,6 +244,9 @@ struct hf_uns {
     hf::UnsCtrl* dctrl = nullptr;
     std::vector<void*> allocs;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    bool edge_mode = false;
+    int* d_pair_edge = nullptr;
+    signed char* d_pair_sign = nullptr;
     std::string err;
 };
 
@@ -415,6 +461,46 @@ int finish_create(hf_uns* u, const Json& cfg) {
     if ((r = upload(u, &ps, u->pair_start)) || (r = upload(u, &nb, u->nbr)) || (r = upload(u, &g, geo)) ||
         (r = upload(u, &ia, inv)) || (r = upload(u, &ri, u->rin)))
         return r;
+    // unique interior edges, owned by the lower-indexed cell (edge-based mode)
+    {
+        std::vector<int> pe(np, -1), ep, ec;
+        std::vector<signed char> sg(np, 0);
+        std::unordered_map<uint64_t, int> owner;   // (cell, nbr) -> owner pair
+        owner.reserve(np);
+        for (int c = 0; c < n; ++c)
+            for (int q = u->pair_start[c]; q < u->pair_start[c + 1]; ++q) {
+                const int k = u->nbr[q];
+                if (k < 0) continue;
+                if (c < k) {
+                    pe[q] = (int)ep.size();
+                    sg[q] = 1;
+                    ep.push_back(q);
+                    ec.push_back(c);
+                    owner[((uint64_t)c << 32) | (uint32_t)k] = q;
+                }
+            }
+        for (int c = 0; c < n; ++c)
+            for (int q = u->pair_start[c]; q < u->pair_start[c + 1]; ++q) {
+                const int k = u->nbr[q];
+                if (k < 0 || c < k) continue;
+                auto it = owner.find(((uint64_t)k << 32) | (uint32_t)c);
+                if (it == owner.end()) continue;        // unmatched: keep the per-side flux
+                pe[q] = pe[it->second];
+                sg[q] = -1;
+            }
+        int* d_pe; signed char* d_sg; int* d_ep; int* d_ec; double* d_ef;
+        if ((r = upload(u, &d_pe, pe)) || (r = upload(u, &d_sg, sg)) || (r = upload(u, &d_ep, ep)) ||
+            (r = upload(u, &d_ec, ec)))
+            return r;
+        UCK(cudaMalloc(&d_ef, 4 * (ep.size() + 1) * sizeof(double)));
+        u->allocs.push_back(d_ef);
+        u->d_pair_edge = d_pe;
+        u->d_pair_sign = d_sg;
+        u->dm.edge_pair = d_ep;
+        u->dm.edge_cell = d_ec;
+        u->dm.edge_flux = d_ef;
+        u->dm.nedges = (int)ep.size();
+    }
     u->dm.ncells = n;
     u->dm.pair_start = ps;
     u->dm.nbr = nb;
@@ -443,7 +529,16 @@ int finish_create(hf_uns* u, const Json& cfg) {
 int enqueue_uns_step(hf_uns* u, bool prep) {
     int grid = (u->ncells + hf::kUnsNT - 1) / hf::kUnsNT;
     if (prep) hf::uns_prep_kernel<<<1, 1, 0, u->stream>>>(u->dctrl);
-    hf::uns_step_kernel<<<grid, hf::kUnsNT, 0, u->stream>>>(u->dctrl, u->dm);
+    hf::UnsMesh m = u->dm;
+    if (u->edge_mode) {
+        m.pair_edge = u->d_pair_edge;
+        m.pair_sign = u->d_pair_sign;
+        int eg = (m.nedges + hf::kUnsNT - 1) / hf::kUnsNT;
+        hf::uns_edge_flux_kernel<<<eg < 1 ? 1 : eg, hf::kUnsNT, 0, u->stream>>>(u->dctrl, m);
+    } else {
+        m.pair_edge = nullptr;
+    }
+    hf::uns_step_kernel<<<grid, hf::kUnsNT, 0, u->stream>>>(u->dctrl, m);
     hf::uns_finalize_kernel<<<1, 1, 0, u->stream>>>(u->dctrl);
     UCK(cudaGetLastError());
     return HF_OK;
@@ -631,6 +726,15 @@ int hf_uns_hllc_errors(hf_uns* u, int64_t* count) {
     UCK(cudaStreamSynchronize(u->stream));
     UCK(cudaMemcpy(&v, &u->dctrl->hllc_errors, sizeof v, cudaMemcpyDeviceToHost));
     *count = v;
+    return HF_OK;
+}
+
+int hf_uns_set_edge_mode(hf_uns* u, int edge_based) {
+    if (!u || !u->dctrl) return HF_ERR_ARG;
+    UCK(cudaStreamSynchronize(u->stream));
+    u->edge_mode = edge_based != 0;
+    for (int k = 0; k < 2; ++k)
+        if (u->graph[k]) { cudaGraphExecDestroy(u->graph[k]); u->graph[k] = nullptr; }
     return HF_OK;
 }
 

@@ -22,6 +22,7 @@ class CartSolver:
 
     def __init__(self, case):
         text = case if isinstance(case, str) else json.dumps(case)
+        self.case = json.loads(text)
         raw = text.encode()
         L = lib()
         h = C.c_void_p()
@@ -111,14 +112,95 @@ class CartSolver:
         check(lib().hf_run(self._h, n, int(clamp_t_end), int(graph), C.byref(done)), self._h)
         return done.value
 
-    def solve(self) -> int:
-        """Runs to t_end like Simulation::solve (without frame output); returns steps taken."""
-        total = 0
-        while True:
-            k = self.run(1000, clamp_t_end=True)
-            total += k
-            if k < 1000:
-                return total
+    def solve(self, out_dir: str | None = None, fmt: str = "hfb", ring_slots: int = 8,
+              chunk: int = 1000) -> int:
+        """Runs to t_end like Simulation::solve (simulation.cpp:51-124); returns steps taken.
+
+        Without out_dir: the t_end clamp only (no frame clamp, no output).  With out_dir: the
+        reference's frame dt clamp and output cadence as well (the case's
+        simulation.animation), frames captured on the device and written by a background
+        thread as results_%06d.hfb (binary, full precision; ``frames.read_frame``) or, with
+        fmt="csv", as the reference's own results_%06d.csv text."""
+        if out_dir is None:
+            total = 0
+            while True:
+                k = self.run(chunk, clamp_t_end=True)
+                total += k
+                if k < chunk:
+                    return total
+        from . import frames
+        meta = frames.case_meta(self.case)
+        self.enable_frames(ring_slots)
+        writer = frames.FrameWriter(out_dir, meta, fmt)
+        total, next_index = 0, 0
+        try:
+            while True:
+                k = self.run(chunk, clamp_t_end=True)
+                total += k
+                popped = 0
+                while self.frames_pending() > 0:
+                    idx, t, blocks = self.pop_frame()
+                    writer.put(idx, t, blocks)
+                    next_index = idx + 1
+                    popped += 1
+                t_now = self.time()[0]
+                if t_now == meta["t_end"]:
+                    break
+                if k == 0 and popped == 0:
+                    raise RuntimeError("device loop made no progress before t_end")
+            g = self.block_dims(0)["ghost"]
+            writer.put(next_index, t_now, [self.state(b)[:, g:-g, g:-g].copy() for b in range(self.nblocks)])
+        finally:
+            paths = writer.close()
+            self.enable_frames(0)
+        self.frame_paths = paths
+        return total
+
+    # --- frames (Simulation::solve's output cadence, captured on the device) ---
+    def enable_frames(self, ring_slots: int = 8):
+        check(lib().hf_frames_enable(self._h, ring_slots), self._h)
+
+    def frames_pending(self) -> int:
+        n = C.c_int64()
+        check(lib().hf_frames_pending(self._h, C.byref(n)), self._h)
+        return n.value
+
+    def pop_frame(self):
+        """(frame index, time label, per-block interior states [4][ny][nx])"""
+        n = C.c_int64()
+        check(lib().hf_frame_len(self._h, C.byref(n)), self._h)
+        buf = np.empty(n.value)
+        t, idx = C.c_double(), C.c_int64()
+        check(lib().hf_frame_pop(self._h, buf.ctypes.data, C.byref(t), C.byref(idx)), self._h)
+        blocks, o = [], 0
+        for b in range(self.nblocks):
+            d = self.block_dims(b)
+            m = 4 * d["x_cells"] * d["y_cells"]
+            blocks.append(buf[o:o + m].reshape(4, d["y_cells"], d["x_cells"]))
+            o += m
+        return idx.value, t.value, blocks
+
+    # --- checkpoint / restart ---
+    def checkpoint(self) -> bytes:
+        """The whole simulation state (both state buffers, ghosts, t, call count, frame
+        cadence) as bytes; ``restore`` on a solver of the same case continues bit for bit."""
+        n = C.c_size_t()
+        check(lib().hf_checkpoint_size(self._h, C.byref(n)), self._h)
+        buf = np.empty(n.value, np.uint8)
+        check(lib().hf_checkpoint_save(self._h, buf.ctypes.data, n.value), self._h)
+        return buf.tobytes()
+
+    def restore(self, blob: bytes):
+        buf = np.frombuffer(blob, np.uint8)
+        check(lib().hf_checkpoint_load(self._h, buf.ctypes.data, buf.size), self._h)
+
+    def save_checkpoint(self, path: str):
+        with open(path, "wb") as fh:
+            fh.write(self.checkpoint())
+
+    def load_checkpoint(self, path: str):
+        with open(path, "rb") as fh:
+            self.restore(fh.read())
 
     def sync(self):
         check(lib().hf_sync(self._h), self._h)

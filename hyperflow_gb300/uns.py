@@ -94,6 +94,11 @@ class UnsSolver:
         check(lib().hf_uns_hllc_errors(self._h, C.byref(n)), self._h, _MSG)
         return n.value
 
+    def set_edge_mode(self, edge_based: bool):
+        """False: per-(cell, edge) fluxes, bit-identical to the reference (default).
+        True: one flux per unique interior edge (half the HLLC work)."""
+        check(lib().hf_uns_set_edge_mode(self._h, int(edge_based)), self._h, _MSG)
+
     def stream(self) -> int:
         s = C.c_void_p()
         check(lib().hf_uns_stream(self._h, C.byref(s)), self._h, _MSG)

@@ -103,6 +103,42 @@ int hf_stream(hf_ctx* ctx, void** stream);
 int hf_profile(hf_ctx* ctx, int enable);
 int hf_kernel_time(hf_ctx* ctx, int kind, double* ms, int64_t* launches);
 
+/* Frame output with the cadence of Simulation::solve (src/fvm_2d_cart/simulation/simulation/
+ * simulation.cpp:57-122), replacing the per-frame EulerIdealGasDataOutput::to_file call
+ * (src/fvm_2d_cart/simulation/output/euler_data_output/euler_data_output.cpp:37-84) with
+ * full-precision device snapshots.  With frames enabled, hf_run(clamp_t_end = 1) also applies
+ * the reference's frame dt clamp (dt = cur_frame_out - t, simulation.cpp:98-102, interval =
+ * t_end / (animation.duration * animation.fps)) and copies, on the device, the interior of
+ * every block into a ring of ring_slots frames (2..32): before the first update, and after
+ * every update that starts within 1e-12 of a frame time, labelled with the time before that
+ * update -- the reference's own points and labels.  The last frame the reference writes after
+ * its loop is the state at t_end (hf_get_state).  The loop pauses (hf_run returns fewer
+ * steps than asked, t < t_end) while the ring lacks room for two frames; hf_frame_pop frees
+ * a slot.  ring_slots = 0 disables frames.  HF_ERR_ARG when the case has no
+ * simulation.animation.  The cadence (next frame time, frame count) belongs to the
+ * simulation state and is kept by checkpoints; the ring does not. */
+int hf_frames_enable(hf_ctx* ctx, int ring_slots);
+/* doubles in one frame: sum over blocks of 4 * nx * ny (interior cells, SoA per block,
+ * [block][var][y][x], x fastest) */
+int hf_frame_len(const hf_ctx* ctx, int64_t* n);
+/* frames in the ring not yet popped (synchronises the context's stream) */
+int hf_frames_pending(hf_ctx* ctx, int64_t* n);
+/* copies the oldest pending frame to cons (hf_frame_len doubles; NULL skips the copy), its
+ * time label and frame index (the reference's frame_idx, the n of results_%06d); HF_ERR_STATE
+ * when none is pending */
+int hf_frame_pop(hf_ctx* ctx, double* cons, double* t, int64_t* index);
+
+/* Checkpoint / restart of the whole simulation state: both state buffers of every block
+ * (ghosts included) and the control block (t, TimeStep call count, step parity, interior
+ * wave-speed maxima, frame cadence).  No counterpart in the reference, whose only output is
+ * the 6-digit CSV frame.  A run restored into a context created from the same case continues
+ * bit for bit as the run that saved it.  hf_checkpoint_save needs the pending frames popped
+ * (HF_ERR_STATE otherwise); hf_checkpoint_load rejects a blob of another case, scheme, block
+ * layout or build (HF_ERR_ARG / HF_ERR_PARSE).  Both synchronise the context's stream. */
+int hf_checkpoint_size(const hf_ctx* ctx, size_t* bytes);
+int hf_checkpoint_save(hf_ctx* ctx, void* buf, size_t bytes);
+int hf_checkpoint_load(hf_ctx* ctx, const void* buf, size_t bytes);
+
 /* The CFL time step of one block for callers that cannot allocate device memory (a
  * pool-managed application, a no-allocation time loop).  No counterpart in the reference:
  * it computes what TimeStep::operator() computes, over all total_x * total_y cells of one

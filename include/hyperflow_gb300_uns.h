@@ -55,6 +55,14 @@ int hf_uns_advance(hf_uns* u, double dt);
 /* n steps of the loop body on the device (dt stays on the device); clamp_t_end stops at t_end */
 int hf_uns_run(hf_uns* u, int64_t n, int clamp_t_end, int use_graph, int64_t* steps_done);
 
+/* Flux evaluation mode.  0 (default, the parity path): every (cell, edge) pair evaluates its
+ * own HLLC flux in its own rotated frame, exactly as GodunovScheme::operator() does -- results
+ * equal the reference bit for bit, and every interior edge is evaluated twice.  1: edge-based --
+ * one flux per unique interior edge, evaluated from the lower-indexed cell's side (bit-equal
+ * for that cell) and applied negated to the other cell; half the HLLC work, and the other cell's
+ * flux differs from the reference's own evaluation by rounding only. */
+int hf_uns_set_edge_mode(hf_uns* u, int edge_based);
+
 int hf_uns_get_time(hf_uns* u, double* t, int64_t* calls, double* last_dt);
 int hf_uns_hllc_errors(hf_uns* u, int64_t* count);
 int hf_uns_stream(hf_uns* u, void** stream);

@@ -560,6 +560,58 @@ int hfo_run(hfo_mesh *m, int n, int clamp_t_end, double *dts) {
     return taken;
 }
 
+/* copies the interior of every block, SoA per block ([var][y][x]), into out */
+static void frame_copy(const hfo_mesh *m, double *out) {
+    size_t o = 0;
+    for (int b = 0; b < m->nblocks; ++b)
+        for (int v = 0; v < 4; ++v)
+            for (int j = 0; j < m->ny[b]; ++j)
+                for (int i = 0; i < m->nx[b]; ++i)
+                    out[o++] = AT(m, b, v, i + m->ghost, j + m->ghost);
+}
+
+/* Simulation::solve (simulation.cpp:51-124) with its output cadence: the t_end clamp
+ * (88-90), the frame clamp (98-102), a frame before the first update (93-96), a frame after
+ * every update that starts within 1e-12 of the frame time, labelled with the time before
+ * that update (106-113), and a last frame after the loop (122).  interval is
+ * t_end / (duration * fps).  Frames beyond max_frames are counted but not stored; dts
+ * beyond max_dts likewise.  Returns the steps taken. */
+int64_t hfo_solve(hfo_mesh *m, double interval, int64_t max_steps, double *dts, int64_t max_dts,
+                  double *frames, double *frame_t, int64_t max_frames, int64_t *nframes) {
+    size_t fcells = 0;
+    for (int b = 0; b < m->nblocks; ++b) fcells += (size_t)4 * m->nx[b] * m->ny[b];
+    double cur = 0.0;
+    int64_t nf = 0, taken = 0;
+#define HFO_FRAME(label)                                                     \
+    do {                                                                     \
+        if (nf < max_frames) {                                               \
+            if (frames) frame_copy(m, frames + (size_t)nf * fcells);         \
+            if (frame_t) frame_t[nf] = (label);                              \
+        }                                                                    \
+        ++nf;                                                                \
+    } while (0)
+    for (int64_t n = 1; n < 1000000000 && taken < max_steps; ++n) {
+        if (m->t == m->t_end) break;
+        hfo_apply_bcs(m);
+        double dt = hfo_time_step(m);
+        if (m->t + dt > m->t_end) dt = m->t_end - m->t;
+        if (cur == 0.0) HFO_FRAME(m->t);
+        if ((m->t + dt > cur) && (cur > 0.0)) dt = cur - m->t;
+        hfo_advance(m, dt);
+        if (fabs(m->t - cur) < 1e-12) {
+            HFO_FRAME(m->t);
+            cur += interval;
+        }
+        if (dts && taken < max_dts) dts[taken] = dt;
+        m->t += dt;
+        ++taken;
+    }
+    if (m->t == m->t_end) HFO_FRAME(m->t);
+#undef HFO_FRAME
+    if (nframes) *nframes = nf;
+    return taken;
+}
+
 /* ---------------- unstructured: src/fvm_2d_uns ------------------------------------------ */
 
 /* Edge::calculate_outward_unit_normal + calculate_outward_normal_angle (edge.cpp:189-218),

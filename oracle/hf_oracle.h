@@ -72,6 +72,10 @@ double hfo_time_step(hfo_mesh *m);
 void hfo_advance(hfo_mesh *m, double dt);
 /* runs n steps (apply_bcs, dt, optional t_end clamp, blocks in order); writes each dt */
 int hfo_run(hfo_mesh *m, int n, int clamp_t_end, double *dts);
+/* Simulation::solve with its t_end and frame-output clamps and its frame cadence; frames are
+ * every block's interior, SoA per block, with the reference's time labels */
+int64_t hfo_solve(hfo_mesh *m, double interval, int64_t max_steps, double *dts, int64_t max_dts,
+                  double *frames, double *frame_t, int64_t max_frames, int64_t *nframes);
 
 /* unstructured Godunov (src/fvm_2d_uns): cells in order, their (cell, edge) pairs
  * contiguous in pair order; verts holds each cell's vertices, 2 doubles each */

@@ -77,6 +77,8 @@ def port_lib():
         lib.hfo_init_double.argtypes = [p, i, d, d, p, p, p]
         lib.hfo_init_sphere.argtypes = [p, i, d, d, d, p, p]
         lib.hfo_init_shock_bubble.argtypes = [p, i, d, d, d, d, p, p, p]
+        lib.hfo_solve.restype = C.c_int64
+        lib.hfo_solve.argtypes = [p, d, C.c_int64, p, C.c_int64, p, p, C.c_int64, p]
         lib.hfo_uns_geometry.argtypes = [i, p, p, p, p, p, p]
         lib.hfo_uns_run.restype = i
         lib.hfo_uns_run.argtypes = [d, d, p, i, p, p, p, p, p, p, p, p, i, p, i]
@@ -215,6 +217,31 @@ class Oracle:
         k = self.lib.hfo_run(C.byref(self.m), n, int(clamp_t_end), _ptr(dts))
         return dts[:k]
 
+    def frame_interval(self) -> float:
+        """simulation.cpp:57: t_end / (anim_duration * anim_fps)"""
+        sim = self.case["simulation"]
+        return float(sim["t_end"]) / (float(sim["animation"]["duration"]) * float(sim["animation"]["fps"]))
+
+    def solve(self, max_steps: int = 10**9, max_frames: int = 64, max_dts: int = 100000):
+        """Simulation::solve with frames: returns (applied dts, frame time labels, frames);
+        frames[k] is a list of per-block interior states [4][ny][nx]."""
+        dims = [(self.m.nx[b], self.m.ny[b]) for b in range(self.m.nblocks)]
+        fcells = sum(4 * nx * ny for nx, ny in dims)
+        frames = np.zeros((max_frames, fcells))
+        ft = np.zeros(max_frames)
+        dts = np.zeros(max_dts)
+        nf = C.c_int64()
+        k = self.lib.hfo_solve(C.byref(self.m), self.frame_interval(), max_steps, _ptr(dts), max_dts,
+                               _ptr(frames), _ptr(ft), max_frames, C.byref(nf))
+        out = []
+        for f in range(min(nf.value, max_frames)):
+            o, blocks = 0, []
+            for nx, ny in dims:
+                blocks.append(frames[f, o:o + 4 * nx * ny].reshape(4, ny, nx))
+                o += 4 * nx * ny
+            out.append(blocks)
+        return dts[:min(k, max_dts)], ft[:min(nf.value, max_frames)], out
+
     @property
     def t(self) -> float:
         return self.m.t
@@ -264,6 +291,8 @@ def ref_cart_lib():
         lib.hfref_cart_calls.argtypes = [p, p]
         lib.hfref_cart_step_dts.argtypes = [p, p]
         lib.hfref_cart_apply_bcs.argtypes = [p]
+        lib.hfref_cart_solve.restype = i
+        lib.hfref_cart_solve.argtypes = [p, C.c_char_p]
         lib.hfref_cart_time.restype = d
         lib.hfref_cart_time.argtypes = [p]
         lib.hfref_hllc.argtypes = [d, p, p, i, p]
@@ -293,6 +322,11 @@ class RefCart:
 
     def apply_bcs(self):
         self.lib.hfref_cart_apply_bcs(self.h)
+
+    def solve(self, outdir: str):
+        """The reference's own Simulation::solve; its CSV frames are written into outdir."""
+        if self.lib.hfref_cart_solve(self.h, os.fsencode(outdir)) != 0:
+            raise OSError(f"cannot run the reference solve in {outdir}")
 
     def nblocks(self) -> int:
         return self.lib.hfref_cart_num_blocks(self.h)

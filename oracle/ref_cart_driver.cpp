@@ -10,8 +10,10 @@
 // body of Simulation::solve (simulation.cpp:85-120) for exactly N steps:
 //   apply_bcs -> calculate_time_step -> optional t_end clamp -> per-block
 //   ODE(Scheme) + set_fields, in block order -> t += dt.
-// Frame-output clamps (simulation.cpp:93-102) are left out: they belong to the
-// CSV writer, which is not on the hot path.
+// hfref_cart_run leaves the frame-output clamps (simulation.cpp:93-102) out;
+// hfref_cart_solve runs the reference's own Simulation::solve, frames and all.
+#include <unistd.h>
+
 #include <cstring>
 #include <functional>
 #include <memory>
@@ -22,6 +24,7 @@
 #include <nlohmann/json.hpp>
 
 #include "simulation/parser/parser.h"
+#include "simulation/simulation/simulation.h"
 #include "scheme/riemann/riemann_hllc/riemann_hllc.h"
 #include "scheme/limiter/minbee/minbee.h"
 #include "scheme/limiter/vanleer/vanleer.h"
@@ -116,6 +119,24 @@ int hfref_cart_run(void* h, int n, int clamp_t_end) {
         ++taken;
     }
     return taken;
+}
+
+// The reference's own Simulation::solve (simulation.cpp:51-124) on this context's objects,
+// as main.cpp:73-88 runs it, inside `outdir` (the CSV frames results_%06d.csv land there).
+// Returns 0, or -1 when outdir cannot be entered.
+int hfref_cart_solve(void* h, const char* outdir) {
+    RefCart* r = static_cast<RefCart*>(h);
+    char cwd[4096];
+    if (!getcwd(cwd, sizeof cwd) || chdir(outdir) != 0) return -1;
+    auto out = r->parser->generate_data_output();
+    auto sim = std::make_shared<Simulation>(r->model, out, r->mesh, r->initcon, r->ode, r->scheme,
+                                            r->riemann, r->time_step, r->parser->get_cfl(),
+                                            r->parser->get_t_start(), r->parser->get_t_end(),
+                                            r->parser->get_anim_duration(),
+                                            r->parser->get_anim_fps());
+    sim->solve();
+    r->t = r->parser->get_t_end();
+    return chdir(cwd) == 0 ? 0 : -1;
 }
 
 // Applies only the ghost fill (mesh.cpp:31-39).

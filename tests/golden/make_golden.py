@@ -10,7 +10,8 @@ step dt stream, every TimeStep call it made (step calls and MUSCL-Hancock predic
 calls), and the final state of every block (SoA [var][y][x], ghosts included) -- or,
 for the full-size 256x256 Godunov workload, per-variable checksums and a seeded sample
 of cells instead of the whole state.  Unit fixtures hold HLLC fluxes and limiter values
-for random and edge-case inputs.
+for random and edge-case inputs.  Frame fixtures hold what the reference's own
+Simulation::solve writes (the hash of every CSV frame), its TimeStep calls and final state.
 """
 from __future__ import annotations
 
@@ -94,6 +95,33 @@ def make_cart():
             data["sumsq"] = np.array([math.fsum((U[v] * U[v]).ravel()) for v in range(4)])
         np.savez_compressed(os.path.join(HERE, f"cart_{name}.npz"), **data)
         print(name, taken, "steps")
+
+
+FRAME_CASES = ["shock_tubes/toro/toro_shock_tube_01_godunov_hllc_100x5.json",
+               "shock_tubes/toro/toro_shock_tube_01_muscl_hancock_vanleer_hllc_100x5.json",
+               "sphericalrp/sphericalrp_godunov_hllc_50x50.json"]
+
+
+def make_frames():
+    """The reference's own Simulation::solve with its frame output: the sha256 of every CSV
+    frame it writes (results_%06d.csv), its TimeStep call stream and its final state."""
+    import hashlib
+    import tempfile
+    for rel in FRAME_CASES:
+        with open(os.path.join(REF_CASES, rel)) as f:
+            case = json.load(f)
+        name = os.path.splitext(os.path.basename(rel))[0]
+        ref = oracle.RefCart(case)
+        with tempfile.TemporaryDirectory() as d:
+            ref.solve(d)
+            files = sorted(os.listdir(d))
+            hashes = [hashlib.sha256(open(os.path.join(d, fn), "rb").read()).hexdigest() for fn in files]
+        data = {"case": json.dumps(case), "csv_sha256": np.array(hashes), "calls": ref.calls(),
+                "nblocks": ref.nblocks()}
+        for b in range(ref.nblocks()):
+            data[f"U{b}"] = ref.state(b)
+        np.savez_compressed(os.path.join(HERE, f"frames_{name}.npz"), **data)
+        print(name, len(files), "frames")
 
 
 def unit_states(n=4000, seed=11):
@@ -180,10 +208,12 @@ def make_uns():
 
 if __name__ == "__main__":
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref"], check=True)
-    which = sys.argv[1:] or ["units", "cart", "uns"]
+    which = sys.argv[1:] or ["units", "cart", "uns", "frames"]
     if "units" in which:
         make_units()
     if "cart" in which:
         make_cart()
     if "uns" in which:
         make_uns()
+    if "frames" in which:
+        make_frames()

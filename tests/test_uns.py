@@ -121,3 +121,27 @@ def test_uns_gpu_full_size_matches_oracle(tmp_path):
     dts, _ = oracle.uns_run(1.4, 0.5, 0, m["pair_start"], m["nbr"], m["angle"], m["length"], m["area"],
                             m["rin"], _inlet(case), U, steps, nthreads=os.cpu_count() or 4)
     np.testing.assert_array_equal(s.state(), U)
+
+
+@pytest.mark.gpu
+def test_uns_edge_mode_within_tolerance(port_lib):
+    """Edge-based mode (one HLLC per unique interior edge) against the per-side oracle after
+    2000 steps: the lower-indexed cell's flux is the reference's own; the other cell's is the
+    negation, which differs by rounding -- within 1e-10 relative."""
+    from hyperflow_gb300 import UnsSolver, meshgen
+    from oracle import oracle
+    g = load("tri_hole_3k")
+    s = UnsSolver(g["case"], mesh_text=meshgen.hmsh_text(g["verts"], g["codes"]))
+    s.set_edge_mode(True)
+    steps = 2000
+    s.run(steps)
+    m = s.mesh_arrays()
+    U = np.zeros((4, s.ncells))
+    U[:] = oracle.prim_to_cons(g["case"]["initial_condition"]["init_state"])[:, None]
+    oracle.uns_run(1.4, g["case"]["simulation"]["cfl"], 0, m["pair_start"], m["nbr"], m["angle"],
+                   m["length"], m["area"], m["rin"], _inlet(g["case"]), U, steps, nthreads=4)
+    V = s.state()
+    scale = np.abs(U).max(axis=1, keepdims=True)
+    rel = np.abs(V - U) / scale
+    assert rel.max() <= 1e-10, rel.max()
+    s.set_edge_mode(False)   # the parity path is still available on the same solver
