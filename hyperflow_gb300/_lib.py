@@ -61,6 +61,10 @@ SIGNATURES = {
     "hf_uns_time_step": (_i, [_p, C.POINTER(_d)]),
     "hf_uns_advance": (_i, [_p, _d]),
     "hf_uns_run": (_i, [_p, _i64, _i, _i, C.POINTER(_i64)]),
+    "hf_uns_centroids": (_i, [_p, _p]),
+    "hf_uns_frames_enable": (_i, [_p, _i]),
+    "hf_uns_frames_pending": (_i, [_p, C.POINTER(_i64)]),
+    "hf_uns_frame_pop": (_i, [_p, _p, C.POINTER(_d), C.POINTER(_i64)]),
     "hf_uns_get_time": (_i, [_p, C.POINTER(_d), C.POINTER(_i64), C.POINTER(_d)]),
     "hf_uns_hllc_errors": (_i, [_p, C.POINTER(_i64)]),
     "hf_uns_stream": (_i, [_p, C.POINTER(_p)]),

@@ -26,6 +26,7 @@
 #include <vector>
 
 #include "../../include/hyperflow_gb300_uns.h"
+#include "hf_ctrl.h"
 #include "hf_device.cuh"
 #include "hf_json.hpp"
 
@@ -39,6 +40,12 @@ struct UnsCtrl {
     unsigned long long min_dt[2];   // [parity] min over cells of r_in / (|V| + c), bit pattern
     int err;
     long long hllc_errors;
+    // frame output with Simulation::solve's cadence (device loop only, i.e. clamp set)
+    int frames, ring_slots, snap_pre, snap_post;
+    double frame_next, frame_interval, snap_t;
+    long long frame_idx, captured, drained;
+    double ring_t[HF_MAXRING];
+    long long ring_idx[HF_MAXRING];
 };
 
 struct UnsMesh {
@@ -159,12 +166,26 @@ __global__ void __launch_bounds__(kUnsNT) uns_cfl_kernel(UnsCtrl* __restrict__ c
 // start of a device-loop step: stop at t_end, form dt (TimeStep call), reset the accumulator
 __global__ void uns_prep_kernel(UnsCtrl* c) {
     int p = (int)(c->step & 1);
+    c->snap_pre = c->snap_post = 0;
     if (c->clamp && c->t == c->t_end) { c->done = 1; return; }
+    // a step takes at most two frames: pause the loop while the ring lacks room for them
+    if (c->clamp && c->frames && c->captured - c->drained > c->ring_slots - 2) { c->done = 1; return; }
     c->done = 0;
     double dtr = smin(1e16, bitsd(c->min_dt[p]));
     double final_cfl = (c->calls + 1 <= 10) ? 0.2 * c->cfl : c->cfl;
     double dt = final_cfl * dtr;
-    if (c->clamp && c->t + dt > c->t_end) dt = c->t_end - c->t;   // simulation.cpp:85-88
+    const double t = c->t;
+    if (c->clamp && t + dt > c->t_end) dt = c->t_end - t;        // simulation.cpp:85-88
+    if (c->clamp && c->frames) {
+        const double cur = c->frame_next;
+        c->snap_pre = (cur == 0.0);                              // simulation.cpp:91-94
+        if ((t + dt > cur) && (cur > 0.0)) dt = cur - t;         // simulation.cpp:96-100
+        if (fabs(t - cur) < 1e-12) {                             // simulation.cpp:107-113
+            c->snap_post = 1;
+            c->frame_next = cur + c->frame_interval;
+        }
+        c->snap_t = t;
+    }
     c->dt = dt;
     c->calls = c->calls + 1;
     c->min_dt[p ^ 1] = dbits(1e16);
@@ -176,8 +197,38 @@ __global__ void uns_set_dt_kernel(UnsCtrl* c, double dt) {
     c->min_dt[(c->step & 1) ^ 1] = dbits(1e16);
 }
 
+// this step's frames into the ring (cell states SoA [4][ncells]); the state before the
+// update is in buffer `step & 1`, the updated one in the other buffer
+__global__ void __launch_bounds__(256) uns_frame_copy_kernel(const UnsCtrl* __restrict__ c,
+                                                             UnsMesh m, double* __restrict__ ring) {
+    if (c->done) return;
+    const int pre = c->snap_pre, post = c->snap_post;
+    if (!pre && !post) return;
+    const int p = (int)(c->step & 1);
+    const long long R = c->ring_slots, len = 4LL * m.ncells;
+    for (int which = 0; which < 2; ++which) {
+        if (which == 0 ? !pre : !post) continue;
+        const long long slot = (c->captured + (which == 0 ? 0 : pre)) % R;
+        const double* __restrict__ src = m.U[which == 0 ? p : p ^ 1];
+        double* __restrict__ dst = ring + slot * len;
+        for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < len;
+             k += (long long)gridDim.x * blockDim.x)
+            dst[k] = src[k];
+    }
+}
+
 __global__ void uns_finalize_kernel(UnsCtrl* c) {
     if (c->done) return;
+    if (c->clamp && c->frames) {
+        for (int which = 0; which < 2; ++which) {
+            if (which == 0 ? !c->snap_pre : !c->snap_post) continue;
+            const long long slot = c->captured % c->ring_slots;
+            c->ring_t[slot] = c->snap_t;
+            c->ring_idx[slot] = c->frame_idx;
+            c->frame_idx = c->frame_idx + 1;
+            c->captured = c->captured + 1;
+        }
+    }
     c->t = c->t + c->dt;
     c->step = c->step + 1;
 }
@@ -245,6 +296,11 @@ struct hf_uns {
     std::vector<void*> allocs;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     bool edge_mode = false;
+    bool has_anim = false;
+    double anim_duration = 0.0, anim_fps = 0.0;
+    double* ring = nullptr;             // device frame ring
+    int ring_slots = 0;
+    long long drained = 0;
     int* d_pair_edge = nullptr;
     signed char* d_pair_sign = nullptr;
     std::string err;
@@ -539,6 +595,7 @@ int enqueue_uns_step(hf_uns* u, bool prep) {
         m.pair_edge = nullptr;
     }
     hf::uns_step_kernel<<<grid, hf::kUnsNT, 0, u->stream>>>(u->dctrl, m);
+    if (u->ring_slots > 0) hf::uns_frame_copy_kernel<<<4 * 152, 256, 0, u->stream>>>(u->dctrl, m, u->ring);
     hf::uns_finalize_kernel<<<1, 1, 0, u->stream>>>(u->dctrl);
     UCK(cudaGetLastError());
     return HF_OK;
@@ -560,6 +617,11 @@ int create_common(const char* case_json, size_t len, const std::string* mesh_tex
         u->cfl = cfg["simulation"]["cfl"].number();
         u->t_start = cfg["simulation"]["t_start"].number();
         u->t_end = cfg["simulation"]["t_end"].number();
+        if (cfg["simulation"].has("animation")) {
+            u->has_anim = true;
+            u->anim_duration = cfg["simulation"]["animation"]["duration"].number();
+            u->anim_fps = cfg["simulation"]["animation"]["fps"].number();
+        }
         double w[4];
         for (int k = 0; k < 4; ++k) w[k] = cfg["mesh"]["boundaries"]["inlet"][k].number();
         prim_to_cons(u->gamma, w, u->inlet);   // parser.cpp:211-217
@@ -605,6 +667,7 @@ void hf_uns_destroy(hf_uns* u) {
     for (int k = 0; k < 2; ++k)
         if (u->graph[k]) cudaGraphExecDestroy(u->graph[k]);
     for (void* p : u->allocs) cudaFree(p);
+    if (u->ring) cudaFree(u->ring);
     if (u->dctrl) cudaFree(u->dctrl);
     if (u->stream) cudaStreamDestroy(u->stream);
     delete u;
@@ -629,6 +692,31 @@ int hf_uns_mesh_arrays(const hf_uns* u, int32_t* pair_start, int32_t* nbr, doubl
     if (length) std::memcpy(length, u->length.data(), np * sizeof(double));
     if (area) std::memcpy(area, u->area.data(), n * sizeof(double));
     if (rin) std::memcpy(rin, u->rin.data(), n * sizeof(double));
+    return HF_OK;
+}
+
+// Polygon::calculate_centroid (src/fvm_2d_uns/geometry/polygon/polygon.cpp:188-212) over the
+// signed area the reference divides by
+int hf_uns_centroids(const hf_uns* u, double* xy) {
+    if (!u || !xy) return HF_ERR_ARG;
+    const size_t n = u->ncells;
+    size_t vo = 0;
+    for (size_t c = 0; c < n; ++c) {
+        const int nv = u->nverts[c];
+        const double* V = u->verts.data() + 2 * vo;
+        double cx = 0.0, cy = 0.0;
+        for (int i = 0; i < nv; ++i) {
+            const int j = (i == nv - 1) ? 0 : i + 1;
+            const double second = (V[2 * i] * V[2 * j + 1] - V[2 * j] * V[2 * i + 1]);
+            cx += ((V[2 * i] + V[2 * j]) * second);
+            cy += ((V[2 * i + 1] + V[2 * j + 1]) * second);
+        }
+        cx /= (6.0 * u->area[c]);
+        cy /= (6.0 * u->area[c]);
+        xy[c] = cx;
+        xy[n + c] = cy;
+        vo += nv;
+    }
     return HF_OK;
 }
 
@@ -706,6 +794,59 @@ int hf_uns_run(hf_uns* u, int64_t n, int clamp_t_end, int use_graph, int64_t* st
     long long s1;
     if ((r = read_step(u, &s1))) return r;
     if (steps_done) *steps_done = s1 - s0;
+    return HF_OK;
+}
+
+int hf_uns_frames_enable(hf_uns* u, int ring_slots) {
+    if (!u || !u->dctrl || ring_slots < 0 || ring_slots == 1 || ring_slots > HF_MAXRING)
+        return HF_ERR_ARG;
+    if (ring_slots > 0 && !u->has_anim)
+        return ufail(u, HF_ERR_ARG, "the case has no simulation.animation {duration, fps}");
+    UCK(cudaStreamSynchronize(u->stream));
+    for (int k = 0; k < 2; ++k)
+        if (u->graph[k]) { cudaGraphExecDestroy(u->graph[k]); u->graph[k] = nullptr; }
+    if (u->ring) { UCK(cudaFree(u->ring)); u->ring = nullptr; }
+    u->ring_slots = 0;
+    if (ring_slots > 0) {
+        UCK(cudaMalloc(&u->ring, (size_t)ring_slots * 4 * u->ncells * sizeof(double)));
+        u->ring_slots = ring_slots;
+    }
+    // the interval exactly as simulation.cpp:57 forms it
+    const double interval = ring_slots > 0 ? u->t_end / (u->anim_duration * u->anim_fps) : 0.0;
+    hf::UnsCtrl C;
+    UCK(cudaMemcpy(&C, u->dctrl, sizeof C, cudaMemcpyDeviceToHost));
+    C.frames = ring_slots > 0 ? 1 : 0;
+    C.ring_slots = ring_slots;
+    C.frame_interval = interval;
+    C.captured = C.drained = 0;
+    u->drained = 0;
+    UCK(cudaMemcpy(u->dctrl, &C, sizeof C, cudaMemcpyHostToDevice));
+    return HF_OK;
+}
+
+int hf_uns_frames_pending(hf_uns* u, int64_t* n) {
+    if (!u || !u->dctrl || !n) return HF_ERR_ARG;
+    long long cap = 0;
+    UCK(cudaStreamSynchronize(u->stream));
+    UCK(cudaMemcpy(&cap, &u->dctrl->captured, sizeof cap, cudaMemcpyDeviceToHost));
+    *n = u->ring_slots > 0 ? cap - u->drained : 0;
+    return HF_OK;
+}
+
+int hf_uns_frame_pop(hf_uns* u, double* cons, double* t, int64_t* index) {
+    if (!u || !u->dctrl) return HF_ERR_ARG;
+    if (u->ring_slots == 0) return ufail(u, HF_ERR_STATE, "frames are not enabled");
+    hf::UnsCtrl C;
+    UCK(cudaStreamSynchronize(u->stream));
+    UCK(cudaMemcpy(&C, u->dctrl, sizeof C, cudaMemcpyDeviceToHost));
+    if (C.captured == u->drained) return ufail(u, HF_ERR_STATE, "no frame pending");
+    const long long slot = u->drained % u->ring_slots, len = 4LL * u->ncells;
+    if (cons) UCK(cudaMemcpy(cons, u->ring + slot * len, (size_t)len * sizeof(double), cudaMemcpyDeviceToHost));
+    if (t) *t = C.ring_t[slot];
+    if (index) *index = C.ring_idx[slot];
+    u->drained += 1;
+    long long d = u->drained;
+    UCK(cudaMemcpy(&u->dctrl->drained, &d, sizeof d, cudaMemcpyHostToDevice));
     return HF_OK;
 }
 

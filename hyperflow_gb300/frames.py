@@ -49,8 +49,17 @@ def case_meta(case: dict) -> dict:
             "blocks": blocks}
 
 
+def uns_case_meta(case: dict, ncells: int) -> dict:
+    """Frame header fields of an unstructured case (the state is one [4][ncells] array)."""
+    dom, sim = case["domain"], case["simulation"]
+    return {"gamma": float(case["model"]["gamma"]), "ncells": int(ncells),
+            "t_start": float(sim["t_start"]), "t_end": float(sim["t_end"]),
+            "domain": {k: float(dom[k]) for k in ("x_left", "x_right", "y_bottom", "y_top")}}
+
+
 def write_frame(path: str, meta: dict, index: int, t: float, blocks) -> None:
-    """blocks: per block an array [4][ny][nx] (interior cells)."""
+    """blocks: per block an array [4][ny][nx] (interior cells); for an unstructured case
+    (meta without "blocks") one array [4][ncells]."""
     head = dict(meta, format="hyperflow-gb300 frame", version=1, index=int(index), t=float(t),
                 vars=["rho", "rho_u", "rho_v", "E"])
     hj = json.dumps(head).encode()
@@ -75,9 +84,10 @@ def read_frame(path: str):
     off = 16 + hl
     off += (-off) % ALIGN
     blocks = []
-    for b in head["blocks"]:
-        n = 4 * b["nx"] * b["ny"]
-        blocks.append(np.frombuffer(raw, "<f8", n, off).reshape(4, b["ny"], b["nx"]).copy())
+    shapes = [(4, b["ny"], b["nx"]) for b in head["blocks"]] if "blocks" in head else [(4, head["ncells"])]
+    for shp in shapes:
+        n = int(np.prod(shp))
+        blocks.append(np.frombuffer(raw, "<f8", n, off).reshape(shp).copy())
         off += 8 * n
     return head, blocks
 
@@ -86,13 +96,36 @@ def _g(x: float) -> str:
     return "%g" % x
 
 
+def _csv_head(head: dict):
+    d = head["domain"]
+    return [f"X_LEFT={_g(d['x_left'])}", f"X_RIGHT={_g(d['x_right'])}",
+            f"Y_BOTTOM={_g(d['y_bottom'])}", f"Y_TOP={_g(d['y_top'])}",
+            f"T_START={_g(head['t_start'])}", f"T_END={_g(head['t_end'])}", f"T={_g(head['t'])}", "",
+            "x,y,rho,rho_u,rho_v,E,u,v,p"]
+
+
+def _row(x, y, r, ru, rv, E, gm1):
+    # EulerIdealGasModel::cons_to_prim, euler_ideal_gas.cpp:76-92
+    u = ru / r
+    v = rv / r
+    p = gm1 * (E - 0.5 * r * (u * u + v * v))
+    return ",".join(_g(z) for z in (x, y, r, ru, rv, E, u, v, p))
+
+
+def uns_csv_text(head: dict, U, centroids) -> str:
+    """The reference's unstructured CSV text of one frame (src/fvm_2d_uns/simulation/output/
+    euler_data_output/euler_data_output.cpp:37-82): cells in mesh order, centroid first."""
+    out = _csv_head(head)
+    gm1 = head["gamma"] - 1.0
+    for c in range(U.shape[1]):
+        out.append(_row(float(centroids[0, c]), float(centroids[1, c]), float(U[0, c]), float(U[1, c]),
+                        float(U[2, c]), float(U[3, c]), gm1))
+    return "\n".join(out) + "\n"
+
+
 def csv_text(head: dict, blocks) -> str:
     """The reference's CSV text of one frame (euler_data_output.cpp:48-82)."""
-    d = head["domain"]
-    out = [f"X_LEFT={_g(d['x_left'])}", f"X_RIGHT={_g(d['x_right'])}",
-           f"Y_BOTTOM={_g(d['y_bottom'])}", f"Y_TOP={_g(d['y_top'])}",
-           f"T_START={_g(head['t_start'])}", f"T_END={_g(head['t_end'])}", f"T={_g(head['t'])}", "",
-           "x,y,rho,rho_u,rho_v,E,u,v,p"]
+    out = _csv_head(head)
     g = head["ghost"]
     gm1 = head["gamma"] - 1.0
     for b, U in zip(head["blocks"], blocks):
@@ -105,11 +138,7 @@ def csv_text(head: dict, blocks) -> str:
             x = sx + float(i + g) * dx
             for j in range(ny):
                 y = sy + float(j + g) * dy
-                r, ru, rv, E = (float(U[k, j, i]) for k in range(4))
-                u = ru / r
-                v = rv / r
-                p = gm1 * (E - 0.5 * r * (u * u + v * v))
-                out.append(",".join(_g(z) for z in (x, y, r, ru, rv, E, u, v, p)))
+                out.append(_row(x, y, *(float(U[k, j, i]) for k in range(4)), gm1))
     return "\n".join(out) + "\n"
 
 
@@ -123,11 +152,11 @@ class FrameWriter:
     """Writes frames from a background thread so file output overlaps the device loop.
     fmt "hfb" writes results_%06d.hfb; "csv" writes the reference's results_%06d.csv."""
 
-    def __init__(self, out_dir: str, meta: dict, fmt: str = "hfb"):
+    def __init__(self, out_dir: str, meta: dict, fmt: str = "hfb", centroids=None):
         if fmt not in ("hfb", "csv"):
             raise ValueError("fmt must be 'hfb' or 'csv'")
         os.makedirs(out_dir, exist_ok=True)
-        self.out_dir, self.meta, self.fmt = out_dir, meta, fmt
+        self.out_dir, self.meta, self.fmt, self.centroids = out_dir, meta, fmt, centroids
         self.paths: list[str] = []
         self._q: queue.Queue = queue.Queue(maxsize=4)
         self._err: BaseException | None = None
@@ -146,8 +175,10 @@ class FrameWriter:
                     write_frame(path, self.meta, index, t, blocks)
                 else:
                     head = dict(self.meta, index=index, t=t)
+                    text = csv_text(head, blocks) if "blocks" in head else \
+                        uns_csv_text(head, blocks[0], self.centroids)
                     with open(path, "w") as fh:
-                        fh.write(csv_text(head, blocks))
+                        fh.write(text)
                 self.paths.append(path)
             except BaseException as e:  # reported by close()
                 self._err = e

@@ -20,6 +20,7 @@ _MSG = "hf_uns_last_error_message"
 class UnsSolver:
     def __init__(self, case, mesh_text: str | None = None):
         text = case if isinstance(case, str) else json.dumps(case)
+        self.case = json.loads(text)
         raw = text.encode()
         L = lib()
         h = C.c_void_p()
@@ -98,6 +99,67 @@ class UnsSolver:
         """False: per-(cell, edge) fluxes, bit-identical to the reference (default).
         True: one flux per unique interior edge (half the HLLC work)."""
         check(lib().hf_uns_set_edge_mode(self._h, int(edge_based)), self._h, _MSG)
+
+    def centroids(self) -> np.ndarray:
+        """[2][ncells] cell centroids as the reference computes them"""
+        out = np.empty((2, self.ncells))
+        check(lib().hf_uns_centroids(self._h, out.ctypes.data), self._h, _MSG)
+        return out
+
+    # --- frames (Simulation::solve's output cadence, captured on the device) ---
+    def enable_frames(self, ring_slots: int = 8):
+        check(lib().hf_uns_frames_enable(self._h, ring_slots), self._h, _MSG)
+
+    def frames_pending(self) -> int:
+        n = C.c_int64()
+        check(lib().hf_uns_frames_pending(self._h, C.byref(n)), self._h, _MSG)
+        return n.value
+
+    def pop_frame(self):
+        """(frame index, time label, cell states [4][ncells])"""
+        buf = np.empty((4, self.ncells))
+        t, idx = C.c_double(), C.c_int64()
+        check(lib().hf_uns_frame_pop(self._h, buf.ctypes.data, C.byref(t), C.byref(idx)), self._h, _MSG)
+        return idx.value, t.value, buf
+
+    def solve(self, out_dir: str | None = None, fmt: str = "hfb", ring_slots: int = 8,
+              chunk: int = 1000) -> int:
+        """Runs to t_end like the unstructured Simulation::solve (simulation.cpp:51-120);
+        with out_dir, also its frame dt clamp and output cadence, frames written as
+        results_%06d.hfb (binary) or, with fmt="csv", the reference's own CSV text."""
+        if out_dir is None:
+            total = 0
+            while True:
+                k = self.run(chunk, clamp_t_end=True)
+                total += k
+                if k < chunk:
+                    return total
+        from . import frames
+        meta = frames.uns_case_meta(self.case, self.ncells)
+        self.enable_frames(ring_slots)
+        writer = frames.FrameWriter(out_dir, meta, fmt, centroids=self.centroids())
+        total, next_index = 0, 0
+        try:
+            while True:
+                k = self.run(chunk, clamp_t_end=True)
+                total += k
+                popped = 0
+                while self.frames_pending() > 0:
+                    idx, t, U = self.pop_frame()
+                    writer.put(idx, t, [U])
+                    next_index = idx + 1
+                    popped += 1
+                t_now = self.time()[0]
+                if t_now == meta["t_end"]:
+                    break
+                if k == 0 and popped == 0:
+                    raise RuntimeError("device loop made no progress before t_end")
+            writer.put(next_index, t_now, [self.state()])
+        finally:
+            paths = writer.close()
+            self.enable_frames(0)
+        self.frame_paths = paths
+        return total
 
     def stream(self) -> int:
         s = C.c_void_p()

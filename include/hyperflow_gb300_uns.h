@@ -44,6 +44,10 @@ int hf_uns_sizes(const hf_uns* u, int64_t* ncells, int64_t* npairs);
 int hf_uns_mesh_arrays(const hf_uns* u, int32_t* pair_start, int32_t* nbr, double* angle,
                        double* length, double* area, double* rin);
 
+/* cell centroids [2][ncells] as Polygon::calculate_centroid computes them
+ * (src/fvm_2d_uns/geometry/polygon/polygon.cpp:188-212); host-side, no device work */
+int hf_uns_centroids(const hf_uns* u, double* xy);
+
 /* Mesh::set_cells_flow_values / get_cells_flow_values (src/fvm_2d_uns/mesh/mesh/mesh.cpp:153-168) */
 int hf_uns_set_state(hf_uns* u, const double* cons);
 int hf_uns_get_state(hf_uns* u, double* cons);
@@ -62,6 +66,18 @@ int hf_uns_run(hf_uns* u, int64_t n, int clamp_t_end, int use_graph, int64_t* st
  * for that cell) and applied negated to the other cell; half the HLLC work, and the other cell's
  * flux differs from the reference's own evaluation by rounding only. */
 int hf_uns_set_edge_mode(hf_uns* u, int edge_based);
+
+/* Frame output with the cadence of the unstructured Simulation::solve
+ * (src/fvm_2d_uns/simulation/simulation/simulation.cpp:57-120), replacing its per-frame
+ * EulerIdealGasDataOutput::to_file (src/fvm_2d_uns/simulation/output/euler_data_output/
+ * euler_data_output.cpp:37-82) with full-precision device snapshots -- the same contract as
+ * hf_frames_enable / hf_frames_pending / hf_frame_pop of hyperflow_gb300.h: with frames
+ * enabled, hf_uns_run(clamp_t_end = 1) applies the frame dt clamp and copies the cell states
+ * (SoA [4][ncells]) into a device ring of ring_slots (2..32) frames, pausing while the ring
+ * lacks room for two; hf_uns_frame_pop returns the oldest with its time label and index. */
+int hf_uns_frames_enable(hf_uns* u, int ring_slots);
+int hf_uns_frames_pending(hf_uns* u, int64_t* n);
+int hf_uns_frame_pop(hf_uns* u, double* cons, double* t, int64_t* index);
 
 int hf_uns_get_time(hf_uns* u, double* t, int64_t* calls, double* last_dt);
 int hf_uns_hllc_errors(hf_uns* u, int64_t* count);

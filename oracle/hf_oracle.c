@@ -672,6 +672,68 @@ static inline void rotate(double deg, const double *f, double *o) {
 /* GodunovScheme::operator() (src/fvm_2d_uns/scheme/godunov/godunov.cpp:31-77) with
  * BoundaryConditions (src/fvm_2d_uns/scheme/boundary/boundary.cpp:29-69), the uns
  * TimeStep (src/fvm_2d_uns/scheme/timestep/timestep.cpp:29-62) and forward Euler. */
+/* the unstructured TimeStep (uns timestep.cpp:29-62): dt for the next step; advances calls */
+static double uns_dt(double g, double cfl, int64_t *calls, int ncells, const double *rin,
+                     const double *U, int nt) {
+    size_t N = (size_t)ncells;
+    double dtr = 1e16;
+#pragma omp parallel num_threads(nt)
+    {
+        double l = 1e16;
+#pragma omp for schedule(static)
+        for (int c = 0; c < ncells; ++c) {
+            double c4[4] = {U[c], U[N + c], U[2 * N + c], U[3 * N + c]}, w[4];
+            hfo_cons_to_prim(g, c4, w);
+            double u = w[1], v = w[2], cs = sound_speed(g, w);
+            l = smin(l, rin[c] / (fabs(sqrt(u * u + v * v)) + cs));
+        }
+#pragma omp critical
+        dtr = smin(dtr, l);
+    }
+    double final_cfl = (*calls + 1 <= 10) ? 0.2 * cfl : cfl;
+    (*calls)++;
+    return final_cfl * dtr;
+}
+
+/* ODESolver(GodunovScheme) + set_cells_flow_values (godunov.cpp:31-77) with dt; U -> Un */
+static void uns_update(double g, int ncells, const int *pair_start, const int *pair_nbr,
+                       const double *angle, const double *length, const double *area,
+                       const double *inlet, const double *U, double *Un, double dt, int nt) {
+    size_t N = (size_t)ncells;
+#pragma omp parallel for num_threads(nt) schedule(static)
+    for (int c = 0; c < ncells; ++c) {
+        double acc[4] = {0.0, 0.0, 0.0, 0.0};
+        double cv[4] = {U[c], U[N + c], U[2 * N + c], U[3 * N + c]};
+        for (int p = pair_start[c]; p < pair_start[c + 1]; ++p) {
+            double ang = angle[p], nb[4];
+            int k = pair_nbr[p];
+            if (k >= 0) {
+                for (int v = 0; v < 4; ++v) nb[v] = U[v * N + k];
+            } else if (k == -1) {            /* Reflective */
+                double r[4];
+                rotate(ang, cv, r);
+                r[1] *= -1.0;
+                rotate(-1.0 * ang, r, nb);
+            } else if (k == -2) {            /* Transmissive */
+                memcpy(nb, cv, sizeof nb);
+            } else {                         /* Inlet */
+                memcpy(nb, inlet, sizeof nb);
+            }
+            double rc[4], rn[4], rf[4], f[4];
+            rotate(ang, cv, rc);
+            rotate(ang, nb, rn);
+            hfo_hllc(g, rc, rn, 0, rf);
+            rotate(-1.0 * ang, rf, f);
+            for (int v = 0; v < 4; ++v) acc[v] += length[p] * f[v];
+        }
+        double inv = 1.0 / area[c];
+        for (int v = 0; v < 4; ++v) {
+            double L = -1.0 * (inv * acc[v]);
+            Un[v * N + c] = dt * L + cv[v];
+        }
+    }
+}
+
 int hfo_uns_run(double g, double cfl, int64_t *calls, int ncells, const int *pair_start,
                 const int *pair_nbr, const double *angle, const double *length,
                 const double *area, const double *rin, const double *inlet, double *U,
@@ -680,58 +742,56 @@ int hfo_uns_run(double g, double cfl, int64_t *calls, int ncells, const int *pai
     double *Un = (double *)malloc(4 * N * sizeof(double));
     int nt = nthreads > 0 ? nthreads : 1;
     for (int s = 0; s < n; ++s) {
-        double dtr = 1e16;
-#pragma omp parallel num_threads(nt)
-        {
-            double l = 1e16;
-#pragma omp for schedule(static)
-            for (int c = 0; c < ncells; ++c) {
-                double c4[4] = {U[c], U[N + c], U[2 * N + c], U[3 * N + c]}, w[4];
-                hfo_cons_to_prim(g, c4, w);
-                double u = w[1], v = w[2], cs = sound_speed(g, w);
-                l = smin(l, rin[c] / (fabs(sqrt(u * u + v * v)) + cs));
-            }
-#pragma omp critical
-            dtr = smin(dtr, l);
-        }
-        double final_cfl = (*calls + 1 <= 10) ? 0.2 * cfl : cfl;
-        (*calls)++;
-        double dt = final_cfl * dtr;
-#pragma omp parallel for num_threads(nt) schedule(static)
-        for (int c = 0; c < ncells; ++c) {
-            double acc[4] = {0.0, 0.0, 0.0, 0.0};
-            double cv[4] = {U[c], U[N + c], U[2 * N + c], U[3 * N + c]};
-            for (int p = pair_start[c]; p < pair_start[c + 1]; ++p) {
-                double ang = angle[p], nb[4];
-                int k = pair_nbr[p];
-                if (k >= 0) {
-                    for (int v = 0; v < 4; ++v) nb[v] = U[v * N + k];
-                } else if (k == -1) {            /* Reflective */
-                    double r[4];
-                    rotate(ang, cv, r);
-                    r[1] *= -1.0;
-                    rotate(-1.0 * ang, r, nb);
-                } else if (k == -2) {            /* Transmissive */
-                    memcpy(nb, cv, sizeof nb);
-                } else {                         /* Inlet */
-                    memcpy(nb, inlet, sizeof nb);
-                }
-                double rc[4], rn[4], rf[4], f[4];
-                rotate(ang, cv, rc);
-                rotate(ang, nb, rn);
-                hfo_hllc(g, rc, rn, 0, rf);
-                rotate(-1.0 * ang, rf, f);
-                for (int v = 0; v < 4; ++v) acc[v] += length[p] * f[v];
-            }
-            double inv = 1.0 / area[c];
-            for (int v = 0; v < 4; ++v) {
-                double L = -1.0 * (inv * acc[v]);
-                Un[v * N + c] = dt * L + cv[v];
-            }
-        }
+        double dt = uns_dt(g, cfl, calls, ncells, rin, U, nt);
+        uns_update(g, ncells, pair_start, pair_nbr, angle, length, area, inlet, U, Un, dt, nt);
         memcpy(U, Un, 4 * N * sizeof(double));
         if (dts) dts[s] = dt;
     }
     free(Un);
     return n;
+}
+
+/* the unstructured Simulation::solve (uns simulation.cpp:51-120) from t = t_start with the
+ * t_end clamp, the frame dt clamp and the frame cadence of the Cartesian hfo_solve; frames
+ * are the cell states [4][ncells].  Returns the steps taken. */
+int64_t hfo_uns_solve(double g, double cfl, int64_t *calls, int ncells, const int *pair_start,
+                      const int *pair_nbr, const double *angle, const double *length,
+                      const double *area, const double *rin, const double *inlet, double *U,
+                      double t_start, double t_end, double interval, double *t_out,
+                      double *frames, double *frame_t, int64_t max_frames, int64_t *nframes,
+                      int nthreads) {
+    size_t N = (size_t)ncells;
+    double *Un = (double *)malloc(4 * N * sizeof(double));
+    int nt = nthreads > 0 ? nthreads : 1;
+    double t = t_start, cur = 0.0;
+    int64_t nf = 0, taken = 0;
+#define HFO_UFRAME(src, label)                                                              \
+    do {                                                                                    \
+        if (nf < max_frames) {                                                              \
+            if (frames) memcpy(frames + (size_t)nf * 4 * N, (src), 4 * N * sizeof(double)); \
+            if (frame_t) frame_t[nf] = (label);                                             \
+        }                                                                                   \
+        ++nf;                                                                               \
+    } while (0)
+    for (int64_t n = 1; n < 1000000000; ++n) {
+        if (t == t_end) break;
+        double dt = uns_dt(g, cfl, calls, ncells, rin, U, nt);
+        if (t + dt > t_end) dt = t_end - t;
+        if (cur == 0.0) HFO_UFRAME(U, t);
+        if ((t + dt > cur) && (cur > 0.0)) dt = cur - t;
+        uns_update(g, ncells, pair_start, pair_nbr, angle, length, area, inlet, U, Un, dt, nt);
+        memcpy(U, Un, 4 * N * sizeof(double));
+        if (fabs(t - cur) < 1e-12) {
+            HFO_UFRAME(U, t);
+            cur += interval;
+        }
+        t += dt;
+        ++taken;
+    }
+    HFO_UFRAME(U, t);
+#undef HFO_UFRAME
+    free(Un);
+    if (t_out) *t_out = t;
+    if (nframes) *nframes = nf;
+    return taken;
 }

@@ -85,6 +85,13 @@ int hfo_uns_run(double gamma, double cfl, int64_t *calls, int ncells, const int 
                 const int *pair_nbr, const double *angle, const double *length,
                 const double *area, const double *rin, const double *inlet,
                 double *U, int n, double *dts, int nthreads);
+/* the unstructured Simulation::solve with its t_end and frame clamps and frame cadence */
+int64_t hfo_uns_solve(double g, double cfl, int64_t *calls, int ncells, const int *pair_start,
+                      const int *pair_nbr, const double *angle, const double *length,
+                      const double *area, const double *rin, const double *inlet, double *U,
+                      double t_start, double t_end, double interval, double *t_out,
+                      double *frames, double *frame_t, int64_t max_frames, int64_t *nframes,
+                      int nthreads);
 
 #ifdef __cplusplus
 }

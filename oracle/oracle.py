@@ -80,6 +80,9 @@ def port_lib():
         lib.hfo_solve.restype = C.c_int64
         lib.hfo_solve.argtypes = [p, d, C.c_int64, p, C.c_int64, p, p, C.c_int64, p]
         lib.hfo_uns_geometry.argtypes = [i, p, p, p, p, p, p]
+        lib.hfo_uns_solve.restype = C.c_int64
+        lib.hfo_uns_solve.argtypes = [d, d, p, i, p, p, p, p, p, p, p, p, d, d, d, p, p, p,
+                                      C.c_int64, p, i]
         lib.hfo_uns_run.restype = i
         lib.hfo_uns_run.argtypes = [d, d, p, i, p, p, p, p, p, p, p, p, i, p, i]
         _port = lib
@@ -375,6 +378,9 @@ def ref_uns_lib():
         lib.hfref_uns_get_state.argtypes = [p, p]
         lib.hfref_uns_set_state.argtypes = [p, p]
         lib.hfref_uns_geometry.argtypes = [p, p, p, p, p]
+        lib.hfref_uns_solve.restype = i
+        lib.hfref_uns_solve.argtypes = [p, C.c_char_p]
+        lib.hfref_uns_centroids.argtypes = [p, p]
         _refu = lib
     return _refu
 
@@ -418,6 +424,16 @@ class RefUns:
         U = np.ascontiguousarray(U, dtype=np.float64)
         self.lib.hfref_uns_set_state(self.h, _ptr(U))
 
+    def solve(self, outdir: str):
+        """The reference's own Simulation::solve; its CSV frames are written into outdir."""
+        if self.lib.hfref_uns_solve(self.h, os.fsencode(outdir)) != 0:
+            raise OSError(f"cannot run the reference solve in {outdir}")
+
+    def centroids(self) -> np.ndarray:
+        out = np.zeros((2, self.ncells))
+        self.lib.hfref_uns_centroids(self.h, _ptr(out))
+        return out
+
     def geometry(self):
         ang = np.zeros(self.npairs)
         ln = np.zeros(self.npairs)
@@ -437,6 +453,27 @@ def uns_geometry(nverts: np.ndarray, verts: np.ndarray):
     port_lib().hfo_uns_geometry(len(nverts), _ptr(nverts), _ptr(verts), _ptr(ang), _ptr(ln),
                                 _ptr(area), _ptr(rin))
     return ang, ln, area, rin
+
+
+def uns_solve(gamma, cfl, pair_start, pair_nbr, angle, length, area, rin, inlet, U, t_start,
+              t_end, interval, max_frames=64, nthreads=1):
+    """Simulation::solve of the restated unstructured solver with its frame cadence; U
+    ([4][ncells]) ends at t_end.  Returns (steps, TimeStep calls, frame labels, frames)."""
+    c = C.c_int64(0)
+    N = U.shape[1]
+    frames = np.zeros((max_frames, 4, N))
+    ft = np.zeros(max_frames)
+    nf = C.c_int64()
+    t_out = C.c_double()
+    ps = np.ascontiguousarray(pair_start, dtype=np.int32)
+    pn = np.ascontiguousarray(pair_nbr, dtype=np.int32)
+    inlet = np.ascontiguousarray(inlet, dtype=np.float64)
+    k = port_lib().hfo_uns_solve(gamma, cfl, C.byref(c), N, _ptr(ps), _ptr(pn), _ptr(angle),
+                                 _ptr(length), _ptr(area), _ptr(rin), _ptr(inlet), _ptr(U), t_start,
+                                 t_end, interval, C.byref(t_out), _ptr(frames), _ptr(ft), max_frames,
+                                 C.byref(nf), nthreads)
+    m = min(nf.value, max_frames)
+    return k, c.value, ft[:m], frames[:m]
 
 
 def uns_run(gamma, cfl, calls, pair_start, pair_nbr, angle, length, area, rin, inlet, U, n,

@@ -13,6 +13,8 @@
 // Everything else -- Godunov, HLLC, rotation, boundary states, TimeStep, ODE --
 // is the reference's own code, driven as Simulation::solve does
 // (src/fvm_2d_uns/simulation/simulation/simulation.cpp:61-120) for exactly N steps.
+#include <unistd.h>
+
 #include <cstring>
 #include <functional>
 #include <memory>
@@ -22,6 +24,7 @@
 #include <nlohmann/json.hpp>
 
 #include "simulation/parser/parser.h"
+#include "simulation/simulation/simulation.h"
 
 using json = nlohmann::json;
 using namespace HyperFlow;
@@ -102,6 +105,38 @@ int hfref_uns_run(void* h, int n) {
         r->t += dt;
     }
     return n;
+}
+
+// The reference's own Simulation::solve (simulation.cpp:51-120) on this context's mesh,
+// inside `outdir` (its CSV frames results_%06d.csv land there).  Simulation re-applies the
+// initial condition (simulation.cpp:43) and builds its own TimeStep.  0, or -1 when
+// outdir cannot be entered.
+int hfref_uns_solve(void* h, const char* outdir) {
+    RefUns* r = static_cast<RefUns*>(h);
+    char cwd[4096];
+    if (!getcwd(cwd, sizeof cwd) || chdir(outdir) != 0) return -1;
+    auto out = r->parser->generate_data_output();
+    std::shared_ptr<TimeStep> ts = r->parser->generate_time_step();
+    auto sim = std::make_shared<Simulation>(r->model, out, r->mesh, r->initcon, r->ode, r->scheme,
+                                            r->riemann, ts, r->parser->get_cfl(),
+                                            r->parser->get_t_start(), r->parser->get_t_end(),
+                                            r->parser->get_anim_duration(),
+                                            r->parser->get_anim_fps());
+    sim->solve();
+    r->t = r->parser->get_t_end();
+    return chdir(cwd) == 0 ? 0 : -1;
+}
+
+// cell centroids as the reference computes them (Polygon::calculate_centroid,
+// polygon.cpp:188-212), [2][ncells]
+void hfref_uns_centroids(void* h, double* out) {
+    auto& cells = static_cast<RefUns*>(h)->mesh->get_cells();
+    size_t n = cells.size();
+    for (size_t c = 0; c < n; ++c) {
+        Vec1D& x = cells[c].get_centroid();
+        out[c] = x[0];
+        out[n + c] = x[1];
+    }
 }
 
 void hfref_uns_dts(void* h, double* out) {

@@ -124,6 +124,30 @@ def make_frames():
         print(name, len(files), "frames")
 
 
+def make_uns_frames():
+    """The reference's own unstructured Simulation::solve with frame output."""
+    import hashlib
+    import tempfile
+    from hyperflow_gb300 import meshgen
+    sets = [("quad_channel_240", *quad_channel(), 0.05, 20.0),
+            ("tri_hole_3k", *meshgen.jittered_hole_mesh(3000, seed=3), 0.02, 10.0)]
+    for name, verts, codes, t_end, fps in sets:
+        nbr = meshgen.match_neighbours(verts, codes)
+        case = meshgen.channel_case("mesh.hmsh", cfl=0.5, t_end=t_end)
+        case["simulation"]["animation"] = {"duration": 1.0, "fps": fps}
+        nverts = np.full(len(verts), verts.shape[1], np.int32)
+        ref = oracle.RefUns(case, nverts, verts.reshape(-1, 2), nbr)
+        cen = ref.centroids()
+        with tempfile.TemporaryDirectory() as d:
+            ref.solve(d)
+            files = sorted(os.listdir(d))
+            hashes = [hashlib.sha256(open(os.path.join(d, fn), "rb").read()).hexdigest() for fn in files]
+        np.savez_compressed(os.path.join(HERE, f"unsframes_{name}.npz"), case=json.dumps(case),
+                            verts=verts, codes=codes, nbr=nbr, centroids=cen,
+                            csv_sha256=np.array(hashes), U=ref.state())
+        print("uns frames", name, len(files), "frames")
+
+
 def unit_states(n=4000, seed=11):
     """Random conservative states plus hand-picked edge cases (vacuum-like, supersonic,
     zero velocity, equal states, NaN/inf)."""
@@ -208,7 +232,7 @@ def make_uns():
 
 if __name__ == "__main__":
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref"], check=True)
-    which = sys.argv[1:] or ["units", "cart", "uns", "frames"]
+    which = sys.argv[1:] or ["units", "cart", "uns", "frames", "unsframes"]
     if "units" in which:
         make_units()
     if "cart" in which:
@@ -217,3 +241,5 @@ if __name__ == "__main__":
         make_uns()
     if "frames" in which:
         make_frames()
+    if "unsframes" in which:
+        make_uns_frames()

@@ -82,3 +82,47 @@ def test_frame_writer_thread(tmp_path):
     assert [os.path.basename(p) for p in paths] == [f"results_{k:06d}.hfb" for k in range(5)]
     head, blocks = fr.read_frame(paths[4])
     assert head["t"] == 0.4 and blocks[0][2, 3, 4] == 4.0
+
+
+def uns_frame_fixtures():
+    return sorted(os.path.basename(p)[10:-4] for p in glob.glob(os.path.join(GOLDEN, "unsframes_*.npz")))
+
+
+def load_uns_frames(name):
+    d = np.load(os.path.join(GOLDEN, f"unsframes_{name}.npz"))
+    out = {k: d[k] for k in d.files}
+    out["case"] = json.loads(str(out["case"]))
+    return out
+
+
+def uns_oracle_solve(g):
+    from oracle import oracle
+    from hyperflow_gb300 import meshgen  # noqa: F401
+    verts = g["verts"]
+    nverts = np.full(len(verts), verts.shape[1], np.int32)
+    ang, ln, area, rin = oracle.uns_geometry(nverts, verts.reshape(-1, 2))
+    ps = np.concatenate([[0], np.cumsum(nverts)]).astype(np.int32)
+    case = g["case"]
+    gam = float(case["model"]["gamma"])
+    inlet = oracle.prim_to_cons(case["mesh"]["boundaries"]["inlet"], gam)
+    ic = case["initial_condition"]
+    U = np.repeat(oracle.prim_to_cons(ic["init_state"], gam)[:, None], len(verts), axis=1)
+    sim = case["simulation"]
+    interval = float(sim["t_end"]) / (float(sim["animation"]["duration"]) * float(sim["animation"]["fps"]))
+    steps, calls, labels, frames = oracle.uns_solve(gam, float(sim["cfl"]), ps, g["nbr"].ravel(), ang, ln,
+                                                    area, rin, inlet, U, float(sim["t_start"]),
+                                                    float(sim["t_end"]), interval, max_frames=256)
+    return U, labels, frames
+
+
+@pytest.mark.parametrize("name", uns_frame_fixtures())
+def test_oracle_uns_solve_writes_the_reference_frames(name, port_lib):
+    from hyperflow_gb300 import frames as fr
+    g = load_uns_frames(name)
+    U, labels, frames = uns_oracle_solve(g)
+    np.testing.assert_array_equal(U, g["U"])
+    assert len(frames) == len(g["csv_sha256"])
+    meta = fr.uns_case_meta(g["case"], U.shape[1])
+    for k in range(len(frames)):
+        text = fr.uns_csv_text(dict(meta, t=float(labels[k])), frames[k], g["centroids"])
+        assert hashlib.sha256(text.encode()).hexdigest() == g["csv_sha256"][k], k

@@ -139,3 +139,25 @@ def test_gpu_checkpoint_carries_the_frame_cadence(tmp_path):
     for (_, _, x), (_, _, y) in zip(got, want):
         np.testing.assert_array_equal(x[0], y[0])
     np.testing.assert_array_equal(b.state(0), full.state(0))
+
+
+@pytest.mark.parametrize("name", ["quad_channel_240", "tri_hole_3k"])
+@pytest.mark.parametrize("ring", [8, 2])
+def test_gpu_uns_frames_equal_oracle_and_reference(name, ring, tmp_path, port_lib):
+    from hyperflow_gb300 import UnsSolver, frames as fr, meshgen
+    from test_frames import load_uns_frames, uns_oracle_solve
+    g = load_uns_frames(name)
+    U, labels, oframes = uns_oracle_solve(g)
+    s = UnsSolver(g["case"], mesh_text=meshgen.hmsh_text(g["verts"], g["codes"]))
+    np.testing.assert_array_equal(s.centroids(), g["centroids"])
+    s.solve(out_dir=str(tmp_path), ring_slots=ring)
+    np.testing.assert_array_equal(s.state(), g["U"])
+    paths = sorted(s.frame_paths)
+    assert len(paths) == len(g["csv_sha256"]) == len(oframes)
+    cen = s.centroids()
+    for k, p in enumerate(paths):
+        head, (Uk,) = fr.read_frame(p)
+        assert head["index"] == k and head["t"] == labels[k]
+        np.testing.assert_array_equal(Uk, oframes[k])
+        h = hashlib.sha256(fr.uns_csv_text(head, Uk, cen).encode()).hexdigest()
+        assert h == g["csv_sha256"][k], k
