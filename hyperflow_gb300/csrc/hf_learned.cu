@@ -753,6 +753,8 @@ int hf_lc_run_to(hf_lc* L, double t_end, int use_mlp, int64_t* steps, int64_t* r
         // the reference's TimeStep uses 0.2 x CFL for its first 10 calls; a MUSCL-Hancock
         // step makes two (step and predictor), so the first 5 steps are reduced
         if (L->steps < 5) dt *= 0.2;
+        if (!(dt > 0.0) || !std::isfinite(dt))
+            return lfail(L, HF_ERR_DEVICE, "coarse run stopped advancing (non-positive or non-finite dt)");
         if (L->t + dt > t_end) dt = t_end - L->t;
         int64_t rc = 0;
         r = hf_lc_step(L, dt, use_mlp, use_mlp ? &rc : nullptr);

@@ -42,7 +42,7 @@ def box_filter(U: np.ndarray, k: int) -> np.ndarray:
 
 
 class LearnedSolver:
-    def __init__(self, n: int, dx: float, gamma: float = 1.4, cfl: float = 0.8, limiter: int = 0):
+    def __init__(self, n: int, dx: float, gamma: float = 1.4, cfl: float = 0.4, limiter: int = 0):
         L = lib()
         h = C.c_void_p()
         st = L.hf_lc_create(n, dx, gamma, cfl, limiter, C.byref(h))
@@ -151,6 +151,9 @@ def fine_pairs(case_fine: dict, t_end: float, factor: int = 4, stride: int = 8):
         dtc = 0.0
         for _ in range(factor):
             dtc += s.step()
+        if not (dtc > 0.0 and np.isfinite(dtc)):
+            s.close()
+            raise FloatingPointError(f"fine run stopped advancing at t = {t} (dt = {dtc})")
         if take:
             U1 = box_filter(_interior(s.state(0), g), factor)
             pairs.append((U0.astype(np.float32), U1.astype(np.float32), dtc))

@@ -13,6 +13,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import sys
 import time
 
 import numpy as np
@@ -27,6 +28,10 @@ def sb_case(bubble, radius, t_end):
 
 def rp_case(seed):
     return lambda n: cases.random_quadrant_case(n, seed)
+
+
+def _log(msg: str, t0: float):
+    print(f"[{time.perf_counter() - t0:8.1f} s] {msg}", file=sys.stderr, flush=True)
 
 
 def main():
@@ -49,17 +54,20 @@ def main():
         c = fn(nf)
         T = t_end if t_end is not None else c["simulation"]["t_end"]
         pairs += fine_pairs(c, T, factor=f, stride=args.stride)
+        _log(f"fine data {name}: {len(pairs)} pairs", t0)
     report["train_pairs"] = len(pairs)
     report["data_seconds"] = time.perf_counter() - t0
     held_pairs = fine_pairs(rp_case(200)(nf), rp_case(200)(nf)["simulation"]["t_end"], factor=f,
                             stride=args.stride * 2)
     held_pairs += fine_pairs(cases.shock_bubble_case(nf, bubble=(0.42, 0.55)), 0.2, factor=f,
                              stride=args.stride * 2)
+    _log(f"held-out data: {len(held_pairs)} pairs", t0)
     ls = LearnedSolver(nc, 1.0 / nc)
     ls.set_params(init_params(0))
     t1 = time.perf_counter()
     losses, w = train(ls, pairs, args.iters, lr=args.lr)
     report["train_seconds"] = time.perf_counter() - t1
+    _log(f"trained {args.iters} iterations in {report['train_seconds']:.1f} s", t0)
     report["train_loss_first100"] = float(losses[:100].mean())
     report["train_loss_last100"] = float(losses[-100:].mean())
     report["heldout_one_step_loss"] = {"plain": one_step_loss(ls, held_pairs, w, False),
@@ -67,10 +75,11 @@ def main():
     params = ls.params()
     ls.close()
     np.save(args.out.replace(".json", "_params.npy"), params)
-    report["eval"] = {
-        "rp_seed_200": evaluate(rp_case(200), nf, rp_case(200)(nf)["simulation"]["t_end"], params),
-        "bubble_heldout": evaluate(sb_case((0.42, 0.55), 0.2, 0.2), nf, 0.2, params),
-    }
+    report["eval"] = {}
+    report["eval"]["rp_seed_200"] = evaluate(rp_case(200), nf, rp_case(200)(nf)["simulation"]["t_end"], params)
+    _log("evaluated rp_seed_200", t0)
+    report["eval"]["bubble_heldout"] = evaluate(sb_case((0.42, 0.55), 0.2, 0.2), nf, 0.2, params)
+    _log("evaluated bubble_heldout", t0)
     with open(args.out, "w") as fh:
         json.dump(report, fh, indent=1)
     print(json.dumps(report))

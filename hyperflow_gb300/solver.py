@@ -124,10 +124,13 @@ class CartSolver:
         if out_dir is None:
             total = 0
             while True:
+                t0 = self.time()[0]
                 k = self.run(chunk, clamp_t_end=True)
                 total += k
                 if k < chunk:
                     return total
+                if not self.time()[0] > t0:
+                    raise FloatingPointError(f"time stopped advancing at t = {t0} (dt = 0 or NaN)")
         from . import frames
         meta = frames.case_meta(self.case)
         self.enable_frames(ring_slots)
