@@ -31,15 +31,19 @@ BYTES_PER_CELL = 64          # 4 FP64 read + 4 FP64 written per cell update
 WORKLOAD = "mach3_forward_facing_step_3block_dx1_1365_muscl_hancock_minbee_hllc_fp64"
 
 
-def make_case(limiter: str = "MinBee", workload: str = "ffs", n: int = 4096):
+def make_case(limiter: str = "MinBee", workload: str = "ffs", n: int = 4096, scheme: str = "MUSCLHancock"):
     from hyperflow_gb300 import cases
     if workload == "square":
+        if scheme == "Godunov":
+            return cases.quadrant_case(n, scheme="Godunov", cfl=0.8)
         return cases.quadrant_case(n, scheme="MUSCLHancock", limiter=limiter, cfl=0.8)
     return cases.forward_facing_step_case(1365, limiter=limiter, cfl=0.8, t_end=4.0)
 
 
 def workload_name(args):
     if args.workload == "square":
+        if args.scheme == "Godunov":
+            return f"quadrant_riemann_{args.n}x{args.n}_godunov_hllc_fp64"
         return f"quadrant_riemann_{args.n}x{args.n}_muscl_hancock_{args.limiter.lower()}_hllc_fp64"
     return WORKLOAD
 
@@ -136,7 +140,7 @@ def reference_arm(args, cells):
     ws, rank, _ = dist_env()
     if rank != 0:
         return
-    case = make_case(args.limiter, args.workload, args.n)
+    case = make_case(args.limiter, args.workload, args.n, args.scheme)
     nth = os.cpu_count() or 1
     from oracle.oracle import Oracle, build_port
     build_port()
@@ -169,13 +173,15 @@ def main():
     ap.add_argument("--workload", default="ffs", choices=["ffs", "square"],
                     help="ffs: the 3-block forward-facing step (default); square: one n x n block")
     ap.add_argument("--n", type=int, default=4096, help="side of the square workload")
+    ap.add_argument("--scheme", default="MUSCLHancock", choices=["MUSCLHancock", "Godunov"],
+                    help="scheme of the square workload")
     ap.add_argument("--quick", action="store_true",
                     help="device-resident timing only (no graph pass, e2e or CPU baseline)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
     from hyperflow_gb300 import cases
-    case = make_case(args.limiter, args.workload, args.n)
+    case = make_case(args.limiter, args.workload, args.n, args.scheme)
     cells = cases.total_cells(case)
 
     if args.impl == "reference":

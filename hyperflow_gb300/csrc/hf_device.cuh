@@ -41,21 +41,19 @@ struct Prim {
 HF_HD Prim to_prim(double g1, double r, double ru, double rv, double E) {
     Prim w;
     w.r = r;
-    w.u = div_rn(ru, r);
-    w.v = div_rn(rv, r);
+    div2_rn(ru, rv, r, w.u, w.v);
     w.q = w.u * w.u + w.v * w.v;
-    w.p = g1 * (E - 0.5 * r * w.q);
+    w.p = g1 * (E - half(r) * w.q);
     double e = div_rn(w.p, w.r * g1);      // prim_internal_energy (32-36)
-    w.Et = w.r * (0.5 * w.q + e);
+    w.Et = w.r * (half(w.q) + e);
     return w;
 }
 
 // only the primitives (no energy): what TimeStep needs
 HF_HD void to_prim_short(double g1, double r, double ru, double rv, double E,
                                               double& u, double& v, double& p) {
-    u = div_rn(ru, r);
-    v = div_rn(rv, r);
-    p = g1 * (E - 0.5 * r * (u * u + v * v));
+    div2_rn(ru, rv, r, u, v);
+    p = g1 * (E - half(r) * (u * u + v * v));
 }
 
 // prim_speed_of_sound (60-64)
@@ -188,7 +186,7 @@ HF_HD double slope(double um, double u0, double up) {
     if (abs_le(dlc, kTol)) dlc = (dlc == 0.0) ? kTol : kTol * sgn(dlc);
     if (abs_le(drc, kTol)) drc = (drc == 0.0) ? kTol : kTol * sgn(drc);
     double xi = limiter<LIM>(div_rn(dlc, drc));
-    return xi * (0.5 * dl + 0.5 * dr);
+    return xi * (half(dl) + half(dr));
 }
 
 // ------------------------------------------------------------------------------

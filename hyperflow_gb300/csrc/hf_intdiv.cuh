@@ -105,46 +105,61 @@ HF_HD bool ge0(double x) {            // 0.0 <= x
 // |x| <= t for a positive finite t (false for NaN)
 HF_HD bool abs_le(double x, double t) { return (f64_bits(x) & kAbs) <= f64_bits(t); }
 
+// 0.5 * x, equal to the FP64 multiplication for every x: a normal x above the lowest binade
+// only has its exponent lowered by one (exact); zeros keep their sign; subnormals, the lowest
+// normal binade (where halving rounds), infinities and NaN take the multiplication.
+HF_HD double half(double x) {
+    const uint64_t u = f64_bits(x);
+    const uint32_t e = (uint32_t)(u >> 52) & 0x7FFu;
+    if (e - 2u < 0x7FDu) return f64_from(u - (1ull << 52));   // exponent field in [2, 0x7FE]
+    if ((u << 1) == 0) return x;
+    return 0.5 * x;
+}
+
 HF_HD double hw_div(double a, double b) { return a / b; }
 HF_HD double hw_sqrt(double x) { return std::sqrt(x); }
 
-HF_HD double div_rn(double a, double b) {
-    const uint64_t A = f64_bits(a), B = f64_bits(b);
+// Fixed-point reciprocal X ~ 2^116 / mb of a divisor mantissa mb in (2^52, 2^53) (not a
+// power of two): an FP32 seed of mb's top 24 bits, then two Newton steps.
+HF_HD uint64_t recip_fixed(uint64_t mb) {
+    // FP32 seed: X0 = 2^87 / dh with dh = mb >> 29 in [2^23, 2^24)
+    const uint32_t dh = (uint32_t)(mb >> 29);
+    const float r = rcp_f32((float)dh);
+    const uint32_t rb = f32_bits(r);
+    const uint64_t mr = (uint64_t)((rb & 0x7FFFFFu) | 0x800000u);
+    const int sh = (int)((rb >> 23) & 0xFFu) - 63;   // r = mr 2^(E-150); X0 = mr 2^(E-63)
+    uint64_t X = sh >= 41 ? 0xFFFFFFFFFFFFFFFFull : (mr << sh);
+#pragma unroll
+    for (int it = 0; it < 2; ++it) {
+        // E = 2^116 - mb X as a signed 128-bit value (small); C = X E / 2^116
+        const uint64_t plo = mb * X, phi = umulhi64(mb, X);
+        const uint64_t elo = 0ull - plo;
+        const uint64_t ehi = (1ull << 52) - phi - (plo != 0 ? 1ull : 0ull);
+        const int64_t e52 = (int64_t)((ehi << 12) | (elo >> 52));     // E >> 52
+        const uint64_t mag = e52 < 0 ? (uint64_t)(-e52) : (uint64_t)e52;
+        const uint64_t c = umulhi64(X, mag);
+        X = e52 < 0 ? X - c : X + c;
+    }
+    return X;
+}
+
+// The quotient of the fast path: a, b as in div_rn with `fast` true and a nonzero; X the
+// reciprocal of b's mantissa (unused when b is a power of two).
+HF_HD double quot_fast(uint64_t A, uint64_t B, uint64_t X) {
     const uint32_t ea = (uint32_t)(A >> 52) & 0x7FFu, eb = (uint32_t)(B >> 52) & 0x7FFu;
     const uint64_t sign = (A ^ B) & 0x8000000000000000ull;
     const uint64_t M52 = 0x000FFFFFFFFFFFFFull, H52 = 0x0010000000000000ull;
-    const bool a_zero = (A << 1) == 0;
     int e = (int)ea - (int)eb + 1023;
-    uint64_t ma = (A & M52) | H52, mb = (B & M52) | H52;
+    uint64_t ma = (A & M52) | H52;
+    const uint64_t mb = (B & M52) | H52;
     const bool shift = ma < mb;
     e -= shift ? 1 : 0;
-    const bool fast = (eb - 1u < 2046u) && (a_zero || ((ea - 1u < 2046u) && e >= 1 && e <= 2045));
-    if (!fast) return hw_div(a, b);
-    if (a_zero) return f64_from(sign);
     if (shift) ma <<= 1;                       // ma / mb in [1, 2)
     uint64_t Q, R;
     if ((B & M52) == 0) {                      // divisor a power of two: exact
         Q = ma;                                // ma in [2^52, 2^53): no shift happened
         R = 0;
     } else {
-        // FP32 seed: X0 = 2^87 / dh with dh = mb >> 29 in [2^23, 2^24)
-        const uint32_t dh = (uint32_t)(mb >> 29);
-        const float r = rcp_f32((float)dh);
-        const uint32_t rb = f32_bits(r);
-        const uint64_t mr = (uint64_t)((rb & 0x7FFFFFu) | 0x800000u);
-        const int sh = (int)((rb >> 23) & 0xFFu) - 63;   // r = mr 2^(E-150); X0 = mr 2^(E-63)
-        uint64_t X = sh >= 41 ? 0xFFFFFFFFFFFFFFFFull : (mr << sh);
-#pragma unroll
-        for (int it = 0; it < 2; ++it) {
-            // E = 2^116 - mb X as a signed 128-bit value (small); C = X E / 2^116
-            const uint64_t plo = mb * X, phi = umulhi64(mb, X);
-            const uint64_t elo = 0ull - plo;
-            const uint64_t ehi = (1ull << 52) - phi - (plo != 0 ? 1ull : 0ull);
-            const int64_t e52 = (int64_t)((ehi << 12) | (elo >> 52));     // E >> 52
-            const uint64_t mag = e52 < 0 ? (uint64_t)(-e52) : (uint64_t)e52;
-            const uint64_t c = umulhi64(X, mag);
-            X = e52 < 0 ? X - c : X + c;
-        }
         Q = umulhi64(ma, X);
         int64_t Rs = (int64_t)((ma << 52) - Q * mb);   // exact: |R| < 2^55
 #pragma unroll
@@ -160,6 +175,38 @@ HF_HD double div_rn(double a, double b) {
     if (r2 > mb || (r2 == mb && (Q & 1ull))) Q += 1;
     if (Q == (H52 << 1)) { Q = H52; e += 1; }
     return f64_from(sign | ((uint64_t)e << 52) | (Q & M52));
+}
+
+// true when a / b takes the integer path: b normal, and a zero, or a normal with a normal
+// quotient exponent
+HF_HD bool div_fast(uint64_t A, uint64_t B) {
+    const uint32_t ea = (uint32_t)(A >> 52) & 0x7FFu, eb = (uint32_t)(B >> 52) & 0x7FFu;
+    const uint64_t M52 = 0x000FFFFFFFFFFFFFull, H52 = 0x0010000000000000ull;
+    const bool a_zero = (A << 1) == 0;
+    int e = (int)ea - (int)eb + 1023;
+    e -= (((A & M52) | H52) < ((B & M52) | H52)) ? 1 : 0;
+    return (eb - 1u < 2046u) && (a_zero || ((ea - 1u < 2046u) && e >= 1 && e <= 2045));
+}
+
+HF_HD double div_rn(double a, double b) {
+    const uint64_t A = f64_bits(a), B = f64_bits(b);
+    if (!div_fast(A, B)) return hw_div(a, b);
+    if ((A << 1) == 0) return f64_from((A ^ B) & 0x8000000000000000ull);
+    const uint64_t M52 = 0x000FFFFFFFFFFFFFull, H52 = 0x0010000000000000ull;
+    const uint64_t X = (B & M52) == 0 ? 0ull : recip_fixed((B & M52) | H52);
+    return quot_fast(A, B, X);
+}
+
+// a1 / b and a2 / b with one shared reciprocal; each result equals the IEEE quotient
+HF_HD void div2_rn(double a1, double a2, double b, double& q1, double& q2) {
+    const uint64_t A1 = f64_bits(a1), A2 = f64_bits(a2), B = f64_bits(b);
+    const uint64_t M52 = 0x000FFFFFFFFFFFFFull, H52 = 0x0010000000000000ull;
+    const bool f1 = div_fast(A1, B), f2 = div_fast(A2, B);
+    uint64_t X = 0ull;
+    if ((f1 || f2) && (B & M52) != 0) X = recip_fixed((B & M52) | H52);
+    const uint64_t S = B & 0x8000000000000000ull;
+    q1 = !f1 ? hw_div(a1, b) : ((A1 << 1) == 0 ? f64_from((A1 & 0x8000000000000000ull) ^ S) : quot_fast(A1, B, X));
+    q2 = !f2 ? hw_div(a2, b) : ((A2 << 1) == 0 ? f64_from((A2 & 0x8000000000000000ull) ^ S) : quot_fast(A2, B, X));
 }
 
 }  // namespace hf

@@ -50,8 +50,9 @@ __device__ __forceinline__ int mh_tile_fluxes(const double* __restrict__ sU, dou
             const double* row = sU + (v * L::UY + sy) * L::UX;
             const double u0 = row[sx];
             const double s = slope<LIM>(row[sx - 1], u0, row[sx + 1]);
-            e0[v] = u0 - 0.5 * s;
-            e1[v] = u0 + 0.5 * s;
+            const double hs = half(s);
+            e0[v] = u0 - hs;
+            e1[v] = u0 + hs;
         }
         Prim w0 = to_prim(g1, e0[0], e0[1], e0[2], e0[3]);
         Prim w1 = to_prim(g1, e1[0], e1[1], e1[2], e1[3]);
@@ -92,8 +93,9 @@ __device__ __forceinline__ int mh_tile_fluxes(const double* __restrict__ sU, dou
             const double* col = sU + (v * L::UY + sy) * L::UX + sx;
             const double u0 = col[0];
             const double s = slope<LIM>(col[-L::UX], u0, col[L::UX]);
-            e2[v] = u0 - 0.5 * s;
-            e3[v] = u0 + 0.5 * s;
+            const double hs = half(s);
+            e2[v] = u0 - hs;
+            e3[v] = u0 + hs;
         }
         Prim w2 = to_prim(g1, e2[0], e2[1], e2[2], e2[3]);
         Prim w3 = to_prim(g1, e3[0], e3[1], e3[2], e3[3]);

@@ -22,6 +22,8 @@ def hm():
     p, d, i, i64 = C.c_void_p, C.c_double, C.c_int, C.c_int64
     L.hm_div.argtypes = [p, p, p, i64]
     L.hm_sqrt.argtypes = [p, p, i64]
+    L.hm_half.argtypes = [p, p, i64]
+    L.hm_div2.argtypes = [p, p, p, p, p, i64]
     L.hm_hllc.argtypes = [d, p, p, i, p]
     L.hm_hllc.restype = i
     L.hm_limiter.argtypes = [i, d]
@@ -142,3 +144,31 @@ def test_limiters_on_special_ratios(hm, port_lib):
             got, want = hm.hm_limiter(kind, float(r)), port_lib.hfo_limiter(kind, float(r))
             assert (np.isnan(got) and np.isnan(want)) or \
                 np.float64(got).view(np.uint64) == np.float64(want).view(np.uint64), (kind, r, got, want)
+
+
+def test_half_equals_multiplication(hm):
+    rng = np.random.default_rng(5)
+    x = np.concatenate([_specials(), _operands(rng, 500_000)[0],
+                        np.array([2.2250738585072014e-308 * k for k in (1.0, 1.5, 2.0, 3.0, 4.0)]),
+                        -np.array([2.2250738585072014e-308 * k for k in (1.0, 1.5, 2.0, 3.0, 4.0)]),
+                        np.array([5e-324 * k for k in range(1, 40)])])
+    out = np.empty_like(x)
+    hm.hm_half(x.ctypes.data, out.ctypes.data, x.size)
+    want = 0.5 * x
+    same = (out.view(np.uint64) == want.view(np.uint64)) | (np.isnan(out) & np.isnan(want))
+    assert same.all(), x[~same][:5]
+
+
+def test_shared_divisor_division_equals_ieee(hm):
+    rng = np.random.default_rng(6)
+    a, b = _operands(rng, 600_000)
+    a2 = np.roll(a, 7)
+    a2[:50] = 0.0
+    a2[50:100] = -0.0
+    q1, q2 = np.empty_like(a), np.empty_like(a)
+    hm.hm_div2(a.ctypes.data, a2.ctypes.data, b.ctypes.data, q1.ctypes.data, q2.ctypes.data, a.size)
+    with np.errstate(all="ignore"):
+        w1, w2 = a / b, a2 / b
+    for got, want in ((q1, w1), (q2, w2)):
+        same = (got.view(np.uint64) == want.view(np.uint64)) | (np.isnan(got) & np.isnan(want))
+        assert same.all()
