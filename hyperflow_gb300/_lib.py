@@ -44,6 +44,7 @@ SIGNATURES = {
     "hf_frame_len": (_i, [_p, C.POINTER(_i64)]),
     "hf_frames_pending": (_i, [_p, C.POINTER(_i64)]),
     "hf_frame_pop": (_i, [_p, _p, C.POINTER(_d), C.POINTER(_i64)]),
+    "hf_coarsen": (_i, [_p, _i, _i, _p]),
     "hf_checkpoint_size": (_i, [_p, C.POINTER(_sz)]),
     "hf_checkpoint_save": (_i, [_p, _p, _sz]),
     "hf_checkpoint_load": (_i, [_p, _p, _sz]),

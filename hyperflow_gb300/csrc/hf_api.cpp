@@ -88,6 +88,8 @@ struct hf_ctx {
     hf::FrameRing ring{};
     int ring_slots = 0;
     long long drained = 0;      // host count of frames popped from the ring
+    float* coarse = nullptr;    // device scratch of hf_coarsen
+    size_t coarse_n = 0;
     int next_block = 0;         // next block hf_advance_block expects
     long long host_step = 0;    // mirror of ctrl.step while the host drives the steps
     // graphs of one step (index = clamp flag)
@@ -530,6 +532,7 @@ void hf_destroy(hf_ctx* ctx) {
     }
     for (double* p : ctx->allocs) cudaFree(p);
     if (ctx->ring.base) cudaFree(ctx->ring.base);
+    if (ctx->coarse) cudaFree(ctx->coarse);
     if (ctx->dmesh) cudaFree(ctx->dmesh);
     if (ctx->dctrl) cudaFree(ctx->dctrl);
     if (ctx->pinned) cudaFreeHost(ctx->pinned);
@@ -802,6 +805,28 @@ int hf_frame_pop(hf_ctx* ctx, double* cons, double* t, int64_t* index) {
     ctx->drained += 1;
     long long d = ctx->drained;
     CK(cudaMemcpy(&ctx->dctrl->drained, &d, sizeof d, cudaMemcpyHostToDevice));
+    return HF_OK;
+}
+
+// ---- coarse copies of the state (training data of the learned coarse solver) ----
+
+int hf_coarsen(hf_ctx* ctx, int b, int factor, float* out) {
+    if (!ctx || !out || b < 0 || b >= ctx->nblocks || factor < 1) return HF_ERR_ARG;
+    const BlockHost& B = ctx->blocks[b];
+    if (B.nx % factor != 0 || B.ny % factor != 0)
+        return fail(ctx, HF_ERR_ARG, "block sides must be multiples of the coarsening factor");
+    if (ctx->next_block != 0) return fail(ctx, HF_ERR_STATE, "coarsen in the middle of a step");
+    const size_t n = (size_t)4 * (B.nx / factor) * (B.ny / factor);
+    if (ctx->coarse_n < n) {
+        if (ctx->coarse) CK(cudaFree(ctx->coarse));
+        ctx->coarse = nullptr;
+        ctx->coarse_n = 0;
+        CK(cudaMalloc(&ctx->coarse, n * sizeof(float)));
+        ctx->coarse_n = n;
+    }
+    CK(hf::launch_coarsen(ctx->dctrl, ctx->dmesh, b, factor, (long long)n, ctx->coarse, ctx->stream));
+    CK(cudaMemcpyAsync(out, ctx->coarse, n * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
     return HF_OK;
 }
 

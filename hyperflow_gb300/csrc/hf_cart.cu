@@ -478,7 +478,7 @@ __global__ void __launch_bounds__(NT) godunov_kernel(Ctrl* __restrict__ c,
 // ------------------------------------------------------------------------------------
 // launchers
 // ------------------------------------------------------------------------------------
-constexpr int kMhTX = 32, kMhTY = 16, kMhNT = 256;
+constexpr int kMhTX = 32, kMhTY = 14, kMhNT = 256;
 constexpr int kGoTX = 32, kGoTY = 16, kGoNT = 256;
 
 StencilTiles stencil_tiles(int scheme) {
@@ -528,6 +528,36 @@ cudaError_t launch_interior_cfl(Ctrl* c, const MeshDev* m, int b, int nx, int ny
 
 cudaError_t launch_set_dt(Ctrl* c, double dt, cudaStream_t s) {
     set_dt_kernel<<<1, 1, 0, s>>>(c, dt);
+    return cudaGetLastError();
+}
+
+// k x k box average of one block's interior in FP64, stored as FP32 [4][ny/k][nx/k]
+__global__ void __launch_bounds__(256) coarsen_kernel(const Ctrl* __restrict__ c,
+                                                      const MeshDev* __restrict__ m, int b, int k,
+                                                      float* __restrict__ out) {
+    const BlockDev& B = m->b[b];
+    const double* __restrict__ U = B.buf[(int)(c->step & 1)];
+    const int g = m->ghost, cx = B.nx / k, cy = B.ny / k;
+    const long long n = 4LL * cx * cy;
+    const double inv = 1.0 / ((double)k * (double)k);
+    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n;
+         q += (long long)gridDim.x * blockDim.x) {
+        const int v = (int)(q / ((long long)cx * cy));
+        const long long r = q - (long long)v * cx * cy;
+        const int j = (int)(r / cx), i = (int)(r - (long long)j * cx);
+        const double* base = U + (size_t)v * B.ty * B.pitch + (size_t)(j * k + g) * B.pitch + (i * k + g);
+        double acc = 0.0;
+        for (int jj = 0; jj < k; ++jj)
+            for (int ii = 0; ii < k; ++ii) acc += base[(size_t)jj * B.pitch + ii];
+        out[q] = (float)(acc * inv);
+    }
+}
+
+cudaError_t launch_coarsen(const Ctrl* c, const MeshDev* m, int b, int k, long long n, float* out,
+                           cudaStream_t s) {
+    long long want = (n + 255) / 256;
+    int grid = (int)(want < 1 ? 1 : (want > 8 * 152 ? 8 * 152 : want));
+    coarsen_kernel<<<grid, 256, 0, s>>>(c, m, b, k, out);
     return cudaGetLastError();
 }
 

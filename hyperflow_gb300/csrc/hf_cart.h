@@ -54,6 +54,9 @@ cudaError_t launch_interior_cfl(Ctrl* c, const MeshDev* m, int b, int nx, int ny
                                 cudaStream_t s);
 cudaError_t launch_set_dt(Ctrl* c, double dt, cudaStream_t s);
 cudaError_t launch_finalize(Ctrl* c, cudaStream_t s);
+// k x k box average of block b's interior (FP64 sums) as FP32 [4][ny/k][nx/k]; n = its length
+cudaError_t launch_coarsen(const Ctrl* c, const MeshDev* m, int b, int k, long long n, float* out,
+                           cudaStream_t s);
 // this step's frames (if any) into the ring; between the stencils and launch_finalize
 cudaError_t launch_frame_copy(Ctrl* c, const MeshDev* m, const FrameRing& ring, cudaStream_t s);
 cudaError_t launch_stencil(Ctrl* c, const MeshDev* m, int b, int nx, int ny, int scheme, int limiter,

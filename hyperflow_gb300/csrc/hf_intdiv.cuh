@@ -105,15 +105,19 @@ HF_HD bool ge0(double x) {            // 0.0 <= x
 // |x| <= t for a positive finite t (false for NaN)
 HF_HD bool abs_le(double x, double t) { return (f64_bits(x) & kAbs) <= f64_bits(t); }
 
-// 0.5 * x, equal to the FP64 multiplication for every x: a normal x above the lowest binade
-// only has its exponent lowered by one (exact); zeros keep their sign; subnormals, the lowest
-// normal binade (where halving rounds), infinities and NaN take the multiplication.
+// 0.5 * x, equal to the FP64 multiplication for every x, on the integer pipe and without a
+// branch: a normal x above the lowest binade has its exponent lowered by one (exact); for
+// zeros, subnormals and the lowest normal binade the 53-bit significand-with-exponent-bit
+// field is shifted right by one with round to nearest even (a carry into the exponent field
+// gives the smallest normal, as the multiplication does); infinities and NaN are returned as
+// they are.
 HF_HD double half(double x) {
     const uint64_t u = f64_bits(x);
-    const uint32_t e = (uint32_t)(u >> 52) & 0x7FFu;
-    if (e - 2u < 0x7FDu) return f64_from(u - (1ull << 52));   // exponent field in [2, 0x7FE]
-    if ((u << 1) == 0) return x;
-    return 0.5 * x;
+    const uint64_t sgn = u & 0x8000000000000000ull, a = u & 0x7FFFFFFFFFFFFFFFull;
+    const uint32_t e = (uint32_t)(a >> 52);
+    const uint64_t low = sgn | ((a >> 1) + (a & (a >> 1) & 1ull));   // e <= 1
+    const uint64_t r = (e - 2u < 0x7FDu) ? u - (1ull << 52) : (e <= 1u ? low : u);
+    return f64_from(r);
 }
 
 HF_HD double hw_div(double a, double b) { return a / b; }

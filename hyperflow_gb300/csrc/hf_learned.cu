@@ -778,14 +778,15 @@ int hf_lc_get_time(hf_lc* L, double* t) { if (!L || !t) return HF_ERR_ARG; *t = 
 int hf_lc_set_bound(hf_lc* L, double bound) { if (!L || bound <= 0) return HF_ERR_ARG; L->bound = bound; return HF_OK; }
 
 // One training iteration on the pair (U0, T) with step dt: forward (plain + MLP, no guard),
-// loss and dL/dY, backward, Adam.  U0/T are host arrays [4][n][n]; w = 4 variable weights.
+// loss and dL/dY, backward, Adam.  U0/T are host arrays [4][n][n] (U0 null: the solver's
+// current state, left unchanged); w = 4 variable weights.
 int hf_lc_train_step(hf_lc* L, const float* U0, const float* T, const float* w, double dt, double lr,
                      double* loss) {
-    if (!L || !U0 || !T || !w || dt <= 0) return HF_ERR_ARG;
+    if (!L || !T || !w || dt <= 0) return HF_ERR_ARG;
     const size_t bytes = (size_t)4 * L->n * L->n * sizeof(float);
     const int nf = nfaces(L);
     hf::lc::Grid G = grid(L);
-    LCK(cudaMemcpyAsync(L->U[L->cur], U0, bytes, cudaMemcpyHostToDevice, L->stream));
+    if (U0) LCK(cudaMemcpyAsync(L->U[L->cur], U0, bytes, cudaMemcpyHostToDevice, L->stream));
     LCK(cudaMemcpyAsync(L->T, T, bytes, cudaMemcpyHostToDevice, L->stream));
     LCK(cudaMemcpyAsync(L->wv, w, 4 * sizeof(float), cudaMemcpyHostToDevice, L->stream));
     int r = fluxes(L, (float)dt, true, true);

@@ -110,12 +110,15 @@ class LearnedSolver:
         return k.value, r.value
 
     def train_step(self, U0, T, w, dt: float, lr: float) -> float:
-        U0 = np.ascontiguousarray(U0, dtype=np.float32)
+        """U0 None: from the current device state (kept)."""
+        ptr = None
+        if U0 is not None:
+            U0 = np.ascontiguousarray(U0, dtype=np.float32)
+            ptr = U0.ctypes.data
         T = np.ascontiguousarray(T, dtype=np.float32)
         w = np.ascontiguousarray(w, dtype=np.float32)
         loss = C.c_double()
-        self._c(lib().hf_lc_train_step(self._h, U0.ctypes.data, T.ctypes.data, w.ctypes.data, dt, lr,
-                                       C.byref(loss)))
+        self._c(lib().hf_lc_train_step(self._h, ptr, T.ctypes.data, w.ctypes.data, dt, lr, C.byref(loss)))
         return loss.value
 
     def mlp_forward(self, x_bits: np.ndarray) -> np.ndarray:
@@ -163,6 +166,53 @@ def fine_pairs(case_fine: dict, t_end: float, factor: int = 4, stride: int = 8):
     return pairs
 
 
+def fine_sequence(case_fine: dict, t_end: float, factor: int = 4):
+    """The plain FP64 solver on the fine case until t_end, box-filtered by `factor` after
+    every window of `factor` fine steps: (states [m+1] of [4][n/f][n/f] float32, dts [m])."""
+    s = CartSolver(case_fine)
+    states = [s.coarsen(0, factor)]
+    dts, t = [], 0.0
+    while t < t_end:
+        dtc = 0.0
+        for _ in range(factor):
+            dtc += s.step()
+        if not (dtc > 0.0 and np.isfinite(dtc)):
+            s.close()
+            raise FloatingPointError(f"fine run stopped advancing at t = {t} (dt = {dtc})")
+        states.append(s.coarsen(0, factor))
+        dts.append(dtc)
+        t += dtc
+    s.close()
+    return states, dts
+
+
+def train_rollout(ls: "LearnedSolver", seqs, iters: int, lr: float = 1e-3, max_roll: int = 4,
+                  p_roll: float = 0.5, seed: int = 0, w=None):
+    """One-step training on the solver's own inputs ("pushforward"): with probability p_roll
+    the input is the learned solver's state after r = 1..max_roll of its own steps from a
+    filtered fine state (no gradient through those steps), else the filtered state itself;
+    the target is the filtered fine state one window after the input.  seqs: list of
+    (states, dts) from fine_sequence."""
+    rng = np.random.default_rng(seed)
+    if w is None:
+        pairs = [(st[k], st[k + 1], dts[k]) for st, dts in seqs for k in range(len(dts))]
+        w = change_weights(pairs)
+    losses = []
+    for it in range(iters):
+        st, dts = seqs[int(rng.integers(len(seqs)))]
+        r = int(rng.integers(1, max_roll + 1)) if rng.random() < p_roll else 0
+        k = int(rng.integers(0, len(dts) - r))
+        lr_it = lr * (0.5 * (1 + np.cos(np.pi * it / iters)))
+        if r == 0:
+            losses.append(ls.train_step(st[k], st[k + 1], w, dts[k], lr_it))
+            continue
+        ls.set_state(st[k])
+        for j in range(r):
+            ls.step(dts[k + j], True)
+        losses.append(ls.train_step(None, st[k + r + 1], w, dts[k + r], lr_it))
+    return np.array(losses), w
+
+
 def change_weights(pairs) -> np.ndarray:
     """Per-variable loss weights: the inverse mean squared one-step change."""
     acc = np.zeros(4)
@@ -203,10 +253,10 @@ def _timed(fn):
     return out, time.perf_counter() - t0
 
 
-def evaluate(case_fn, n_fine: int, t_end: float, params, factor: int = 4, limiter: int = 0):
-    """L1 density error against the filtered FP64 fine solution, and wall time, for:
-    plain FP64 at n_fine, n_fine/2, n_fine/4 (CartSolver), and plain / learned FP32 at
-    n_fine/4 (LearnedSolver).  case_fn(n) builds the case at resolution n."""
+def evaluate_plain(case_fn, n_fine: int, t_end: float, factor: int = 4, limiter: int = 0):
+    """L1 density error against the filtered FP64 fine solution, and wall time, of plain FP64
+    at n_fine, n_fine/2, n_fine/4 (CartSolver) and plain FP32 at n_fine/4 (LearnedSolver
+    without the MLP).  Returns (results, filtered reference density, coarse initial state)."""
     out = {}
     nc = n_fine // factor
 
@@ -231,12 +281,29 @@ def evaluate(case_fn, n_fine: int, t_end: float, params, factor: int = 4, limite
     U0 = _interior(s0.state(0), s0.block_dims(0)["ghost"]).astype(np.float32)
     s0.close()
     ls = LearnedSolver(nc, 1.0 / nc, limiter=limiter)
-    ls.set_params(params)
-    for tag, use in (("fp32_plain", False), ("fp32_learned", True)):
-        ls.set_state(U0, 0.0)
-        (steps, rej), sec = _timed(lambda: ls.run_to(t_end, use))
-        rho = ls.state()[0].astype(np.float64)
-        out[tag] = {"n": nc, "seconds": sec, "steps": steps, "rejected_cells": rej,
-                    "l1_rho": float(np.abs(rho - ref).mean())}
+    ls.set_state(U0, 0.0)
+    (steps, _), sec = _timed(lambda: ls.run_to(t_end, False))
+    rho = ls.state()[0].astype(np.float64)
+    out["fp32_plain"] = {"n": nc, "seconds": sec, "steps": steps, "l1_rho": float(np.abs(rho - ref).mean())}
     ls.close()
+    return out, ref, U0
+
+
+def evaluate_learned(t_end: float, params, ref, U0, limiter: int = 0) -> dict:
+    """The learned FP32 coarse run from U0 to t_end: L1 density error against ref, wall time."""
+    nc = U0.shape[1]
+    ls = LearnedSolver(nc, 1.0 / nc, limiter=limiter)
+    ls.set_params(params)
+    ls.set_state(U0, 0.0)
+    (steps, rej), sec = _timed(lambda: ls.run_to(t_end, True))
+    rho = ls.state()[0].astype(np.float64)
+    ls.close()
+    return {"n": nc, "seconds": sec, "steps": steps, "rejected_cells": rej,
+            "l1_rho": float(np.abs(rho - ref).mean())}
+
+
+def evaluate(case_fn, n_fine: int, t_end: float, params, factor: int = 4, limiter: int = 0):
+    """evaluate_plain plus the learned run (key fp32_learned)."""
+    out, ref, U0 = evaluate_plain(case_fn, n_fine, t_end, factor, limiter)
+    out["fp32_learned"] = evaluate_learned(t_end, params, ref, U0, limiter)
     return out

@@ -19,7 +19,8 @@ import time
 import numpy as np
 
 from . import cases
-from .learned import LearnedSolver, evaluate, fine_pairs, init_params, one_step_loss, train
+from .learned import (LearnedSolver, change_weights, evaluate_learned, evaluate_plain, fine_sequence,
+                      init_params, one_step_loss, train, train_rollout)
 
 
 def sb_case(bubble, radius, t_end):
@@ -39,47 +40,66 @@ def main():
     ap.add_argument("--n-fine", type=int, default=2048)
     ap.add_argument("--iters", type=int, default=3000)
     ap.add_argument("--lr", type=float, default=2e-3)
-    ap.add_argument("--stride", type=int, default=8)
+    ap.add_argument("--stride", type=int, default=8, help="pairs mode: every stride-th window")
+    ap.add_argument("--modes", default="pairs,roll4",
+                    help="comma list of training modes: pairs (one-step pairs from the filtered "
+                         "fine runs) or rollK (one-step training on the solver's own states after "
+                         "up to K of its steps)")
     ap.add_argument("--out", default="learned_report.json")
     args = ap.parse_args()
     nf, f = args.n_fine, 4
     nc = nf // f
-    report = {"n_fine": nf, "n_coarse": nc}
+    report = {"n_fine": nf, "n_coarse": nc, "iters": args.iters, "lr": args.lr}
     t0 = time.perf_counter()
     train_sets = [("rp_seed_100", rp_case(100), None), ("rp_seed_101", rp_case(101), None),
                   ("bubble_a", sb_case((0.4, 0.5), 0.2, 1.0), 0.25),
                   ("bubble_b", sb_case((0.45, 0.45), 0.2, 1.0), 0.25)]
-    pairs = []
+    seqs = []
     for name, fn, t_end in train_sets:
         c = fn(nf)
         T = t_end if t_end is not None else c["simulation"]["t_end"]
-        pairs += fine_pairs(c, T, factor=f, stride=args.stride)
-        _log(f"fine data {name}: {len(pairs)} pairs", t0)
-    report["train_pairs"] = len(pairs)
+        seqs.append(fine_sequence(c, T, factor=f))
+        _log(f"fine data {name}: {len(seqs[-1][1])} windows", t0)
+    pairs = [(st[k], st[k + 1], dts[k]) for st, dts in seqs for k in range(len(dts))]
+    report["train_windows"] = len(pairs)
     report["data_seconds"] = time.perf_counter() - t0
-    held_pairs = fine_pairs(rp_case(200)(nf), rp_case(200)(nf)["simulation"]["t_end"], factor=f,
-                            stride=args.stride * 2)
-    held_pairs += fine_pairs(cases.shock_bubble_case(nf, bubble=(0.42, 0.55)), 0.2, factor=f,
-                             stride=args.stride * 2)
+    held = [fine_sequence(rp_case(200)(nf), rp_case(200)(nf)["simulation"]["t_end"], factor=f),
+            fine_sequence(cases.shock_bubble_case(nf, bubble=(0.42, 0.55)), 0.2, factor=f)]
+    held_pairs = [(st[k], st[k + 1], dts[k]) for st, dts in held for k in range(0, len(dts), 4)]
     _log(f"held-out data: {len(held_pairs)} pairs", t0)
-    ls = LearnedSolver(nc, 1.0 / nc)
-    ls.set_params(init_params(0))
-    t1 = time.perf_counter()
-    losses, w = train(ls, pairs, args.iters, lr=args.lr)
-    report["train_seconds"] = time.perf_counter() - t1
-    _log(f"trained {args.iters} iterations in {report['train_seconds']:.1f} s", t0)
-    report["train_loss_first100"] = float(losses[:100].mean())
-    report["train_loss_last100"] = float(losses[-100:].mean())
-    report["heldout_one_step_loss"] = {"plain": one_step_loss(ls, held_pairs, w, False),
-                                       "learned": one_step_loss(ls, held_pairs, w, True)}
-    params = ls.params()
-    ls.close()
-    np.save(args.out.replace(".json", "_params.npy"), params)
+    evals = {"rp_seed_200": (rp_case(200), rp_case(200)(nf)["simulation"]["t_end"]),
+             "bubble_heldout": (sb_case((0.42, 0.55), 0.2, 0.2), 0.2)}
     report["eval"] = {}
-    report["eval"]["rp_seed_200"] = evaluate(rp_case(200), nf, rp_case(200)(nf)["simulation"]["t_end"], params)
-    _log("evaluated rp_seed_200", t0)
-    report["eval"]["bubble_heldout"] = evaluate(sb_case((0.42, 0.55), 0.2, 0.2), nf, 0.2, params)
-    _log("evaluated bubble_heldout", t0)
+    base = {}
+    for name, (fn, t_end) in evals.items():
+        res, ref, U0 = evaluate_plain(fn, nf, t_end, factor=f)
+        report["eval"][name] = res
+        base[name] = (ref, U0, t_end)
+    _log("plain runs evaluated", t0)
+    w = change_weights(pairs)
+    report["models"] = {}
+    for mode in args.modes.split(","):
+        ls = LearnedSolver(nc, 1.0 / nc)
+        ls.set_params(init_params(0))
+        t1 = time.perf_counter()
+        if mode == "pairs":
+            sub = pairs[::args.stride]
+            losses, _ = train(ls, sub, args.iters, lr=args.lr, w=w)
+        elif mode.startswith("roll"):
+            losses, _ = train_rollout(ls, seqs, args.iters, lr=args.lr, max_roll=int(mode[4:]), w=w)
+        else:
+            raise SystemExit(f"unknown mode {mode}")
+        m = {"train_seconds": time.perf_counter() - t1,
+             "train_loss_first100": float(losses[:100].mean()),
+             "train_loss_last100": float(losses[-100:].mean()),
+             "heldout_one_step_loss": {"plain": one_step_loss(ls, held_pairs, w, False),
+                                       "learned": one_step_loss(ls, held_pairs, w, True)}}
+        params = ls.params()
+        ls.close()
+        np.save(args.out.replace(".json", f"_{mode}_params.npy"), params)
+        m["eval"] = {name: evaluate_learned(t_end, params, ref, U0) for name, (ref, U0, t_end) in base.items()}
+        report["models"][mode] = m
+        _log(f"model {mode}: " + ", ".join(f"{k} l1 {v['l1_rho']:.5f}" for k, v in m["eval"].items()), t0)
     with open(args.out, "w") as fh:
         json.dump(report, fh, indent=1)
     print(json.dumps(report))

@@ -183,6 +183,14 @@ class CartSolver:
             o += m
         return idx.value, t.value, blocks
 
+    def coarsen(self, b: int = 0, factor: int = 4) -> np.ndarray:
+        """factor x factor box average of block b's interior, FP32 [4][ny/f][nx/f], formed
+        on the device."""
+        d = self.block_dims(b)
+        out = np.empty((4, d["y_cells"] // factor, d["x_cells"] // factor), np.float32)
+        check(lib().hf_coarsen(self._h, b, factor, out.ctypes.data), self._h)
+        return out
+
     # --- checkpoint / restart ---
     def checkpoint(self) -> bytes:
         """The whole simulation state (both state buffers, ghosts, t, call count, frame

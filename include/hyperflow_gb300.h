@@ -128,6 +128,12 @@ int hf_frames_pending(hf_ctx* ctx, int64_t* n);
  * when none is pending */
 int hf_frame_pop(hf_ctx* ctx, double* cons, double* t, int64_t* index);
 
+/* factor x factor box average of block b's interior cells (FP64 sums) as FP32
+ * [4][ny/factor][nx/factor], written to out (host).  No counterpart in the reference: it makes
+ * the training data of the learned coarse solver from the solver's own fine runs without
+ * copying the fine state off the device.  nx and ny must be multiples of factor. */
+int hf_coarsen(hf_ctx* ctx, int block, int factor, float* out);
+
 /* Checkpoint / restart of the whole simulation state: both state buffers of every block
  * (ghosts included) and the control block (t, TimeStep call count, step parity, interior
  * wave-speed maxima, frame cadence).  No counterpart in the reference, whose only output is

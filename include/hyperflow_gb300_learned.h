@@ -49,7 +49,8 @@ int hf_lc_step(hf_lc* L, double dt, int use_mlp, int64_t* rejected_cells);
 /* steps with the CFL dt until t_end (dt clamped to reach it) */
 int hf_lc_run_to(hf_lc* L, double t_end, int use_mlp, int64_t* steps, int64_t* rejected_cells);
 
-/* one Adam iteration on the pair (U0 -> T over dt) with variable weights w[4]; loss written */
+/* one Adam iteration on the pair (U0 -> T over dt) with variable weights w[4]; loss written.
+ * U0 null trains from the solver's current state (e.g. after its own steps), which stays. */
 int hf_lc_train_step(hf_lc* L, const float* U0, const float* T, const float* w, double dt, double lr,
                      double* loss);
 

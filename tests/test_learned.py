@@ -141,3 +141,17 @@ def test_training_beats_the_plain_coarse_step():
     assert np.isfinite(losses).all()
     assert losses[-50:].mean() < losses[:50].mean()
     assert learned < 0.9 * plain, (learned, plain)
+
+
+@pytest.mark.gpu
+def test_coarsen_on_device_equals_box_filter():
+    """hf_coarsen (the training-data filter formed on the device) against the host box filter."""
+    from hyperflow_gb300 import CartSolver, cases
+    from hyperflow_gb300.learned import box_filter
+    s = CartSolver(cases.shock_bubble_case(128))
+    s.run(20)
+    g = s.block_dims(0)["ghost"]
+    want = box_filter(s.state(0)[:, g:-g, g:-g], 4)
+    got = s.coarsen(0, 4)
+    assert got.dtype == np.float32 and got.shape == (4, 32, 32)
+    np.testing.assert_allclose(got, want, rtol=2e-7, atol=0)
