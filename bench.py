@@ -162,6 +162,120 @@ def reference_arm(args, cells):
     }), flush=True)
 
 
+def timed_device(stream, fn):
+    """CUDA-event milliseconds of fn() on `stream` (synchronised on both sides)."""
+    import torch
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1)
+
+
+def bench_batch(args):
+    """The batched workload: 512 seeded four-quadrant Riemann problems (sides log-uniform in
+    64..1024), MUSCL-Hancock MinBee, per-instance dt, autotuned launch shape, the run of
+    `steps` steps in one persistent launch captured in a CUDA graph."""
+    import numpy as np  # noqa: F401
+    import torch
+    from hyperflow_gb300 import BatchSolver, cases
+    from oracle.oracle import Oracle, build_port
+    m = cases.batch_manifest(512, seed=0)
+    b = BatchSolver(m)
+    best, trial_ms = b.autotune(steps_per_trial=2)
+    stream = torch.cuda.ExternalStream(b.stream())
+    b.run(args.warmup, graph=True)
+    b.sync()
+    with Clocks(0) as clk:
+        ms = timed_device(stream, lambda: b.run(args.steps, graph=True))
+    b.sync()
+    cells = b.total_cells
+    value = cells * args.steps / (ms / 1e3) / 1e6
+    hbm, peak_kind = peaks()
+    achieved = BYTES_PER_CELL * cells * args.steps / (ms / 1e3) / 1e9
+    # CPU baseline: the oracle on all host cores over a bounded sample of the instances
+    build_port()
+    nth = os.cpu_count() or 1
+    sample = list(range(0, 512, 16))
+    sample_cells, t0 = 0, time.perf_counter()
+    for i in sample:
+        o = Oracle(m["cases"][i], nthreads=nth)
+        o.run(20)
+        sample_cells += 20 * m["cases"][i]["mesh"]["blocks"][0]["x_cells"] ** 2
+    cpu_s = time.perf_counter() - t0
+    print(json.dumps({
+        "metric": "Mcell-updates/s", "value": value, "unit": "Mcell-updates/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded four-quadrant Riemann problems)",
+        "config": {"workload": "batched_512_quadrant_riemann_sides_64_1024_muscl_hancock_minbee_hllc_fp64",
+                   "instances": 512, "cells": cells, "cfl": cases.CFL_2D, "autotuned_config": best,
+                   "autotune_trial_ms": [float(x) for x in trial_ms],
+                   "l2": "state 2 x %.0f MB > 129 MB L2, no flush needed" % (cells * 32 / 1e6)},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved / hbm, "traffic": None, "peak_kind": peak_kind,
+                     "kernel": "batch_mh_kernel (persistent, all instances, one launch per run)"},
+        "cpu_baseline": {"value": sample_cells / cpu_s / 1e6, "unit": "Mcell-updates/s", "cores": nth,
+                         "kind": "port", "sample": f"instances 0, 16, ..., 496 ({len(sample)}), 20 steps each"},
+        "e2e": None, "gpu_launches": 1, "clocks": clk.summary()}), flush=True)
+    b.close()
+
+
+def bench_uns(args):
+    """The unstructured workload: ~1M triangles of a jittered-lattice Delaunay mesh of
+    [0,4]x[0,2] minus a disc, Mach 2 inflow, CFL 0.5, Godunov + HLLC, edge-based fluxes,
+    `steps` steps in the device loop (CUDA graph)."""
+    import tempfile
+    import numpy as np
+    import torch
+    from hyperflow_gb300 import UnsSolver, meshgen
+    from oracle import oracle
+    V, codes = meshgen.jittered_hole_mesh(1_000_000, seed=0)
+    with tempfile.TemporaryDirectory() as d:
+        path = os.path.join(d, "channel.hmsh")
+        meshgen.write_hmsh(path, V, codes)
+        case = meshgen.channel_case(path, cfl=0.5)
+        s = UnsSolver(case)
+    s.set_edge_mode(not args.uns_per_side)
+    stream = torch.cuda.ExternalStream(s.stream())
+    s.run(args.warmup)
+    with Clocks(0) as clk:
+        ms = timed_device(stream, lambda: s.run(args.steps))
+    cells = s.ncells
+    m = s.mesh_arrays()
+    nedges = int((m["nbr"] >= 0).sum() // 2 + (m["nbr"] < 0).sum())
+    value = cells * args.steps / (ms / 1e3) / 1e6
+    hbm, peak_kind = peaks()
+    achieved = (64 * cells + 40 * nedges) * args.steps / (ms / 1e3) / 1e9
+    nth = os.cpu_count() or 1
+    U = np.zeros((4, cells))
+    U[:] = oracle.prim_to_cons(case["initial_condition"]["init_state"])[:, None]
+    inlet = oracle.prim_to_cons(case["mesh"]["boundaries"]["inlet"])
+    n_cpu = 20
+    t0 = time.perf_counter()
+    oracle.uns_run(1.4, 0.5, 0, m["pair_start"], m["nbr"], m["angle"], m["length"], m["area"], m["rin"],
+                   inlet, U, n_cpu, nthreads=nth)
+    cpu_s = time.perf_counter() - t0
+    print(json.dumps({
+        "metric": "Mcell-updates/s", "value": value, "unit": "Mcell-updates/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded jittered-lattice Delaunay mesh, uniform Mach 2 start)",
+        "config": {"workload": "unstructured_1M_triangles_hole_channel_godunov_hllc_fp64",
+                   "cells": cells, "unique_edges": nedges, "cfl": 0.5,
+                   "flux": "per (cell, edge) pair" if args.uns_per_side else "edge-based"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved / hbm, "traffic": None, "peak_kind": peak_kind,
+                     "kernel": "uns_step_kernel (+ uns_edge_flux_kernel)"},
+        "cpu_baseline": {"value": cells * n_cpu / cpu_s / 1e6, "unit": "Mcell-updates/s", "cores": nth,
+                         "kind": "port", "sample": f"first {n_cpu} steps, per-pair fluxes"},
+        "e2e": None, "gpu_launches": 4 * args.steps, "clocks": clk.summary()}), flush=True)
+    s.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -170,8 +284,11 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--limiter", default="MinBee", choices=["MinBee", "VanLeer"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="CPU-baseline sample budget")
-    ap.add_argument("--workload", default="ffs", choices=["ffs", "square"],
-                    help="ffs: the 3-block forward-facing step (default); square: one n x n block")
+    ap.add_argument("--workload", default="ffs", choices=["ffs", "square", "batch", "uns"],
+                    help="ffs: the 3-block forward-facing step (default); square: one n x n block; "
+                         "batch: 512 batched Riemann problems; uns: the 1M-triangle channel")
+    ap.add_argument("--uns-per-side", action="store_true",
+                    help="uns workload: per-(cell, edge) fluxes (bit-exact mode) instead of edge-based")
     ap.add_argument("--n", type=int, default=4096, help="side of the square workload")
     ap.add_argument("--scheme", default="MUSCLHancock", choices=["MUSCLHancock", "Godunov"],
                     help="scheme of the square workload")
@@ -179,6 +296,17 @@ def main():
                     help="device-resident timing only (no graph pass, e2e or CPU baseline)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+
+    if args.workload in ("batch", "uns"):
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable":
+                              "the reference arm is timed on the forward-facing step and square workloads"}))
+            return
+        import numpy as np  # noqa: F401
+        import torch
+        torch.cuda.set_device(0)
+        (bench_batch if args.workload == "batch" else bench_uns)(args)
+        return
 
     from hyperflow_gb300 import cases
     case = make_case(args.limiter, args.workload, args.n, args.scheme)

@@ -41,7 +41,8 @@ struct Prim {
 HF_HD Prim to_prim(double g1, double r, double ru, double rv, double E) {
     Prim w;
     w.r = r;
-    div2_rn(ru, rv, r, w.u, w.v);
+    w.u = div_rn(ru, r);
+    w.v = div_rn(rv, r);
     w.q = w.u * w.u + w.v * w.v;
     w.p = g1 * (E - half(r) * w.q);
     double e = div_rn(w.p, w.r * g1);      // prim_internal_energy (32-36)
@@ -52,7 +53,8 @@ HF_HD Prim to_prim(double g1, double r, double ru, double rv, double E) {
 // only the primitives (no energy): what TimeStep needs
 HF_HD void to_prim_short(double g1, double r, double ru, double rv, double E,
                                               double& u, double& v, double& p) {
-    div2_rn(ru, rv, r, u, v);
+    u = div_rn(ru, r);
+    v = div_rn(rv, r);
     p = g1 * (E - half(r) * (u * u + v * v));
 }
 

@@ -12,10 +12,6 @@ void hm_div(const double* a, const double* b, double* out, int64_t n) {
     for (int64_t i = 0; i < n; ++i) out[i] = hf::div_rn(a[i], b[i]);
 }
 
-void hm_div2(const double* a1, const double* a2, const double* b, double* q1, double* q2, int64_t n) {
-    for (int64_t i = 0; i < n; ++i) hf::div2_rn(a1[i], a2[i], b[i], q1[i], q2[i]);
-}
-
 void hm_half(const double* x, double* out, int64_t n) {
     for (int64_t i = 0; i < n; ++i) out[i] = hf::half(x[i]);
 }

@@ -201,18 +201,6 @@ HF_HD double div_rn(double a, double b) {
     return quot_fast(A, B, X);
 }
 
-// a1 / b and a2 / b with one shared reciprocal; each result equals the IEEE quotient
-HF_HD void div2_rn(double a1, double a2, double b, double& q1, double& q2) {
-    const uint64_t A1 = f64_bits(a1), A2 = f64_bits(a2), B = f64_bits(b);
-    const uint64_t M52 = 0x000FFFFFFFFFFFFFull, H52 = 0x0010000000000000ull;
-    const bool f1 = div_fast(A1, B), f2 = div_fast(A2, B);
-    uint64_t X = 0ull;
-    if ((f1 || f2) && (B & M52) != 0) X = recip_fixed((B & M52) | H52);
-    const uint64_t S = B & 0x8000000000000000ull;
-    q1 = !f1 ? hw_div(a1, b) : ((A1 << 1) == 0 ? f64_from((A1 & 0x8000000000000000ull) ^ S) : quot_fast(A1, B, X));
-    q2 = !f2 ? hw_div(a2, b) : ((A2 << 1) == 0 ? f64_from((A2 & 0x8000000000000000ull) ^ S) : quot_fast(A2, B, X));
-}
-
 }  // namespace hf
 
 namespace hf {

@@ -23,7 +23,6 @@ def hm():
     L.hm_div.argtypes = [p, p, p, i64]
     L.hm_sqrt.argtypes = [p, p, i64]
     L.hm_half.argtypes = [p, p, i64]
-    L.hm_div2.argtypes = [p, p, p, p, p, i64]
     L.hm_hllc.argtypes = [d, p, p, i, p]
     L.hm_hllc.restype = i
     L.hm_limiter.argtypes = [i, d]
@@ -158,17 +157,3 @@ def test_half_equals_multiplication(hm):
     same = (out.view(np.uint64) == want.view(np.uint64)) | (np.isnan(out) & np.isnan(want))
     assert same.all(), x[~same][:5]
 
-
-def test_shared_divisor_division_equals_ieee(hm):
-    rng = np.random.default_rng(6)
-    a, b = _operands(rng, 600_000)
-    a2 = np.roll(a, 7)
-    a2[:50] = 0.0
-    a2[50:100] = -0.0
-    q1, q2 = np.empty_like(a), np.empty_like(a)
-    hm.hm_div2(a.ctypes.data, a2.ctypes.data, b.ctypes.data, q1.ctypes.data, q2.ctypes.data, a.size)
-    with np.errstate(all="ignore"):
-        w1, w2 = a / b, a2 / b
-    for got, want in ((q1, w1), (q2, w2)):
-        same = (got.view(np.uint64) == want.view(np.uint64)) | (np.isnan(got) & np.isnan(want))
-        assert same.all()

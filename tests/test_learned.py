@@ -154,4 +154,4 @@ def test_coarsen_on_device_equals_box_filter():
     want = box_filter(s.state(0)[:, g:-g, g:-g], 4)
     got = s.coarsen(0, 4)
     assert got.dtype == np.float32 and got.shape == (4, 32, 32)
-    np.testing.assert_allclose(got, want, rtol=2e-7, atol=0)
+    np.testing.assert_allclose(got, want, rtol=2e-7, atol=1e-12)
