@@ -274,7 +274,7 @@ struct BatchConfig {
     int tx, ty, threads, stages;
 };
 
-constexpr BatchConfig kConfigs[] = {{32, 16, 256, 1}, {32, 16, 256, 2}, {32, 8, 128, 2}, {64, 8, 256, 2}};
+constexpr BatchConfig kConfigs[] = {{32, 14, 256, 1}, {32, 14, 256, 2}, {32, 16, 256, 1}, {32, 16, 256, 2}};
 constexpr int kNumConfigs = 4;
 
 template <int TX, int TY, int NT, int ST>
@@ -314,10 +314,10 @@ cudaError_t launch_batch(const BatchDev& d, int nsteps, int sms, cudaStream_t s,
 
 cudaError_t launch_batch_config(int k, const BatchDev& d, int nsteps, int sms, cudaStream_t s, bool cfl_only) {
     switch (k) {
-        case 0: return launch_batch<32, 16, 256, 1>(d, nsteps, sms, s, cfl_only);
-        case 1: return launch_batch<32, 16, 256, 2>(d, nsteps, sms, s, cfl_only);
-        case 2: return launch_batch<32, 8, 128, 2>(d, nsteps, sms, s, cfl_only);
-        default: return launch_batch<64, 8, 256, 2>(d, nsteps, sms, s, cfl_only);
+        case 0: return launch_batch<32, 14, 256, 1>(d, nsteps, sms, s, cfl_only);
+        case 1: return launch_batch<32, 14, 256, 2>(d, nsteps, sms, s, cfl_only);
+        case 2: return launch_batch<32, 16, 256, 1>(d, nsteps, sms, s, cfl_only);
+        default: return launch_batch<32, 16, 256, 2>(d, nsteps, sms, s, cfl_only);
     }
 }
 

@@ -67,22 +67,46 @@ HF_HD uint64_t umulhi64(uint64_t a, uint64_t b) {
     return (uint64_t)(((unsigned __int128)a * b) >> 64);
 #endif
 }
-// FP32 seeds: a correctly rounded reciprocal and an approximate reciprocal square root
+HF_HD float f32_from(uint32_t u) {
+#ifdef __CUDA_ARCH__
+    return __uint_as_float(u);
+#else
+    float x;
+    std::memcpy(&x, &u, 4);
+    return x;
+#endif
+}
+// FP32 seeds of the Newton iterations: approximate reciprocal and reciprocal square root
+// (one special-function instruction each on the device).  The iterations converge from any
+// seed within a few ulp, so the host build perturbs the exact value by up to +-4 ulp to
+// exercise that margin.
 HF_HD float rcp_f32(float x) {
 #ifdef __CUDA_ARCH__
-    return __frcp_rn(x);
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
 #else
     volatile float one = 1.0f;
-    return one / x;
+    const uint32_t b = f32_bits(one / x);
+    return f32_from(b + ((b * 2654435761u) >> 29) - 4u);
 #endif
 }
 HF_HD float rsqrt_f32(float x) {
 #ifdef __CUDA_ARCH__
-    return rsqrtf(x);
+    float r;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
 #else
     volatile float one = 1.0f;
-    return one / std::sqrt(x);
+    const uint32_t b = f32_bits(one / std::sqrt(x));
+    return f32_from(b + ((b * 2654435761u) >> 29) - 4u);
 #endif
+}
+// an integer in [2^23, 2^24) as an FP32 value, from its bits (no conversion instruction)
+HF_HD float u24_float(uint32_t m) { return f32_from(0x4B000000u | (m & 0x7FFFFFu)); }
+// an integer in [2^22, 2^24) as an FP32 value
+HF_HD float u22_24_float(uint32_t m) {
+    return (m >> 23) ? f32_from(0x4B000000u | (m & 0x7FFFFFu)) : f32_from(0x4A800000u | ((m << 1) & 0x7FFFFFu));
 }
 // IEEE comparisons on the integer pipes (NaN compares false, -0 equals +0).  A double's
 // sign-magnitude bits map to an order-preserving signed key: key = sign ? -|x| : |x|.
@@ -128,7 +152,7 @@ HF_HD double hw_sqrt(double x) { return std::sqrt(x); }
 HF_HD uint64_t recip_fixed(uint64_t mb) {
     // FP32 seed: X0 = 2^87 / dh with dh = mb >> 29 in [2^23, 2^24)
     const uint32_t dh = (uint32_t)(mb >> 29);
-    const float r = rcp_f32((float)dh);
+    const float r = rcp_f32(u24_float(dh));
     const uint32_t rb = f32_bits(r);
     const uint64_t mr = (uint64_t)((rb & 0x7FFFFFu) | 0x800000u);
     const int sh = (int)((rb >> 23) & 0xFFu) - 63;   // r = mr 2^(E-150); X0 = mr 2^(E-63)
@@ -225,7 +249,7 @@ HF_HD double sqrt_rn(double x) {
         S = H52;                                   // x is an even power of two
     } else {
         const uint32_t mh = (uint32_t)(m >> 30);   // [2^22, 2^24), exact in FP32
-        const float rs = rsqrt_f32((float)mh);
+        const float rs = rsqrt_f32(u22_24_float(mh));
         const uint32_t rb = f32_bits(rs);
         const uint64_t mr = (uint64_t)((rb & 0x7FFFFFu) | 0x800000u);
         const int sh = (int)((rb >> 23) & 0xFFu) - 75;        // Y0 = 2^75 rs = mr 2^(E_r - 75)

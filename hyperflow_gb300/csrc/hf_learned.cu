@@ -214,95 +214,208 @@ __global__ void features_kernel(const float* __restrict__ U, Grid G, __nv_bfloat
 }
 
 // ---------------------------------------------------------------------------------
-// MLP forward on the tensor cores: mma.sync m16n8k16 BF16 x BF16 -> FP32
+// MLP forward on the 5th-generation tensor cores: tcgen05.mma, BF16 x BF16 -> FP32 in TMEM
 // ---------------------------------------------------------------------------------
-__device__ __forceinline__ void mma_bf16(float* c, const uint32_t* a, uint32_t b0, uint32_t b1) {
-    asm volatile(
-        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
-        "{%8,%9}, {%0,%1,%2,%3};"
-        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
-        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+// A CTA of 128 threads takes 128 faces per tile, one face per thread and per TMEM lane.
+// Operands sit in shared memory in the canonical K-major layout without swizzle: 8 x 8 BF16
+// core matrices of 128 contiguous bytes, core matrices adjacent along K 128 B apart (the
+// descriptor's leading-dimension offset), 8-row groups 1024 B apart (its stride offset).
+// Each layer is 4 MMAs of K = 16 issued by one thread and committed to an mbarrier; the
+// 64 FP32 accumulator columns are read back with tcgen05.ld, biased, passed through GELU,
+// rounded to BF16 and stored as the next layer's A operand.  The output layer runs with
+// N = 16 (rows 4..15 of its weight tile are zero).
+constexpr int kTcRows = 128;       // faces per tile = threads per CTA = TMEM lanes
+constexpr int kTcCols = 64;        // TMEM columns held by a CTA (one layer's accumulator)
+constexpr uint32_t kTcWaitLimit = 1u << 22;
+
+__device__ __forceinline__ uint32_t canon_off(int r, int k) {   // bytes; K = 64 BF16 per row
+    return (uint32_t)((r >> 3) * 1024 + (k >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2);
 }
+// shared-memory matrix descriptor: start >> 4, leading offset 128 B, stride offset 1024 B,
+// descriptor version 1, no swizzle
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr) {
+    return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)(128u >> 4) << 16) |
+           ((uint64_t)(1024u >> 4) << 32) | (1ull << 46);
+}
+// kind::f16 instruction descriptor: D FP32, A and B BF16, both K-major, M = 128, N = n
+__host__ __device__ constexpr uint32_t idesc_bf16(int n) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(kTcRows >> 4) << 24);
+}
+__device__ __forceinline__ void tc_mma(uint32_t dtmem, uint64_t a, uint64_t b, uint32_t idesc, int acc) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(dtmem),
+        "l"(a), "l"(b), "r"(idesc), "r"(acc)
+        : "memory");
+}
+__device__ __forceinline__ void tc_commit(uint64_t* bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                     smem_u32(bar))
+                 : "memory");
+}
+__device__ __forceinline__ void tc_before_sync() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_after_sync() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void async_smem_fence() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// 16 consecutive accumulator columns of this thread's TMEM lane; the wait is tied to the
+// registers so no use of them moves above it
+__device__ __forceinline__ void tc_ld16(uint32_t taddr, float* v) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;"
+                 : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]),
+                   "+r"(r[7]), "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]), "+r"(r[12]), "+r"(r[13]),
+                   "+r"(r[14]), "+r"(r[15])
+                 :
+                 : "memory");
+#pragma unroll
+    for (int k = 0; k < 16; ++k) v[k] = __uint_as_float(r[k]);
+}
+
 __device__ __forceinline__ uint32_t pack2(float lo, float hi) {
     __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
     return *reinterpret_cast<uint32_t*>(&v);
 }
 
-constexpr int kMlpWarps = 8;
+// 8 BF16 values into row r, columns k0..k0+7, of a canonical operand tile
+__device__ __forceinline__ void put8(unsigned char* tile, int r, int k0, const float* h) {
+    uint4 q;
+    q.x = pack2(h[0], h[1]);
+    q.y = pack2(h[2], h[3]);
+    q.z = pack2(h[4], h[5]);
+    q.w = pack2(h[6], h[7]);
+    *reinterpret_cast<uint4*>(tile + canon_off(r, k0)) = q;
+}
+
+struct __align__(1024) TcSmem {
+    unsigned char a[kTcRows * 64 * 2];     // activations of the tile (A operand)
+    unsigned char w1[64 * 64 * 2], w2[64 * 64 * 2], w3[16 * 64 * 2];
+    float b1[64], b2[64], b3[4];
+    uint64_t bar;
+    uint32_t taddr;
+};
 
 // Y[nf][4] = MLP(X).  When Z1/Z2 are given (training), the hidden pre-activations are saved.
-__global__ void __launch_bounds__(kMlpWarps * 32)
+// A bounded wait that gives up sets *err, waits (bounded) for the CTA's MMAs in flight,
+// frees the TMEM columns and returns.
+__global__ void __launch_bounds__(kTcRows)
 mlp_forward_kernel(const __nv_bfloat16* __restrict__ X, int nf, const __nv_bfloat16* __restrict__ Wb,
                    const float* __restrict__ P, float* __restrict__ Y, float* __restrict__ Z1,
-                   float* __restrict__ Z2) {
-    __shared__ __align__(16) __nv_bfloat16 sW1[H * NIN], sW2[H * H], sW3[8 * H];
-    __shared__ float sb1[H], sb2[H], sb3[8];
-    for (int k = threadIdx.x; k < H * NIN; k += blockDim.x) { sW1[k] = Wb[k]; sW2[k] = Wb[H * NIN + k]; }
-    for (int k = threadIdx.x; k < 8 * H; k += blockDim.x)
-        sW3[k] = k < NOUT * H ? Wb[H * NIN + H * H + k] : __float2bfloat16_rn(0.0f);
-    for (int k = threadIdx.x; k < H; k += blockDim.x) { sb1[k] = P[OFF_B1 + k]; sb2[k] = P[OFF_B2 + k]; }
-    if (threadIdx.x < 8) sb3[threadIdx.x] = threadIdx.x < NOUT ? P[OFF_B3 + threadIdx.x] : 0.0f;
+                   float* __restrict__ Z2, int* __restrict__ err) {
+    extern __shared__ unsigned char smem_raw[];
+    TcSmem& S = *reinterpret_cast<TcSmem*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    const int tid = threadIdx.x, warp = tid >> 5;
+    // weights into the canonical layout (W3 padded to 16 rows), biases
+    for (int c = tid; c < 64 * 8; c += kTcRows) {
+        const int n = c >> 3, kb = c & 7;
+        *reinterpret_cast<uint4*>(S.w1 + canon_off(n, kb * 8)) =
+            *reinterpret_cast<const uint4*>(Wb + (size_t)n * NIN + kb * 8);
+        *reinterpret_cast<uint4*>(S.w2 + canon_off(n, kb * 8)) =
+            *reinterpret_cast<const uint4*>(Wb + H * NIN + (size_t)n * H + kb * 8);
+    }
+    for (int c = tid; c < 16 * 8; c += kTcRows) {
+        const int n = c >> 3, kb = c & 7;
+        uint4 q = make_uint4(0u, 0u, 0u, 0u);
+        if (n < NOUT) q = *reinterpret_cast<const uint4*>(Wb + H * NIN + H * H + (size_t)n * H + kb * 8);
+        *reinterpret_cast<uint4*>(S.w3 + canon_off(n, kb * 8)) = q;
+    }
+    for (int k = tid; k < H; k += kTcRows) { S.b1[k] = P[OFF_B1 + k]; S.b2[k] = P[OFF_B2 + k]; }
+    if (tid < NOUT) S.b3[tid] = P[OFF_B3 + tid];
+    if (tid == 0) mbar_init(&S.bar, 1);
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&S.taddr)),
+                     "r"(kTcCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    async_smem_fence();
+    tc_before_sync();
     __syncthreads();
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int g = lane >> 2, t = lane & 3;
-    for (int base = (blockIdx.x * kMlpWarps + w) * 16; base < nf; base += gridDim.x * kMlpWarps * 16) {
-        const int r0 = base + g, r1 = base + g + 8;
-        const bool v0 = r0 < nf, v1 = r1 < nf;
-        uint32_t a[4][4];
-        const uint32_t* x0 = reinterpret_cast<const uint32_t*>(X + (size_t)r0 * NIN);
-        const uint32_t* x1 = reinterpret_cast<const uint32_t*>(X + (size_t)r1 * NIN);
+    tc_after_sync();
+    const uint32_t tm = S.taddr;
+    const uint32_t tm_row = tm + ((uint32_t)(warp * 32) << 16);   // this warp's lane quarter
+    const uint32_t sa = smem_u32(S.a), sw1 = smem_u32(S.w1), sw2 = smem_u32(S.w2), sw3 = smem_u32(S.w3);
+    uint32_t phase = 0;
+    bool failed = false;
+
+    for (int base = blockIdx.x * kTcRows; base < nf && !failed; base += gridDim.x * kTcRows) {
+        const int face = base + tid;
+        const bool valid = face < nf;
+        // features -> A
+        {
+            const uint4* x = reinterpret_cast<const uint4*>(X + (size_t)(valid ? face : 0) * NIN);
 #pragma unroll
-        for (int kt = 0; kt < 4; ++kt) {
-            a[kt][0] = v0 ? x0[kt * 8 + t] : 0u;
-            a[kt][1] = v1 ? x1[kt * 8 + t] : 0u;
-            a[kt][2] = v0 ? x0[kt * 8 + 4 + t] : 0u;
-            a[kt][3] = v1 ? x1[kt * 8 + 4 + t] : 0u;
+            for (int kb = 0; kb < 8; ++kb)
+                *reinterpret_cast<uint4*>(S.a + canon_off(tid, kb * 8)) = valid ? x[kb] : make_uint4(0u, 0u, 0u, 0u);
         }
-        // two hidden layers
+#pragma unroll 1
+        for (int layer = 0; layer < 3; ++layer) {
+            async_smem_fence();
+            tc_before_sync();
+            __syncthreads();
+            if (tid == 0) {
+                tc_after_sync();
+                const uint32_t wb = layer == 0 ? sw1 : (layer == 1 ? sw2 : sw3);
+                const uint32_t id = idesc_bf16(layer == 2 ? 16 : 64);
 #pragma unroll
-        for (int layer = 0; layer < 2; ++layer) {
-            const __nv_bfloat16* sW = layer == 0 ? sW1 : sW2;
-            const float* sb = layer == 0 ? sb1 : sb2;
-            float* Zs = layer == 0 ? Z1 : Z2;
-            float c[8][4];
-#pragma unroll
-            for (int nt = 0; nt < 8; ++nt) {
-                c[nt][0] = c[nt][1] = c[nt][2] = c[nt][3] = 0.0f;
-                const uint32_t* wrow = reinterpret_cast<const uint32_t*>(sW + (nt * 8 + g) * 64);
-#pragma unroll
-                for (int kt = 0; kt < 4; ++kt) mma_bf16(c[nt], a[kt], wrow[kt * 8 + t], wrow[kt * 8 + 4 + t]);
+                for (int kk = 0; kk < 4; ++kk)
+                    tc_mma(tm, smem_desc(sa + kk * 256), smem_desc(wb + kk * 256), id, kk);
+                tc_commit(&S.bar);
             }
-            float h[8][4];
-#pragma unroll
-            for (int nt = 0; nt < 8; ++nt) {
-                const int col = nt * 8 + 2 * t;
-                const float z0 = c[nt][0] + sb[col], z1 = c[nt][1] + sb[col + 1];
-                const float z2 = c[nt][2] + sb[col], z3 = c[nt][3] + sb[col + 1];
-                if (Zs) {
-                    if (v0) { Zs[(size_t)r0 * H + col] = z0; Zs[(size_t)r0 * H + col + 1] = z1; }
-                    if (v1) { Zs[(size_t)r1 * H + col] = z2; Zs[(size_t)r1 * H + col + 1] = z3; }
+            const bool ok = mbar_wait_bounded(&S.bar, phase, kTcWaitLimit);
+            phase ^= 1u;
+            if (__syncthreads_or(!ok)) {
+                if (tid == 0) {
+                    atomicExch(err, 1);
+                    mbar_wait_bounded(&S.bar, phase ^ 1u, kTcWaitLimit);   // let the MMAs land
                 }
-                h[nt][0] = gelu(z0); h[nt][1] = gelu(z1); h[nt][2] = gelu(z2); h[nt][3] = gelu(z3);
+                failed = true;
+                break;
             }
+            tc_after_sync();
+            if (layer < 2) {
+                const float* b = layer == 0 ? S.b1 : S.b2;
+                float* Zs = layer == 0 ? Z1 : Z2;
+#pragma unroll 1
+                for (int q = 0; q < 4; ++q) {
+                    float z[16];
+                    tc_ld16(tm_row + q * 16, z);
+                    float h[16];
 #pragma unroll
-            for (int kt = 0; kt < 4; ++kt) {
-                a[kt][0] = pack2(h[2 * kt][0], h[2 * kt][1]);
-                a[kt][1] = pack2(h[2 * kt][2], h[2 * kt][3]);
-                a[kt][2] = pack2(h[2 * kt + 1][0], h[2 * kt + 1][1]);
-                a[kt][3] = pack2(h[2 * kt + 1][2], h[2 * kt + 1][3]);
+                    for (int k = 0; k < 16; ++k) {
+                        z[k] += b[q * 16 + k];
+                        h[k] = gelu(z[k]);
+                    }
+                    if (Zs && valid) {
+                        float4* zo = reinterpret_cast<float4*>(Zs + (size_t)face * H + q * 16);
+#pragma unroll
+                        for (int k = 0; k < 4; ++k) zo[k] = make_float4(z[4 * k], z[4 * k + 1], z[4 * k + 2], z[4 * k + 3]);
+                    }
+                    put8(S.a, tid, q * 16, h);
+                    put8(S.a, tid, q * 16 + 8, h + 8);
+                }
+            } else {
+                float y[16];
+                tc_ld16(tm_row, y);
+                if (valid)
+                    *reinterpret_cast<float4*>(Y + (size_t)face * 4) =
+                        make_float4(y[0] + S.b3[0], y[1] + S.b3[1], y[2] + S.b3[2], y[3] + S.b3[3]);
             }
-        }
-        float c[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-        const uint32_t* wrow = reinterpret_cast<const uint32_t*>(sW3 + g * 64);
-#pragma unroll
-        for (int kt = 0; kt < 4; ++kt) mma_bf16(c, a[kt], wrow[kt * 8 + t], wrow[kt * 8 + 4 + t]);
-        if (t < 2) {
-            const int col = 2 * t;
-            if (v0) { Y[(size_t)r0 * 4 + col] = c[0] + sb3[col]; Y[(size_t)r0 * 4 + col + 1] = c[1] + sb3[col + 1]; }
-            if (v1) { Y[(size_t)r1 * 4 + col] = c[2] + sb3[col]; Y[(size_t)r1 * 4 + col + 1] = c[3] + sb3[col + 1]; }
         }
     }
+    tc_before_sync();
+    __syncthreads();
+    if (warp == 0) {
+        tc_after_sync();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tm), "r"(kTcCols) : "memory");
+    }
 }
+
+size_t mlp_forward_smem() { return sizeof(TcSmem) + 1024; }
 
 // ---------------------------------------------------------------------------------
 // MLP backward (FP32 on the CUDA cores, the forward's BF16 weights and activations)
@@ -565,6 +678,7 @@ struct hf_lc {
     unsigned char* ok = nullptr;
     unsigned long long* rejected = nullptr;
     double* loss = nullptr;
+    int* derr = nullptr;       // device error word (a bounded wait gave up)
     int cur = 0;
     long long steps = 0;       // steps since time 0 (TimeStep's start-up multiplier)
     long long adam_t = 0;
@@ -607,6 +721,21 @@ hf::lc::Grid grid(const hf_lc* L) {
 int nfaces(const hf_lc* L) { return 2 * (L->n + 1) * L->n; }
 int blocks_for(long long n, int t) { long long b = (n + t - 1) / t; return (int)(b > 4096 ? 4096 : (b < 1 ? 1 : b)); }
 
+void launch_forward(hf_lc* L, int nf, bool save_acts) {
+    const int tiles = (nf + hf::lc::kTcRows - 1) / hf::lc::kTcRows;
+    const int grid = tiles < 4 * 152 ? tiles : 4 * 152;
+    hf::lc::mlp_forward_kernel<<<grid, hf::lc::kTcRows, hf::lc::mlp_forward_smem(), L->stream>>>(
+        L->X, nf, L->Wb, L->P, L->Y, save_acts ? L->Z1 : nullptr, save_acts ? L->Z2 : nullptr, L->derr);
+}
+
+// the device error word: a bounded wait in a kernel gave up
+int check_derr(hf_lc* L) {
+    int e = 0;
+    LCK(cudaMemcpy(&e, L->derr, sizeof e, cudaMemcpyDeviceToHost));
+    if (e) return lfail(L, HF_ERR_DEVICE, "a bounded device wait gave up (tensor-core MLP)");
+    return HF_OK;
+}
+
 // plain fluxes, and (use_mlp) features -> MLP -> corrections for state U[cur]
 int fluxes(hf_lc* L, float dt, bool use_mlp, bool save_acts) {
     hf::lc::Grid G = grid(L);
@@ -614,8 +743,7 @@ int fluxes(hf_lc* L, float dt, bool use_mlp, bool save_acts) {
     plain_flux_kernel<<<blocks_for(nf, 256), 256, 0, L->stream>>>(L->U[L->cur], G, dt, L->F);
     if (use_mlp) {
         features_kernel<<<blocks_for(nf, 256), 256, 0, L->stream>>>(L->U[L->cur], G, L->X, L->scale);
-        mlp_forward_kernel<<<blocks_for(nf, kMlpWarps * 16), kMlpWarps * 32, 0, L->stream>>>(
-            L->X, nf, L->Wb, L->P, L->Y, save_acts ? L->Z1 : nullptr, save_acts ? L->Z2 : nullptr);
+        launch_forward(L, nf, save_acts);
         correction_kernel<<<blocks_for(nf, 256), 256, 0, L->stream>>>(L->Y, L->scale, L->n, L->dF);
     }
     LCK(cudaGetLastError());
@@ -649,7 +777,7 @@ int hf_lc_create(int n, double dx, double gamma, double cfl, int limiter, hf_lc*
         (r = alloc(L, &L->Wb, (size_t)(H * NIN + H * H + NOUT * H))) || (r = alloc(L, &L->P, (size_t)NPARAM)) ||
         (r = alloc(L, &L->grad, (size_t)NPARAM)) || (r = alloc(L, &L->m1, (size_t)NPARAM)) ||
         (r = alloc(L, &L->m2, (size_t)NPARAM)) || (r = alloc(L, &L->maxs, 4)) || (r = alloc(L, &L->ok, nf)) ||
-        (r = alloc(L, &L->rejected, 1)) || (r = alloc(L, &L->loss, 1)))
+        (r = alloc(L, &L->rejected, 1)) || (r = alloc(L, &L->loss, 1)) || (r = alloc(L, &L->derr, 1)))
         return r;
     return HF_OK;
 }
@@ -738,6 +866,7 @@ int hf_lc_step(hf_lc* L, double dt, int use_mlp, int64_t* rejected_cells) {
         if (use_mlp) LCK(cudaMemcpyAsync(&v, L->rejected, 8, cudaMemcpyDeviceToHost, L->stream));
         LCK(cudaStreamSynchronize(L->stream));
         *rejected_cells = (int64_t)v;
+        if (use_mlp) return check_derr(L);
     }
     return HF_OK;
 }
@@ -765,7 +894,7 @@ int hf_lc_run_to(hf_lc* L, double t_end, int use_mlp, int64_t* steps, int64_t* r
     LCK(cudaStreamSynchronize(L->stream));
     if (steps) *steps = k;
     if (rejected_cells) *rejected_cells = rej;
-    return HF_OK;
+    return check_derr(L);
 }
 
 int hf_lc_set_time(hf_lc* L, double t) {
@@ -810,26 +939,24 @@ int hf_lc_train_step(hf_lc* L, const float* U0, const float* T, const float* w, 
         LCK(cudaMemcpyAsync(loss, L->loss, 8, cudaMemcpyDeviceToHost, L->stream));
     }
     LCK(cudaStreamSynchronize(L->stream));
-    return HF_OK;
+    return check_derr(L);
 }
 
 // ---- test entry points: the MLP alone on given inputs ----
 int hf_lc_mlp_forward(hf_lc* L, const uint16_t* x_bf16, int nf, float* y) {
     if (!L || !x_bf16 || !y || nf < 1 || nf > nfaces(L)) return HF_ERR_ARG;
     LCK(cudaMemcpy(L->X, x_bf16, (size_t)nf * NIN * 2, cudaMemcpyHostToDevice));
-    mlp_forward_kernel<<<blocks_for(nf, kMlpWarps * 16), kMlpWarps * 32, 0, L->stream>>>(L->X, nf, L->Wb, L->P, L->Y,
-                                                                                         L->Z1, L->Z2);
+    launch_forward(L, nf, true);
     LCK(cudaGetLastError());
     LCK(cudaStreamSynchronize(L->stream));
     LCK(cudaMemcpy(y, L->Y, (size_t)nf * 4 * sizeof(float), cudaMemcpyDeviceToHost));
-    return HF_OK;
+    return check_derr(L);
 }
 
 int hf_lc_mlp_backward(hf_lc* L, const uint16_t* x_bf16, const float* dy, int nf, float* grad) {
     if (!L || !x_bf16 || !dy || !grad || nf < 1 || nf > nfaces(L)) return HF_ERR_ARG;
     LCK(cudaMemcpy(L->X, x_bf16, (size_t)nf * NIN * 2, cudaMemcpyHostToDevice));
-    mlp_forward_kernel<<<blocks_for(nf, kMlpWarps * 16), kMlpWarps * 32, 0, L->stream>>>(L->X, nf, L->Wb, L->P, L->Y,
-                                                                                         L->Z1, L->Z2);
+    launch_forward(L, nf, true);
     LCK(cudaMemcpyAsync(L->dY, dy, (size_t)nf * 4 * sizeof(float), cudaMemcpyHostToDevice, L->stream));
     LCK(cudaMemsetAsync(L->grad, 0, NPARAM * sizeof(float), L->stream));
     mlp_backward_kernel<<<blocks_for(nf, kBwdFaces) > 1024 ? 1024 : blocks_for(nf, kBwdFaces), 256, 0, L->stream>>>(
@@ -837,7 +964,7 @@ int hf_lc_mlp_backward(hf_lc* L, const uint16_t* x_bf16, const float* dy, int nf
     LCK(cudaGetLastError());
     LCK(cudaStreamSynchronize(L->stream));
     LCK(cudaMemcpy(grad, L->grad, NPARAM * sizeof(float), cudaMemcpyDeviceToHost));
-    return HF_OK;
+    return check_derr(L);
 }
 
 int hf_lc_stream(hf_lc* L, void** s) { if (!L || !s) return HF_ERR_ARG; *s = (void*)L->stream; return HF_OK; }
