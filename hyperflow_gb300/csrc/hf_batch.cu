@@ -148,7 +148,7 @@ __global__ void __launch_bounds__(NT) batch_mh_kernel(BatchDev d, int nsteps) {
     double* sA = smem + STAGES * T::U_SIZE;
     double* sF = sA + T::A_SIZE;
     double* sG = sF + T::F_SIZE;
-    __shared__ double sdt[2];
+    __shared__ double sdt[5];
 
     BatchCtrl* c = d.ctrl;
     const long long step0 = c->step, calls0 = c->calls;
@@ -194,13 +194,15 @@ __global__ void __launch_bounds__(NT) batch_mh_kernel(BatchDev d, int nsteps) {
                 const unsigned long long* a = d.acc + ((size_t)ar * ninst + inst) * 2;
                 const double dtx = smin(1e16, I.dx / bitsd(a[0]));
                 const double dty = smin(1e16, I.dy / bitsd(a[1]));
+                const double dtp = m1 * smin(dtx, dty);
                 sdt[0] = m0 * smin(dtx, dty);
-                sdt[1] = m1 * smin(dtx, dty);
+                sdt[1] = 0.5 * dtp / I.dx;   // muscl_hancock.cpp:248-249
+                sdt[2] = 0.5 * dtp / I.dy;
+                sdt[3] = 1.0 / I.dx;         // 352-353
+                sdt[4] = 1.0 / I.dy;
             }
             __syncthreads();
-            const double dt = sdt[0], dtp = sdt[1];
-            const double hdx = 0.5 * dtp / I.dx, hdy = 0.5 * dtp / I.dy;
-            const double one_dx = 1.0 / I.dx, one_dy = 1.0 / I.dy;
+            const double dt = sdt[0], hdx = sdt[1], hdy = sdt[2], one_dx = sdt[3], one_dy = sdt[4];
             if (lim == 0)
                 herr += mh_tile_fluxes<TX, TY, NT, 0>(sU, sA, sF, sG, g, g1, hdx, hdy, x0, y0, I.n, I.n);
             else

@@ -321,17 +321,24 @@ __global__ void __launch_bounds__(NT) mh_kernel(Ctrl* __restrict__ c, const Mesh
     const int tiles_x = (B.nx + TX - 1) / TX;
     const int x0 = (blockIdx.x % tiles_x) * TX, y0 = (blockIdx.x / tiles_x) * TY;
 
-    // scalars of this step while the tile is in flight
+    // scalars of this step, formed once per CTA by thread 0 while the tile is in flight and
+    // published by the barrier in load_tile
+    __shared__ double sc[5];
     const double g = c->gamma, g1 = c->g1;
     const double dt = c->dt;
-    // the predictor's own TimeStep call (muscl_hancock.cpp:246): blocks < b already advanced
-    const double dtp = cfl_dt(c, c->calls + b, b, p, p ^ 1);
-    const double dx = c->dx[b], dy = c->dy[b];
-    const double hdx = 0.5 * dtp / dx, hdy = 0.5 * dtp / dy;   // 248-249
-    const double one_dx = 1.0 / dx, one_dy = 1.0 / dy;          // 352-353
-    if (blockIdx.x == 0 && threadIdx.x == 0) c->dt_pred[b] = dtp;
+    if (threadIdx.x == 0) {
+        // the predictor's own TimeStep call (muscl_hancock.cpp:246): blocks < b already advanced
+        const double dtp = cfl_dt(c, c->calls + b, b, p, p ^ 1);
+        const double dx = c->dx[b], dy = c->dy[b];
+        sc[0] = 0.5 * dtp / dx;   // 248-249
+        sc[1] = 0.5 * dtp / dy;
+        sc[2] = 1.0 / dx;         // 352-353
+        sc[3] = 1.0 / dy;
+        if (blockIdx.x == 0) c->dt_pred[b] = dtp;
+    }
 
     if (!load_tile<L::TMA_BYTES>(sU, bar, p ? &tm1 : &tm0, x0, y0, c)) return;
+    const double hdx = sc[0], hdy = sc[1], one_dx = sc[2], one_dy = sc[3];
 
     const int herr = mh_tile_fluxes<TX, TY, NT, LIM>(sU, sA, sF, sG, g, g1, hdx, hdy, x0, y0, B.nx, B.ny);
     // conservative update + forward Euler, and the next step's TimeStep terms
@@ -395,9 +402,14 @@ __global__ void __launch_bounds__(NT) godunov_kernel(Ctrl* __restrict__ c,
     const int x0 = (blockIdx.x % tiles_x) * TX, y0 = (blockIdx.x / tiles_x) * TY;
     const double g = c->gamma, g1 = c->g1;
     const double dt = c->dt;
-    const double one_dx = 1.0 / c->dx[b], one_dy = 1.0 / c->dy[b];   // godunov.cpp:97-98
+    __shared__ double sc[2];
+    if (threadIdx.x == 0) {
+        sc[0] = 1.0 / c->dx[b];   // godunov.cpp:97-98
+        sc[1] = 1.0 / c->dy[b];
+    }
 
     if (!load_tile<L::TMA_BYTES>(sU, bar, p ? &tm1 : &tm0, x0, y0, c)) return;
+    const double one_dx = sc[0], one_dy = sc[1];
 
 #define Q(k, cell) sQ[(k) * L::NC + (cell)]
     for (int cell = threadIdx.x; cell < L::NC; cell += NT) {
