@@ -560,7 +560,6 @@ int hf_set_state(hf_ctx* ctx, int b, const double* cons, int layout) {
     const BlockHost& B = ctx->blocks[b];
     const hf::BlockDev& D = ctx->hmesh.b[b];
     size_t n = (size_t)4 * B.ty * B.tx;
-    CK(cudaStreamSynchronize(ctx->stream));
     const double* st = cons;   // SoA uploads go straight from the caller's buffer
     if (layout == HF_LAYOUT_AOS_XY) {
         double* tmp = staging(ctx, n);
@@ -573,9 +572,12 @@ int hf_set_state(hf_ctx* ctx, int b, const double* cons, int layout) {
     }
     long long step = read_step(ctx);
     int p = (int)(step & 1);
-    for (int k = 0; k < 2; ++k)
-        CK(cudaMemcpy2DAsync(D.buf[k], (size_t)B.pitch * 8, st, (size_t)B.tx * 8, (size_t)B.tx * 8,
-                             (size_t)4 * B.ty, cudaMemcpyHostToDevice, ctx->stream));
+    // into the current buffer, then a device copy into the other (the ghost fill relies on
+    // both holding the same values)
+    CK(cudaMemcpy2DAsync(D.buf[p], (size_t)B.pitch * 8, st, (size_t)B.tx * 8, (size_t)B.tx * 8,
+                         (size_t)4 * B.ty, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(D.buf[p ^ 1], D.buf[p], (size_t)4 * B.ty * B.pitch * 8, cudaMemcpyDeviceToDevice,
+                       ctx->stream));
     // TimeStep terms of the uploaded interior
     unsigned long long zero[2] = {0ull, 0ull};
     CK(cudaMemcpyAsync(&ctx->dctrl->int_s[p][b][0], zero, sizeof zero, cudaMemcpyHostToDevice, ctx->stream));

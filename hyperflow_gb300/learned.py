@@ -289,11 +289,14 @@ def evaluate_plain(case_fn, n_fine: int, t_end: float, factor: int = 4, limiter:
     return out, ref, U0
 
 
-def evaluate_learned(t_end: float, params, ref, U0, limiter: int = 0) -> dict:
-    """The learned FP32 coarse run from U0 to t_end: L1 density error against ref, wall time."""
+def evaluate_learned(t_end: float, params, ref, U0, limiter: int = 0, bound: float | None = None) -> dict:
+    """The learned FP32 coarse run from U0 to t_end: L1 density error against ref, wall time.
+    bound: the guard's per-cell bound (default: the solver's)."""
     nc = U0.shape[1]
     ls = LearnedSolver(nc, 1.0 / nc, limiter=limiter)
     ls.set_params(params)
+    if bound is not None:
+        ls.set_bound(bound)
     ls.set_state(U0, 0.0)
     (steps, rej), sec = _timed(lambda: ls.run_to(t_end, True))
     rho = ls.state()[0].astype(np.float64)

@@ -45,6 +45,7 @@ def main():
                     help="comma list of training modes: pairs (one-step pairs from the filtered "
                          "fine runs) or rollK (one-step training on the solver's own states after "
                          "up to K of its steps)")
+    ap.add_argument("--bounds", default="0.5", help="comma list of guard bounds to evaluate each model with")
     ap.add_argument("--out", default="learned_report.json")
     args = ap.parse_args()
     nf, f = args.n_fine, 4
@@ -79,14 +80,19 @@ def main():
     w = change_weights(pairs)
     report["models"] = {}
     for mode in args.modes.split(","):
+        # mode[:iterations[:learning rate]]
+        parts = mode.split(":")
+        kind = parts[0]
+        iters = int(parts[1]) if len(parts) > 1 else args.iters
+        lr = float(parts[2]) if len(parts) > 2 else args.lr
         ls = LearnedSolver(nc, 1.0 / nc)
         ls.set_params(init_params(0))
         t1 = time.perf_counter()
-        if mode == "pairs":
+        if kind == "pairs":
             sub = pairs[::args.stride]
-            losses, _ = train(ls, sub, args.iters, lr=args.lr, w=w)
-        elif mode.startswith("roll"):
-            losses, _ = train_rollout(ls, seqs, args.iters, lr=args.lr, max_roll=int(mode[4:]), w=w)
+            losses, _ = train(ls, sub, iters, lr=lr, w=w)
+        elif kind.startswith("roll"):
+            losses, _ = train_rollout(ls, seqs, iters, lr=lr, max_roll=int(kind[4:]), w=w)
         else:
             raise SystemExit(f"unknown mode {mode}")
         m = {"train_seconds": time.perf_counter() - t1,
@@ -96,10 +102,15 @@ def main():
                                        "learned": one_step_loss(ls, held_pairs, w, True)}}
         params = ls.params()
         ls.close()
-        np.save(args.out.replace(".json", f"_{mode}_params.npy"), params)
-        m["eval"] = {name: evaluate_learned(t_end, params, ref, U0) for name, (ref, U0, t_end) in base.items()}
+        np.save(args.out.replace(".json", f"_{mode.replace(':', '_')}_params.npy"), params)
+        m["eval"] = {}
+        for bound in (float(b) for b in args.bounds.split(",")):
+            ev = {name: evaluate_learned(t_end, params, ref, U0, bound=bound)
+                  for name, (ref, U0, t_end) in base.items()}
+            m["eval"][f"bound_{bound:g}"] = ev
+            _log(f"model {mode}, bound {bound:g}: " +
+                 ", ".join(f"{k} l1 {v['l1_rho']:.5f}" for k, v in ev.items()), t0)
         report["models"][mode] = m
-        _log(f"model {mode}: " + ", ".join(f"{k} l1 {v['l1_rho']:.5f}" for k, v in m["eval"].items()), t0)
     with open(args.out, "w") as fh:
         json.dump(report, fh, indent=1)
     print(json.dumps(report))
