@@ -138,8 +138,8 @@ __device__ __forceinline__ void stage_tile(const BatchDev& d, const double* __re
     cp_async_commit();
 }
 
-template <int TX, int TY, int NT, int STAGES>
-__global__ void __launch_bounds__(NT) batch_mh_kernel(BatchDev d, int nsteps) {
+template <int TX, int TY, int NT, int STAGES, int MINB>
+__global__ void __launch_bounds__(NT, MINB) batch_mh_kernel(BatchDev d, int nsteps) {
     using T = MhTile<TX, TY>;
     extern __shared__ __align__(1024) double smem[];
     double* sUb[STAGES];
@@ -273,11 +273,13 @@ __global__ void __launch_bounds__(NT) batch_cfl_kernel(BatchDev d) {
 }
 
 struct BatchConfig {
-    int tx, ty, threads, stages;
+    int tx, ty, threads, stages, min_ctas_per_sm;
 };
 
-constexpr BatchConfig kConfigs[] = {{32, 14, 256, 1}, {32, 14, 256, 2}, {32, 16, 256, 1}, {32, 16, 256, 2}};
-constexpr int kNumConfigs = 4;
+// tile shape, threads, halo staging buffers, CTAs per SM the registers are budgeted for
+constexpr BatchConfig kConfigs[] = {{32, 14, 256, 1, 2}, {32, 14, 256, 2, 2}, {32, 16, 256, 1, 2},
+                                    {32, 12, 256, 1, 3}, {32, 12, 256, 2, 2}};
+constexpr int kNumConfigs = 5;
 
 template <int TX, int TY, int NT, int ST>
 size_t batch_smem() {
@@ -285,9 +287,9 @@ size_t batch_smem() {
     return (size_t)(ST * T::U_SIZE + T::A_SIZE + T::F_SIZE + T::G_SIZE) * 8;
 }
 
-template <int TX, int TY, int NT, int ST>
+template <int TX, int TY, int NT, int ST, int MINB>
 cudaError_t launch_batch(const BatchDev& d, int nsteps, int sms, cudaStream_t s, bool cfl_only) {
-    auto k = batch_mh_kernel<TX, TY, NT, ST>;
+    auto k = batch_mh_kernel<TX, TY, NT, ST, MINB>;
     const size_t smem = batch_smem<TX, TY, NT, ST>();
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
@@ -316,10 +318,11 @@ cudaError_t launch_batch(const BatchDev& d, int nsteps, int sms, cudaStream_t s,
 
 cudaError_t launch_batch_config(int k, const BatchDev& d, int nsteps, int sms, cudaStream_t s, bool cfl_only) {
     switch (k) {
-        case 0: return launch_batch<32, 14, 256, 1>(d, nsteps, sms, s, cfl_only);
-        case 1: return launch_batch<32, 14, 256, 2>(d, nsteps, sms, s, cfl_only);
-        case 2: return launch_batch<32, 16, 256, 1>(d, nsteps, sms, s, cfl_only);
-        default: return launch_batch<32, 16, 256, 2>(d, nsteps, sms, s, cfl_only);
+        case 0: return launch_batch<32, 14, 256, 1, 2>(d, nsteps, sms, s, cfl_only);
+        case 1: return launch_batch<32, 14, 256, 2, 2>(d, nsteps, sms, s, cfl_only);
+        case 2: return launch_batch<32, 16, 256, 1, 2>(d, nsteps, sms, s, cfl_only);
+        case 3: return launch_batch<32, 12, 256, 1, 3>(d, nsteps, sms, s, cfl_only);
+        default: return launch_batch<32, 12, 256, 2, 2>(d, nsteps, sms, s, cfl_only);
     }
 }
 

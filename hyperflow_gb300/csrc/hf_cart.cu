@@ -304,7 +304,9 @@ struct MhLayout {
 };
 
 template <int TX, int TY, int LIM, int NT>
-__global__ void __launch_bounds__(NT) mh_kernel(Ctrl* __restrict__ c, const MeshDev* __restrict__ m,
+// three 256-thread CTAs per SM (80 registers, 73 KB of shared memory each): 24 warps hide more
+// of the integer sequences' latency than 16 (measured faster despite a few spilled registers)
+__global__ void __launch_bounds__(NT, 3) mh_kernel(Ctrl* __restrict__ c, const MeshDev* __restrict__ m,
                                                 int b, const __grid_constant__ CUtensorMap tm0,
                                                 const __grid_constant__ CUtensorMap tm1) {
     using L = MhLayout<TX, TY>;
@@ -490,7 +492,7 @@ __global__ void __launch_bounds__(NT) godunov_kernel(Ctrl* __restrict__ c,
 // ------------------------------------------------------------------------------------
 // launchers
 // ------------------------------------------------------------------------------------
-constexpr int kMhTX = 32, kMhTY = 14, kMhNT = 256;
+constexpr int kMhTX = 32, kMhTY = 12, kMhNT = 256;
 constexpr int kGoTX = 32, kGoTY = 16, kGoNT = 256;
 
 StencilTiles stencil_tiles(int scheme) {
