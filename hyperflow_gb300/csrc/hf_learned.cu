@@ -569,9 +569,41 @@ __device__ __forceinline__ bool cell_bad(float g1, const float* un, const float*
     return dr > bound * sr || de > bound * se;
 }
 
+// Local-extremum guard (flux-corrected-transport bounds, Zalesak 1979): the corrected density
+// and energy must stay within the minimum and maximum, over the cell and its 8 neighbours, of
+// both the old state and the plain (uncorrected) update; and density and pressure positive.
+__device__ __forceinline__ bool cell_bad_local(const float* __restrict__ U, const float* __restrict__ F,
+                                               Grid G, float r, int i, int j, const float* un) {
+    PrimF w = prim(G.g1, un);
+    if (!(w.r > 0.0f) || !(w.p > 0.0f)) return true;
+    const int n = G.n;
+    const size_t pl = (size_t)n * n;
+    float lo0 = 3.4e38f, hi0 = -3.4e38f, lo3 = 3.4e38f, hi3 = -3.4e38f;
+    for (int b = -1; b <= 1; ++b)
+        for (int a = -1; a <= 1; ++a) {
+            const int ii = i + a, jj = j + b;
+            if (ii < 0 || jj < 0 || ii >= n || jj >= n) continue;
+            float up[4];
+            cell_update(U, F, nullptr, nullptr, n, r, ii, jj, up);
+            const size_t o = (size_t)jj * n + ii;
+            lo0 = fminf(lo0, fminf(up[0], U[o]));
+            hi0 = fmaxf(hi0, fmaxf(up[0], U[o]));
+            lo3 = fminf(lo3, fminf(up[3], U[3 * pl + o]));
+            hi3 = fmaxf(hi3, fmaxf(up[3], U[3 * pl + o]));
+        }
+    return un[0] < lo0 || un[0] > hi0 || un[3] < lo3 || un[3] > hi3;
+}
+
+// mode 0: the change bound of cell_bad; mode 1: the local-extremum bounds of cell_bad_local
+__device__ __forceinline__ bool guard_bad(const float* __restrict__ U, const float* __restrict__ F, Grid G,
+                                          float r, int i, int j, const float* un, const float* up,
+                                          const float* u0, float bound, int mode) {
+    return mode == 1 ? cell_bad_local(U, F, G, r, i, j, un) : cell_bad(G.g1, un, up, u0, bound);
+}
+
 // pass 1: mark faces whose correction is rejected (any adjacent cell violates)
 __global__ void guard_kernel(const float* __restrict__ U, const float* __restrict__ F, const float* __restrict__ dF,
-                             Grid G, float r, float bound, unsigned char* __restrict__ ok,
+                             Grid G, float r, float bound, int mode, unsigned char* __restrict__ ok,
                              unsigned long long* __restrict__ rejected) {
     const int n = G.n;
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n * n; c += gridDim.x * blockDim.x) {
@@ -580,7 +612,7 @@ __global__ void guard_kernel(const float* __restrict__ U, const float* __restric
         cell_update(U, F, dF, nullptr, n, r, i, j, un);
         cell_update(U, F, nullptr, nullptr, n, r, i, j, up);
         for (int v = 0; v < 4; ++v) u0[v] = U[(size_t)v * n * n + (size_t)j * n + i];
-        if (cell_bad(G.g1, un, up, u0, bound)) {
+        if (guard_bad(U, F, G, r, i, j, un, up, u0, bound, mode)) {
             ok[xf(n, i, j)] = 0; ok[xf(n, i + 1, j)] = 0; ok[yf(n, i, j)] = 0; ok[yf(n, i, j + 1)] = 0;
             atomicAdd(rejected, 1ull);
         }
@@ -589,7 +621,7 @@ __global__ void guard_kernel(const float* __restrict__ U, const float* __restric
 
 // pass 2: the update (corrections where accepted); a cell still violating takes its plain update
 __global__ void update_kernel(const float* __restrict__ U, const float* __restrict__ F, const float* __restrict__ dF,
-                              const unsigned char* __restrict__ ok, Grid G, float r, float bound,
+                              const unsigned char* __restrict__ ok, Grid G, float r, float bound, int mode,
                               float* __restrict__ Un, float* __restrict__ maxs) {
     const int n = G.n;
     float m = 0.0f;
@@ -600,7 +632,7 @@ __global__ void update_kernel(const float* __restrict__ U, const float* __restri
         if (dF) {
             cell_update(U, F, dF, ok, n, r, i, j, un);
             for (int v = 0; v < 4; ++v) u0[v] = U[(size_t)v * n * n + (size_t)j * n + i];
-            if (ok && cell_bad(G.g1, un, up, u0, bound))
+            if (ok && guard_bad(U, F, G, r, i, j, un, up, u0, bound, mode))
                 for (int v = 0; v < 4; ++v) un[v] = up[v];
         } else {
             for (int v = 0; v < 4; ++v) un[v] = up[v];
@@ -670,6 +702,7 @@ using namespace hf::lc;
 struct hf_lc {
     int n = 0, lim = 0;
     double dx = 0, gamma = 1.4, cfl = 0.8, bound = 0.5;
+    int guard_mode = 0;        // 0: change bound, 1: local-extremum bounds
     cudaStream_t stream = nullptr;
     float *U[2] = {nullptr, nullptr}, *F = nullptr, *dF = nullptr, *scale = nullptr, *Y = nullptr;
     float *Z1 = nullptr, *Z2 = nullptr, *dY = nullptr, *T = nullptr, *wv = nullptr;
@@ -832,7 +865,7 @@ int hf_lc_cfl_dt(hf_lc* L, double* dt) {
     LCK(cudaMemsetAsync(L->maxs, 0, 4, L->stream));
     LCK(cudaMemsetAsync(L->F, 0, (size_t)4 * nfaces(L) * sizeof(float), L->stream));
     update_kernel<<<blocks_for((long long)L->n * L->n, 256), 256, 0, L->stream>>>(
-        L->U[L->cur], L->F, nullptr, nullptr, G, 0.0f, 0.0f, L->U[L->cur ^ 1], L->maxs);
+        L->U[L->cur], L->F, nullptr, nullptr, G, 0.0f, 0.0f, 0, L->U[L->cur ^ 1], L->maxs);
     LCK(cudaGetLastError());
     LCK(cudaStreamSynchronize(L->stream));
     *dt = L->cfl * L->dx / max_speed(L);
@@ -852,11 +885,11 @@ int hf_lc_step(hf_lc* L, double dt, int use_mlp, int64_t* rejected_cells) {
         LCK(cudaMemsetAsync(L->ok, 1, nf, L->stream));
         LCK(cudaMemsetAsync(L->rejected, 0, 8, L->stream));
         guard_kernel<<<blocks_for((long long)L->n * L->n, 256), 256, 0, L->stream>>>(
-            L->U[L->cur], L->F, L->dF, G, rr, (float)L->bound, L->ok, L->rejected);
+            L->U[L->cur], L->F, L->dF, G, rr, (float)L->bound, L->guard_mode, L->ok, L->rejected);
     }
     update_kernel<<<blocks_for((long long)L->n * L->n, 256), 256, 0, L->stream>>>(
         L->U[L->cur], L->F, use_mlp ? L->dF : nullptr, use_mlp ? L->ok : nullptr, G, rr, (float)L->bound,
-        L->U[L->cur ^ 1], L->maxs);
+        L->guard_mode, L->U[L->cur ^ 1], L->maxs);
     LCK(cudaGetLastError());
     L->cur ^= 1;
     L->t += dt;
@@ -905,6 +938,11 @@ int hf_lc_set_time(hf_lc* L, double t) {
 }
 int hf_lc_get_time(hf_lc* L, double* t) { if (!L || !t) return HF_ERR_ARG; *t = L->t; return HF_OK; }
 int hf_lc_set_bound(hf_lc* L, double bound) { if (!L || bound <= 0) return HF_ERR_ARG; L->bound = bound; return HF_OK; }
+int hf_lc_set_guard_mode(hf_lc* L, int mode) {
+    if (!L || mode < 0 || mode > 1) return HF_ERR_ARG;
+    L->guard_mode = mode;
+    return HF_OK;
+}
 
 // One training iteration on the pair (U0, T) with step dt: forward (plain + MLP, no guard),
 // loss and dL/dY, backward, Adam.  U0/T are host arrays [4][n][n] (U0 null: the solver's
@@ -922,7 +960,7 @@ int hf_lc_train_step(hf_lc* L, const float* U0, const float* T, const float* w, 
     if (r) return r;
     const float rr = (float)(dt / L->dx);
     update_kernel<<<blocks_for((long long)L->n * L->n, 256), 256, 0, L->stream>>>(
-        L->U[L->cur], L->F, L->dF, nullptr, G, rr, 0.0f, L->U[L->cur ^ 1], L->maxs);
+        L->U[L->cur], L->F, L->dF, nullptr, G, rr, 0.0f, 0, L->U[L->cur ^ 1], L->maxs);
     LCK(cudaMemsetAsync(L->loss, 0, 8, L->stream));
     loss_grad_kernel<<<blocks_for(nf, 256), 256, 0, L->stream>>>(L->U[L->cur ^ 1], L->T, L->scale, L->n, rr, L->wv,
                                                                   L->dY, L->loss);

@@ -83,6 +83,10 @@ class LearnedSolver:
     def set_bound(self, b: float):
         self._c(lib().hf_lc_set_bound(self._h, b))
 
+    def set_guard_mode(self, mode: int):
+        """0: change bound (set_bound); 1: local-extremum (flux-corrected transport) bounds"""
+        self._c(lib().hf_lc_set_guard_mode(self._h, mode))
+
     def set_state(self, U, t: float = 0.0):
         U = np.ascontiguousarray(U, dtype=np.float32)
         assert U.shape == (4, self.n, self.n)
@@ -289,14 +293,17 @@ def evaluate_plain(case_fn, n_fine: int, t_end: float, factor: int = 4, limiter:
     return out, ref, U0
 
 
-def evaluate_learned(t_end: float, params, ref, U0, limiter: int = 0, bound: float | None = None) -> dict:
+def evaluate_learned(t_end: float, params, ref, U0, limiter: int = 0, bound: float | None = None,
+                     guard_mode: int = 0) -> dict:
     """The learned FP32 coarse run from U0 to t_end: L1 density error against ref, wall time.
-    bound: the guard's per-cell bound (default: the solver's)."""
+    bound: the change guard's per-cell bound (default: the solver's); guard_mode 1: the
+    local-extremum guard instead."""
     nc = U0.shape[1]
     ls = LearnedSolver(nc, 1.0 / nc, limiter=limiter)
     ls.set_params(params)
     if bound is not None:
         ls.set_bound(bound)
+    ls.set_guard_mode(guard_mode)
     ls.set_state(U0, 0.0)
     (steps, rej), sec = _timed(lambda: ls.run_to(t_end, True))
     rho = ls.state()[0].astype(np.float64)

@@ -45,7 +45,9 @@ def main():
                     help="comma list of training modes: pairs (one-step pairs from the filtered "
                          "fine runs) or rollK (one-step training on the solver's own states after "
                          "up to K of its steps)")
-    ap.add_argument("--bounds", default="0.5", help="comma list of guard bounds to evaluate each model with")
+    ap.add_argument("--bounds", default="0.5,local",
+                    help="comma list of guards to evaluate each model with: a number is the change "
+                         "bound, 'local' the local-extremum bounds")
     ap.add_argument("--out", default="learned_report.json")
     args = ap.parse_args()
     nf, f = args.n_fine, 4
@@ -104,12 +106,18 @@ def main():
         ls.close()
         np.save(args.out.replace(".json", f"_{mode.replace(':', '_')}_params.npy"), params)
         m["eval"] = {}
-        for bound in (float(b) for b in args.bounds.split(",")):
-            ev = {name: evaluate_learned(t_end, params, ref, U0, bound=bound)
-                  for name, (ref, U0, t_end) in base.items()}
-            m["eval"][f"bound_{bound:g}"] = ev
-            _log(f"model {mode}, bound {bound:g}: " +
-                 ", ".join(f"{k} l1 {v['l1_rho']:.5f}" for k, v in ev.items()), t0)
+        for guard in args.bounds.split(","):
+            kw = {"guard_mode": 1} if guard == "local" else {"bound": float(guard)}
+            tag = "guard_local" if guard == "local" else f"bound_{float(guard):g}"
+            try:
+                ev = {name: evaluate_learned(t_end, params, ref, U0, **kw)
+                      for name, (ref, U0, t_end) in base.items()}
+            except Exception as e:   # a run the guard let blow up
+                ev = {"failed": str(e)}
+            m["eval"][tag] = ev
+            _log(f"model {mode}, {tag}: " +
+                 ", ".join(f"{k} l1 {v['l1_rho']:.5f}" if isinstance(v, dict) else f"{k} {v}"
+                           for k, v in ev.items()), t0)
         report["models"][mode] = m
     with open(args.out, "w") as fh:
         json.dump(report, fh, indent=1)

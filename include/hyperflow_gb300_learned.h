@@ -35,6 +35,11 @@ int hf_lc_get_params(hf_lc* L, float* params);
 /* the guard's per-cell bound: a corrected density or energy change larger than bound x the
  * plain update's change rejects the correction */
 int hf_lc_set_bound(hf_lc* L, double bound);
+/* guard mode 0 (default): the change bound above; 1: local-extremum bounds (flux-corrected
+ * transport, Zalesak 1979) -- the corrected density and energy must stay within the min and max,
+ * over the cell and its 8 neighbours, of the old state and of the plain update.  Both reject
+ * non-positive density or pressure. */
+int hf_lc_set_guard_mode(hf_lc* L, int mode);
 
 int hf_lc_set_state(hf_lc* L, const float* U);
 int hf_lc_get_state(hf_lc* L, float* U);

@@ -125,6 +125,39 @@ def test_guard_keeps_positivity_and_rejects():
 
 
 @pytest.mark.gpu
+def test_local_extremum_guard_keeps_the_bounds():
+    """Guard mode 1: after a step with absurd corrections, every cell's density and energy lie
+    within the min / max over its 3x3 neighbourhood of the old state and the plain update."""
+    from oracle import mlp_oracle as M
+    from hyperflow_gb300 import CartSolver, cases
+    from hyperflow_gb300.learned import LearnedSolver, init_params
+    s = CartSolver(cases.shock_bubble_case(128))
+    s.run(30)
+    U0 = s.state(0)[:, 2:-2, 2:-2].astype(np.float32)
+    ls = LearnedSolver(128, 1 / 128)
+    p = init_params(0)
+    p[M.OFF_B3:] = [0.5, -0.3, 0.4, -2.0]
+    ls.set_params(p)
+    ls.set_guard_mode(1)
+    ls.set_state(U0)
+    dt = ls.cfl_dt()
+    ls.step(dt, use_mlp=False)
+    Up = ls.state()
+    ls.set_state(U0)
+    rejected = ls.step(dt, use_mlp=True)
+    U1 = ls.state()
+    assert rejected > 0
+    assert not np.array_equal(U1, Up)              # some corrections were kept
+    for v in (0, 3):
+        both = np.stack([U0[v], Up[v]])
+        pad_lo = np.pad(both.min(0), 1, mode="edge")
+        pad_hi = np.pad(both.max(0), 1, mode="edge")
+        lo = np.min([pad_lo[1 + a:129 + a, 1 + b:129 + b] for a in (-1, 0, 1) for b in (-1, 0, 1)], axis=0)
+        hi = np.max([pad_hi[1 + a:129 + a, 1 + b:129 + b] for a in (-1, 0, 1) for b in (-1, 0, 1)], axis=0)
+        assert (U1[v] >= lo).all() and (U1[v] <= hi).all()
+
+
+@pytest.mark.gpu
 def test_training_beats_the_plain_coarse_step():
     """Trained on filtered 256^2 FP64 runs (4x coarser grid: 64^2), the corrected one-step
     error on held-out pairs is below the plain coarse step's -- what the network gains."""
