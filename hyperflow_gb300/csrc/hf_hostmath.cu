@@ -12,14 +12,6 @@ void hm_div(const double* a, const double* b, double* out, int64_t n) {
     for (int64_t i = 0; i < n; ++i) out[i] = hf::div_rn(a[i], b[i]);
 }
 
-void hm_add(const double* a, const double* b, double* out, int64_t n) {
-    for (int64_t i = 0; i < n; ++i) out[i] = hf::add_rn(a[i], b[i]);
-}
-
-void hm_sub(const double* a, const double* b, double* out, int64_t n) {
-    for (int64_t i = 0; i < n; ++i) out[i] = hf::sub_rn(a[i], b[i]);
-}
-
 void hm_half(const double* x, double* out, int64_t n) {
     for (int64_t i = 0; i < n; ++i) out[i] = hf::half(x[i]);
 }

@@ -284,77 +284,3 @@ static __host__ __device__ __noinline__ double sqrt_rn(double x) {
 }
 
 }  // namespace hf
-
-namespace hf {
-
-HF_HD int clz64(uint64_t x) {
-#ifdef __CUDA_ARCH__
-    return __clzll((long long)x);
-#else
-    return x ? __builtin_clzll(x) : 64;
-#endif
-}
-
-// a + b, correctly rounded (nearest, ties to even), on the integer pipes: the textbook
-// significand addition with a guard, a round and a sticky bit (Muller et al., "Handbook of
-// Floating-Point Arithmetic", the chapter on addition).  Operands are ordered by magnitude,
-// the smaller significand is aligned with the dropped bits folded into the sticky bit, added or
-// subtracted, renormalised and rounded.  A zero operand gives the other (two zeros give the
-// IEEE sign); exact cancellation gives +0.  Infinite, NaN or subnormal operands and results
-// that leave the normal range take the hardware addition, so the result equals `a + b` bit for
-// bit for all inputs.
-static __host__ __device__ __noinline__ double add_rn(double a, double b) {
-    const uint64_t A = f64_bits(a), B = f64_bits(b);
-    const uint64_t SGN = 0x8000000000000000ull, M52 = 0x000FFFFFFFFFFFFFull, H52 = 0x0010000000000000ull;
-    const uint64_t absA = A & ~SGN, absB = B & ~SGN;
-    const bool swap = absB > absA;
-    const uint64_t X = swap ? B : A, Y = swap ? A : B;
-    const uint64_t absX = swap ? absB : absA, absY = swap ? absA : absB;
-    const uint32_t ex = (uint32_t)(absX >> 52), ey = (uint32_t)(absY >> 52);
-    if (absY == 0) {
-        if (ex >= 2047u) return a + b;                       // inf / NaN with a zero
-        return absX == 0 ? f64_from(A & B) : f64_from(X);    // +0 unless both zeros are -0
-    }
-    if (ex - 1u >= 2046u || ey - 1u >= 2046u) return a + b;  // subnormal, inf, NaN
-    const uint64_t mx = ((X & M52) | H52) << 3;              // [2^55, 2^56): 3 bits below the lsb
-    uint64_t my = ((Y & M52) | H52) << 3;
-    const uint32_t d = ex - ey;
-    if (d >= 58u) {
-        my = 1ull;                                           // only the sticky bit remains
-    } else {
-        const uint64_t lost = my & ((1ull << d) - 1ull);
-        my = (my >> d) | (lost != 0 ? 1ull : 0ull);
-    }
-    int e = (int)ex;
-    uint64_t m;
-    if (((X ^ Y) & SGN) == 0) {
-        m = mx + my;
-        if (m >> 56) {                                       // carry: renormalise by one
-            m = (m >> 1) | (m & 1ull);
-            e += 1;
-        }
-    } else {
-        m = mx - my;
-        if (m == 0) return 0.0;                              // exact cancellation: +0
-        const int sh = clz64(m) - 8;                         // bring the leading one to bit 55
-        if (sh > 0) {
-            m <<= sh;
-            e -= sh;
-        }
-    }
-    uint64_t q = m >> 3;
-    const uint32_t grs = (uint32_t)(m & 7ull);
-    if (grs > 4u || (grs == 4u && (q & 1ull))) q += 1;
-    if (q == (H52 << 1)) {
-        q = H52;
-        e += 1;
-    }
-    if (e < 1 || e > 2046) return a + b;                    // subnormal or overflowing result
-    return f64_from((X & SGN) | ((uint64_t)e << 52) | (q & M52));
-}
-
-// a - b as a + (-b), which IEEE rounds identically for every operand pair
-HF_HD double sub_rn(double a, double b) { return add_rn(a, f64_from(f64_bits(b) ^ 0x8000000000000000ull)); }
-
-}  // namespace hf
-

@@ -157,3 +157,4 @@ def test_half_equals_multiplication(hm):
     same = (out.view(np.uint64) == want.view(np.uint64)) | (np.isnan(out) & np.isnan(want))
     assert same.all(), x[~same][:5]
 
+
