@@ -10,8 +10,8 @@ TimeStep call), exactly the reference's step.
 
 Prints one JSON line (rank 0).  `value` is device-resident throughput (state in HBM,
 CUDA events on the solver's stream around K steps); `e2e` is the same metric through the
-C ABI with host buffers (per step: upload every block from pinned host memory, one step,
-download every block).  With --gpus N under torchrun, every rank runs an independent
+C ABI with host buffers (per step, hf_step_io: upload every block from pinned host memory,
+one step, download every block, each download overlapping the later blocks' updates).  With --gpus N under torchrun, every rank runs an independent
 replica (the path does not shard across GPUs) and `value` sums the replicas.
 """
 from __future__ import annotations
@@ -394,12 +394,9 @@ def main():
     e2e_steps = max(3, min(args.steps, 30))
     barrier()
     t0 = time.perf_counter()
+    arrays = [h[1] for h in host]
     for _ in range(e2e_steps):
-        for b in range(nb):
-            s.set_state(b, host[b][1])
-        s.step()
-        for b in range(nb):
-            s.state(b, out=host[b][1])
+        s.step_io(arrays)          # upload all blocks, one step, download all blocks
     barrier()
     e2e_s = time.perf_counter() - t0
     e2e_value = ws * cells * e2e_steps / e2e_s / 1e6

@@ -71,6 +71,8 @@ std::vector<double> read_vec4(const Json& a) {
 struct hf_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
+    cudaStream_t copy_stream = nullptr;   // downloads of hf_step_io, created on first use
+    cudaEvent_t block_done[HF_MAXB] = {};
     int scheme = 0, limiter = 0, ghost = 1, nblocks = 0;
     double gamma = 1.4, cfl = 0.5, t_start = 0.0, t_end = 0.0;
     std::vector<BlockHost> blocks;
@@ -536,6 +538,10 @@ void hf_destroy(hf_ctx* ctx) {
     if (ctx->dmesh) cudaFree(ctx->dmesh);
     if (ctx->dctrl) cudaFree(ctx->dctrl);
     if (ctx->pinned) cudaFreeHost(ctx->pinned);
+    if (ctx->copy_stream) cudaStreamSynchronize(ctx->copy_stream);
+    for (int b = 0; b < HF_MAXB; ++b)
+        if (ctx->block_done[b]) cudaEventDestroy(ctx->block_done[b]);
+    if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
 }
@@ -650,6 +656,52 @@ int hf_advance(hf_ctx* ctx, double dt) {
         int r = hf_advance_block(ctx, b, dt);
         if (r != HF_OK) return r;
     }
+    return HF_OK;
+}
+
+// One step with the state in host memory: every block uploaded (into both buffers, with the
+// interior TimeStep terms, as hf_set_state), one step (as hf_step), every block downloaded --
+// each block's download on a second stream as soon as its own update is done, so it overlaps
+// the updates of the blocks after it.  No synchronisation between the pieces.
+int hf_step_io(hf_ctx* ctx, const double* const* in, double* const* out, double* dt) {
+    if (!ctx || !in || !out) return HF_ERR_ARG;
+    for (int b = 0; b < ctx->nblocks; ++b)
+        if (!in[b] || !out[b]) return HF_ERR_ARG;
+    if (ctx->next_block != 0) return fail(ctx, HF_ERR_STATE, "step in the middle of a step");
+    if (!ctx->copy_stream) {
+        CK(cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
+        for (int b = 0; b < ctx->nblocks; ++b)
+            CK(cudaEventCreateWithFlags(&ctx->block_done[b], cudaEventDisableTiming));
+    }
+    const long long step = read_step(ctx);
+    const int p = (int)(step & 1);
+    for (int b = 0; b < ctx->nblocks; ++b) {
+        const BlockHost& B = ctx->blocks[b];
+        const hf::BlockDev& D = ctx->hmesh.b[b];
+        CK(cudaMemcpy2DAsync(D.buf[p], (size_t)B.pitch * 8, in[b], (size_t)B.tx * 8, (size_t)B.tx * 8,
+                             (size_t)4 * B.ty, cudaMemcpyHostToDevice, ctx->stream));
+        CK(cudaMemcpyAsync(D.buf[p ^ 1], D.buf[p], (size_t)4 * B.ty * B.pitch * 8, cudaMemcpyDeviceToDevice,
+                           ctx->stream));
+        CK(cudaMemsetAsync(&ctx->dctrl->int_s[p][b][0], 0, 2 * sizeof(unsigned long long), ctx->stream));
+        CK(hf::launch_interior_cfl(ctx->dctrl, ctx->dmesh, b, B.nx, B.ny, p, ctx->stream));
+    }
+    int clamp = 0;
+    CK(cudaMemcpyAsync(&ctx->dctrl->clamp, &clamp, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+    CK(hf::launch_bc_fill(ctx->dctrl, ctx->dmesh, ctx->side_len, ctx->nblocks, ctx->stream));
+    CK(hf::launch_ghost_cfl(ctx->dctrl, ctx->dmesh, ctx->hmesh.total_ghost, ctx->stream));
+    for (int b = 0; b < ctx->nblocks; ++b) {
+        const BlockHost& B = ctx->blocks[b];
+        CK(hf::launch_stencil(ctx->dctrl, ctx->dmesh, b, B.nx, B.ny, ctx->scheme, ctx->limiter,
+                              &ctx->tmap[b][0], &ctx->tmap[b][1], ctx->stream));
+        CK(cudaEventRecord(ctx->block_done[b], ctx->stream));
+        CK(cudaStreamWaitEvent(ctx->copy_stream, ctx->block_done[b], 0));
+        CK(cudaMemcpy2DAsync(out[b], (size_t)B.tx * 8, ctx->hmesh.b[b].buf[p ^ 1], (size_t)B.pitch * 8,
+                             (size_t)B.tx * 8, (size_t)4 * B.ty, cudaMemcpyDeviceToHost, ctx->copy_stream));
+    }
+    CK(hf::launch_finalize(ctx->dctrl, ctx->stream));
+    if (dt) CK(cudaMemcpyAsync(dt, &ctx->dctrl->dt, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    CK(cudaStreamSynchronize(ctx->copy_stream));
     return HF_OK;
 }
 

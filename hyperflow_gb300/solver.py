@@ -107,6 +107,20 @@ class CartSolver:
         check(lib().hf_step(self._h, C.byref(dt)), self._h)
         return dt.value
 
+    def step_io(self, ins, outs=None) -> float:
+        """One step with every block's state in host arrays (SoA [4][total_y][total_x], ghosts
+        included, C-contiguous float64; pinned memory for full speed): upload, step, download
+        into outs (default: in place).  Returns the step's dt."""
+        outs = ins if outs is None else outs
+        assert len(ins) == len(outs) == self.nblocks
+        for a in list(ins) + list(outs):
+            assert a.dtype == np.float64 and a.flags.c_contiguous
+        pin = (C.c_void_p * self.nblocks)(*[a.ctypes.data for a in ins])
+        pout = (C.c_void_p * self.nblocks)(*[a.ctypes.data for a in outs])
+        dt = C.c_double()
+        check(lib().hf_step_io(self._h, pin, pout, C.byref(dt)), self._h)
+        return dt.value
+
     def run(self, n: int, clamp_t_end: bool = False, graph: bool = True) -> int:
         done = C.c_int64()
         check(lib().hf_run(self._h, n, int(clamp_t_end), int(graph), C.byref(done)), self._h)

@@ -79,6 +79,15 @@ int hf_advance(hf_ctx* ctx, double dt);
 /* one whole step with no clamps: apply_bcs, dt, advance; dt written if non-null */
 int hf_step(hf_ctx* ctx, double* dt);
 
+/* One step with the state in host memory, for callers that keep the fields on the host
+ * between steps (the reference's own per-step set_fields / get_fields pattern,
+ * simulation.cpp:106-110): uploads every block (in[b], SoA [4][total_y][total_x] with ghosts,
+ * as hf_set_state), runs one step without the t_end clamp (hf_step), and downloads every block's
+ * new state into out[b] -- each download starts as soon as that block's update is done, so it
+ * overlaps the updates of the blocks after it.  in and out may be the same arrays; pinned host
+ * memory gives full copy speed.  dt (optional) receives the step's dt. */
+int hf_step_io(hf_ctx* ctx, const double* const* in, double* const* out, double* dt);
+
 /* Simulation::solve's loop body (simulation.cpp:81-120, frame clamps excluded) run n times
  * on the device with no host round trip per step: dt stays on the device.  clamp_t_end != 0
  * applies the t_end clamp and stops at t_end like the reference.  use_graph != 0 replays a

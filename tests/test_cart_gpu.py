@@ -172,3 +172,22 @@ def test_gpu_shock_bubble_matches_oracle(port_lib):
     o.run(40)
     s.run(40)
     np.testing.assert_array_equal(s.state(0), o.state(0))
+
+
+def test_gpu_step_io_equals_upload_step_download():
+    """hf_step_io (upload, step, overlapped per-block download) against hf_set_state + hf_step
+    + hf_get_state, on the 3-block forward-facing step, several steps in a row, in place."""
+    from hyperflow_gb300 import cases
+    case = cases.forward_facing_step_case(40, limiter="VanLeer")
+    a, b = _solver(case), _solver(case)
+    a.run(5)
+    host = [a.state(k).copy() for k in range(a.nblocks)]
+    for _ in range(4):
+        for k in range(b.nblocks):
+            b.set_state(k, host[k])
+        dt_b = b.step()
+        want = [b.state(k) for k in range(b.nblocks)]
+        dt_a = a.step_io(host)
+        assert dt_a == dt_b
+        for k in range(a.nblocks):
+            np.testing.assert_array_equal(host[k], want[k])
