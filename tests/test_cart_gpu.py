@@ -181,6 +181,7 @@ def test_gpu_step_io_equals_upload_step_download():
     case = cases.forward_facing_step_case(40, limiter="VanLeer")
     a, b = _solver(case), _solver(case)
     a.run(5)
+    b.run(5)                       # the same TimeStep call count (it sets the CFL factor)
     host = [a.state(k).copy() for k in range(a.nblocks)]
     for _ in range(4):
         for k in range(b.nblocks):
