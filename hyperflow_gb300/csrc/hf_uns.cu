@@ -136,7 +136,7 @@ __device__ __forceinline__ int pair_flux(const UnsMesh& m, const double* __restr
 }
 
 // edge-based mode, pass 1: one flux per unique interior edge, from its owner's side
-__global__ void __launch_bounds__(kUnsNT) uns_edge_flux_kernel(UnsCtrl* __restrict__ c, UnsMesh m) {
+__global__ void __launch_bounds__(kUnsNT, 3) uns_edge_flux_kernel(UnsCtrl* __restrict__ c, UnsMesh m) {
     if (c->done) return;
     const int p = (int)(c->step & 1);
     const double g = c->gamma, g1 = c->g1;
@@ -233,7 +233,11 @@ __global__ void uns_finalize_kernel(UnsCtrl* c) {
     c->step = c->step + 1;
 }
 
-__global__ void __launch_bounds__(kUnsNT) uns_step_kernel(UnsCtrl* __restrict__ c, UnsMesh m) {
+// MINB: CTAs per SM the registers are budgeted for -- three in edge mode (the per-cell work is a
+// gather of precomputed edge fluxes, and more warps hide its latency), one in the per-pair mode
+// (its HLLC needs the registers; measured faster unbounded)
+template <int MINB>
+__global__ void __launch_bounds__(kUnsNT, MINB) uns_step_kernel(UnsCtrl* __restrict__ c, UnsMesh m) {
     if (c->done) return;
     const int p = (int)(c->step & 1);
     const double g = c->gamma, g1 = c->g1, dt = c->dt;
@@ -594,7 +598,10 @@ int enqueue_uns_step(hf_uns* u, bool prep) {
     } else {
         m.pair_edge = nullptr;
     }
-    hf::uns_step_kernel<<<grid, hf::kUnsNT, 0, u->stream>>>(u->dctrl, m);
+    if (u->edge_mode)
+        hf::uns_step_kernel<3><<<grid, hf::kUnsNT, 0, u->stream>>>(u->dctrl, m);
+    else
+        hf::uns_step_kernel<1><<<grid, hf::kUnsNT, 0, u->stream>>>(u->dctrl, m);
     if (u->ring_slots > 0) hf::uns_frame_copy_kernel<<<4 * 152, 256, 0, u->stream>>>(u->dctrl, m, u->ring);
     hf::uns_finalize_kernel<<<1, 1, 0, u->stream>>>(u->dctrl);
     UCK(cudaGetLastError());
