@@ -48,6 +48,9 @@ def main():
     ap.add_argument("--bounds", default="0.5,local",
                     help="comma list of guards to evaluate each model with: a number is the change "
                          "bound, 'local' the local-extremum bounds")
+    ap.add_argument("--extra-cases", type=int, default=0,
+                    help="additional training cases: this many more Riemann seeds (102, 103, ...) and "
+                         "as many more bubble placements")
     ap.add_argument("--out", default="learned_report.json")
     args = ap.parse_args()
     nf, f = args.n_fine, 4
@@ -57,6 +60,12 @@ def main():
     train_sets = [("rp_seed_100", rp_case(100), None), ("rp_seed_101", rp_case(101), None),
                   ("bubble_a", sb_case((0.4, 0.5), 0.2, 1.0), 0.25),
                   ("bubble_b", sb_case((0.45, 0.45), 0.2, 1.0), 0.25)]
+    rng = np.random.default_rng(1)
+    for k in range(args.extra_cases):
+        train_sets.append((f"rp_seed_{102 + k}", rp_case(102 + k), None))
+        bx, by = float(rng.uniform(0.35, 0.5)), float(rng.uniform(0.4, 0.6))
+        r = float(rng.uniform(0.15, 0.22))
+        train_sets.append((f"bubble_{k}", sb_case((bx, by), r, 1.0), 0.25))
     seqs = []
     for name, fn, t_end in train_sets:
         c = fn(nf)
