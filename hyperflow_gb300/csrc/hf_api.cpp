@@ -93,7 +93,6 @@ struct hf_ctx {
     float* coarse = nullptr;    // device scratch of hf_coarsen
     size_t coarse_n = 0;
     int next_block = 0;         // next block hf_advance_block expects
-    long long host_step = 0;    // mirror of ctrl.step while the host drives the steps
     // graphs of one step (index = clamp flag)
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     // profiling
@@ -989,7 +988,6 @@ int hf_checkpoint_load(hf_ctx* ctx, const void* buf, size_t bytes) {
             p += n;
         }
     CK(cudaMemcpy(ctx->dctrl, &C, sizeof C, cudaMemcpyHostToDevice));
-    ctx->host_step = C.step;
     return HF_OK;
 }
 

@@ -11,12 +11,14 @@
 //     u_n/c_ref, u_t/c_ref, p/p_ref - 1) with rho_ref, p_ref the mean of the two face
 //     cells and c_ref = sqrt(gamma p_ref / rho_ref): 64 inputs, rounded to BF16;
 //   MLP: 64 -> 64 (GELU) -> 64 (GELU) -> 4, BF16 weights and activations on the tensor
-//     cores (mma.sync m16n8k16, FP32 accumulation), FP32 biases;
+//     cores (tcgen05.mma, BF16 x BF16 -> FP32 accumulators in TMEM), FP32 biases;
 //   correction: dF = rho_ref c_ref * (o0, o1 c_ref, o2 c_ref, o3 c_ref^2) in the face frame
 //     (normal, tangential), rotated back to (x, y);
-//   guard: a cell whose corrected update has rho <= 0, p <= 0, or a density / energy change
-//     beyond `bound` times the plain update's, rejects the corrections on all its faces (they
-//     fall back to the plain flux); a cell still violating after that takes its plain update.
+//   guard: a cell whose corrected update has rho <= 0, p <= 0, or (mode 0) a density / energy
+//     change beyond `bound` times the plain update's, or (mode 1) a density / energy outside the
+//     min / max of its 3x3 neighbourhood's old and plainly updated values, rejects the
+//     corrections on all its faces (they fall back to the plain flux); a cell still violating
+//     after that takes its plain update.
 // Training: one-step loss L = mean_cells sum_v w_v (U^{n+1}_v - T_v)^2 against the filtered
 // fine solution T; dL/dF flows only through the linear conservative update.  Backward and
 // Adam are hand-written FP32 kernels (weight gradients on the CUDA cores).
