@@ -413,6 +413,19 @@ def main():
             "algorithmic_bytes_per_launch": BYTES_PER_CELL * cells / nb,
             "avg_launch_ms": stencil_ms / max(stencil_launches * nb, 1),
             "kernel": "mh_kernel (fused MUSCL-Hancock + HLLC + forward Euler + CFL epilogue)"}
+    # the bound that binds on this part: FP64 issue (2 lanes per SM per clock)
+    if tr and tr.get("workload") == workload_name(args) and tr.get("fp64_ops_per_cell_update"):
+        sm_mhz = 2070.0
+        pk = os.path.join(ROOT, "MEASURED_PEAKS.json")
+        if os.path.exists(pk):
+            with open(pk) as f:
+                sm_mhz = float(json.load(f).get("sm_max_mhz", sm_mhz))
+        nsm = torch.cuda.get_device_properties(local).multi_processor_count
+        ops = tr["fp64_ops_per_cell_update"] * cells * args.steps / (stencil_ms / 1e3) / 1e9
+        peak_ops = 2.0 * nsm * sm_mhz / 1e3
+        roof["fp64_pipe"] = {"achieved": ops, "peak": peak_ops, "unit": "G FP64 ops/s (FMA = 1)",
+                             "frac": ops / peak_ops,
+                             "ops_per_cell_update": tr["fp64_ops_per_cell_update"]}
 
     # ---- CPU baseline (rank 0, N=1): the oracle on all host cores, bounded sample ----
     cpu = None
