@@ -234,8 +234,8 @@ __global__ void uns_finalize_kernel(UnsCtrl* c) {
 }
 
 // MINB: CTAs per SM the registers are budgeted for -- three in edge mode (the per-cell work is a
-// gather of precomputed edge fluxes, and more warps hide its latency), one in the per-pair mode
-// (its HLLC needs the registers; measured faster unbounded)
+// gather of precomputed edge fluxes, and more warps hide its latency), two in the per-pair mode
+// (its HLLC needs the registers: 128 per thread; at 148 only one CTA fits and it runs 27 % slower)
 template <int MINB>
 __global__ void __launch_bounds__(kUnsNT, MINB) uns_step_kernel(UnsCtrl* __restrict__ c, UnsMesh m) {
     if (c->done) return;
@@ -601,7 +601,7 @@ int enqueue_uns_step(hf_uns* u, bool prep) {
     if (u->edge_mode)
         hf::uns_step_kernel<3><<<grid, hf::kUnsNT, 0, u->stream>>>(u->dctrl, m);
     else
-        hf::uns_step_kernel<1><<<grid, hf::kUnsNT, 0, u->stream>>>(u->dctrl, m);
+        hf::uns_step_kernel<2><<<grid, hf::kUnsNT, 0, u->stream>>>(u->dctrl, m);
     if (u->ring_slots > 0) hf::uns_frame_copy_kernel<<<4 * 152, 256, 0, u->stream>>>(u->dctrl, m, u->ring);
     hf::uns_finalize_kernel<<<1, 1, 0, u->stream>>>(u->dctrl);
     UCK(cudaGetLastError());
