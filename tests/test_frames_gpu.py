@@ -161,3 +161,26 @@ def test_gpu_uns_frames_equal_oracle_and_reference(name, ring, tmp_path, port_li
         np.testing.assert_array_equal(Uk, oframes[k])
         h = hashlib.sha256(fr.uns_csv_text(head, Uk, cen).encode()).hexdigest()
         assert h == g["csv_sha256"][k], k
+
+
+@pytest.mark.parametrize("scheme", ["MUSCLHancock", "Godunov"])
+def test_gpu_multiblock_frames_equal_oracle(scheme, tmp_path, port_lib):
+    """Frames of the 3-block forward-facing step (internal, inflow, reflective and
+    transmissive sides) against the oracle's Simulation::solve, bit for bit."""
+    from hyperflow_gb300 import CartSolver, cases, frames as fr
+    from oracle.oracle import Oracle
+    case = cases.forward_facing_step_case(30, scheme=scheme, t_end=0.05)
+    case["simulation"]["animation"] = {"duration": 1.0, "fps": 16.0}
+    o = Oracle(case, nthreads=4)
+    _, labels, oframes = o.solve(max_frames=64)
+    s = CartSolver(case)
+    s.solve(out_dir=str(tmp_path), ring_slots=4)
+    paths = sorted(s.frame_paths)
+    assert len(paths) == len(oframes) > 10
+    for k, p in enumerate(paths):
+        head, blocks = fr.read_frame(p)
+        assert head["index"] == k and head["t"] == labels[k]
+        for a, b in zip(blocks, oframes[k]):
+            np.testing.assert_array_equal(a, b)
+    for b in range(s.nblocks):
+        np.testing.assert_array_equal(s.state(b), o.state(b))
