@@ -183,9 +183,13 @@ def bench_batch(args):
     import torch
     from hyperflow_gb300 import BatchSolver, cases
     from oracle.oracle import Oracle, build_port
-    m = cases.batch_manifest(512, seed=0)
+    m = cases.batch_manifest(args.instances, seed=0)
     b = BatchSolver(m)
-    best, trial_ms = b.autotune(steps_per_trial=2)
+    if args.batch_config >= 0:
+        b.set_config(args.batch_config)
+        best, trial_ms = args.batch_config, []
+    else:
+        best, trial_ms = b.autotune(steps_per_trial=2)
     stream = torch.cuda.ExternalStream(b.stream())
     b.run(args.warmup, graph=True)
     b.sync()
@@ -199,7 +203,7 @@ def bench_batch(args):
     # CPU baseline: the oracle on all host cores over a bounded sample of the instances
     build_port()
     nth = os.cpu_count() or 1
-    sample = list(range(0, 512, 16))
+    sample = list(range(0, args.instances, 16))
     sample_cells, t0 = 0, time.perf_counter()
     for i in sample:
         o = Oracle(m["cases"][i], nthreads=nth)
@@ -211,15 +215,15 @@ def bench_batch(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded four-quadrant Riemann problems)",
-        "config": {"workload": "batched_512_quadrant_riemann_sides_64_1024_muscl_hancock_minbee_hllc_fp64",
-                   "instances": 512, "cells": cells, "cfl": cases.CFL_2D, "autotuned_config": best,
+        "config": {"workload": f"batched_{args.instances}_quadrant_riemann_sides_64_1024_muscl_hancock_minbee_hllc_fp64",
+                   "instances": args.instances, "cells": cells, "cfl": cases.CFL_2D, "autotuned_config": best,
                    "autotune_trial_ms": [float(x) for x in trial_ms],
                    "l2": "state 2 x %.0f MB > 129 MB L2, no flush needed" % (cells * 32 / 1e6)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "traffic": None, "peak_kind": peak_kind,
                      "kernel": "batch_mh_kernel (persistent, all instances, one launch per run)"},
         "cpu_baseline": {"value": sample_cells / cpu_s / 1e6, "unit": "Mcell-updates/s", "cores": nth,
-                         "kind": "port", "sample": f"instances 0, 16, ..., 496 ({len(sample)}), 20 steps each"},
+                         "kind": "port", "sample": f"every 16th instance ({len(sample)}), 20 steps each"},
         "e2e": None, "gpu_launches": 1, "clocks": clk.summary()}), flush=True)
     b.close()
 
@@ -287,6 +291,9 @@ def main():
     ap.add_argument("--workload", default="ffs", choices=["ffs", "square", "batch", "uns"],
                     help="ffs: the 3-block forward-facing step (default); square: one n x n block; "
                          "batch: 512 batched Riemann problems; uns: the 1M-triangle channel")
+    ap.add_argument("--instances", type=int, default=512, help="batch workload: number of instances")
+    ap.add_argument("--batch-config", type=int, default=-1,
+                    help="batch workload: this launch configuration instead of the autotuner's choice")
     ap.add_argument("--uns-per-side", action="store_true",
                     help="uns workload: per-(cell, edge) fluxes (bit-exact mode) instead of edge-based")
     ap.add_argument("--n", type=int, default=4096, help="side of the square workload")
