@@ -651,8 +651,8 @@ __global__ void update_kernel(const float* __restrict__ U, const float* __restri
 
 // dL/dY for L = (1/N) sum_cells sum_v w_v (U^{n+1}_v - T_v)^2, U^{n+1} with every correction
 __global__ void loss_grad_kernel(const float* __restrict__ Un, const float* __restrict__ T, const float* __restrict__ scale,
-                                 int n, float r, const float* __restrict__ wv, float* __restrict__ dY,
-                                 double* __restrict__ loss) {
+                                 int n, float r, const float* __restrict__ wv, const unsigned char* __restrict__ ok,
+                                 float* __restrict__ dY, double* __restrict__ loss) {
     const int nf = 2 * (n + 1) * n;
     const float invN = 1.0f / ((float)n * n);
     double ls = 0.0;
@@ -673,8 +673,9 @@ __global__ void loss_grad_kernel(const float* __restrict__ Un, const float* __re
                 const size_t o = (size_t)v * n * n + (size_t)ju * n + iu;
                 gu = 2.0f * wv[v] * (Un[o] - T[o]) * invN;
             }
-            // U_lower gets -r*F, U_upper gets +r*F
-            gF[v] = r * (gu - gl);
+            // U_lower gets -r*F, U_upper gets +r*F; a face whose correction the guard rejected
+            // does not take part
+            gF[v] = (ok && !ok[f]) ? 0.0f : r * (gu - gl);
         }
         const float rr = scale[2 * (size_t)f], c = scale[2 * (size_t)f + 1], m = rr * c;
         const bool xface = dir == 0;
@@ -705,6 +706,7 @@ struct hf_lc {
     int n = 0, lim = 0;
     double dx = 0, gamma = 1.4, cfl = 0.8, bound = 0.5;
     int guard_mode = 0;        // 0: change bound, 1: local-extremum bounds
+    int train_guard = 0;       // training applies the guard as inference does
     cudaStream_t stream = nullptr;
     float *U[2] = {nullptr, nullptr}, *F = nullptr, *dF = nullptr, *scale = nullptr, *Y = nullptr;
     float *Z1 = nullptr, *Z2 = nullptr, *dY = nullptr, *T = nullptr, *wv = nullptr;
@@ -940,6 +942,11 @@ int hf_lc_set_time(hf_lc* L, double t) {
 }
 int hf_lc_get_time(hf_lc* L, double* t) { if (!L || !t) return HF_ERR_ARG; *t = L->t; return HF_OK; }
 int hf_lc_set_bound(hf_lc* L, double bound) { if (!L || bound <= 0) return HF_ERR_ARG; L->bound = bound; return HF_OK; }
+int hf_lc_set_train_guard(hf_lc* L, int on) {
+    if (!L) return HF_ERR_ARG;
+    L->train_guard = on ? 1 : 0;
+    return HF_OK;
+}
 int hf_lc_set_guard_mode(hf_lc* L, int mode) {
     if (!L || mode < 0 || mode > 1) return HF_ERR_ARG;
     L->guard_mode = mode;
@@ -961,11 +968,20 @@ int hf_lc_train_step(hf_lc* L, const float* U0, const float* T, const float* w, 
     int r = fluxes(L, (float)dt, true, true);
     if (r) return r;
     const float rr = (float)(dt / L->dx);
-    update_kernel<<<blocks_for((long long)L->n * L->n, 256), 256, 0, L->stream>>>(
-        L->U[L->cur], L->F, L->dF, nullptr, G, rr, 0.0f, 0, L->U[L->cur ^ 1], L->maxs);
+    if (L->train_guard) {   // the guard of inference: rejected faces take the plain flux
+        LCK(cudaMemsetAsync(L->ok, 1, nf, L->stream));
+        LCK(cudaMemsetAsync(L->rejected, 0, 8, L->stream));
+        guard_kernel<<<blocks_for((long long)L->n * L->n, 256), 256, 0, L->stream>>>(
+            L->U[L->cur], L->F, L->dF, G, rr, (float)L->bound, L->guard_mode, L->ok, L->rejected);
+        update_kernel<<<blocks_for((long long)L->n * L->n, 256), 256, 0, L->stream>>>(
+            L->U[L->cur], L->F, L->dF, L->ok, G, rr, (float)L->bound, L->guard_mode, L->U[L->cur ^ 1], L->maxs);
+    } else {
+        update_kernel<<<blocks_for((long long)L->n * L->n, 256), 256, 0, L->stream>>>(
+            L->U[L->cur], L->F, L->dF, nullptr, G, rr, 0.0f, 0, L->U[L->cur ^ 1], L->maxs);
+    }
     LCK(cudaMemsetAsync(L->loss, 0, 8, L->stream));
     loss_grad_kernel<<<blocks_for(nf, 256), 256, 0, L->stream>>>(L->U[L->cur ^ 1], L->T, L->scale, L->n, rr, L->wv,
-                                                                  L->dY, L->loss);
+                                                                  L->train_guard ? L->ok : nullptr, L->dY, L->loss);
     LCK(cudaMemsetAsync(L->grad, 0, NPARAM * sizeof(float), L->stream));
     mlp_backward_kernel<<<blocks_for(nf, kBwdFaces) > 1024 ? 1024 : blocks_for(nf, kBwdFaces), 256, 0, L->stream>>>(
         L->X, nf, L->Wb, L->Z1, L->Z2, L->dY, L->grad);

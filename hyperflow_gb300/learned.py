@@ -83,6 +83,10 @@ class LearnedSolver:
     def set_bound(self, b: float):
         self._c(lib().hf_lc_set_bound(self._h, b))
 
+    def set_train_guard(self, on: bool):
+        """training steps apply the guard as inference does"""
+        self._c(lib().hf_lc_set_train_guard(self._h, int(on)))
+
     def set_guard_mode(self, mode: int):
         """0: change bound (set_bound); 1: local-extremum (flux-corrected transport) bounds"""
         self._c(lib().hf_lc_set_guard_mode(self._h, mode))

@@ -43,7 +43,7 @@ def main():
     ap.add_argument("--stride", type=int, default=8, help="pairs mode: every stride-th window")
     ap.add_argument("--modes", default="pairs,roll4",
                     help="comma list of training modes: pairs (one-step pairs from the filtered "
-                         "fine runs) or rollK (one-step training on the solver's own states after "
+                         "fine runs), gpairs (the same, trained with the guard applied) or rollK (one-step training on the solver's own states after "
                          "up to K of its steps)")
     ap.add_argument("--bounds", default="0.5,local",
                     help="comma list of guards to evaluate each model with: a number is the change "
@@ -98,6 +98,10 @@ def main():
         lr = float(parts[2]) if len(parts) > 2 else args.lr
         ls = LearnedSolver(nc, 1.0 / nc)
         ls.set_params(init_params(0))
+        if kind == "gpairs":          # pairs, trained with the change guard (bound 2) applied
+            ls.set_bound(2.0)
+            ls.set_train_guard(True)
+            kind = "pairs"
         t1 = time.perf_counter()
         if kind == "pairs":
             sub = pairs[::args.stride]

@@ -40,6 +40,9 @@ int hf_lc_set_bound(hf_lc* L, double bound);
  * over the cell and its 8 neighbours, of the old state and of the plain update.  Both reject
  * non-positive density or pressure. */
 int hf_lc_set_guard_mode(hf_lc* L, int mode);
+/* on != 0: training steps apply the guard as inference does (rejected faces take the plain
+ * flux and pass no gradient); default off */
+int hf_lc_set_train_guard(hf_lc* L, int on);
 
 int hf_lc_set_state(hf_lc* L, const float* U);
 int hf_lc_get_state(hf_lc* L, float* U);
