@@ -493,7 +493,7 @@ __global__ void __launch_bounds__(NT) godunov_kernel(Ctrl* __restrict__ c,
 // launchers
 // ------------------------------------------------------------------------------------
 constexpr int kMhTX = 32, kMhTY = 12, kMhNT = 256;
-constexpr int kGoTX = 32, kGoTY = 16, kGoNT = 256;
+constexpr int kGoTX = 32, kGoTY = 14, kGoNT = 256;
 
 StencilTiles stencil_tiles(int scheme) {
     return scheme == 0 ? StencilTiles{kGoTX, kGoTY} : StencilTiles{kMhTX, kMhTY};
