@@ -47,7 +47,11 @@ enum {
 /* Parses a case file (the JSON read by src/fvm_2d_cart/simulation/parser/parser.cpp:13-488,
  * same keys and meaning), allocates device state, and initialises the interior from the
  * initial condition exactly as Simulation::Simulation does (simulation.cpp:43).
- * Replaces: JSONParser + generate_* + Simulation construction (src/fvm_2d_cart/main.cpp:33-86). */
+ * Replaces: JSONParser + generate_* + Simulation construction (src/fvm_2d_cart/main.cpp:33-86).
+ * Supported: EulerIdealGas, Godunov or MUSCLHancock (MinBee / VanLeer), HLLCEuler, ForwardEuler,
+ * up to 16 blocks, each at least 2 x ghost cells wide along both axes (2 for Godunov, 4 for
+ * MUSCL-Hancock; narrower blocks would mirror ghost cells into ghost cells): anything else
+ * returns HF_ERR_UNSUPPORTED with the reason in hf_last_error_message. */
 int hf_create(const char* case_json, size_t len, hf_ctx** out);
 void hf_destroy(hf_ctx* ctx);
 

@@ -87,3 +87,21 @@ def test_no_device_is_reported_not_faked():
     from hyperflow_gb300 import cases
     st, _ = _create(json.dumps(cases.quadrant_case(16)))
     assert st == 7
+
+
+def test_blocks_narrower_than_two_ghosts_are_refused():
+    """hf_create refuses them before touching the GPU (no device needed)."""
+    import ctypes as C
+    import json
+    from hyperflow_gb300 import cases
+    from hyperflow_gb300._lib import lib
+    L = lib()
+    for scheme, nx, ny in (("Godunov", 1, 5), ("MUSCLHancock", 3, 8), ("MUSCLHancock", 8, 2)):
+        raw = json.dumps(cases.quadrant_case(nx, ny=ny, scheme=scheme,
+                                             limiter=None if scheme == "Godunov" else "MinBee")).encode()
+        h = C.c_void_p()
+        st = L.hf_create(raw, len(raw), C.byref(h))
+        msg = L.hf_last_error_message(h).decode()
+        if h:
+            L.hf_destroy(h)
+        assert st == 3 and "2*ghost" in msg

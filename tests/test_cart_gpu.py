@@ -192,3 +192,28 @@ def test_gpu_step_io_equals_upload_step_download():
         assert dt_a == dt_b
         for k in range(a.nblocks):
             np.testing.assert_array_equal(host[k], want[k])
+
+
+@pytest.mark.parametrize("scheme,limiter", [("Godunov", None), ("MUSCLHancock", "MinBee"),
+                                            ("MUSCLHancock", "VanLeer")])
+@pytest.mark.parametrize("nx,ny", [(1, 1), (1, 5), (3, 2), (33, 1), (33, 13), (65, 29), (31, 43)])
+def test_gpu_tiny_and_ragged_grids_match_oracle(scheme, limiter, nx, ny, port_lib):
+    """Grids smaller than one tile, and one cell past a tile edge in x and y (tiles 32x12 /
+    32x14): partial tiles and clipped faces.  Blocks narrower than 2 x ghost cells (the ghost
+    fill would mirror ghost cells into ghost cells, in the reference's sequential order) are
+    refused with HF_ERR_UNSUPPORTED instead of computed."""
+    from oracle.oracle import Oracle
+    from hyperflow_gb300 import HyperFlowError, cases
+    case = cases.quadrant_case(nx, ny=ny, scheme=scheme, limiter=limiter, split=(0.45, 0.55))
+    g = 1 if scheme == "Godunov" else 2
+    if nx < 2 * g or ny < 2 * g:
+        with pytest.raises(HyperFlowError, match="2\\*ghost"):
+            _solver(case)
+        return
+    o = Oracle(case)
+    s = _solver(case)
+    dts_o = o.run(25)
+    dts = [s.step() for _ in range(25)]
+    np.testing.assert_array_equal(np.array(dts), dts_o)
+    np.testing.assert_array_equal(s.state(0), o.state(0))
+    assert s.hllc_errors() == o.hllc_errors
