@@ -67,6 +67,9 @@ SIGNATURES = {
     "hf_uns_frames_enable": (_i, [_p, _i]),
     "hf_uns_frames_pending": (_i, [_p, C.POINTER(_i64)]),
     "hf_uns_frame_pop": (_i, [_p, _p, C.POINTER(_d), C.POINTER(_i64)]),
+    "hf_uns_checkpoint_size": (_i, [_p, C.POINTER(_sz)]),
+    "hf_uns_checkpoint_save": (_i, [_p, _p, _sz]),
+    "hf_uns_checkpoint_load": (_i, [_p, _p, _sz]),
     "hf_uns_get_time": (_i, [_p, C.POINTER(_d), C.POINTER(_i64), C.POINTER(_d)]),
     "hf_uns_hllc_errors": (_i, [_p, C.POINTER(_i64)]),
     "hf_uns_stream": (_i, [_p, C.POINTER(_p)]),

@@ -840,6 +840,116 @@ int hf_uns_frames_pending(hf_uns* u, int64_t* n) {
     return HF_OK;
 }
 
+// ---- checkpoint / restart ----
+namespace {
+struct UnsCkptHeader {
+    char magic[8];
+    uint32_t version, ctrl_bytes;
+    int64_t ncells, npairs;
+    uint64_t mesh_hash;
+    double gamma, cfl, t_end;
+};
+
+// FNV-1a over the mesh connectivity and cell areas: a checkpoint of another mesh with the
+// same cell and pair counts is refused too
+uint64_t uns_mesh_hash(const hf_uns* u) {
+    uint64_t h = 1469598103934665603ull;
+    auto mix = [&h](const void* p, size_t n) {
+        const unsigned char* b = static_cast<const unsigned char*>(p);
+        for (size_t i = 0; i < n; ++i) {
+            h ^= b[i];
+            h *= 1099511628211ull;
+        }
+    };
+    mix(u->pair_start.data(), u->pair_start.size() * sizeof(int));
+    mix(u->nbr.data(), u->nbr.size() * sizeof(int));
+    mix(u->area.data(), u->area.size() * sizeof(double));
+    return h;
+}
+const char kUnsCkptMagic[8] = {'H', 'F', 'U', 'C', 'K', 'P', '0', '1'};
+
+UnsCkptHeader uns_ckpt_header(const hf_uns* u) {
+    UnsCkptHeader h;
+    std::memset(&h, 0, sizeof h);
+    std::memcpy(h.magic, kUnsCkptMagic, 8);
+    h.version = 1;
+    h.ctrl_bytes = (uint32_t)sizeof(hf::UnsCtrl);
+    h.ncells = u->ncells;
+    h.npairs = u->pair_start.empty() ? 0 : u->pair_start.back();
+    h.mesh_hash = uns_mesh_hash(u);
+    h.gamma = u->gamma;
+    h.cfl = u->cfl;
+    h.t_end = u->t_end;
+    return h;
+}
+}  // namespace
+
+int hf_uns_checkpoint_size(const hf_uns* u, size_t* bytes) {
+    if (!u || !bytes) return HF_ERR_ARG;
+    *bytes = sizeof(UnsCkptHeader) + sizeof(hf::UnsCtrl) + 2 * (size_t)4 * u->ncells * sizeof(double);
+    return HF_OK;
+}
+
+int hf_uns_checkpoint_save(hf_uns* u, void* buf, size_t bytes) {
+    if (!u || !u->dctrl || !buf) return HF_ERR_ARG;
+    size_t need = 0;
+    hf_uns_checkpoint_size(u, &need);
+    if (bytes < need) return ufail(u, HF_ERR_ARG, "checkpoint buffer too small");
+    hf::UnsCtrl C;
+    UCK(cudaStreamSynchronize(u->stream));
+    UCK(cudaMemcpy(&C, u->dctrl, sizeof C, cudaMemcpyDeviceToHost));
+    if (u->ring_slots > 0 && C.captured != u->drained)
+        return ufail(u, HF_ERR_STATE, "pop the pending frames before a checkpoint");
+    const UnsCkptHeader h = uns_ckpt_header(u);
+    char* p = static_cast<char*>(buf);
+    std::memcpy(p, &h, sizeof h);
+    p += sizeof h;
+    std::memcpy(p, &C, sizeof C);
+    p += sizeof C;
+    const size_t n = (size_t)4 * u->ncells * sizeof(double);
+    for (int k = 0; k < 2; ++k) {
+        UCK(cudaMemcpy(p, u->dm.U[k], n, cudaMemcpyDeviceToHost));
+        p += n;
+    }
+    return HF_OK;
+}
+
+int hf_uns_checkpoint_load(hf_uns* u, const void* buf, size_t bytes) {
+    if (!u || !u->dctrl || !buf) return HF_ERR_ARG;
+    size_t need = 0;
+    hf_uns_checkpoint_size(u, &need);
+    if (bytes < need) return ufail(u, HF_ERR_ARG, "checkpoint too short for this mesh");
+    UnsCkptHeader got;
+    std::memcpy(&got, buf, sizeof got);
+    const UnsCkptHeader want = uns_ckpt_header(u);
+    if (std::memcmp(got.magic, kUnsCkptMagic, 8) != 0 || got.version != want.version)
+        return ufail(u, HF_ERR_PARSE, "not an unstructured checkpoint of this format version");
+    if (std::memcmp(&got, &want, sizeof got) != 0)
+        return ufail(u, HF_ERR_ARG, "checkpoint was taken from a different case, mesh or build");
+    const char* p = static_cast<const char*>(buf) + sizeof got;
+    hf::UnsCtrl C, cur;
+    std::memcpy(&C, p, sizeof C);
+    p += sizeof C;
+    UCK(cudaStreamSynchronize(u->stream));
+    UCK(cudaMemcpy(&cur, u->dctrl, sizeof cur, cudaMemcpyDeviceToHost));
+    // the frame ring belongs to this context: keep its configuration, start it empty
+    C.frames = cur.frames;
+    C.ring_slots = cur.ring_slots;
+    C.frame_interval = cur.frame_interval;
+    C.captured = C.drained = 0;
+    C.clamp = 0;
+    C.done = 0;
+    C.err = 0;
+    u->drained = 0;
+    const size_t n = (size_t)4 * u->ncells * sizeof(double);
+    for (int k = 0; k < 2; ++k) {
+        UCK(cudaMemcpy(u->dm.U[k], p, n, cudaMemcpyHostToDevice));
+        p += n;
+    }
+    UCK(cudaMemcpy(u->dctrl, &C, sizeof C, cudaMemcpyHostToDevice));
+    return HF_OK;
+}
+
 int hf_uns_frame_pop(hf_uns* u, double* cons, double* t, int64_t* index) {
     if (!u || !u->dctrl) return HF_ERR_ARG;
     if (u->ring_slots == 0) return ufail(u, HF_ERR_STATE, "frames are not enabled");

@@ -164,6 +164,20 @@ class UnsSolver:
         self.frame_paths = paths
         return total
 
+    # --- checkpoint / restart ---
+    def checkpoint(self) -> bytes:
+        """The whole simulation state as bytes; ``restore`` on a solver of the same case and
+        mesh continues bit for bit."""
+        n = C.c_size_t()
+        check(lib().hf_uns_checkpoint_size(self._h, C.byref(n)), self._h, _MSG)
+        buf = np.empty(n.value, np.uint8)
+        check(lib().hf_uns_checkpoint_save(self._h, buf.ctypes.data, n.value), self._h, _MSG)
+        return buf.tobytes()
+
+    def restore(self, blob: bytes):
+        buf = np.frombuffer(blob, np.uint8)
+        check(lib().hf_uns_checkpoint_load(self._h, buf.ctypes.data, buf.size), self._h, _MSG)
+
     def stream(self) -> int:
         s = C.c_void_p()
         check(lib().hf_uns_stream(self._h, C.byref(s)), self._h, _MSG)

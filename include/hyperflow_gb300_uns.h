@@ -79,6 +79,15 @@ int hf_uns_frames_enable(hf_uns* u, int ring_slots);
 int hf_uns_frames_pending(hf_uns* u, int64_t* n);
 int hf_uns_frame_pop(hf_uns* u, double* cons, double* t, int64_t* index);
 
+/* Checkpoint / restart of the whole unstructured simulation state (both cell-state buffers and
+ * the control block: t, TimeStep call count, step parity, the CFL minimum, frame cadence), as
+ * hf_checkpoint_* of hyperflow_gb300.h.  No counterpart in the reference.  A run restored into a
+ * context created from the same case and mesh continues bit for bit; a blob of another case,
+ * mesh or build is refused (HF_ERR_ARG / HF_ERR_PARSE). */
+int hf_uns_checkpoint_size(const hf_uns* u, size_t* bytes);
+int hf_uns_checkpoint_save(hf_uns* u, void* buf, size_t bytes);
+int hf_uns_checkpoint_load(hf_uns* u, const void* buf, size_t bytes);
+
 int hf_uns_get_time(hf_uns* u, double* t, int64_t* calls, double* last_dt);
 int hf_uns_hllc_errors(hf_uns* u, int64_t* count);
 int hf_uns_stream(hf_uns* u, void** stream);

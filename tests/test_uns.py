@@ -145,3 +145,37 @@ def test_uns_edge_mode_within_tolerance(port_lib):
     rel = np.abs(V - U) / scale
     assert rel.max() <= 1e-10, rel.max()
     s.set_edge_mode(False)   # the parity path is still available on the same solver
+
+
+@pytest.mark.gpu
+def test_uns_gpu_checkpoint_restart_is_bit_exact():
+    """A run restored from a checkpoint taken inside the start-up calls continues bit for bit,
+    through the device loop and the per-step API; another mesh's checkpoint is refused."""
+    from hyperflow_gb300 import HyperFlowError, UnsSolver, meshgen
+    g = load("tri_hole_3k")
+    text = meshgen.hmsh_text(g["verts"], g["codes"])
+    a = UnsSolver(g["case"], mesh_text=text)
+    a.run(4)
+    blob = a.checkpoint()
+    a.run(40)
+    b = UnsSolver(g["case"], mesh_text=text)
+    b.restore(blob)
+    b.run(40)
+    assert a.time() == b.time()
+    np.testing.assert_array_equal(a.state(), b.state())
+    b.restore(blob)
+    dts = []
+    for _ in range(5):
+        dt = b.calculate_time_step()
+        b.advance(dt)
+        dts.append(dt)
+    a.restore(blob)
+    for dt in dts:
+        assert a.calculate_time_step() == dt
+        a.advance(dt)
+    np.testing.assert_array_equal(a.state(), b.state())
+    other = UnsSolver(g["case"], mesh_text=meshgen.hmsh_text(*meshgen.jittered_hole_mesh(4000, seed=1)))
+    with pytest.raises(HyperFlowError):
+        other.restore(blob)
+    with pytest.raises(HyperFlowError):
+        a.restore(blob[:64])
