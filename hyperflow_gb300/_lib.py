@@ -34,6 +34,7 @@ SIGNATURES = {
     "hf_advance": (_i, [_p, _d]),
     "hf_step": (_i, [_p, C.POINTER(_d)]),
     "hf_step_io": (_i, [_p, _p, _p, C.POINTER(_d)]),
+    "hf_host_mapped": (_i, [_p, C.POINTER(_i)]),
     "hf_run": (_i, [_p, _i64, _i, _i, C.POINTER(_i64)]),
     "hf_get_time": (_i, [_p, C.POINTER(_d), C.POINTER(_i64), C.POINTER(_d)]),
     "hf_hllc_errors": (_i, [_p, C.POINTER(_i64)]),

@@ -662,6 +662,28 @@ int hf_advance(hf_ctx* ctx, double dt) {
 // interior TimeStep terms, as hf_set_state), one step (as hf_step), every block downloaded --
 // each block's download on a second stream as soon as its own update is done, so it overlaps
 // the updates of the blocks after it.  No synchronisation between the pieces.
+// true when every pointer is 8-byte aligned host memory that kernels may address as it is
+// (pinned by cudaHostAlloc / cudaHostRegister: the device pointer is the host pointer)
+static bool host_mapped(const double* const* p, int n) {
+    for (int b = 0; b < n; ++b) {
+        if (reinterpret_cast<uintptr_t>(p[b]) % 8 != 0) return false;
+        cudaPointerAttributes a;
+        if (cudaPointerGetAttributes(&a, p[b]) != cudaSuccess) {
+            cudaGetLastError();
+            return false;
+        }
+        if (a.type != cudaMemoryTypeHost || a.devicePointer != static_cast<const void*>(p[b])) return false;
+    }
+    return true;
+}
+
+int hf_host_mapped(const void* p, int* mapped) {
+    if (!mapped) return HF_ERR_ARG;
+    const double* q = static_cast<const double*>(p);
+    *mapped = p && host_mapped(&q, 1) ? 1 : 0;
+    return HF_OK;
+}
+
 int hf_step_io(hf_ctx* ctx, const double* const* in, double* const* out, double* dt) {
     if (!ctx || !in || !out) return HF_ERR_ARG;
     for (int b = 0; b < ctx->nblocks; ++b)
@@ -674,6 +696,33 @@ int hf_step_io(hf_ctx* ctx, const double* const* in, double* const* out, double*
     }
     const long long step = read_step(ctx);
     const int p = (int)(step & 1);
+    if (host_mapped(in, ctx->nblocks) && host_mapped((const double* const*)out, ctx->nblocks)) {
+        // pinned host memory: the kernels read and write it over the link themselves -- one
+        // pass uploads each block into both buffers with its TimeStep terms, and every stencil
+        // stores its updated cells to the host as it goes, so no download trails the last
+        // block's update
+        for (int b = 0; b < ctx->nblocks; ++b) {
+            const BlockHost& B = ctx->blocks[b];
+            CK(cudaMemsetAsync(&ctx->dctrl->int_s[p][b][0], 0, 2 * sizeof(unsigned long long), ctx->stream));
+            CK(hf::launch_upload(ctx->dctrl, ctx->dmesh, b, B.tx, B.ty, p, in[b], ctx->stream));
+        }
+        int clamp = 0;
+        CK(cudaMemcpyAsync(&ctx->dctrl->clamp, &clamp, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+        CK(hf::launch_bc_fill(ctx->dctrl, ctx->dmesh, ctx->side_len, ctx->nblocks, ctx->stream));
+        CK(hf::launch_ghost_cfl(ctx->dctrl, ctx->dmesh, ctx->hmesh.total_ghost, ctx->stream));
+        for (int b = 0; b < ctx->nblocks; ++b)
+            CK(hf::launch_ghost_store(ctx->dmesh, b, ctx->blocks[b].tx, ctx->blocks[b].ny, ctx->ghost, p,
+                                      out[b], ctx->stream));
+        for (int b = 0; b < ctx->nblocks; ++b) {
+            const BlockHost& B = ctx->blocks[b];
+            CK(hf::launch_stencil(ctx->dctrl, ctx->dmesh, b, B.nx, B.ny, ctx->scheme, ctx->limiter,
+                                  &ctx->tmap[b][0], &ctx->tmap[b][1], ctx->stream, out[b]));
+        }
+        CK(hf::launch_finalize(ctx->dctrl, ctx->stream));
+        if (dt) CK(cudaMemcpyAsync(dt, &ctx->dctrl->dt, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+        return HF_OK;
+    }
     for (int b = 0; b < ctx->nblocks; ++b) {
         const BlockHost& B = ctx->blocks[b];
         const hf::BlockDev& D = ctx->hmesh.b[b];

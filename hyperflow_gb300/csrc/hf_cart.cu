@@ -210,6 +210,70 @@ __global__ void __launch_bounds__(kRedThreads) interior_cfl_kernel(Ctrl* __restr
     block_max2_atomic<kRedThreads>(mx, my, &c->int_s[parity][b][0], &c->int_s[parity][b][1]);
 }
 
+// A block's whole state ([4][total_y][total_x], ghosts included) read from host memory the GPU
+// maps (pinned), written into both buffers, with the TimeStep terms of the interior cells -- the
+// upload, buffer copy and interior_cfl of a host-buffer step in one pass over the link.
+__global__ void __launch_bounds__(kRedThreads) upload_kernel(Ctrl* __restrict__ c, const MeshDev* __restrict__ m,
+                                                             int b, int parity, const double* __restrict__ hin) {
+    const BlockDev& B = m->b[b];
+    const int g = m->ghost;
+    const size_t plane = (size_t)B.ty * B.pitch, hplane = (size_t)B.ty * B.tx;
+    double* __restrict__ U0 = B.buf[parity];
+    double* __restrict__ U1 = B.buf[parity ^ 1];
+    const double gm = c->gamma, g1 = c->g1;
+    double mx = 0.0, my = 0.0;
+    const long long n = (long long)B.tx * B.ty;
+    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n;
+         k += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(k % B.tx), j = (int)(k / B.tx);
+        const size_t o = (size_t)j * B.pitch + i;
+        double u[4];
+#pragma unroll
+        for (int v = 0; v < 4; ++v) u[v] = __ldcs(&hin[v * hplane + (size_t)k]);
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+            U0[v * plane + o] = u[v];
+            U1[v * plane + o] = u[v];
+        }
+        if (i >= g && i < B.tx - g && j >= g && j < B.ty - g) {
+            double sx, sy;
+            wave_terms(gm, g1, u[0], u[1], u[2], u[3], sx, sy);
+            mx = nmax(mx, sx);
+            my = nmax(my, sy);
+        }
+    }
+    block_max2_atomic<kRedThreads>(mx, my, &c->int_s[parity][b][0], &c->int_s[parity][b][1]);
+}
+
+// The ghost cells of the updated buffer (filled this step, never written by the stencil) into
+// host memory the GPU maps: with the stencil's own host stores, the whole block downloaded.
+__global__ void __launch_bounds__(256) ghost_store_kernel(const MeshDev* __restrict__ m, int b, int parity,
+                                                          double* __restrict__ hout) {
+    const BlockDev& B = m->b[b];
+    const int g = m->ghost;
+    const size_t plane = (size_t)B.ty * B.pitch, hplane = (size_t)B.ty * B.tx;
+    const double* __restrict__ U = B.buf[parity ^ 1];
+    const long long rows = (long long)g * B.tx;          // cells in the g bottom (or top) rows
+    const long long n = 2 * rows + 2LL * g * B.ny;       // + g columns each side of the interior rows
+    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n;
+         k += (long long)gridDim.x * blockDim.x) {
+        int i, j;
+        if (k < 2 * rows) {
+            const long long r = k < rows ? k : k - rows;
+            i = (int)(r % B.tx);
+            j = (int)(r / B.tx) + (k < rows ? 0 : B.ty - g);
+        } else {
+            const long long r = k - 2 * rows;
+            const int col = (int)(r % (2 * g));
+            j = g + (int)(r / (2 * g));
+            i = col < g ? col : B.tx - 2 * g + col;
+        }
+        const size_t o = (size_t)j * B.pitch + i, h = (size_t)j * B.tx + i;
+#pragma unroll
+        for (int v = 0; v < 4; ++v) __stcs(&hout[v * hplane + h], U[v * plane + o]);
+    }
+}
+
 __global__ void set_dt_kernel(Ctrl* c, double dt) { c->dt = dt; }
 
 // Frames of this step into the device ring: the interior of every block, SoA per block,
@@ -308,7 +372,8 @@ template <int TX, int TY, int LIM, int NT>
 // of the integer sequences' latency than 16 (measured faster despite a few spilled registers)
 __global__ void __launch_bounds__(NT, 3) mh_kernel(Ctrl* __restrict__ c, const MeshDev* __restrict__ m,
                                                 int b, const __grid_constant__ CUtensorMap tm0,
-                                                const __grid_constant__ CUtensorMap tm1) {
+                                                const __grid_constant__ CUtensorMap tm1,
+                                                double* __restrict__ hout) {
     using L = MhLayout<TX, TY>;
     extern __shared__ __align__(1024) double smem[];
     double* sU = smem + L::U_OFF;
@@ -357,6 +422,7 @@ __global__ void __launch_bounds__(NT, 3) mh_kernel(Ctrl* __restrict__ c, const M
             for (int v = 0; v < 4; ++v) {
                 un[v] = mh_update<TX, TY>(sU, sF, sG, v, ox, oy, dt, one_dx, one_dy);
                 out[v * plane + o] = un[v];
+                if (hout) __stcs(&hout[((size_t)v * B.ty + gyy + 2) * B.tx + gxx + 2], un[v]);
             }
             double sx, sy;
             wave_terms(g, g1, un[0], un[1], un[2], un[3], sx, sy);
@@ -388,7 +454,8 @@ template <int TX, int TY, int NT>
 __global__ void __launch_bounds__(NT) godunov_kernel(Ctrl* __restrict__ c,
                                                      const MeshDev* __restrict__ m, int b,
                                                      const __grid_constant__ CUtensorMap tm0,
-                                                     const __grid_constant__ CUtensorMap tm1) {
+                                                     const __grid_constant__ CUtensorMap tm1,
+                                                     double* __restrict__ hout) {
     using L = GoLayout<TX, TY>;
     extern __shared__ __align__(1024) double smem[];
     double* sU = smem + L::U_OFF;
@@ -478,6 +545,7 @@ __global__ void __launch_bounds__(NT) godunov_kernel(Ctrl* __restrict__ c,
                                              sG[(v * (TY + 1) + oy + 1) * TX + ox]));
                 un[v] = dt * Lv + sU[v * L::NC + (oy + 1) * L::UX + ox + 1];
                 out[v * plane + o] = un[v];
+                if (hout) __stcs(&hout[((size_t)v * B.ty + gyy + 1) * B.tx + gxx + 1], un[v]);
             }
             double sx, sy;
             wave_terms(g, g1, un[0], un[1], un[2], un[3], sx, sy);
@@ -586,20 +654,36 @@ cudaError_t launch_finalize(Ctrl* c, cudaStream_t s) {
 }
 
 cudaError_t launch_stencil(Ctrl* c, const MeshDev* m, int b, int nx, int ny, int scheme, int limiter,
-                           const CUtensorMap* tm0, const CUtensorMap* tm1, cudaStream_t s) {
+                           const CUtensorMap* tm0, const CUtensorMap* tm1, cudaStream_t s, double* hout) {
     if (scheme == 0) {
         int tiles = ((nx + kGoTX - 1) / kGoTX) * ((ny + kGoTY - 1) / kGoTY);
         godunov_kernel<kGoTX, kGoTY, kGoNT>
-            <<<tiles, kGoNT, GoLayout<kGoTX, kGoTY>::BYTES, s>>>(c, m, b, *tm0, *tm1);
+            <<<tiles, kGoNT, GoLayout<kGoTX, kGoTY>::BYTES, s>>>(c, m, b, *tm0, *tm1, hout);
     } else {
         int tiles = ((nx + kMhTX - 1) / kMhTX) * ((ny + kMhTY - 1) / kMhTY);
         if (limiter == 0)
             mh_kernel<kMhTX, kMhTY, 0, kMhNT>
-                <<<tiles, kMhNT, MhLayout<kMhTX, kMhTY>::BYTES, s>>>(c, m, b, *tm0, *tm1);
+                <<<tiles, kMhNT, MhLayout<kMhTX, kMhTY>::BYTES, s>>>(c, m, b, *tm0, *tm1, hout);
         else
             mh_kernel<kMhTX, kMhTY, 1, kMhNT>
-                <<<tiles, kMhNT, MhLayout<kMhTX, kMhTY>::BYTES, s>>>(c, m, b, *tm0, *tm1);
+                <<<tiles, kMhNT, MhLayout<kMhTX, kMhTY>::BYTES, s>>>(c, m, b, *tm0, *tm1, hout);
     }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_upload(Ctrl* c, const MeshDev* m, int b, int tx, int ty, int parity, const double* hin,
+                          cudaStream_t s) {
+    long long want = ((long long)tx * ty + kRedThreads - 1) / kRedThreads;
+    int grid = (int)(want < 1 ? 1 : (want > 8 * 152 ? 8 * 152 : want));
+    upload_kernel<<<grid, kRedThreads, 0, s>>>(c, m, b, parity, hin);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_ghost_store(const MeshDev* m, int b, int tx, int ny, int ghost, int parity, double* hout,
+                               cudaStream_t s) {
+    long long n = 2LL * ghost * (tx + ny);
+    int grid = (int)((n + 255) / 256);
+    ghost_store_kernel<<<grid < 1 ? 1 : grid, 256, 0, s>>>(m, b, parity, hout);
     return cudaGetLastError();
 }
 

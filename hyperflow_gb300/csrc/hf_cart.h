@@ -59,8 +59,18 @@ cudaError_t launch_coarsen(const Ctrl* c, const MeshDev* m, int b, int k, long l
                            cudaStream_t s);
 // this step's frames (if any) into the ring; between the stencils and launch_finalize
 cudaError_t launch_frame_copy(Ctrl* c, const MeshDev* m, const FrameRing& ring, cudaStream_t s);
+// hout (optional): host memory the GPU maps, [4][total_y][total_x]; the stencil also stores its
+// updated interior cells there
 cudaError_t launch_stencil(Ctrl* c, const MeshDev* m, int b, int nx, int ny, int scheme, int limiter,
-                           const CUtensorMap* tm0, const CUtensorMap* tm1, cudaStream_t s);
+                           const CUtensorMap* tm0, const CUtensorMap* tm1, cudaStream_t s,
+                           double* hout = nullptr);
+// host-buffer steps over mapped host memory: block b's state [4][total_y][total_x] into both
+// buffers with the interior TimeStep terms (int_s[parity][b] zeroed before), and, after the
+// ghost fill, the updated buffer's ghost cells back out
+cudaError_t launch_upload(Ctrl* c, const MeshDev* m, int b, int tx, int ty, int parity, const double* hin,
+                          cudaStream_t s);
+cudaError_t launch_ghost_store(const MeshDev* m, int b, int tx, int ny, int ghost, int parity, double* hout,
+                               cudaStream_t s);
 // halo-tile box of the stencil for the scheme (TMA box = tile + 2*ghost per axis)
 StencilTiles stencil_tiles(int scheme);
 cudaError_t stencil_prepare();   // sets the large dynamic shared-memory opt-ins once

@@ -109,8 +109,9 @@ class CartSolver:
 
     def step_io(self, ins, outs=None) -> float:
         """One step with every block's state in host arrays (SoA [4][total_y][total_x], ghosts
-        included, C-contiguous float64; pinned memory for full speed): upload, step, download
-        into outs (default: in place).  Returns the step's dt."""
+        included, C-contiguous float64): upload, step, download into outs (default: in place).
+        Pinned arrays (``host_mapped``) are read and written by the kernels directly; others
+        are copied.  Returns the step's dt."""
         outs = ins if outs is None else outs
         assert len(ins) == len(outs) == self.nblocks
         for a in list(ins) + list(outs):
@@ -120,6 +121,13 @@ class CartSolver:
         dt = C.c_double()
         check(lib().hf_step_io(self._h, pin, pout, C.byref(dt)), self._h)
         return dt.value
+
+    @staticmethod
+    def host_mapped(a: np.ndarray) -> bool:
+        """True when the kernels address this host array directly (pinned memory)."""
+        m = C.c_int()
+        check(lib().hf_host_mapped(a.ctypes.data, C.byref(m)))
+        return bool(m.value)
 
     def run(self, n: int, clamp_t_end: bool = False, graph: bool = True) -> int:
         done = C.c_int64()

@@ -87,10 +87,15 @@ int hf_step(hf_ctx* ctx, double* dt);
  * between steps (the reference's own per-step set_fields / get_fields pattern,
  * simulation.cpp:106-110): uploads every block (in[b], SoA [4][total_y][total_x] with ghosts,
  * as hf_set_state), runs one step without the t_end clamp (hf_step), and downloads every block's
- * new state into out[b] -- each download starts as soon as that block's update is done, so it
- * overlaps the updates of the blocks after it.  in and out may be the same arrays; pinned host
- * memory gives full copy speed.  dt (optional) receives the step's dt. */
+ * new state into out[b].  in and out may be the same arrays.  dt (optional) receives the step's
+ * dt.  When every array is pinned host memory (hf_host_mapped), the kernels read and write it
+ * directly: one pass per block uploads it, and each stencil stores its updated cells to the host
+ * as it computes them, so no download trails the last block's update.  Otherwise the arrays are
+ * copied, each block's download starting as soon as its update is done. */
 int hf_step_io(hf_ctx* ctx, const double* const* in, double* const* out, double* dt);
+/* *mapped = 1 when p is 8-byte aligned host memory that the kernels address directly (pinned by
+ * cudaHostAlloc / cudaHostRegister), i.e. hf_step_io's direct path applies to it. */
+int hf_host_mapped(const void* p, int* mapped);
 
 /* Simulation::solve's loop body (simulation.cpp:81-120, frame clamps excluded) run n times
  * on the device with no host round trip per step: dt stays on the device.  clamp_t_end != 0

@@ -174,24 +174,52 @@ def test_gpu_shock_bubble_matches_oracle(port_lib):
     np.testing.assert_array_equal(s.state(0), o.state(0))
 
 
-def test_gpu_step_io_equals_upload_step_download():
-    """hf_step_io (upload, step, overlapped per-block download) against hf_set_state + hf_step
-    + hf_get_state, on the 3-block forward-facing step, several steps in a row, in place."""
-    from hyperflow_gb300 import cases
-    case = cases.forward_facing_step_case(40, limiter="VanLeer")
+def _host_arrays(like, memory):
+    if memory == "pageable":
+        return [x.copy() for x in like]
+    import torch
+    out = []
+    for x in like:
+        t = torch.empty(x.shape, dtype=torch.float64).pin_memory()
+        a = t.numpy()
+        a[...] = x
+        out.append(a)              # the array's base keeps the pinned tensor alive
+    return out
+
+
+@pytest.mark.parametrize("memory", ["pageable", "pinned", "pinned-separate-out"])
+@pytest.mark.parametrize("scheme", ["Godunov", "MUSCLHancock"])
+def test_gpu_step_io_equals_upload_step_download(memory, scheme):
+    """hf_step_io against hf_set_state + hf_step + hf_get_state on the 3-block forward-facing
+    step, several steps in a row: pageable arrays take the copy path (overlapped per-block
+    downloads); pinned arrays the direct path (the kernels read the host arrays and the
+    stencils store their cells to them), in place and into separate output arrays."""
+    from hyperflow_gb300 import CartSolver, cases
+    case = cases.forward_facing_step_case(40, scheme="Godunov") if scheme == "Godunov" else \
+        cases.forward_facing_step_case(40, limiter="VanLeer")
     a, b = _solver(case), _solver(case)
     a.run(5)
     b.run(5)                       # the same TimeStep call count (it sets the CFL factor)
-    host = [a.state(k).copy() for k in range(a.nblocks)]
+    host = _host_arrays([a.state(k) for k in range(a.nblocks)], memory.split("-")[0])
+    outs = None
+    if memory == "pinned-separate-out":
+        outs = _host_arrays([np.full_like(x, np.nan) for x in host], "pinned")
+    for x in host + (outs or []):
+        assert CartSolver.host_mapped(x) == memory.startswith("pinned")
     for _ in range(4):
         for k in range(b.nblocks):
             b.set_state(k, host[k])
         dt_b = b.step()
         want = [b.state(k) for k in range(b.nblocks)]
-        dt_a = a.step_io(host)
+        dt_a = a.step_io(host, outs)
         assert dt_a == dt_b
         for k in range(a.nblocks):
-            np.testing.assert_array_equal(host[k], want[k])
+            np.testing.assert_array_equal((outs or host)[k], want[k])
+            np.testing.assert_array_equal(a.state(k), want[k])
+        if outs is not None:
+            for k in range(a.nblocks):
+                host[k][...] = outs[k]
+                outs[k][...] = np.nan
 
 
 @pytest.mark.parametrize("scheme,limiter", [("Godunov", None), ("MUSCLHancock", "MinBee"),
