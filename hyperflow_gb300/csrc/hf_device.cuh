@@ -103,41 +103,70 @@ HF_HD void star_flux(const double* UK, const Prim& wK, double SK, double Ss,
     for (int i = 0; i < 4; ++i) F[i] = FK[i] + SK * (us[i] - UK[i]);
 }
 
-template <int DIR>
-HF_HD int hllc(const double* UL, const Prim& wL, double aL, const double* FL,
-                                    const double* UR, const Prim& wR, double aR, const double* FR,
-                                    double* F) {
+// The branches of riemann_hllc.cpp:179-211 in the reference's order.  After the supersonic-left
+// test every branch uses one side only, so that side's state, flux and wave speed are selected
+// first and one flux / one star state is formed: a warp whose faces take different branches
+// runs the star-state arithmetic once, not once per branch.  LAZY forms the side's flux from its
+// primitives (the MUSCL-Hancock and unstructured faces); otherwise FL / FR are given.
+template <int DIR, bool LAZY>
+HF_HD int hllc_sel(const double* UL, const Prim& wL, double aL, const double* FL,
+                   const double* UR, const Prim& wR, double aR, const double* FR, double* F) {
     double velL = DIR == 0 ? wL.u : wL.v;
     double velR = DIR == 0 ? wR.u : wR.v;
     double SL = smin(velL - aL, velR - aR);
     double SR = smax(velL + aL, velR + aR);
     if (ge0(SL)) {
+        if (LAZY) {
+            flux<DIR>(wL, F);
+        } else {
 #pragma unroll
-        for (int i = 0; i < 4; ++i) F[i] = FL[i];
+            for (int i = 0; i < 4; ++i) F[i] = FL[i];
+        }
         return 0;
     }
     double num = wR.p - wL.p + wL.r * velL * (SL - velL) - wR.r * velR * (SR - velR);
     double den = wL.r * (SL - velL) - wR.r * (SR - velR);
     double Ss = div_rn(num, den);
-    if (le0(SL) && ge0(Ss)) {
-        star_flux<DIR>(UL, wL, SL, Ss, FL, F);
-        return 0;
-    }
-    if (le0(Ss) && ge0(SR)) {
-        star_flux<DIR>(UR, wR, SR, Ss, FR, F);
-        return 0;
-    }
-    if (le0(SR)) {
+    const bool star_l = le0(SL) && ge0(Ss);
+    const bool star_r = !star_l && le0(Ss) && ge0(SR);
+    const bool right = !star_l && !star_r && le0(SR);
+    if (!(star_l || star_r || right)) {
 #pragma unroll
-        for (int i = 0; i < 4; ++i) F[i] = FR[i];
+        for (int i = 0; i < 4; ++i) F[i] = 0.0;
+        return 1;
+    }
+    Prim w;
+    w.r = star_l ? wL.r : wR.r;
+    w.u = star_l ? wL.u : wR.u;
+    w.v = star_l ? wL.v : wR.v;
+    w.p = star_l ? wL.p : wR.p;
+    w.q = star_l ? wL.q : wR.q;
+    w.Et = star_l ? wL.Et : wR.Et;
+    double UK[4], FK[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) UK[i] = star_l ? UL[i] : UR[i];
+    if (LAZY) {
+        flux<DIR>(w, FK);
+    } else {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) FK[i] = star_l ? FL[i] : FR[i];
+    }
+    if (right) {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) F[i] = FK[i];
         return 0;
     }
-#pragma unroll
-    for (int i = 0; i < 4; ++i) F[i] = 0.0;
-    return 1;
+    star_flux<DIR>(UK, w, star_l ? SL : SR, Ss, FK, F);
+    return 0;
 }
 
-// HLLC from two conservative states (computes primitives, sound speeds, fluxes)
+template <int DIR>
+HF_HD int hllc(const double* UL, const Prim& wL, double aL, const double* FL,
+               const double* UR, const Prim& wR, double aR, const double* FR, double* F) {
+    return hllc_sel<DIR, false>(UL, wL, aL, FL, UR, wR, aR, FR, F);
+}
+
+// HLLC from two conservative states (computes primitives, sound speeds, the used flux)
 template <int DIR>
 HF_HD int hllc_cons(double g, double g1, const double* UL, const double* UR,
                                          double* F) {
@@ -146,10 +175,7 @@ HF_HD int hllc_cons(double g, double g1, const double* UL, const double* UR,
     // calc_wave_speeds_direct_min_max (127-150): sqrt(gamma * p / rho)
     double aL = sound(g, wL.r, wL.p);
     double aR = sound(g, wR.r, wR.p);
-    double FL[4], FR[4];
-    flux<DIR>(wL, FL);
-    flux<DIR>(wR, FR);
-    return hllc<DIR>(UL, wL, aL, FL, UR, wR, aR, FR, F);
+    return hllc_sel<DIR, true>(UL, wL, aL, nullptr, UR, wR, aR, nullptr, F);
 }
 
 // ------------------------------------------------------------------------------
