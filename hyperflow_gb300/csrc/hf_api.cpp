@@ -343,7 +343,7 @@ int make_tmaps(hf_ctx* ctx) {
         for (int k = 0; k < 2; ++k) {
             cuuint64_t dims[3] = {(cuuint64_t)B.tx, (cuuint64_t)B.ty, 4};
             cuuint64_t strides[2] = {(cuuint64_t)B.pitch * 8, (cuuint64_t)B.pitch * B.ty * 8};
-            cuuint32_t box[3] = {(cuuint32_t)(t.tx + 2 * ctx->ghost), (cuuint32_t)(t.ty + 2 * ctx->ghost), 4};
+            cuuint32_t box[3] = {(cuuint32_t)t.box_x, (cuuint32_t)t.box_y, 4};
             cuuint32_t es[3] = {1, 1, 1};
             CUresult r = enc(&ctx->tmap[b][k], CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3,
                              ctx->hmesh.b[b].buf[k], dims, strides, box, es,

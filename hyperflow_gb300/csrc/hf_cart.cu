@@ -481,7 +481,10 @@ __global__ void __launch_bounds__(NT) godunov_kernel(Ctrl* __restrict__ c,
     const double one_dx = sc[0], one_dy = sc[1];
 
 #define Q(k, cell) sQ[(k) * L::NC + (cell)]
+    // cells beyond the first ghost layer and faces beyond the last face are skipped: no in-block
+    // cell reads them, and their zero-filled states would only take the slow division paths
     for (int cell = threadIdx.x; cell < L::NC; cell += NT) {
+        if (x0 - 1 + cell % L::UX > B.nx || y0 - 1 + cell / L::UX > B.ny) continue;
         Prim w = to_prim(g1, sU[cell], sU[L::NC + cell], sU[2 * L::NC + cell], sU[3 * L::NC + cell]);
         double fx[4], fy[4];
         flux<0>(w, fx);
@@ -504,6 +507,7 @@ __global__ void __launch_bounds__(NT) godunov_kernel(Ctrl* __restrict__ c,
     // x faces: face f of row r sits between tile cells (f-1, r) and (f, r)
     for (int it = threadIdx.x; it < (TX + 1) * TY; it += NT) {
         const int fx = it % (TX + 1), fy = it / (TX + 1);
+        if (x0 + fx > B.nx || y0 + fy >= B.ny) continue;
         const int cl = (fy + 1) * L::UX + fx, cr = cl + 1;
         double UL[4], UR[4], FL[4], FR[4], F[4], aL, aR;
         Prim wL, wR;
@@ -516,6 +520,7 @@ __global__ void __launch_bounds__(NT) godunov_kernel(Ctrl* __restrict__ c,
     }
     for (int it = threadIdx.x; it < TX * (TY + 1); it += NT) {
         const int gx = it % TX, gy = it / TX;
+        if (x0 + gx >= B.nx || y0 + gy > B.ny) continue;
         const int cb = gy * L::UX + gx + 1, ct = cb + L::UX;
         double UB[4], UT[4], FB[4], FT[4], F[4], aB, aT;
         Prim wB, wT;
@@ -564,7 +569,7 @@ constexpr int kMhTX = 32, kMhTY = 12, kMhNT = 256;
 constexpr int kGoTX = 32, kGoTY = 14, kGoNT = 256;
 
 StencilTiles stencil_tiles(int scheme) {
-    return scheme == 0 ? StencilTiles{kGoTX, kGoTY} : StencilTiles{kMhTX, kMhTY};
+    return scheme == 0 ? StencilTiles{kGoTX + 2, kGoTY + 2} : StencilTiles{kMhTX + 4, kMhTY + 4};
 }
 
 cudaError_t stencil_prepare() {

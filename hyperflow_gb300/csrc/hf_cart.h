@@ -42,7 +42,7 @@ struct FrameRing {
 };
 
 struct StencilTiles {
-    int tx, ty;   // output cells per CTA tile
+    int box_x, box_y;   // the stencil's TMA box per variable plane (tile + halo)
 };
 
 // launchers (all asynchronous on `s`)
@@ -71,7 +71,7 @@ cudaError_t launch_upload(Ctrl* c, const MeshDev* m, int b, int tx, int ty, int 
                           cudaStream_t s);
 cudaError_t launch_ghost_store(const MeshDev* m, int b, int tx, int ny, int ghost, int parity, double* hout,
                                cudaStream_t s);
-// halo-tile box of the stencil for the scheme (TMA box = tile + 2*ghost per axis)
+// TMA box of the stencil for the scheme
 StencilTiles stencil_tiles(int scheme);
 cudaError_t stencil_prepare();   // sets the large dynamic shared-memory opt-ins once
 

@@ -31,6 +31,54 @@ __device__ __forceinline__ bool owned_face(int gf, int lf, int T, int n, int gr,
     return gr < nr && gf <= n && (lf < T || gf == n);
 }
 
+// One cell of the half-step predictor along DIR: limited slopes of the four variables from the
+// cell and its two neighbours (u points at the cell's variable 0; plane and stride step to the
+// next variable and the next cell along DIR), the extrapolated face states, their fluxes and the
+// evolved states.  The minus-side state goes to lo[v * los], the plus-side one to hi[v * his].
+template <int DIR, int LIM>
+__device__ __forceinline__ void mh_predict(const double* __restrict__ u, int plane, int stride, double g1,
+                                           double h, double* __restrict__ lo, int los,
+                                           double* __restrict__ hi, int his) {
+    double e0[4], e1[4];
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+        const double* q = u + v * plane;
+        const double u0 = q[0];
+        const double s = slope<LIM>(q[-stride], u0, q[stride]);
+        const double hs = half(s);
+        e0[v] = u0 - hs;
+        e1[v] = u0 + hs;
+    }
+    Prim w0 = to_prim(g1, e0[0], e0[1], e0[2], e0[3]);
+    Prim w1 = to_prim(g1, e1[0], e1[1], e1[2], e1[3]);
+    double f0[4], f1[4];
+    flux<DIR>(w0, f0);
+    flux<DIR>(w1, f1);
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+        const double d = h * (f0[v] - f1[v]);
+        lo[v * los] = e0[v] + d;
+        hi[v * his] = e1[v] + d;
+    }
+}
+
+// One face along DIR: HLLC between the evolved states l[v * ls] (minus side) and r[v * rs];
+// the flux goes to f[v * fs].  Returns 1 for the zero-flux fallback.
+template <int DIR>
+__device__ __forceinline__ int mh_face(const double* __restrict__ l, int ls, const double* __restrict__ r,
+                                       int rs, double g, double g1, double* __restrict__ f, int fs) {
+    double UL[4], UR[4], F[4];
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+        UL[v] = l[v * ls];
+        UR[v] = r[v * rs];
+    }
+    const int bad = hllc_cons<DIR>(g, g1, UL, UR, F);
+#pragma unroll
+    for (int v = 0; v < 4; ++v) f[v * fs] = F[v];
+    return bad;
+}
+
 // Computes sF and sG from sU.  Ends with __syncthreads().  Returns the number of owned
 // faces whose HLLC took the zero-flux branch (tile origin x0, y0 in interior cells).
 template <int TX, int TY, int NT, int LIM>
@@ -39,90 +87,44 @@ __device__ __forceinline__ int mh_tile_fluxes(const double* __restrict__ sU, dou
                                               double g, double g1, double hdx, double hdy, int x0,
                                               int y0, int nx, int ny) {
     using L = MhTile<TX, TY>;
+    constexpr int PL = L::UY * L::UX;
     int herr = 0;
+    // Items past the block (cells beyond the first ghost layer, faces beyond the last face) are
+    // skipped: no in-block cell reads them, and their zero-filled states would only take the
+    // slow special-operand division paths.
     // x phase: slopes, extrapolation, half-step predictor of the x face pair, cells -1..TX
     for (int it = threadIdx.x; it < L::AXN; it += NT) {
         const int lx = it % (TX + 2), ly = it / (TX + 2);
-        const int sx = lx + 1, sy = ly + 2;
-        double e0[4], e1[4];
-#pragma unroll
-        for (int v = 0; v < 4; ++v) {
-            const double* row = sU + (v * L::UY + sy) * L::UX;
-            const double u0 = row[sx];
-            const double s = slope<LIM>(row[sx - 1], u0, row[sx + 1]);
-            const double hs = half(s);
-            e0[v] = u0 - hs;
-            e1[v] = u0 + hs;
-        }
-        Prim w0 = to_prim(g1, e0[0], e0[1], e0[2], e0[3]);
-        Prim w1 = to_prim(g1, e1[0], e1[1], e1[2], e1[3]);
-        double f0[4], f1[4];
-        flux<0>(w0, f0);
-        flux<0>(w1, f1);
-#pragma unroll
-        for (int v = 0; v < 4; ++v) {
-            const double d = hdx * (f0[v] - f1[v]);
-            sA[(0 * 4 + v) * L::AN + it] = e0[v] + d;
-            sA[(1 * 4 + v) * L::AN + it] = e1[v] + d;
-        }
+        if (x0 - 1 + lx > nx || y0 + ly >= ny) continue;
+        mh_predict<0, LIM>(sU + (ly + 2) * L::UX + lx + 1, PL, 1, g1, hdx, sA + it, L::AN,
+                           sA + 4 * L::AN + it, L::AN);
     }
     __syncthreads();
     // x faces 0..TX of each tile row (face f is the left face of output cell f)
     for (int it = threadIdx.x; it < (TX + 1) * TY; it += NT) {
         const int fx = it % (TX + 1), fy = it / (TX + 1);
+        if (x0 + fx > nx || y0 + fy >= ny) continue;
         const int al = fy * (TX + 2) + fx;
-        double UL[4], UR[4], F[4];
-#pragma unroll
-        for (int v = 0; v < 4; ++v) {
-            UL[v] = sA[(1 * 4 + v) * L::AN + al];
-            UR[v] = sA[(0 * 4 + v) * L::AN + al + 1];
-        }
-        const int bad = hllc_cons<0>(g, g1, UL, UR, F);
+        const int bad = mh_face<0>(sA + 4 * L::AN + al, L::AN, sA + al + 1, L::AN, g, g1,
+                                   sF + fy * (TX + 1) + fx, TY * (TX + 1));
         herr += bad && owned_face(x0 + fx, fx, TX, nx, y0 + fy, ny);
-#pragma unroll
-        for (int v = 0; v < 4; ++v) sF[(v * TY + fy) * (TX + 1) + fx] = F[v];
     }
     __syncthreads();
     // y phase, cells -1..TY of each tile column
     for (int it = threadIdx.x; it < L::AYN; it += NT) {
         const int lx = it % TX, ly = it / TX;
-        const int sx = lx + 2, sy = ly + 1;
-        double e2[4], e3[4];
-#pragma unroll
-        for (int v = 0; v < 4; ++v) {
-            const double* col = sU + (v * L::UY + sy) * L::UX + sx;
-            const double u0 = col[0];
-            const double s = slope<LIM>(col[-L::UX], u0, col[L::UX]);
-            const double hs = half(s);
-            e2[v] = u0 - hs;
-            e3[v] = u0 + hs;
-        }
-        Prim w2 = to_prim(g1, e2[0], e2[1], e2[2], e2[3]);
-        Prim w3 = to_prim(g1, e3[0], e3[1], e3[2], e3[3]);
-        double f2[4], f3[4];
-        flux<1>(w2, f2);
-        flux<1>(w3, f3);
-#pragma unroll
-        for (int v = 0; v < 4; ++v) {
-            const double d = hdy * (f2[v] - f3[v]);
-            sA[(0 * 4 + v) * L::AN + it] = e2[v] + d;
-            sA[(1 * 4 + v) * L::AN + it] = e3[v] + d;
-        }
+        if (x0 + lx >= nx || y0 - 1 + ly > ny) continue;
+        mh_predict<1, LIM>(sU + (ly + 1) * L::UX + lx + 2, PL, L::UX, g1, hdy, sA + it, L::AN,
+                           sA + 4 * L::AN + it, L::AN);
     }
     __syncthreads();
     // y faces 0..TY of each tile column
     for (int it = threadIdx.x; it < TX * (TY + 1); it += NT) {
         const int gx = it % TX, gy = it / TX;
-        double UB[4], UT[4], F[4];
-#pragma unroll
-        for (int v = 0; v < 4; ++v) {
-            UB[v] = sA[(1 * 4 + v) * L::AN + gy * TX + gx];
-            UT[v] = sA[(0 * 4 + v) * L::AN + (gy + 1) * TX + gx];
-        }
-        const int bad = hllc_cons<1>(g, g1, UB, UT, F);
+        if (x0 + gx >= nx || y0 + gy > ny) continue;
+        const int bad = mh_face<1>(sA + 4 * L::AN + gy * TX + gx, L::AN, sA + (gy + 1) * TX + gx, L::AN, g, g1,
+                                   sG + gy * TX + gx, (TY + 1) * TX);
         herr += bad && owned_face(y0 + gy, gy, TY, ny, x0 + gx, nx);
-#pragma unroll
-        for (int v = 0; v < 4; ++v) sG[(v * (TY + 1) + gy) * TX + gx] = F[v];
     }
     __syncthreads();
     return herr;
