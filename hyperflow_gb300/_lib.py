@@ -35,6 +35,9 @@ SIGNATURES = {
     "hf_step": (_i, [_p, C.POINTER(_d)]),
     "hf_step_io": (_i, [_p, _p, _p, C.POINTER(_d)]),
     "hf_host_mapped": (_i, [_p, C.POINTER(_i)]),
+    "hf_set_strict": (_i, [_p, _i]),
+    "hf_last_error_cell": (_i, [_p, C.POINTER(_i), C.POINTER(_i), C.POINTER(_i), C.POINTER(_i), C.POINTER(_i64)]),
+    "hf_clear_error_cell": (_i, [_p]),
     "hf_run": (_i, [_p, _i64, _i, _i, C.POINTER(_i64)]),
     "hf_get_time": (_i, [_p, C.POINTER(_d), C.POINTER(_i64), C.POINTER(_d)]),
     "hf_hllc_errors": (_i, [_p, C.POINTER(_i64)]),
@@ -68,6 +71,9 @@ SIGNATURES = {
     "hf_uns_frames_enable": (_i, [_p, _i]),
     "hf_uns_frames_pending": (_i, [_p, C.POINTER(_i64)]),
     "hf_uns_frame_pop": (_i, [_p, _p, C.POINTER(_d), C.POINTER(_i64)]),
+    "hf_uns_set_strict": (_i, [_p, _i]),
+    "hf_uns_last_error_cell": (_i, [_p, C.POINTER(_i64), C.POINTER(_i64)]),
+    "hf_uns_clear_error_cell": (_i, [_p]),
     "hf_uns_checkpoint_size": (_i, [_p, C.POINTER(_sz)]),
     "hf_uns_checkpoint_save": (_i, [_p, _p, _sz]),
     "hf_uns_checkpoint_load": (_i, [_p, _p, _sz]),

@@ -97,6 +97,7 @@ struct hf_ctx {
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     // profiling
     bool profile = false;
+    int strict = 0;             // hf_set_strict
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev[2];
     size_t ev_used[2] = {0, 0};
     std::string err;
@@ -427,6 +428,7 @@ const char* hf_status_string(int s) {
         case HF_ERR_STATE: return "call out of order";
         case HF_ERR_NO_DEVICE: return "no CUDA device";
         case HF_ERR_TOO_LARGE: return "problem exceeds the fixed-size working area";
+        case HF_ERR_NUMERIC: return "strict mode: an HLLC zero-flux fallback occurred";
         default: return "unknown status";
     }
 }
@@ -503,6 +505,7 @@ int hf_create(const char* case_json, size_t len, hf_ctx** out) {
     }
     C.t = ctx->t_start;
     C.t_end = ctx->t_end;
+    C.first_bad = ~0ull;
     CK(cudaMalloc(&ctx->dctrl, sizeof(hf::Ctrl)));
     CK(cudaMemcpyAsync(ctx->dctrl, &C, sizeof C, cudaMemcpyHostToDevice, ctx->stream));
     int r = make_tmaps(ctx);
@@ -662,6 +665,21 @@ int hf_advance(hf_ctx* ctx, double dt) {
 // interior TimeStep terms, as hf_set_state), one step (as hf_step), every block downloaded --
 // each block's download on a second stream as soon as its own update is done, so it overlaps
 // the updates of the blocks after it.  No synchronisation between the pieces.
+// strict mode, after a synchronisation: HF_ERR_NUMERIC once a zero-flux face is recorded
+static int strict_check(hf_ctx* ctx) {
+    if (!ctx->strict) return HF_OK;
+    unsigned long long k = ~0ull;
+    CK(cudaMemcpy(&k, &ctx->dctrl->first_bad, sizeof k, cudaMemcpyDeviceToHost));
+    if (k == ~0ull) return HF_OK;
+    const long long step = (long long)(k >> 42);
+    const int b = (int)((k >> 38) & 0xF), dir = (int)((k >> 37) & 1);
+    const int j = (int)((k >> 19) & 0x3FFFF), i = (int)(k & 0x7FFFF);
+    return fail(ctx, HF_ERR_NUMERIC,
+                "HLLC zero flux (all wave-speed branches failed) at step " + std::to_string(step) + ", block " +
+                    std::to_string(b) + ", " + (dir ? "y" : "x") + " face (i " + std::to_string(i) + ", j " +
+                    std::to_string(j) + ")");
+}
+
 // true when every pointer is 8-byte aligned host memory that kernels may address as it is
 // (pinned by cudaHostAlloc / cudaHostRegister: the device pointer is the host pointer)
 static bool host_mapped(const double* const* p, int n) {
@@ -721,7 +739,7 @@ int hf_step_io(hf_ctx* ctx, const double* const* in, double* const* out, double*
         CK(hf::launch_finalize(ctx->dctrl, ctx->stream));
         if (dt) CK(cudaMemcpyAsync(dt, &ctx->dctrl->dt, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
         CK(cudaStreamSynchronize(ctx->stream));
-        return HF_OK;
+        return strict_check(ctx);
     }
     for (int b = 0; b < ctx->nblocks; ++b) {
         const BlockHost& B = ctx->blocks[b];
@@ -750,7 +768,7 @@ int hf_step_io(hf_ctx* ctx, const double* const* in, double* const* out, double*
     if (dt) CK(cudaMemcpyAsync(dt, &ctx->dctrl->dt, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
     CK(cudaStreamSynchronize(ctx->copy_stream));
-    return HF_OK;
+    return strict_check(ctx);
 }
 
 int hf_step(hf_ctx* ctx, double* dt) {
@@ -763,6 +781,7 @@ int hf_step(hf_ctx* ctx, double* dt) {
     if (dt) {
         CK(cudaMemcpyAsync(dt, &ctx->dctrl->dt, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
         CK(cudaStreamSynchronize(ctx->stream));
+        return strict_check(ctx);
     }
     return HF_OK;
 }
@@ -792,7 +811,10 @@ int hf_run(hf_ctx* ctx, int64_t n, int clamp_t_end, int use_graph, int64_t* step
             if (r != HF_OK) return r;
         }
     }
-    if (steps_done) *steps_done = read_step(ctx) - s0;
+    if (steps_done) {
+        *steps_done = read_step(ctx) - s0;
+        return strict_check(ctx);
+    }
     return HF_OK;
 }
 
@@ -822,6 +844,36 @@ int hf_sync(hf_ctx* ctx) {
     int e = 0;
     CK(cudaMemcpy(&e, &ctx->dctrl->err, sizeof e, cudaMemcpyDeviceToHost));
     if (e != 0) return fail(ctx, HF_ERR_DEVICE, "device error word " + std::to_string(e));
+    return strict_check(ctx);
+}
+
+int hf_set_strict(hf_ctx* ctx, int on) {
+    if (!ctx) return HF_ERR_ARG;
+    ctx->strict = on ? 1 : 0;
+    CK(cudaMemcpyAsync(&ctx->dctrl->strict, &ctx->strict, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return HF_OK;
+}
+
+int hf_last_error_cell(hf_ctx* ctx, int* block, int* i, int* j, int* dir, int64_t* step) {
+    if (!ctx) return HF_ERR_ARG;
+    unsigned long long k = ~0ull;
+    CK(cudaStreamSynchronize(ctx->stream));
+    CK(cudaMemcpy(&k, &ctx->dctrl->first_bad, sizeof k, cudaMemcpyDeviceToHost));
+    const bool none = k == ~0ull;
+    if (block) *block = none ? -1 : (int)((k >> 38) & 0xF);
+    if (dir) *dir = none ? -1 : (int)((k >> 37) & 1);
+    if (j) *j = none ? -1 : (int)((k >> 19) & 0x3FFFF);
+    if (i) *i = none ? -1 : (int)(k & 0x7FFFF);
+    if (step) *step = none ? -1 : (int64_t)(k >> 42);
+    return HF_OK;
+}
+
+int hf_clear_error_cell(hf_ctx* ctx) {
+    if (!ctx) return HF_ERR_ARG;
+    const unsigned long long none = ~0ull;
+    CK(cudaMemcpyAsync(&ctx->dctrl->first_bad, &none, sizeof none, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
     return HF_OK;
 }
 
@@ -1029,6 +1081,7 @@ int hf_checkpoint_load(hf_ctx* ctx, const void* buf, size_t bytes) {
     C.clamp = 0;
     C.done = 0;
     C.err = 0;
+    C.strict = cur.strict;
     ctx->drained = 0;
     for (int b = 0; b < ctx->nblocks; ++b)
         for (int k = 0; k < 2; ++k) {

@@ -84,6 +84,7 @@ __device__ void fill_side(const MeshDev* __restrict__ m, int b, int side, int p)
 __global__ void step_begin_kernel(Ctrl* __restrict__ c) {
     const int p = (int)(c->step & 1);
     int done = c->clamp && (c->t == c->t_end);
+    if (c->strict && c->first_bad != ~0ull) done = 1;   // strict mode: a zero flux stops the loop
     // a step takes at most two frames: pause the loop while the ring lacks room for them
     if (c->clamp && c->frames && c->captured - c->drained > c->ring_slots - 2) done = 1;
     c->done = done;
@@ -407,7 +408,8 @@ __global__ void __launch_bounds__(NT, 3) mh_kernel(Ctrl* __restrict__ c, const M
     if (!load_tile<L::TMA_BYTES>(sU, bar, p ? &tm1 : &tm0, x0, y0, c)) return;
     const double hdx = sc[0], hdy = sc[1], one_dx = sc[2], one_dy = sc[3];
 
-    const int herr = mh_tile_fluxes<TX, TY, NT, LIM>(sU, sA, sF, sG, g, g1, hdx, hdy, x0, y0, B.nx, B.ny);
+    const int herr = mh_tile_fluxes<TX, TY, NT, LIM>(sU, sA, sF, sG, g, g1, hdx, hdy, x0, y0, B.nx, B.ny,
+                                                     &c->first_bad, face_key(c->step, b, 0, 0, 0));
     // conservative update + forward Euler, and the next step's TimeStep terms
     double* __restrict__ out = B.buf[p ^ 1];
     const size_t plane = (size_t)B.ty * B.pitch;
@@ -514,7 +516,10 @@ __global__ void __launch_bounds__(NT) godunov_kernel(Ctrl* __restrict__ c,
         load(cl, UL, wL, aL, FL, nullptr);
         load(cr, UR, wR, aR, FR, nullptr);
         const int bad = hllc<0>(UL, wL, aL, FL, UR, wR, aR, FR, F);
-        herr += bad && owned_face(x0 + fx, fx, TX, B.nx, y0 + fy, B.ny);
+        if (bad && owned_face(x0 + fx, fx, TX, B.nx, y0 + fy, B.ny)) {
+            ++herr;
+            atomicMin(&c->first_bad, face_key(c->step, b, 0, y0 + fy, x0 + fx));
+        }
 #pragma unroll
         for (int v = 0; v < 4; ++v) sF[(v * TY + fy) * (TX + 1) + fx] = F[v];
     }
@@ -527,7 +532,10 @@ __global__ void __launch_bounds__(NT) godunov_kernel(Ctrl* __restrict__ c,
         load(cb, UB, wB, aB, nullptr, FB);
         load(ct, UT, wT, aT, nullptr, FT);
         const int bad = hllc<1>(UB, wB, aB, FB, UT, wT, aT, FT, F);
-        herr += bad && owned_face(y0 + gy, gy, TY, B.ny, x0 + gx, B.nx);
+        if (bad && owned_face(y0 + gy, gy, TY, B.ny, x0 + gx, B.nx)) {
+            ++herr;
+            atomicMin(&c->first_bad, face_key(c->step, b, 1, y0 + gy, x0 + gx));
+        }
 #pragma unroll
         for (int v = 0; v < 4; ++v) sG[(v * (TY + 1) + gy) * TX + gx] = F[v];
     }

@@ -26,6 +26,8 @@ struct Ctrl {
     unsigned int ticket;
     int err;                                // first error code raised on the device
     long long hllc_errors;                  // HLLC "should not get here" zero fluxes
+    unsigned long long first_bad;           // least face_key of such a face, ~0 when none
+    int strict;                             // a recorded zero flux stops the loop
     // frame output with Simulation::solve's cadence (device loop only, i.e. clamp set)
     int frames;                             // frame clamp and capture on
     int ring_slots;                         // depth of the device frame ring
@@ -44,5 +46,19 @@ enum : int {
     HF_DEV_TIMEOUT = 1,   // a bounded wait gave up
     HF_DEV_BOUNDS = 2,    // a checked index fell outside its buffer
 };
+
+// Key of a Cartesian face for the earliest zero-flux record: ordered by step, block, direction
+// (0: x face i between interior cells (i-1, j) and (i, j); 1: y face j between (i, j-1) and
+// (i, j)), row, column.  Fields saturate at their widths.
+#if defined(__CUDACC__)
+__host__ __device__
+#endif
+inline unsigned long long face_key(long long step, int block, int dir, int j, int i) {
+    const unsigned long long s = step < 0 ? 0ull : (step > 0x3FFFFFll ? 0x3FFFFFull : (unsigned long long)step);
+    const unsigned long long jj = j < 0 ? 0ull : (j > 0x3FFFF ? 0x3FFFFull : (unsigned long long)j);
+    const unsigned long long ii = i < 0 ? 0ull : (i > 0x7FFFF ? 0x7FFFFull : (unsigned long long)i);
+    return (s << 42) | ((unsigned long long)(block & 0xF) << 38) | ((unsigned long long)(dir & 1) << 37) |
+           (jj << 19) | ii;
+}
 
 }  // namespace hf

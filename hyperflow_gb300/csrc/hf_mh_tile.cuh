@@ -80,12 +80,14 @@ __device__ __forceinline__ int mh_face(const double* __restrict__ l, int ls, con
 }
 
 // Computes sF and sG from sU.  Ends with __syncthreads().  Returns the number of owned
-// faces whose HLLC took the zero-flux branch (tile origin x0, y0 in interior cells).
+// faces whose HLLC took the zero-flux branch (tile origin x0, y0 in interior cells); with
+// first_bad, each such face's face_key (key_base: its step and block bits) is min-reduced there.
 template <int TX, int TY, int NT, int LIM>
 __device__ __forceinline__ int mh_tile_fluxes(const double* __restrict__ sU, double* __restrict__ sA,
                                               double* __restrict__ sF, double* __restrict__ sG,
                                               double g, double g1, double hdx, double hdy, int x0,
-                                              int y0, int nx, int ny) {
+                                              int y0, int nx, int ny, unsigned long long* first_bad = nullptr,
+                                              unsigned long long key_base = 0) {
     using L = MhTile<TX, TY>;
     constexpr int PL = L::UY * L::UX;
     int herr = 0;
@@ -107,7 +109,10 @@ __device__ __forceinline__ int mh_tile_fluxes(const double* __restrict__ sU, dou
         const int al = fy * (TX + 2) + fx;
         const int bad = mh_face<0>(sA + 4 * L::AN + al, L::AN, sA + al + 1, L::AN, g, g1,
                                    sF + fy * (TX + 1) + fx, TY * (TX + 1));
-        herr += bad && owned_face(x0 + fx, fx, TX, nx, y0 + fy, ny);
+        if (bad && owned_face(x0 + fx, fx, TX, nx, y0 + fy, ny)) {
+            ++herr;
+            if (first_bad) atomicMin(first_bad, key_base | face_key(0, 0, 0, y0 + fy, x0 + fx));
+        }
     }
     __syncthreads();
     // y phase, cells -1..TY of each tile column
@@ -124,7 +129,10 @@ __device__ __forceinline__ int mh_tile_fluxes(const double* __restrict__ sU, dou
         if (x0 + gx >= nx || y0 + gy > ny) continue;
         const int bad = mh_face<1>(sA + 4 * L::AN + gy * TX + gx, L::AN, sA + (gy + 1) * TX + gx, L::AN, g, g1,
                                    sG + gy * TX + gx, (TY + 1) * TX);
-        herr += bad && owned_face(y0 + gy, gy, TY, ny, x0 + gx, nx);
+        if (bad && owned_face(y0 + gy, gy, TY, ny, x0 + gx, nx)) {
+            ++herr;
+            if (first_bad) atomicMin(first_bad, key_base | face_key(0, 0, 1, y0 + gy, x0 + gx));
+        }
     }
     __syncthreads();
     return herr;

@@ -40,6 +40,8 @@ struct UnsCtrl {
     unsigned long long min_dt[2];   // [parity] min over cells of r_in / (|V| + c), bit pattern
     int err;
     long long hllc_errors;
+    unsigned long long first_bad;   // least uns_key of a zero-flux pair, ~0 when none
+    int strict;                     // a recorded zero flux stops the loop
     // frame output with Simulation::solve's cadence (device loop only, i.e. clamp set)
     int frames, ring_slots, snap_pre, snap_post;
     double frame_next, frame_interval, snap_t;
@@ -105,6 +107,12 @@ __device__ __forceinline__ void block_min_atomic(double v, unsigned long long* a
 
 constexpr int kUnsNT = 256;
 
+// key of a (cell, pair) whose HLLC took the zero flux: step (24 bits), then cell (40 bits)
+__device__ __forceinline__ unsigned long long uns_key(long long step, long long cell) {
+    const unsigned long long s = step > 0xFFFFFFll ? 0xFFFFFFull : (unsigned long long)step;
+    return (s << 40) | ((unsigned long long)cell & 0xFFFFFFFFFFull);
+}
+
 // length x rotated-back HLLC flux of the pair (owner cell c, neighbour cell k)
 __device__ __forceinline__ int pair_flux(const UnsMesh& m, const double* __restrict__ U, size_t N, double g,
                                          double g1, int e, const double* cv, double* f) {
@@ -146,7 +154,10 @@ __global__ void __launch_bounds__(kUnsNT, 3) uns_edge_flux_kernel(UnsCtrl* __res
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < m.nedges; e += gridDim.x * blockDim.x) {
         const int i = m.edge_cell[e];
         double cv[4] = {U[i], U[N + i], U[2 * N + i], U[3 * N + i]}, f[4];
-        herr += pair_flux(m, U, N, g, g1, m.edge_pair[e], cv, f);
+        if (pair_flux(m, U, N, g, g1, m.edge_pair[e], cv, f)) {
+            ++herr;
+            atomicMin(&c->first_bad, uns_key(c->step, i));
+        }
 #pragma unroll
         for (int v = 0; v < 4; ++v) m.edge_flux[(size_t)v * m.nedges + e] = f[v];
     }
@@ -168,6 +179,7 @@ __global__ void uns_prep_kernel(UnsCtrl* c) {
     int p = (int)(c->step & 1);
     c->snap_pre = c->snap_post = 0;
     if (c->clamp && c->t == c->t_end) { c->done = 1; return; }
+    if (c->strict && c->first_bad != ~0ull) { c->done = 1; return; }   // strict mode
     // a step takes at most two frames: pause the loop while the ring lacks room for them
     if (c->clamp && c->frames && c->captured - c->drained > c->ring_slots - 2) { c->done = 1; return; }
     c->done = 0;
@@ -257,8 +269,9 @@ __global__ void __launch_bounds__(kUnsNT, MINB) uns_step_kernel(UnsCtrl* __restr
                 const double sg = (double)m.pair_sign[e];
 #pragma unroll
                 for (int v = 0; v < 4; ++v) f[v] = sg * m.edge_flux[(size_t)v * m.nedges + ed];
-            } else {
-                herr += pair_flux(m, U, N, g, g1, e, cv, f);
+            } else if (pair_flux(m, U, N, g, g1, e, cv, f)) {
+                ++herr;
+                atomicMin(&c->first_bad, uns_key(c->step, i));
             }
 #pragma unroll
             for (int v = 0; v < 4; ++v) acc[v] = acc[v] + f[v];
@@ -300,6 +313,7 @@ struct hf_uns {
     std::vector<void*> allocs;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     bool edge_mode = false;
+    int strict = 0;                     // hf_uns_set_strict
     bool has_anim = false;
     double anim_duration = 0.0, anim_fps = 0.0;
     double* ring = nullptr;             // device frame ring
@@ -581,6 +595,7 @@ int finish_create(hf_uns* u, const Json& cfg) {
     C.cfl = u->cfl;
     C.t = u->t_start;
     C.t_end = u->t_end;
+    C.first_bad = ~0ull;
     UCK(cudaMalloc(&u->dctrl, sizeof C));
     UCK(cudaMemcpy(u->dctrl, &C, sizeof C, cudaMemcpyHostToDevice));
     return hf_uns_set_state(u, u->init.data());
@@ -756,6 +771,44 @@ int hf_uns_get_state(hf_uns* u, double* cons) {
     return HF_OK;
 }
 
+// strict mode, after a synchronisation: HF_ERR_NUMERIC once a zero-flux pair is recorded
+static int uns_strict_check(hf_uns* u) {
+    if (!u->strict) return HF_OK;
+    unsigned long long k = ~0ull;
+    UCK(cudaMemcpy(&k, &u->dctrl->first_bad, sizeof k, cudaMemcpyDeviceToHost));
+    if (k == ~0ull) return HF_OK;
+    return ufail(u, HF_ERR_NUMERIC,
+                 "HLLC zero flux (all wave-speed branches failed) at step " + std::to_string(k >> 40) +
+                     ", cell " + std::to_string(k & 0xFFFFFFFFFFull));
+}
+
+int hf_uns_set_strict(hf_uns* u, int on) {
+    if (!u || !u->dctrl) return HF_ERR_ARG;
+    u->strict = on ? 1 : 0;
+    UCK(cudaMemcpyAsync(&u->dctrl->strict, &u->strict, sizeof(int), cudaMemcpyHostToDevice, u->stream));
+    UCK(cudaStreamSynchronize(u->stream));
+    return HF_OK;
+}
+
+int hf_uns_last_error_cell(hf_uns* u, int64_t* cell, int64_t* step) {
+    if (!u || !u->dctrl) return HF_ERR_ARG;
+    unsigned long long k = ~0ull;
+    UCK(cudaStreamSynchronize(u->stream));
+    UCK(cudaMemcpy(&k, &u->dctrl->first_bad, sizeof k, cudaMemcpyDeviceToHost));
+    const bool none = k == ~0ull;
+    if (cell) *cell = none ? -1 : (int64_t)(k & 0xFFFFFFFFFFull);
+    if (step) *step = none ? -1 : (int64_t)(k >> 40);
+    return HF_OK;
+}
+
+int hf_uns_clear_error_cell(hf_uns* u) {
+    if (!u || !u->dctrl) return HF_ERR_ARG;
+    const unsigned long long none = ~0ull;
+    UCK(cudaMemcpyAsync(&u->dctrl->first_bad, &none, sizeof none, cudaMemcpyHostToDevice, u->stream));
+    UCK(cudaStreamSynchronize(u->stream));
+    return HF_OK;
+}
+
 int hf_uns_time_step(hf_uns* u, double* dt) {
     if (!u || !u->dctrl) return HF_ERR_ARG;
     int clamp = 0;
@@ -765,6 +818,7 @@ int hf_uns_time_step(hf_uns* u, double* dt) {
     if (dt) {
         UCK(cudaMemcpyAsync(dt, &u->dctrl->dt, sizeof(double), cudaMemcpyDeviceToHost, u->stream));
         UCK(cudaStreamSynchronize(u->stream));
+        return uns_strict_check(u);
     }
     return HF_OK;
 }
@@ -801,7 +855,7 @@ int hf_uns_run(hf_uns* u, int64_t n, int clamp_t_end, int use_graph, int64_t* st
     long long s1;
     if ((r = read_step(u, &s1))) return r;
     if (steps_done) *steps_done = s1 - s0;
-    return HF_OK;
+    return uns_strict_check(u);
 }
 
 int hf_uns_frames_enable(hf_uns* u, int ring_slots) {
@@ -940,6 +994,7 @@ int hf_uns_checkpoint_load(hf_uns* u, const void* buf, size_t bytes) {
     C.clamp = 0;
     C.done = 0;
     C.err = 0;
+    C.strict = cur.strict;
     u->drained = 0;
     const size_t n = (size_t)4 * u->ncells * sizeof(double);
     for (int k = 0; k < 2; ++k) {

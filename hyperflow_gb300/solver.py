@@ -249,6 +249,23 @@ class CartSolver:
         check(lib().hf_hllc_errors(self._h, C.byref(n)), self._h)
         return n.value
 
+    def set_strict(self, on: bool = True):
+        """Strict mode: a zero-flux HLLC face stops the loop and raises HyperFlowError
+        (HF_ERR_NUMERIC); off (the default) the run continues as the reference's does."""
+        check(lib().hf_set_strict(self._h, int(bool(on))), self._h)
+
+    def last_error_cell(self):
+        """The earliest zero-flux face: dict(step, block, dir, i, j), or None."""
+        v = [C.c_int() for _ in range(4)]
+        st = C.c_int64()
+        check(lib().hf_last_error_cell(self._h, *[C.byref(x) for x in v], C.byref(st)), self._h)
+        if v[0].value < 0:
+            return None
+        return {"step": st.value, "block": v[0].value, "i": v[1].value, "j": v[2].value, "dir": v[3].value}
+
+    def clear_error_cell(self):
+        check(lib().hf_clear_error_cell(self._h), self._h)
+
     def stream(self) -> int:
         s = C.c_void_p()
         check(lib().hf_stream(self._h, C.byref(s)), self._h)

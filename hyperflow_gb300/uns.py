@@ -164,6 +164,19 @@ class UnsSolver:
         self.frame_paths = paths
         return total
 
+    def set_strict(self, on: bool = True):
+        """Strict mode: a zero-flux HLLC pair stops the loop and raises HyperFlowError."""
+        check(lib().hf_uns_set_strict(self._h, int(bool(on))), self._h, _MSG)
+
+    def last_error_cell(self):
+        """The earliest zero-flux (cell, pair): dict(step, cell), or None."""
+        cell, st = C.c_int64(), C.c_int64()
+        check(lib().hf_uns_last_error_cell(self._h, C.byref(cell), C.byref(st)), self._h, _MSG)
+        return None if cell.value < 0 else {"step": st.value, "cell": cell.value}
+
+    def clear_error_cell(self):
+        check(lib().hf_uns_clear_error_cell(self._h), self._h, _MSG)
+
     # --- checkpoint / restart ---
     def checkpoint(self) -> bytes:
         """The whole simulation state as bytes; ``restore`` on a solver of the same case and

@@ -34,7 +34,8 @@ enum {
     HF_ERR_DEVICE = 5,       /* a kernel raised its error word (bounded wait timed out, ...) */
     HF_ERR_STATE = 6,        /* call out of order (e.g. advancing block 2 before block 1) */
     HF_ERR_NO_DEVICE = 7,    /* no CUDA device is visible */
-    HF_ERR_TOO_LARGE = 8     /* the problem exceeds a fixed-size working area */
+    HF_ERR_TOO_LARGE = 8,    /* the problem exceeds a fixed-size working area */
+    HF_ERR_NUMERIC = 9       /* strict mode: an HLLC zero-flux fallback occurred (hf_last_error_cell) */
 };
 
 /* state layouts for hf_set_state / hf_get_state */
@@ -109,8 +110,23 @@ int hf_get_time(hf_ctx* ctx, double* t, int64_t* calls, double* last_dt);
 /* number of HLLC zero-flux fallbacks (riemann_hllc.cpp:207-211) seen so far */
 int hf_hllc_errors(hf_ctx* ctx, int64_t* count);
 
-/* waits for the context's stream; returns HF_ERR_DEVICE if a kernel raised its error word */
+/* waits for the context's stream; returns HF_ERR_DEVICE if a kernel raised its error word
+ * (and HF_ERR_NUMERIC in strict mode once a zero-flux face is recorded) */
 int hf_sync(hf_ctx* ctx);
+
+/* Faces whose HLLC takes none of its four branches (riemann_hllc.cpp:199-211: NaN wave speeds,
+ * e.g. a negative pressure) get the zero flux and the run continues, as in the reference, which
+ * prints a message there; hf_hllc_errors counts them.  hf_last_error_cell gives the earliest such
+ * face since the context was created or hf_clear_error_cell: the least (step, block, direction,
+ * j, i), where direction 0 is the x face i between interior cells (i-1, j) and (i, j) and 1 the
+ * y face j between (i, j-1) and (i, j); step counts the steps completed before it.  All outputs
+ * are -1 when there is none; any pointer may be null.
+ * hf_set_strict(ctx, 1): once such a face is recorded the step completes, later steps do
+ * nothing, and hf_step / hf_run (with steps_done) / hf_step_io / hf_sync return HF_ERR_NUMERIC
+ * with the face in hf_last_error_message.  hf_clear_error_cell lets the run go on. */
+int hf_set_strict(hf_ctx* ctx, int on);
+int hf_last_error_cell(hf_ctx* ctx, int* block, int* i, int* j, int* dir, int64_t* step);
+int hf_clear_error_cell(hf_ctx* ctx);
 
 /* the context's CUDA stream (a cudaStream_t), for callers that time or order work on it */
 int hf_stream(hf_ctx* ctx, void** stream);

@@ -79,6 +79,16 @@ int hf_uns_frames_enable(hf_uns* u, int ring_slots);
 int hf_uns_frames_pending(hf_uns* u, int64_t* n);
 int hf_uns_frame_pop(hf_uns* u, double* cons, double* t, int64_t* index);
 
+/* Pairs whose HLLC takes the zero flux (NaN wave speeds) are counted by hf_uns_hllc_errors and
+ * the run continues, as in the reference.  hf_uns_last_error_cell gives the earliest one since
+ * creation or hf_uns_clear_error_cell: the least (step, cell) -- in edge-based mode the edge's
+ * owner cell -- or -1.  Strict mode (hf_uns_set_strict(u, 1)): once one is recorded the step
+ * completes, later device-loop steps do nothing, and hf_uns_run / hf_uns_time_step return
+ * HF_ERR_NUMERIC with the cell in hf_uns_last_error_message. */
+int hf_uns_set_strict(hf_uns* u, int on);
+int hf_uns_last_error_cell(hf_uns* u, int64_t* cell, int64_t* step);
+int hf_uns_clear_error_cell(hf_uns* u);
+
 /* Checkpoint / restart of the whole unstructured simulation state (both cell-state buffers and
  * the control block: t, TimeStep call count, step parity, the CFL minimum, frame cadence), as
  * hf_checkpoint_* of hyperflow_gb300.h.  No counterpart in the reference.  A run restored into a

@@ -382,6 +382,18 @@ double hfo_time_step(hfo_mesh *m) {
     return final_cfl * smin(dtx, dty);
 }
 
+/* The earliest zero-flux face as a key ordered by step, block, direction (0: x face i between
+ * interior cells (i-1, j) and (i, j); 1: y face j between (i, j-1) and (i, j)), j, i; fields
+ * saturate at 22, 4, 1, 18 and 19 bits.  Not in the reference, which prints a message
+ * (riemann_hllc.cpp:199-211); the GPU records the same key. */
+static void note_bad(hfo_mesh *m, int b, int dir, int j, int i) {
+    uint64_t s = m->steps > 0x3FFFFF ? 0x3FFFFFu : (uint64_t)m->steps;
+    uint64_t jj = j > 0x3FFFF ? 0x3FFFFu : (uint64_t)j, ii = i > 0x7FFFF ? 0x7FFFFu : (uint64_t)i;
+    uint64_t k = (s << 42) | ((uint64_t)(b & 0xF) << 38) | ((uint64_t)(dir & 1) << 37) | (jj << 19) | ii;
+#pragma omp critical(hfo_first_bad)
+    if (k < m->first_bad) m->first_bad = k;
+}
+
 /* ---------------- Godunov block update, src/fvm_2d_cart/scheme/godunov/godunov.cpp:27-118,
  * fused with ForwardEulerODESolver (forward_euler.cpp:15-33) ---------------------------- */
 
@@ -399,7 +411,9 @@ static void godunov_block(hfo_mesh *m, int b, double dt, double *Unew) {
         for (int i = 0; i <= nx; ++i) {
             double a[4], c[4], f[4];
             for (int v = 0; v < 4; ++v) { a[v] = AT(m, b, v, i, j); c[v] = AT(m, b, v, i + 1, j); }
-            err += hfo_hllc(m->gamma, a, c, 0, f);
+            int bad = hfo_hllc(m->gamma, a, c, 0, f);
+            err += bad;
+            if (bad && j <= ny) note_bad(m, b, 0, j - 1, i);
             for (int v = 0; v < 4; ++v) FX[((size_t)v * ty + j) * (nx + 1) + i] = f[v];
         }
 #pragma omp parallel for num_threads(nt) reduction(+ : err) schedule(static)
@@ -407,7 +421,9 @@ static void godunov_block(hfo_mesh *m, int b, double dt, double *Unew) {
         for (int i = 1; i < tx - 1; ++i) {
             double a[4], c[4], f[4];
             for (int v = 0; v < 4; ++v) { a[v] = AT(m, b, v, i, j); c[v] = AT(m, b, v, i, j + 1); }
-            err += hfo_hllc(m->gamma, a, c, 1, f);
+            int bad = hfo_hllc(m->gamma, a, c, 1, f);
+            err += bad;
+            if (bad && i <= nx) note_bad(m, b, 1, j, i - 1);
             for (int v = 0; v < 4; ++v) FY[((size_t)v * (ny + 1) + j) * tx + i] = f[v];
         }
     m->hllc_errors += err;
@@ -491,7 +507,9 @@ static void mh_block(hfo_mesh *m, int b, double dt, double dt_pred, double *Unew
             size_t cl = (size_t)(j + 2) * tx + (i + 1), cr = (size_t)(j + 2) * tx + (i + 2);
             double a[4], c4[4], f[4];
             for (int v = 0; v < 4; ++v) { a[v] = R(1, v, cl); c4[v] = R(0, v, cr); }
-            err += hfo_hllc(g, a, c4, 0, f);
+            int bad = hfo_hllc(g, a, c4, 0, f);
+            err += bad;
+            if (bad) note_bad(m, b, 0, j, i);
             for (int v = 0; v < 4; ++v) FX[((size_t)v * ny + j) * (nx + 1) + i] = f[v];
         }
     /* calculate_fluxes_y (316-345) */
@@ -501,7 +519,9 @@ static void mh_block(hfo_mesh *m, int b, double dt, double dt_pred, double *Unew
             size_t cb = (size_t)(j + 1) * tx + (i + 2), ct = (size_t)(j + 2) * tx + (i + 2);
             double a[4], c4[4], f[4];
             for (int v = 0; v < 4; ++v) { a[v] = R(3, v, cb); c4[v] = R(2, v, ct); }
-            err += hfo_hllc(g, a, c4, 1, f);
+            int bad = hfo_hllc(g, a, c4, 1, f);
+            err += bad;
+            if (bad) note_bad(m, b, 1, j, i);
             for (int v = 0; v < 4; ++v) FY[((size_t)v * (ny + 1) + j) * nx + i] = f[v];
         }
     m->hllc_errors += err;
@@ -542,6 +562,7 @@ void hfo_advance(hfo_mesh *m, double dt) {
         memcpy(m->U[b], Unew, n * sizeof(double));
         free(Unew);
     }
+    m->steps++;
 }
 
 /* Simulation::solve body (simulation.cpp:81-120) without the frame-output clamps */

@@ -40,6 +40,8 @@ typedef struct {
     double *U[HFO_MAXB];               /* SoA [var][y][x] incl. ghosts, x fastest */
     int nthreads;
     int64_t hllc_errors;               /* times the HLLC "should not get here" branch ran */
+    int64_t steps;                     /* hfo_advance calls completed */
+    uint64_t first_bad;                /* least key (step, block, direction, j, i) of such a face */
 } hfo_mesh;
 
 #ifdef __cplusplus

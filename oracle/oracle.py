@@ -40,6 +40,7 @@ class _Mesh(C.Structure):
         ("bc_type", (C.c_int * 4) * MAXB), ("bc_block", (C.c_int * 4) * MAXB),
         ("bc_state", ((C.c_double * 4) * 4) * MAXB),
         ("U", C.c_void_p * MAXB), ("nthreads", C.c_int), ("hllc_errors", C.c_int64),
+        ("steps", C.c_int64), ("first_bad", C.c_uint64),
     ]
 
 
@@ -134,6 +135,7 @@ class Oracle:
         m.t = float(case["simulation"]["t_start"])
         m.t_end = float(case["simulation"]["t_end"])
         m.nthreads = nthreads
+        m.first_bad = (1 << 64) - 1
         blocks = case["mesh"]["blocks"]
         m.nblocks = len(blocks)
         self.U = []
@@ -256,6 +258,15 @@ class Oracle:
     @property
     def hllc_errors(self) -> int:
         return self.m.hllc_errors
+
+    @property
+    def first_bad(self):
+        """The earliest zero-flux face (step, block, dir, i, j) as the GPU reports it, or None."""
+        k = self.m.first_bad
+        if k == (1 << 64) - 1:
+            return None
+        return {"step": k >> 42, "block": (k >> 38) & 0xF, "dir": (k >> 37) & 1,
+                "j": (k >> 19) & 0x3FFFF, "i": k & 0x7FFFF}
 
     def state(self, b: int = 0) -> np.ndarray:
         return self.U[b].copy()

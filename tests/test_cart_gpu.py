@@ -57,6 +57,76 @@ def test_gpu_hllc_fallback_count_matches_oracle(port_lib):
     assert s.hllc_errors() == o.hllc_errors
 
 
+def test_gpu_first_zero_flux_face_matches_oracle(port_lib):
+    """The earliest zero-flux face (step, block, direction, j, i) equals the oracle's on the
+    vacuum-forming fixture; clearing forgets it."""
+    from oracle.oracle import Oracle
+    g = load_golden("mh_vanleer_vacuum_hllc_fallback")
+    o = Oracle(g["case"], nthreads=4)
+    o.run(int(g["steps"]))
+    s = _solver(g["case"])
+    s.run(int(g["steps"]))
+    assert o.first_bad is not None
+    assert s.last_error_cell() == o.first_bad
+    s.clear_error_cell()
+    assert s.last_error_cell() is None
+
+
+def _negative_pressure_case(scheme):
+    from hyperflow_gb300 import cases
+    case = cases.quadrant_case(40, ny=36, scheme=scheme, limiter="MinBee", split=(0.45, 0.55))
+    g = 1 if scheme == "Godunov" else 2
+    return case, (g + 17, g + 23)   # interior cell (i 23, j 17)
+
+
+@pytest.mark.parametrize("scheme", ["Godunov", "MUSCLHancock"])
+def test_gpu_negative_pressure_cell_matches_oracle(scheme, port_lib):
+    """A cell with negative total energy (pressure < 0, NaN sound speed): the NaNs, the
+    zero-flux count and the earliest zero-flux face all match the oracle, step by step."""
+    from oracle.oracle import Oracle
+    case, (j, i) = _negative_pressure_case(scheme)
+    o, s = Oracle(case), _solver(case)
+    U = s.state(0)
+    U[3, j, i] = -1.0
+    s.set_state(0, U)
+    o.U[0][...] = U
+    dts_o = o.run(4)
+    dts = [s.step() for _ in range(4)]
+    np.testing.assert_array_equal(np.array(dts), dts_o)
+    np.testing.assert_array_equal(s.state(0), o.state(0))
+    assert s.hllc_errors() == o.hllc_errors > 0
+    bad = s.last_error_cell()
+    assert bad == o.first_bad
+    assert bad["step"] == 0 and bad["dir"] == 0 and abs(bad["i"] - 23) <= 3   # next to cell (23, 17)
+
+
+def test_gpu_strict_mode_stops_at_the_zero_flux_step():
+    """Strict mode: the step that met the zero flux completes, the loop stops there and the
+    calls raise; clearing the record lets one more step run; strict off runs on."""
+    from hyperflow_gb300 import HyperFlowError
+    case, (j, i) = _negative_pressure_case("MUSCLHancock")
+    s, ref = _solver(case), _solver(case)
+    U = s.state(0)
+    U[3, j, i] = -1.0
+    s.set_state(0, U)
+    ref.set_state(0, U)
+    ref.step()
+    s.set_strict(True)
+    with pytest.raises(HyperFlowError, match="zero flux"):
+        s.run(5)
+    assert s.time()[0] == ref.time()[0]          # exactly one step ran
+    with pytest.raises(HyperFlowError, match="zero flux"):
+        s.run(3)
+    assert s.time()[0] == ref.time()[0]          # stopped
+    s.clear_error_cell()
+    with pytest.raises(HyperFlowError, match="zero flux"):
+        s.run(3)
+    ref.step()
+    assert s.time()[0] == ref.time()[0]          # one more step, then stopped again
+    s.set_strict(False)
+    assert s.run(3) == 3
+
+
 def test_gpu_piecewise_api_equals_device_loop():
     """apply_bcs / calculate_time_step / advance_block driven from the host (the
     reference's Simulation::solve sequence) equals hf_run's device loop, with and

@@ -179,3 +179,36 @@ def test_uns_gpu_checkpoint_restart_is_bit_exact():
         other.restore(blob)
     with pytest.raises(HyperFlowError):
         a.restore(blob[:64])
+
+
+@pytest.mark.gpu
+def test_uns_gpu_negative_pressure_cell_and_strict_mode():
+    """A cell with negative total energy: the NaNs spread exactly as in the oracle, the
+    earliest zero-flux pair is at step 0 on that cell or a neighbour, and strict mode stops
+    the device loop after that step."""
+    from hyperflow_gb300 import HyperFlowError, UnsSolver, meshgen
+    from oracle import oracle
+    g = load("tri_hole_3k")
+    text = meshgen.hmsh_text(g["verts"], g["codes"])
+    s = UnsSolver(g["case"], mesh_text=text)
+    U = s.state()
+    U[3, 100] = -1.0
+    s.set_state(U)
+    s.run(3)
+    m = s.mesh_arrays()
+    V = U.copy()
+    oracle.uns_run(1.4, g["case"]["simulation"]["cfl"], 0, m["pair_start"], m["nbr"], m["angle"],
+                   m["length"], m["area"], m["rin"], _inlet(g["case"]), V, 3)
+    np.testing.assert_array_equal(s.state(), V)
+    assert s.hllc_errors() > 0
+    bad = s.last_error_cell()
+    nbrs = {100} | {int(k) for k in m["nbr"][m["pair_start"][100]:m["pair_start"][101]] if k >= 0}
+    assert bad["step"] == 0 and bad["cell"] in nbrs
+    t = UnsSolver(g["case"], mesh_text=text)
+    t.set_state(U)
+    t.set_strict(True)
+    with pytest.raises(HyperFlowError, match="zero flux"):
+        t.run(5)
+    assert t.time()[1] == 1
+    s.clear_error_cell()
+    assert s.last_error_cell() is None
