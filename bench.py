@@ -222,11 +222,62 @@ def bench_batch(args):
                    "l2": "state 2 x %.0f MB > 129 MB L2, no flush needed" % (cells * 32 / 1e6)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "traffic": None, "peak_kind": peak_kind,
-                     "kernel": "batch_mh_kernel (persistent, all instances, one launch per run)"},
+                     "kernel": "batch_kernel<MUSCL-Hancock> (persistent, all instances, one launch per run)"},
         "cpu_baseline": {"value": sample_cells / cpu_s / 1e6, "unit": "Mcell-updates/s", "cores": nth,
                          "kind": "port", "sample": f"every 16th instance ({len(sample)}), 20 steps each"},
         "e2e": None, "gpu_launches": 1, "clocks": clk.summary()}), flush=True)
     b.close()
+
+
+def bench_quad256(args):
+    """The reference's first configuration: the 256^2 four-quadrant Riemann problem, Godunov +
+    HLLC, CFL 0.8, `steps` steps (200 in the reference's run).  At 65,536 cells a step is too
+    small to fill the GPU through per-step launches, so the whole run goes through the batched
+    path as a batch of one: one persistent launch, grid barriers between steps.  The per-block
+    solver's device loop (CUDA graph of the per-step launches) is timed beside it."""
+    import torch
+    from hyperflow_gb300 import BatchSolver, CartSolver, cases
+    from oracle.oracle import Oracle, build_port
+    case = cases.quadrant_case(256)
+    b = BatchSolver({"cases": [case]})
+    best, trial_ms = b.autotune(steps_per_trial=20)
+    stream = torch.cuda.ExternalStream(b.stream())
+    b.run(args.warmup, graph=True)
+    b.sync()
+    with Clocks(0) as clk:
+        ms = timed_device(stream, lambda: b.run(args.steps, graph=True))
+    b.sync()
+    cells = 256 * 256
+    value = cells * args.steps / (ms / 1e3) / 1e6
+    s = CartSolver(case)
+    s.run(args.warmup)
+    sstream = torch.cuda.ExternalStream(s.stream())
+    ms_pb = timed_device(sstream, lambda: s.run(args.steps, graph=True))
+    hbm, peak_kind = peaks()
+    achieved = BYTES_PER_CELL * cells * args.steps / (ms / 1e3) / 1e9
+    build_port()
+    nth = os.cpu_count() or 1
+    o = Oracle(case, nthreads=nth)
+    t0 = time.perf_counter()
+    o.run(args.steps)
+    cpu_s = time.perf_counter() - t0
+    print(json.dumps({
+        "metric": "Mcell-updates/s", "value": value, "unit": "Mcell-updates/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (the case's own initial condition)",
+        "config": {"workload": "quadrant_riemann_256x256_godunov_hllc_fp64", "cells": cells, "cfl": 0.8,
+                   "path": "batch of one: one persistent launch for the whole run", "autotuned_config": best,
+                   "l2": "state 2 x 2 MB, L2-resident by nature across the steps of the one launch"},
+        "per_block_device_loop_value": cells * args.steps / (ms_pb / 1e3) / 1e6,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved / hbm, "traffic": None, "peak_kind": peak_kind,
+                     "kernel": "batch_kernel<Godunov> (persistent)"},
+        "cpu_baseline": {"value": cells * args.steps / cpu_s / 1e6, "unit": "Mcell-updates/s", "cores": nth,
+                         "kind": "port", "sample": f"the whole run ({args.steps} steps)"},
+        "e2e": None, "gpu_launches": 1, "clocks": clk.summary()}), flush=True)
+    b.close()
+    s.close()
 
 
 def bench_uns(args):
@@ -289,7 +340,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--limiter", default="MinBee", choices=["MinBee", "VanLeer"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="CPU-baseline sample budget")
-    ap.add_argument("--workload", default="ffs", choices=["ffs", "square", "batch", "uns"],
+    ap.add_argument("--workload", default="ffs", choices=["ffs", "square", "batch", "uns", "quad256"],
                     help="ffs: the 3-block forward-facing step (default); square: one n x n block; "
                          "batch: 512 batched Riemann problems; uns: the 1M-triangle channel")
     ap.add_argument("--instances", type=int, default=512, help="batch workload: number of instances")
@@ -305,7 +356,7 @@ def main():
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
-    if args.workload in ("batch", "uns"):
+    if args.workload in ("batch", "uns", "quad256"):
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "unavailable":
                               "the reference arm is timed on the forward-facing step and square workloads"}))
@@ -313,7 +364,7 @@ def main():
         import numpy as np  # noqa: F401
         import torch
         torch.cuda.set_device(0)
-        (bench_batch if args.workload == "batch" else bench_uns)(args)
+        {"batch": bench_batch, "uns": bench_uns, "quad256": bench_quad256}[args.workload](args)
         return
 
     from hyperflow_gb300 import cases

@@ -164,11 +164,11 @@ def random_quadrant_case(n: int, seed: int, limiter: str = "MinBee", cfl: float 
 
 
 def batch_manifest(count: int = 512, seed: int = 0, side_min: int = 64, side_max: int = 1024,
-                   limiter: str = "MinBee", cfl: float = CFL_2D) -> dict:
+                   limiter: str = "MinBee", cfl: float = CFL_2D, scheme: str = "MUSCLHancock") -> dict:
     """The batched workload: `count` independent square four-quadrant Riemann problems on
     [0,1]^2, sides log-uniform in [side_min, side_max] (rounded), split point uniform in
     [0.3,0.7]^2, and per quadrant rho ~ U[0.1,2], p ~ U[0.1,10], u, v ~ U[-1,1]
-    (primitive), transmissive on every side, MUSCL-Hancock + HLLC.  Seeded."""
+    (primitive), transmissive on every side, MUSCL-Hancock (or Godunov) + HLLC.  Seeded."""
     import numpy as np
     rng = np.random.default_rng(seed)
     out = []
@@ -179,8 +179,8 @@ def batch_manifest(count: int = 512, seed: int = 0, side_min: int = 64, side_max
         for _q in range(4):
             states.append([float(rng.uniform(0.1, 2.0)), float(rng.uniform(-1.0, 1.0)),
                            float(rng.uniform(-1.0, 1.0)), float(rng.uniform(0.1, 10.0))])
-        out.append(quadrant_case(n, scheme="MUSCLHancock", limiter=limiter, cfl=cfl, split=split,
-                                 states=states))
+        out.append(quadrant_case(n, scheme=scheme, limiter=limiter if scheme == "MUSCLHancock" else None,
+                                 cfl=cfl, split=split, states=states))
     return {"cases": out}
 
 

@@ -1,15 +1,17 @@
-// Batched MUSCL-Hancock: hundreds of independent single-block, all-transmissive cases of
-// different sizes advanced together by one persistent cooperative kernel per run of
-// steps, captured in a CUDA graph, each case with its own CFL dt.  C ABI in
-// include/hyperflow_gb300_batch.h.
+// Batched single-block cases: hundreds of independent, all-transmissive cases of different
+// sizes advanced together by one persistent cooperative kernel per run of steps, captured in a
+// CUDA graph, each case with its own CFL dt.  C ABI in include/hyperflow_gb300_batch.h.
 //
 // Each case is the reference's single-block MUSCL-Hancock step
 // (src/fvm_2d_cart/scheme/muscl_hancock/muscl_hancock.cpp:41-376 + TimeStep +
-// ForwardEuler).  With transmissive boundaries on all four sides every ghost value is a
-// mirror copy of an interior value (transmissive_boundary.cpp:25-104; the fill order makes
-// corner ghosts mirror in x and in y).  So the tile loader reads the mirrored interior cell
-// directly and the state is stored without ghosts, and the CFL maximum over ghost cells
-// equals the maximum over the interior.
+// ForwardEuler) or Godunov step (src/fvm_2d_cart/scheme/godunov/godunov.cpp:27-118 + TimeStep +
+// ForwardEuler); all cases of a batch use the same scheme.  With transmissive boundaries on all
+// four sides every ghost value is a mirror copy of an interior value
+// (transmissive_boundary.cpp:25-104; the fill order makes corner ghosts mirror in x and in y).
+// So the tile loader reads the mirrored interior cell directly and the state is stored without
+// ghosts, and the CFL maximum over ghost cells equals the maximum over the interior.  A single
+// small case (the 256^2 Godunov quadrant problem) runs as a batch of one: its whole run of steps
+// is one launch, with no per-step launch chain.
 //
 // Work decomposition: every case is cut into TX x TY tiles; the tiles of all cases form
 // one list that the persistent CTAs walk round-robin.  A step ends at a grid barrier
@@ -31,6 +33,7 @@
 #include "../../include/hyperflow_gb300_batch.h"
 #include "hf_cart.h"
 #include "hf_device.cuh"
+#include "hf_godunov_tile.cuh"
 #include "hf_mh_tile.cuh"
 
 namespace hf {
@@ -47,6 +50,7 @@ struct BatchCtrl {
     long long calls;        // TimeStep calls made by every case so far
     long long step;         // steps completed
     int limiter;
+    int scheme;             // 0 Godunov, 1 MUSCL-Hancock
     int ninst;
     int err;
     unsigned int bar_count;
@@ -117,11 +121,27 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
 
-// stage tile `t`'s state + mirrored 2-cell halo into sU (cp.async, one commit group)
-template <int TX, int TY, int NT>
+// shared-memory tiles of the two schemes: halo H cells, the staged state, the scratch after it
+template <int SCHEME, int TX, int TY>
+struct BatchTile;
+template <int TX, int TY>
+struct BatchTile<0, TX, TY> {   // Godunov: 1-cell halo; per-cell primitives/fluxes, face fluxes
+    using T = GoTile<TX, TY>;
+    static constexpr int H = 1, UX = T::UX, UY = T::UY, U_SIZE = T::U_SIZE;
+    static constexpr int WORK = T::Q_SIZE + T::F_SIZE + T::G_SIZE;
+};
+template <int TX, int TY>
+struct BatchTile<1, TX, TY> {   // MUSCL-Hancock: 2-cell halo; evolved states, face fluxes
+    using T = MhTile<TX, TY>;
+    static constexpr int H = 2, UX = T::UX, UY = T::UY, U_SIZE = T::U_SIZE;
+    static constexpr int WORK = T::A_SIZE + T::F_SIZE + T::G_SIZE;
+};
+
+// stage tile `t`'s state + mirrored halo into sU (cp.async, one commit group)
+template <int SCHEME, int TX, int TY, int NT>
 __device__ __forceinline__ void stage_tile(const BatchDev& d, const double* __restrict__ U, long long t,
                                            double* sU) {
-    using T = MhTile<TX, TY>;
+    using T = BatchTile<SCHEME, TX, TY>;
     const int inst = d.tile_inst[t];
     const int xy = d.tile_xy[t];
     const int x0 = xy & 0xffff, y0 = xy >> 16;
@@ -132,22 +152,23 @@ __device__ __forceinline__ void stage_tile(const BatchDev& d, const double* __re
         const int v = k / (T::UY * T::UX);
         const int r = k - v * (T::UY * T::UX);
         const int ly = r / T::UX, lx = r - ly * T::UX;
-        const int gx = mirror(x0 + lx - 2, I.n), gy = mirror(y0 + ly - 2, I.n);
+        const int gx = mirror(x0 + lx - T::H, I.n), gy = mirror(y0 + ly - T::H, I.n);
         cp_async8(sU + k, base + v * plane + (size_t)gy * I.n + gx);
     }
     cp_async_commit();
 }
 
-template <int TX, int TY, int NT, int STAGES, int MINB>
-__global__ void __launch_bounds__(NT, MINB) batch_mh_kernel(BatchDev d, int nsteps) {
-    using T = MhTile<TX, TY>;
+template <int SCHEME, int TX, int TY, int NT, int STAGES, int MINB>
+__global__ void __launch_bounds__(NT, MINB) batch_kernel(BatchDev d, int nsteps) {
+    using BT = BatchTile<SCHEME, TX, TY>;
+    constexpr int CALLS = SCHEME == 1 ? 2 : 1;   // TimeStep calls per step (+ the predictor's)
     extern __shared__ __align__(1024) double smem[];
     double* sUb[STAGES];
 #pragma unroll
-    for (int k = 0; k < STAGES; ++k) sUb[k] = smem + k * T::U_SIZE;
-    double* sA = smem + STAGES * T::U_SIZE;
-    double* sF = sA + T::A_SIZE;
-    double* sG = sF + T::F_SIZE;
+    for (int k = 0; k < STAGES; ++k) sUb[k] = smem + k * BT::U_SIZE;
+    double* sW = smem + STAGES * BT::U_SIZE;   // MUSCL-Hancock: sA; Godunov: sQ
+    double* sF = sW + (SCHEME == 1 ? MhTile<TX, TY>::A_SIZE : GoTile<TX, TY>::Q_SIZE);
+    double* sG = sF + (SCHEME == 1 ? MhTile<TX, TY>::F_SIZE : GoTile<TX, TY>::F_SIZE);
     __shared__ double sdt[5];
 
     BatchCtrl* c = d.ctrl;
@@ -160,7 +181,7 @@ __global__ void __launch_bounds__(NT, MINB) batch_mh_kernel(BatchDev d, int nste
         const long long step = step0 + s;
         const int p = (int)(step & 1);
         const int ar = (int)(step % 3), aw = (int)((step + 1) % 3), az = (int)((step + 2) % 3);
-        const long long calls = calls0 + 2 * s;
+        const long long calls = calls0 + CALLS * s;
         const double m0 = (calls + 1 <= 10) ? 0.2 * cfl : cfl;        // step TimeStep call
         const double m1 = (calls + 2 <= 10) ? 0.2 * cfl : cfl;        // predictor call
         for (int i = blockIdx.x * NT + threadIdx.x; i < 2 * ninst; i += gridDim.x * NT)
@@ -168,17 +189,17 @@ __global__ void __launch_bounds__(NT, MINB) batch_mh_kernel(BatchDev d, int nste
         const double* __restrict__ U = d.U[p];
         double* __restrict__ Un = d.U[p ^ 1];
         long long t = blockIdx.x;
-        if (STAGES == 2 && t < d.ntiles) stage_tile<TX, TY, NT>(d, U, t, sUb[0]);
+        if (STAGES == 2 && t < d.ntiles) stage_tile<SCHEME, TX, TY, NT>(d, U, t, sUb[0]);
         int buf = 0;
         for (; t < d.ntiles; t += gridDim.x) {
             double* sU = sUb[STAGES == 2 ? buf : 0];
             if (STAGES == 1) {
-                stage_tile<TX, TY, NT>(d, U, t, sU);
+                stage_tile<SCHEME, TX, TY, NT>(d, U, t, sU);
                 cp_async_wait<0>();
             } else {
                 const long long tn = t + gridDim.x;
                 if (tn < d.ntiles) {
-                    stage_tile<TX, TY, NT>(d, U, tn, sUb[buf ^ 1]);
+                    stage_tile<SCHEME, TX, TY, NT>(d, U, tn, sUb[buf ^ 1]);
                     cp_async_wait<1>();
                 } else {
                     cp_async_wait<0>();
@@ -194,19 +215,23 @@ __global__ void __launch_bounds__(NT, MINB) batch_mh_kernel(BatchDev d, int nste
                 const unsigned long long* a = d.acc + ((size_t)ar * ninst + inst) * 2;
                 const double dtx = smin(1e16, I.dx / bitsd(a[0]));
                 const double dty = smin(1e16, I.dy / bitsd(a[1]));
-                const double dtp = m1 * smin(dtx, dty);
                 sdt[0] = m0 * smin(dtx, dty);
-                sdt[1] = 0.5 * dtp / I.dx;   // muscl_hancock.cpp:248-249
-                sdt[2] = 0.5 * dtp / I.dy;
-                sdt[3] = 1.0 / I.dx;         // 352-353
+                if (SCHEME == 1) {
+                    const double dtp = m1 * smin(dtx, dty);
+                    sdt[1] = 0.5 * dtp / I.dx;   // muscl_hancock.cpp:248-249
+                    sdt[2] = 0.5 * dtp / I.dy;
+                }
+                sdt[3] = 1.0 / I.dx;             // muscl_hancock.cpp:352-353, godunov.cpp:97-98
                 sdt[4] = 1.0 / I.dy;
             }
             __syncthreads();
             const double dt = sdt[0], hdx = sdt[1], hdy = sdt[2], one_dx = sdt[3], one_dy = sdt[4];
-            if (lim == 0)
-                herr += mh_tile_fluxes<TX, TY, NT, 0>(sU, sA, sF, sG, g, g1, hdx, hdy, x0, y0, I.n, I.n);
+            if (SCHEME == 0)
+                herr += go_tile_fluxes<TX, TY, NT>(sU, sW, sF, sG, g, g1, x0, y0, I.n, I.n);
+            else if (lim == 0)
+                herr += mh_tile_fluxes<TX, TY, NT, 0>(sU, sW, sF, sG, g, g1, hdx, hdy, x0, y0, I.n, I.n);
             else
-                herr += mh_tile_fluxes<TX, TY, NT, 1>(sU, sA, sF, sG, g, g1, hdx, hdy, x0, y0, I.n, I.n);
+                herr += mh_tile_fluxes<TX, TY, NT, 1>(sU, sW, sF, sG, g, g1, hdx, hdy, x0, y0, I.n, I.n);
             double mx = 0.0, my = 0.0;
             double* __restrict__ out = Un + I.off;
             const size_t plane = (size_t)I.n * I.n;
@@ -217,7 +242,8 @@ __global__ void __launch_bounds__(NT, MINB) batch_mh_kernel(BatchDev d, int nste
                     double un[4];
 #pragma unroll
                     for (int v = 0; v < 4; ++v) {
-                        un[v] = mh_update<TX, TY>(sU, sF, sG, v, ox, oy, dt, one_dx, one_dy);
+                        un[v] = SCHEME == 0 ? go_update<TX, TY>(sU, sF, sG, v, ox, oy, dt, one_dx, one_dy)
+                                            : mh_update<TX, TY>(sU, sF, sG, v, ox, oy, dt, one_dx, one_dy);
                         out[v * plane + (size_t)gy * I.n + gx] = un[v];
                     }
                     double sx, sy;
@@ -240,7 +266,7 @@ __global__ void __launch_bounds__(NT, MINB) batch_mh_kernel(BatchDev d, int nste
     if (herr) atomicAdd(reinterpret_cast<unsigned long long*>(&c->hllc_errors), (unsigned long long)herr);
     if (blockIdx.x == 0 && threadIdx.x == 0 && c->err == 0) {
         c->step = step0 + nsteps;
-        c->calls = calls0 + 2 * nsteps;
+        c->calls = calls0 + CALLS * nsteps;
     }
 }
 
@@ -277,20 +303,22 @@ struct BatchConfig {
 };
 
 // tile shape, threads, halo staging buffers, CTAs per SM the registers are budgeted for
+// (the last, 32x4 tiles of 128 threads at four CTAs per SM, is for batches too small to give
+// every SM several large tiles per step, such as a single 256^2 case)
 constexpr BatchConfig kConfigs[] = {{32, 14, 256, 1, 2}, {32, 14, 256, 2, 2}, {32, 16, 256, 1, 2},
-                                    {32, 12, 256, 1, 3}, {32, 12, 256, 2, 2}};
-constexpr int kNumConfigs = 5;
+                                    {32, 12, 256, 1, 3}, {32, 12, 256, 2, 2}, {32, 4, 128, 1, 4}};
+constexpr int kNumConfigs = 6;
 
-template <int TX, int TY, int NT, int ST>
+template <int SCHEME, int TX, int TY, int ST>
 size_t batch_smem() {
-    using T = MhTile<TX, TY>;
-    return (size_t)(ST * T::U_SIZE + T::A_SIZE + T::F_SIZE + T::G_SIZE) * 8;
+    using T = BatchTile<SCHEME, TX, TY>;
+    return (size_t)(ST * T::U_SIZE + T::WORK) * 8;
 }
 
-template <int TX, int TY, int NT, int ST, int MINB>
+template <int SCHEME, int TX, int TY, int NT, int ST, int MINB>
 cudaError_t launch_batch(const BatchDev& d, int nsteps, int sms, cudaStream_t s, bool cfl_only) {
-    auto k = batch_mh_kernel<TX, TY, NT, ST, MINB>;
-    const size_t smem = batch_smem<TX, TY, NT, ST>();
+    auto k = batch_kernel<SCHEME, TX, TY, NT, ST, MINB>;
+    const size_t smem = batch_smem<SCHEME, TX, TY, ST>();
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     if (cfl_only) {
@@ -316,14 +344,22 @@ cudaError_t launch_batch(const BatchDev& d, int nsteps, int sms, cudaStream_t s,
     return cudaLaunchKernelEx(&cfg, k, d, nsteps);
 }
 
-cudaError_t launch_batch_config(int k, const BatchDev& d, int nsteps, int sms, cudaStream_t s, bool cfl_only) {
+template <int SCHEME>
+cudaError_t launch_scheme_config(int k, const BatchDev& d, int nsteps, int sms, cudaStream_t s, bool cfl_only) {
     switch (k) {
-        case 0: return launch_batch<32, 14, 256, 1, 2>(d, nsteps, sms, s, cfl_only);
-        case 1: return launch_batch<32, 14, 256, 2, 2>(d, nsteps, sms, s, cfl_only);
-        case 2: return launch_batch<32, 16, 256, 1, 2>(d, nsteps, sms, s, cfl_only);
-        case 3: return launch_batch<32, 12, 256, 1, 3>(d, nsteps, sms, s, cfl_only);
-        default: return launch_batch<32, 12, 256, 2, 2>(d, nsteps, sms, s, cfl_only);
+        case 0: return launch_batch<SCHEME, 32, 14, 256, 1, 2>(d, nsteps, sms, s, cfl_only);
+        case 1: return launch_batch<SCHEME, 32, 14, 256, 2, 2>(d, nsteps, sms, s, cfl_only);
+        case 2: return launch_batch<SCHEME, 32, 16, 256, 1, 2>(d, nsteps, sms, s, cfl_only);
+        case 3: return launch_batch<SCHEME, 32, 12, 256, 1, 3>(d, nsteps, sms, s, cfl_only);
+        case 4: return launch_batch<SCHEME, 32, 12, 256, 2, 2>(d, nsteps, sms, s, cfl_only);
+        default: return launch_batch<SCHEME, 32, 4, 128, 1, 4>(d, nsteps, sms, s, cfl_only);
     }
+}
+
+cudaError_t launch_batch_config(int k, int scheme, const BatchDev& d, int nsteps, int sms, cudaStream_t s,
+                                bool cfl_only) {
+    return scheme == 0 ? launch_scheme_config<0>(k, d, nsteps, sms, s, cfl_only)
+                       : launch_scheme_config<1>(k, d, nsteps, sms, s, cfl_only);
 }
 
 }  // namespace hf
@@ -336,6 +372,7 @@ struct hf_batch {
     int sms = 0;
     double gamma = 1.4, cfl = 0.8;
     int limiter = 0;
+    int scheme = 1;             // 0 Godunov, 1 MUSCL-Hancock
     std::vector<hf::BatchInst> inst;
     long long total_cells = 0;
     std::vector<void*> allocs;
@@ -421,7 +458,7 @@ int refresh_cfl(hf_batch* b) {
     BCK(cudaMemsetAsync(b->acc + (size_t)ar * 2 * b->inst.size(), 0, 2 * b->inst.size() * sizeof(unsigned long long), b->stream));
     int r = ensure_tiles(b, 0);
     if (r) return r;
-    BCK(hf::launch_batch_config(0, devview(b, 0), 0, b->sms, b->stream, true));
+    BCK(hf::launch_batch_config(0, b->scheme, devview(b, 0), 0, b->sms, b->stream, true));
     BCK(cudaStreamSynchronize(b->stream));
     return HF_OK;
 }
@@ -453,16 +490,21 @@ int hf_batch_create(const char* manifest, size_t len, hf_batch** out) {
             if (c["model"]["model"].string() != "EulerIdealGas")
                 return bfail(b, HF_ERR_UNSUPPORTED, "model must be EulerIdealGas");
             const Json& sch = c["scheme"];
-            if (sch["type"].string() != "MUSCLHancock" || sch["riemann"].string() != "HLLCEuler" ||
-                sch["ode"].string() != "ForwardEuler")
-                return bfail(b, HF_ERR_UNSUPPORTED, "batched cases are MUSCL-Hancock + HLLC + forward Euler");
-            const std::string lim = sch["limiter"].string();
-            int L = lim == "MinBee" ? 0 : (lim == "VanLeer" ? 1 : -1);
-            if (L < 0) return bfail(b, HF_ERR_UNSUPPORTED, "limiter '" + lim + "' not supported");
+            const std::string type = sch["type"].string();
+            const int S = type == "Godunov" ? 0 : (type == "MUSCLHancock" ? 1 : -1);
+            if (S < 0 || sch["riemann"].string() != "HLLCEuler" || sch["ode"].string() != "ForwardEuler")
+                return bfail(b, HF_ERR_UNSUPPORTED,
+                             "batched cases are Godunov or MUSCL-Hancock + HLLC + forward Euler");
+            int L = 0;
+            if (S == 1) {
+                const std::string lim = sch["limiter"].string();
+                L = lim == "MinBee" ? 0 : (lim == "VanLeer" ? 1 : -1);
+                if (L < 0) return bfail(b, HF_ERR_UNSUPPORTED, "limiter '" + lim + "' not supported");
+            }
             double gamma = c["model"]["gamma"].number(), cfl = c["simulation"]["cfl"].number();
-            if (i == 0) { b->gamma = gamma; b->cfl = cfl; b->limiter = L; }
-            else if (gamma != b->gamma || cfl != b->cfl || L != b->limiter)
-                return bfail(b, HF_ERR_UNSUPPORTED, "all batched cases share gamma, cfl and limiter");
+            if (i == 0) { b->gamma = gamma; b->cfl = cfl; b->limiter = L; b->scheme = S; }
+            else if (gamma != b->gamma || cfl != b->cfl || L != b->limiter || S != b->scheme)
+                return bfail(b, HF_ERR_UNSUPPORTED, "all batched cases share scheme, gamma, cfl and limiter");
             const Json& blocks = c["mesh"]["blocks"];
             if (blocks.size() != 1) return bfail(b, HF_ERR_UNSUPPORTED, "batched cases have one block");
             const Json& blk = blocks[0];
@@ -482,14 +524,17 @@ int hf_batch_create(const char* manifest, size_t len, hf_batch** out) {
             I.dy = (yt - yb) / ny;
             b->inst.push_back(I);
             b->total_cells += (long long)nx * ny;
+            // the centroids depend on the ghost width in floating point (mesh_block.cpp:239-257),
+            // so the initial condition is sampled on the scheme's own ghost layout
+            const int gh = S == 0 ? 1 : 2;
             std::vector<double> soa;
-            hf::BlockGeom G{nx + 4, ny + 4, xl, yb, I.dx, I.dy};
-            hf::build_initial_state(c["initial_condition"], gamma, G, 2, soa);
+            hf::BlockGeom G{nx + 2 * gh, ny + 2 * gh, xl, yb, I.dx, I.dy};
+            hf::build_initial_state(c["initial_condition"], gamma, G, gh, soa);
             std::vector<double> inner((size_t)4 * nx * ny);
             for (int v = 0; v < 4; ++v)
                 for (int j = 0; j < ny; ++j)
-                    std::memcpy(&inner[((size_t)v * ny + j) * nx], &soa[((size_t)v * (ny + 4) + j + 2) * (nx + 4) + 2],
-                                nx * sizeof(double));
+                    std::memcpy(&inner[((size_t)v * ny + j) * nx],
+                                &soa[((size_t)v * (ny + 2 * gh) + j + gh) * (nx + 2 * gh) + gh], nx * sizeof(double));
             init.push_back(std::move(inner));
         }
     } catch (const std::exception& e) {
@@ -521,6 +566,7 @@ int hf_batch_create(const char* manifest, size_t len, hf_batch** out) {
     C.g1 = b->gamma - 1.0;
     C.cfl = b->cfl;
     C.limiter = b->limiter;
+    C.scheme = b->scheme;
     C.ninst = (int)n;
     BCK(cudaMemcpy(b->dctrl, &C, sizeof C, cudaMemcpyHostToDevice));
     for (size_t i = 0; i < n; ++i)
@@ -581,7 +627,7 @@ int hf_batch_run(hf_batch* b, int64_t nsteps, int use_graph) {
     if (r) return r;
     hf::BatchDev d = devview(b, b->config);
     if (!use_graph) {
-        BCK(hf::launch_batch_config(b->config, d, (int)nsteps, b->sms, b->stream, false));
+        BCK(hf::launch_batch_config(b->config, b->scheme, d, (int)nsteps, b->sms, b->stream, false));
         return HF_OK;
     }
     cudaGraphExec_t exec = nullptr;
@@ -590,7 +636,7 @@ int hf_batch_run(hf_batch* b, int64_t nsteps, int use_graph) {
     if (!exec) {
         cudaGraph_t graph;
         BCK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
-        cudaError_t e = hf::launch_batch_config(b->config, d, (int)nsteps, b->sms, b->stream, false);
+        cudaError_t e = hf::launch_batch_config(b->config, b->scheme, d, (int)nsteps, b->sms, b->stream, false);
         cudaError_t e2 = cudaStreamEndCapture(b->stream, &graph);
         if (e != cudaSuccess) return bfail(b, HF_ERR_CUDA, std::string("capture: ") + cudaGetErrorString(e));
         if (e2 != cudaSuccess) return bfail(b, HF_ERR_CUDA, std::string("end capture: ") + cudaGetErrorString(e2));
@@ -633,9 +679,9 @@ int hf_batch_autotune(hf_batch* b, int steps_per_trial, int* best, double* ms_pe
         if (r) return r;
         hf::BatchDev d = devview(b, k);
         // warm (first launch pays the shared-memory opt-in), then time
-        BCK(hf::launch_batch_config(k, d, 1, b->sms, b->stream, false));
+        BCK(hf::launch_batch_config(k, b->scheme, d, 1, b->sms, b->stream, false));
         cudaEventRecord(e0, b->stream);
-        BCK(hf::launch_batch_config(k, d, steps_per_trial, b->sms, b->stream, false));
+        BCK(hf::launch_batch_config(k, b->scheme, d, steps_per_trial, b->sms, b->stream, false));
         cudaEventRecord(e1, b->stream);
         int er = check_device_error(b);
         if (er) return er;

@@ -16,6 +16,7 @@
 
 #include "hf_cart.h"
 #include "hf_device.cuh"
+#include "hf_godunov_tile.cuh"
 #include "hf_mh_tile.cuh"
 
 namespace hf {
@@ -441,15 +442,15 @@ __global__ void __launch_bounds__(NT, 3) mh_kernel(Ctrl* __restrict__ c, const M
 // ------------------------------------------------------------------------------------
 template <int TX, int TY>
 struct GoLayout {
-    static constexpr int UX = TX + 2, UY = TY + 2, NC = UX * UY;
-    static constexpr int NQ = 12;   // u v p Et a fx0 fx1 fx2 fx3 fy0 fy2 fy3 (fy1 == fx2)
+    using T = GoTile<TX, TY>;
+    static constexpr int NC = T::NC;
     static constexpr int U_OFF = 0;
-    static constexpr int Q_OFF = U_OFF + 4 * NC;
-    static constexpr int F_OFF = Q_OFF + NQ * NC;
-    static constexpr int G_OFF = F_OFF + 4 * TY * (TX + 1);
-    static constexpr int END = G_OFF + 4 * (TY + 1) * TX;
-    static constexpr size_t BYTES = (size_t)END * 8 + 16;
-    static constexpr int TMA_BYTES = 4 * NC * 8;
+    static constexpr int Q_OFF = U_OFF + T::U_SIZE;
+    static constexpr int F_OFF = Q_OFF + T::Q_SIZE;
+    static constexpr int G_OFF = F_OFF + T::F_SIZE;
+    static constexpr int END = G_OFF + T::G_SIZE;
+    static constexpr size_t BYTES = (size_t)END * 8 + 16;   // + mbarrier
+    static constexpr int TMA_BYTES = T::U_SIZE * 8;
 };
 
 template <int TX, int TY, int NT>
@@ -482,65 +483,8 @@ __global__ void __launch_bounds__(NT) godunov_kernel(Ctrl* __restrict__ c,
     if (!load_tile<L::TMA_BYTES>(sU, bar, p ? &tm1 : &tm0, x0, y0, c)) return;
     const double one_dx = sc[0], one_dy = sc[1];
 
-#define Q(k, cell) sQ[(k) * L::NC + (cell)]
-    // cells beyond the first ghost layer and faces beyond the last face are skipped: no in-block
-    // cell reads them, and their zero-filled states would only take the slow division paths
-    for (int cell = threadIdx.x; cell < L::NC; cell += NT) {
-        if (x0 - 1 + cell % L::UX > B.nx || y0 - 1 + cell / L::UX > B.ny) continue;
-        Prim w = to_prim(g1, sU[cell], sU[L::NC + cell], sU[2 * L::NC + cell], sU[3 * L::NC + cell]);
-        double fx[4], fy[4];
-        flux<0>(w, fx);
-        flux<1>(w, fy);
-        Q(0, cell) = w.u; Q(1, cell) = w.v; Q(2, cell) = w.p; Q(3, cell) = w.Et;
-        Q(4, cell) = sound(g, w.r, w.p);
-        Q(5, cell) = fx[0]; Q(6, cell) = fx[1]; Q(7, cell) = fx[2]; Q(8, cell) = fx[3];
-        Q(9, cell) = fy[0]; Q(10, cell) = fy[2]; Q(11, cell) = fy[3];
-    }
-    __syncthreads();
-    int herr = 0;
-    auto load = [&](int cell, double* U, Prim& w, double& a, double* fx, double* fy) {
-#pragma unroll
-        for (int v = 0; v < 4; ++v) U[v] = sU[v * L::NC + cell];
-        w.r = U[0]; w.u = Q(0, cell); w.v = Q(1, cell); w.p = Q(2, cell); w.Et = Q(3, cell); w.q = 0.0;
-        a = Q(4, cell);
-        if (fx) { fx[0] = Q(5, cell); fx[1] = Q(6, cell); fx[2] = Q(7, cell); fx[3] = Q(8, cell); }
-        if (fy) { fy[0] = Q(9, cell); fy[1] = Q(7, cell); fy[2] = Q(10, cell); fy[3] = Q(11, cell); }
-    };
-    // x faces: face f of row r sits between tile cells (f-1, r) and (f, r)
-    for (int it = threadIdx.x; it < (TX + 1) * TY; it += NT) {
-        const int fx = it % (TX + 1), fy = it / (TX + 1);
-        if (x0 + fx > B.nx || y0 + fy >= B.ny) continue;
-        const int cl = (fy + 1) * L::UX + fx, cr = cl + 1;
-        double UL[4], UR[4], FL[4], FR[4], F[4], aL, aR;
-        Prim wL, wR;
-        load(cl, UL, wL, aL, FL, nullptr);
-        load(cr, UR, wR, aR, FR, nullptr);
-        const int bad = hllc<0>(UL, wL, aL, FL, UR, wR, aR, FR, F);
-        if (bad && owned_face(x0 + fx, fx, TX, B.nx, y0 + fy, B.ny)) {
-            ++herr;
-            atomicMin(&c->first_bad, face_key(c->step, b, 0, y0 + fy, x0 + fx));
-        }
-#pragma unroll
-        for (int v = 0; v < 4; ++v) sF[(v * TY + fy) * (TX + 1) + fx] = F[v];
-    }
-    for (int it = threadIdx.x; it < TX * (TY + 1); it += NT) {
-        const int gx = it % TX, gy = it / TX;
-        if (x0 + gx >= B.nx || y0 + gy > B.ny) continue;
-        const int cb = gy * L::UX + gx + 1, ct = cb + L::UX;
-        double UB[4], UT[4], FB[4], FT[4], F[4], aB, aT;
-        Prim wB, wT;
-        load(cb, UB, wB, aB, nullptr, FB);
-        load(ct, UT, wT, aT, nullptr, FT);
-        const int bad = hllc<1>(UB, wB, aB, FB, UT, wT, aT, FT, F);
-        if (bad && owned_face(y0 + gy, gy, TY, B.ny, x0 + gx, B.nx)) {
-            ++herr;
-            atomicMin(&c->first_bad, face_key(c->step, b, 1, y0 + gy, x0 + gx));
-        }
-#pragma unroll
-        for (int v = 0; v < 4; ++v) sG[(v * (TY + 1) + gy) * TX + gx] = F[v];
-    }
-#undef Q
-    __syncthreads();
+    const int herr = go_tile_fluxes<TX, TY, NT>(sU, sQ, sF, sG, g, g1, x0, y0, B.nx, B.ny, &c->first_bad,
+                                                face_key(c->step, b, 0, 0, 0));
     double* __restrict__ out = B.buf[p ^ 1];
     const size_t plane = (size_t)B.ty * B.pitch;
     double mx = 0.0, my = 0.0;
@@ -552,11 +496,7 @@ __global__ void __launch_bounds__(NT) godunov_kernel(Ctrl* __restrict__ c,
             const size_t o = (size_t)(gyy + 1) * B.pitch + (gxx + 1);
 #pragma unroll
             for (int v = 0; v < 4; ++v) {
-                const double Lv = (one_dx * (sF[(v * TY + oy) * (TX + 1) + ox] -
-                                             sF[(v * TY + oy) * (TX + 1) + ox + 1])) +
-                                  (one_dy * (sG[(v * (TY + 1) + oy) * TX + ox] -
-                                             sG[(v * (TY + 1) + oy + 1) * TX + ox]));
-                un[v] = dt * Lv + sU[v * L::NC + (oy + 1) * L::UX + ox + 1];
+                un[v] = go_update<TX, TY>(sU, sF, sG, v, ox, oy, dt, one_dx, one_dy);
                 out[v * plane + o] = un[v];
                 if (hout) __stcs(&hout[((size_t)v * B.ty + gyy + 1) * B.tx + gxx + 1], un[v]);
             }

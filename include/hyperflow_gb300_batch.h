@@ -1,12 +1,14 @@
-/* HyperFlow-GB300 -- C ABI of the batched MUSCL-Hancock step.
+/* HyperFlow-GB300 -- C ABI of the batched single-block step.
  *
  * Many independent single-block cases advance together: the reference's MUSCL-Hancock step
- * (src/fvm_2d_cart/scheme/muscl_hancock/muscl_hancock.cpp:41-376, TimeStep
- * src/fvm_2d_cart/scheme/timestep/timestep.cpp:29-68, ForwardEuler forward_euler.cpp:15-33)
+ * (src/fvm_2d_cart/scheme/muscl_hancock/muscl_hancock.cpp:41-376) or Godunov step
+ * (src/fvm_2d_cart/scheme/godunov/godunov.cpp:27-118), with TimeStep
+ * (src/fvm_2d_cart/scheme/timestep/timestep.cpp:29-68) and ForwardEuler (forward_euler.cpp:15-33),
  * applied to every case with its own CFL dt, in one persistent cooperative kernel launch per
  * run of steps (optionally captured in a CUDA graph).  Each case's results equal what the
- * reference computes for that case alone, bit for bit.  Status codes are the HF_* codes of
- * hyperflow_gb300.h.  States are interior-only SoA [4][n][n].
+ * reference computes for that case alone, bit for bit.  A batch of one runs a small case's
+ * whole loop in one launch.  Status codes are the HF_* codes of hyperflow_gb300.h.  States are
+ * interior-only SoA [4][n][n].
  */
 #ifndef HYPERFLOW_GB300_BATCH_H
 #define HYPERFLOW_GB300_BATCH_H
@@ -24,7 +26,8 @@ typedef struct hf_batch hf_batch;
 
 /* manifest: {"cases": [case, case, ...]}, each a case file of the reference's schema
  * (src/fvm_2d_cart/simulation/parser/parser.cpp) with one square block, Transmissive on all
- * sides, MUSCLHancock + HLLCEuler + ForwardEuler; all cases share gamma, cfl and limiter.
+ * sides, Godunov or MUSCLHancock + HLLCEuler + ForwardEuler; all cases share the scheme, gamma,
+ * cfl and limiter.
  * Replaces one JSONParser + Simulation per case.  On failure *out may be set; destroy it. */
 int hf_batch_create(const char* manifest_json, size_t len, hf_batch** out);
 void hf_batch_destroy(hf_batch* b);

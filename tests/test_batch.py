@@ -96,3 +96,42 @@ def test_batch_full_workload_sample_matches_oracle(port_lib):
     for i in sorted(pick):
         ref, t = _oracle_interior(m["cases"][i], 3)
         np.testing.assert_array_equal(b.state(i), ref, err_msg=f"case {i} side {sides[i]}")
+
+
+@pytest.mark.gpu
+def test_batch_godunov_every_config_matches_oracle(port_lib):
+    """Batched Godunov cases (one TimeStep call per step) equal the oracle, bit for bit."""
+    from hyperflow_gb300 import BatchSolver, cases
+    from hyperflow_gb300.batch import configs
+    m = cases.batch_manifest(7, seed=5, side_min=40, side_max=100, scheme="Godunov")
+    steps = 30
+    ref = []
+    for c in m["cases"]:
+        from oracle.oracle import Oracle
+        o = Oracle(c, nthreads=4)
+        o.run(steps)
+        ref.append((o.state(0)[:, 1:-1, 1:-1], o.t))
+    for k in range(len(configs())):
+        b = BatchSolver(m)
+        b.set_config(k)
+        b.run(steps, graph=k % 2 == 0)
+        b.sync()
+        for i in range(b.ninstances):
+            np.testing.assert_array_equal(b.state(i), ref[i][0], err_msg=f"config {k} case {i}")
+            assert b.instance_time(i)[0] == ref[i][1]
+        assert b.counters()["calls"] == steps
+
+
+@pytest.mark.gpu
+def test_batch_of_one_runs_the_256_godunov_workload(port_lib):
+    """The 256^2 Godunov quadrant problem x 200 steps as a batch of one (the whole run in one
+    persistent launch) equals the per-block solver and the oracle's dt stream end state."""
+    from hyperflow_gb300 import BatchSolver, CartSolver, cases
+    case = cases.quadrant_case(256)
+    b = BatchSolver({"cases": [case]})
+    b.run(200, graph=True)
+    b.sync()
+    s = CartSolver(case)
+    s.run(200)
+    np.testing.assert_array_equal(b.state(0), s.state(0)[:, 1:-1, 1:-1])
+    assert b.instance_time(0)[0] == s.time()[0]
