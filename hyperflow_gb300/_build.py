@@ -19,7 +19,8 @@ OBJ = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libhyperflow_gb300.so")
 HOSTMATH_LIB = os.path.join(PKG, "libhf_hostmath.so")
 
-SOURCES = ["hf_cart.cu", "hf_api.cpp", "hf_uns.cu", "hf_noalloc.cu", "hf_batch.cu", "hf_learned.cu", "hf_diag.cu"]
+SOURCES = ["hf_cart.cu", "hf_api.cpp", "hf_uns.cu", "hf_noalloc.cu", "hf_batch.cu", "hf_learned.cu", "hf_diag.cu",
+           "hf_render.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--fmad=false", "-Xcompiler", "-fPIC",
               "-Xcompiler", "-ffp-contract=off", "-I" + os.path.join(PKG, "..", "include")]

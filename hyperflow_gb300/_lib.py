@@ -121,6 +121,7 @@ SIGNATURES = {
     "hf_lc_mlp_backward": (_i, [_p, _p, _p, _i, _p]),
     "hf_lc_stream": (_i, [_p, C.POINTER(_p)]),
     # self-tests (include/hyperflow_gb300_diag.h)
+    "hf_render_gray": (_i, [_p, _i, _i, _d, _d, _i, _d, _d, _p, _p, _p, _p]),
     "hf_diag_div_check": (_i, [C.c_uint64, _i64, _i, C.POINTER(_i64), _p]),
 }
 
