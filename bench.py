@@ -127,6 +127,19 @@ def dist_env():
     return ws, rank, local
 
 
+def replica_value(ms: float, ws: int, cells: int, steps: int, pg=None, device="cuda"):
+    """Whole-job throughput of N independent replicas: the slowest rank's time bounds the job
+    (max over ranks), and every rank updated `cells` cells per step.  Returns (Mcell-updates/s,
+    the max time in ms)."""
+    t_max = ms
+    if pg is not None:
+        import torch
+        tt = torch.tensor([ms], dtype=torch.float64, device=device)
+        pg.all_reduce(tt, op=pg.ReduceOp.MAX)
+        t_max = float(tt.item())
+    return ws * cells * steps / (t_max / 1e3) / 1e6, t_max
+
+
 def cpu_run(case, steps: int, nthreads: int):
     """The oracle (C restatement of the reference step) on host cores."""
     from oracle.oracle import Oracle, build_port
@@ -412,12 +425,7 @@ def main():
     ms = e0.elapsed_time(e1)
     stencil_ms, stencil_launches = s.kernel_time(0)
     s.profile(False)
-    t_max = ms
-    if pg is not None:
-        tt = torch.tensor([ms], device="cuda")
-        pg.all_reduce(tt, op=pg.ReduceOp.MAX)
-        t_max = float(tt.item())
-    value = ws * cells * args.steps / (t_max / 1e3) / 1e6
+    value, t_max = replica_value(ms, ws, cells, args.steps, pg)
     hllc_fallbacks = s.hllc_errors()
 
     if args.quick:
