@@ -36,7 +36,7 @@ def _rank(rank, ws, port, out):
 
 def test_replica_value_takes_the_slowest_rank_and_sums_the_cells():
     ws, port = 2, _free_port()
-    with mp.Manager() as man:
+    with mp.get_context("spawn").Manager() as man:
         out = man.dict()
         mp.spawn(_rank, args=(ws, port, out), nprocs=ws, join=True)
         res = dict(out)
