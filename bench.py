@@ -46,7 +46,7 @@ def workload_name(args):
         if args.scheme == "Godunov":
             return f"quadrant_riemann_{args.n}x{args.n}_godunov_hllc_fp64"
         return f"quadrant_riemann_{args.n}x{args.n}_muscl_hancock_{args.limiter.lower()}_hllc_fp64"
-    return WORKLOAD
+    return WORKLOAD if args.limiter == "MinBee" else WORKLOAD.replace("minbee", args.limiter.lower())
 
 
 def peaks():

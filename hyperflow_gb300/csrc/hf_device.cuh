@@ -202,7 +202,13 @@ HF_HD double limiter(double r) {
         return is_nan(r) ? 1.0 : div_rn(2.0, 1.0 + r);
     } else {          // VanLeerLimiter::operator() vanleer.cpp:29-36
         if (le0(r)) return 0.0;
-        return smin(div_rn(2.0 * r, 1.0 + r), xi_right(r));
+        // min(2r/(1+r), 2/(1+r)) for a finite r > 0: 1 + r > 1 keeps denom_tol out of xi_right,
+        // and correct rounding is monotone, so the minimum is the first quotient when r <= 1 and
+        // the second when r > 1 -- one division instead of two, the same bits.  NaN and +inf
+        // take the reference's expression (2r/(1+r) is NaN there, and so is the minimum).
+        const uint64_t rb = f64_bits(r);
+        if (rb >= 0x7FF0000000000000ull) return smin(div_rn(2.0 * r, 1.0 + r), xi_right(r));
+        return rb <= 0x3FF0000000000000ull ? div_rn(2.0 * r, 1.0 + r) : div_rn(2.0, 1.0 + r);
     }
 }
 

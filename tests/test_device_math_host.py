@@ -137,7 +137,10 @@ def test_limiters_on_special_ratios(hm, port_lib):
     port_lib.hfo_limiter.restype = ctypes.c_double
     port_lib.hfo_limiter.argtypes = [ctypes.c_int, ctypes.c_double]
     rng = np.random.default_rng(4)
-    rs = np.concatenate([_specials(), rng.lognormal(0, 2, 500), -rng.lognormal(0, 2, 50)])
+    near_one = 1.0 + np.concatenate([np.arange(-64, 65) * np.finfo(float).eps, rng.uniform(-1e-3, 1e-3, 200)])
+    tiny = np.array([5e-324, 1e-320, 2.2250738585072014e-308, 1e-300, 1e-200, 1e-20])
+    huge = np.array([1e20, 1e200, 1e300, 1.7976931348623157e308])
+    rs = np.concatenate([_specials(), rng.lognormal(0, 2, 20000), -rng.lognormal(0, 2, 50), near_one, tiny, huge])
     for kind in range(2):
         for r in rs:
             got, want = hm.hm_limiter(kind, float(r)), port_lib.hfo_limiter(kind, float(r))
