@@ -95,9 +95,9 @@ struct hf_ctx {
     int next_block = 0;         // next block hf_advance_block expects
     // graphs of one step (index = clamp flag)
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    int strict = 0;             // hf_set_strict: a zero-flux face stops the loop
     // profiling
     bool profile = false;
-    int strict = 0;             // hf_set_strict
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev[2];
     size_t ev_used[2] = {0, 0};
     std::string err;

@@ -453,8 +453,10 @@ struct GoLayout {
     static constexpr int TMA_BYTES = T::U_SIZE * 8;
 };
 
+// three 256-thread CTAs per SM (80 registers, 74 KB of shared memory with 32x10 tiles): measured
+// 3 % faster than two CTAs of 32x14 tiles at 110 registers, and than 32x8 or 32x6 tiles
 template <int TX, int TY, int NT>
-__global__ void __launch_bounds__(NT) godunov_kernel(Ctrl* __restrict__ c,
+__global__ void __launch_bounds__(NT, 3) godunov_kernel(Ctrl* __restrict__ c,
                                                      const MeshDev* __restrict__ m, int b,
                                                      const __grid_constant__ CUtensorMap tm0,
                                                      const __grid_constant__ CUtensorMap tm1,
@@ -514,7 +516,7 @@ __global__ void __launch_bounds__(NT) godunov_kernel(Ctrl* __restrict__ c,
 // launchers
 // ------------------------------------------------------------------------------------
 constexpr int kMhTX = 32, kMhTY = 12, kMhNT = 256;
-constexpr int kGoTX = 32, kGoTY = 14, kGoNT = 256;
+constexpr int kGoTX = 32, kGoTY = 10, kGoNT = 256;
 
 StencilTiles stencil_tiles(int scheme) {
     return scheme == 0 ? StencilTiles{kGoTX + 2, kGoTY + 2} : StencilTiles{kMhTX + 4, kMhTY + 4};

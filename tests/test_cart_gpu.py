@@ -294,10 +294,11 @@ def test_gpu_step_io_equals_upload_step_download(memory, scheme):
 
 @pytest.mark.parametrize("scheme,limiter", [("Godunov", None), ("MUSCLHancock", "MinBee"),
                                             ("MUSCLHancock", "VanLeer")])
-@pytest.mark.parametrize("nx,ny", [(1, 1), (1, 5), (3, 2), (33, 1), (33, 13), (65, 29), (31, 43)])
+@pytest.mark.parametrize("nx,ny", [(1, 1), (1, 5), (3, 2), (33, 1), (33, 13), (65, 25), (33, 11), (65, 21),
+                                   (31, 43)])
 def test_gpu_tiny_and_ragged_grids_match_oracle(scheme, limiter, nx, ny, port_lib):
-    """Grids smaller than one tile, and one cell past a tile edge in x and y (tiles 32x12 /
-    32x14): partial tiles and clipped faces.  Blocks narrower than 2 x ghost cells (the ghost
+    """Grids smaller than one tile, and one cell past a tile edge in x and y (MUSCL-Hancock
+    tiles 32x12, Godunov 32x10): partial tiles and clipped faces.  Blocks narrower than 2 x ghost cells (the ghost
     fill would mirror ghost cells into ghost cells, in the reference's sequential order) are
     refused with HF_ERR_UNSUPPORTED instead of computed."""
     from oracle.oracle import Oracle
