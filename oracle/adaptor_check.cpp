@@ -4,7 +4,8 @@
 // target `adaptor`).  With a GPU it runs Simulation::solve-style steps on both the reference
 // CPU objects and the adaptor and compares the fields bit for bit; without one, creating the
 // GPU context reports the missing device and the check exits 3, which shows the adaptor
-// compiles and links against the reference's real interfaces.
+// compiles and links against the reference's real interfaces (the reference objects are built
+// first, so that part runs everywhere).
 #include <cstdio>
 #include <fstream>
 #include <functional>
@@ -30,17 +31,11 @@ int main(int argc, char** argv) {
     ss << in.rdbuf();
     const std::string text = ss.str();
     const int steps = std::atoi(argv[2]);
-    std::shared_ptr<GpuContext> gpu;
-    try {
-        gpu = std::make_shared<GpuContext>(text);
-    } catch (const std::exception& e) {
-        std::printf("no GPU context: %s\n", e.what());
-        return 3;
-    }
     json config = json::parse(text);
     // the reference's objects, twice: one mesh stepped by its own scheme, one through the adaptor
     JSONParser p_ref(config), p_gpu(config);
     auto model = p_ref.generate_model();
+    p_gpu.generate_model();   // the parser's Dirichlet states are converted with its own model
     auto mesh_ref = p_ref.generate_mesh(), mesh_gpu = p_gpu.generate_mesh();
     auto ic = p_ref.generate_initial_condition();
     mesh_ref->initialise_field_values(ic);
@@ -49,6 +44,13 @@ int main(int argc, char** argv) {
     auto ts = std::make_shared<TimeStep>(model, p_ref.get_cfl());
     auto scheme = p_ref.generate_spatial_scheme(model, riemann, ts, mesh_ref);
     auto ode = p_ref.generate_ode_solver();
+    std::shared_ptr<GpuContext> gpu;
+    try {
+        gpu = std::make_shared<GpuContext>(text);
+    } catch (const std::exception& e) {
+        std::printf("reference objects built; no GPU context: %s\n", e.what());
+        return 3;
+    }
     auto gscheme = std::make_shared<GpuScheme>(gpu);
     auto gode = std::make_shared<GpuForwardEuler>(gpu);
     for (int s = 0; s < steps; ++s) {   // Simulation::solve's body (simulation.cpp:85-110)
