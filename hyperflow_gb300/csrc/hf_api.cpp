@@ -629,6 +629,9 @@ int hf_time_step(hf_ctx* ctx, double* dt) {
     if (!ctx) return HF_ERR_ARG;
     int r = set_clamp(ctx, 0);
     if (r != HF_OK) return r;
+    // a step's accumulators start from zero whether or not the ghost fill ran on the device
+    // (a caller that fills the ghosts on the host uploads them and calls this directly)
+    CK(hf::launch_step_begin(ctx->dctrl, ctx->stream));
     CK(hf::launch_ghost_cfl(ctx->dctrl, ctx->dmesh, ctx->hmesh.total_ghost, ctx->stream));
     if (dt) {
         CK(cudaMemcpyAsync(dt, &ctx->dctrl->dt_cfl, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));

@@ -537,6 +537,11 @@ cudaError_t stencil_prepare() {
                                 (int)GoLayout<kGoTX, kGoTY>::BYTES);
 }
 
+cudaError_t launch_step_begin(Ctrl* c, cudaStream_t s) {
+    step_begin_kernel<<<1, 1, 0, s>>>(c);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_bc_fill(Ctrl* c, const MeshDev* m, const int* side_len, int nblocks, cudaStream_t s) {
     step_begin_kernel<<<1, 1, 0, s>>>(c);
     for (int b = 0; b < nblocks; ++b)

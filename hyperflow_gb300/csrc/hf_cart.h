@@ -49,6 +49,9 @@ struct StencilTiles {
 // ghost fill: one launch per (block, side) in the reference order; side_len[2b] = total_x,
 // side_len[2b+1] = total_y of block b
 cudaError_t launch_bc_fill(Ctrl* c, const MeshDev* m, const int* side_len, int nblocks, cudaStream_t s);
+// start of a step without a device ghost fill: stop flags, the ghost and next-state maxima and the
+// reduction ticket reset (launch_bc_fill does this first as well)
+cudaError_t launch_step_begin(Ctrl* c, cudaStream_t s);
 cudaError_t launch_ghost_cfl(Ctrl* c, const MeshDev* m, long long total_ghost, cudaStream_t s);
 cudaError_t launch_interior_cfl(Ctrl* c, const MeshDev* m, int b, int nx, int ny, int parity,
                                 cudaStream_t s);

@@ -70,7 +70,9 @@ int hf_get_state(hf_ctx* ctx, int block, double* cons, int layout);
 int hf_apply_bcs(hf_ctx* ctx);
 
 /* TimeStep::operator() (src/fvm_2d_cart/scheme/timestep/timestep.cpp:29-68) as called by
- * Scheme::calculate_time_step: CFL dt over all cells incl. ghosts; advances the call counter */
+ * Scheme::calculate_time_step: CFL dt over all cells incl. ghosts; advances the call counter.
+ * It starts the step (its wave-speed accumulators), so it follows either hf_apply_bcs or
+ * uploads of fields whose ghosts the caller filled on the host. */
 int hf_time_step(hf_ctx* ctx, double* dt);
 
 /* ODESolver(Scheme(block b)) + set_fields for one block (simulation.cpp:106-110, fused

@@ -127,6 +127,33 @@ def test_gpu_strict_mode_stops_at_the_zero_flux_step():
     assert s.run(3) == 3
 
 
+@pytest.mark.parametrize("limiter", ["MinBee", "VanLeer"])
+def test_gpu_adaptor_call_sequence_matches_oracle(limiter, port_lib):
+    """The reference-side adaptor's call sequence (hyperflow_gb300/adaptor/gpu_scheme.h): per
+    step the host applies the boundary conditions, every block's fields are uploaded in MeshBlock
+    order [x][y][var] with ghosts, the device forms dt, and each block is advanced on the device
+    and downloaded into the host fields -- bit for bit against the oracle's own step, dt included.
+    The oracle stands in for the reference's host objects here; tests/test_adaptor.py compiles
+    the adaptor itself against the reference's sources."""
+    from hyperflow_gb300 import cases
+    from oracle.oracle import Oracle
+    case = cases.forward_facing_step_case(20, limiter=limiter)
+    ref, host = Oracle(case), Oracle(case)
+    s = _solver(case)
+    for _ in range(12):
+        dt_ref = float(ref.run(1)[0])
+        host.apply_bcs()                                        # Mesh::apply_bcs on the host
+        for b in range(s.nblocks):
+            s.set_state(b, host.U[b].transpose(2, 1, 0), layout="aos")
+        dt = s.calculate_time_step()                            # GpuScheme::calculate_time_step
+        assert dt == dt_ref
+        for b in range(s.nblocks):                              # GpuForwardEuler, block by block
+            s.advance_block(b, dt)
+            host.U[b][...] = s.state(b, layout="aos").transpose(2, 1, 0)
+    for b in range(s.nblocks):
+        np.testing.assert_array_equal(host.U[b], ref.state(b))
+
+
 def test_gpu_piecewise_api_equals_device_loop():
     """apply_bcs / calculate_time_step / advance_block driven from the host (the
     reference's Simulation::solve sequence) equals hf_run's device loop, with and

@@ -212,3 +212,27 @@ def test_uns_gpu_negative_pressure_cell_and_strict_mode():
     assert t.time()[1] == 1
     s.clear_error_cell()
     assert s.last_error_cell() is None
+
+
+@pytest.mark.gpu
+def test_uns_gpu_adaptor_call_sequence_matches_oracle():
+    """The unstructured adaptor's call sequence (hyperflow_gb300/adaptor/gpu_uns_scheme.h):
+    per step the cells' values are uploaded, the device forms dt (TimeStep), advances, and the
+    values are downloaded -- bit for bit against the oracle stepping its own copy."""
+    from hyperflow_gb300 import UnsSolver, meshgen
+    from oracle import oracle
+    g = load("tri_hole_3k")
+    s = UnsSolver(g["case"], mesh_text=meshgen.hmsh_text(g["verts"], g["codes"]))
+    m = s.mesh_arrays()
+    U = s.state().copy()
+    host = U.copy()
+    calls = 0
+    for _ in range(15):
+        dts, calls = oracle.uns_run(1.4, g["case"]["simulation"]["cfl"], calls, m["pair_start"], m["nbr"],
+                                    m["angle"], m["length"], m["area"], m["rin"], _inlet(g["case"]), U, 1)
+        s.set_state(host)                       # GpuUnsTimeStep: upload the cells' values
+        dt = s.calculate_time_step()
+        assert dt == float(dts[0])
+        s.advance(dt)                           # GpuUnsForwardEuler
+        host = s.state()
+    np.testing.assert_array_equal(host, U)
