@@ -96,6 +96,10 @@ struct hf_ctx {
     // graphs of one step (index = clamp flag)
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     int strict = 0;             // hf_set_strict: a zero-flux face stops the loop
+    // piecewise steps: has this step been started (accumulators reset) and are the ghost
+    // maxima those of the current fields (a TimeStep call since the last fill or upload)?
+    bool step_started = false;
+    bool ghost_fresh = false;
     // profiling
     bool profile = false;
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev[2];
@@ -405,6 +409,7 @@ int enqueue_step(hf_ctx* ctx, bool profiled) {
     if (profiled) ev_record(ctx, 0, false);
     if (ctx->ring_slots > 0) CK(hf::launch_frame_copy(ctx->dctrl, ctx->dmesh, ctx->ring, ctx->stream));
     CK(hf::launch_finalize(ctx->dctrl, ctx->stream));
+    ctx->step_started = ctx->ghost_fresh = false;
     return HF_OK;
 }
 
@@ -591,6 +596,7 @@ int hf_set_state(hf_ctx* ctx, int b, const double* cons, int layout) {
     CK(cudaMemcpyAsync(&ctx->dctrl->int_s[p][b][0], zero, sizeof zero, cudaMemcpyHostToDevice, ctx->stream));
     CK(hf::launch_interior_cfl(ctx->dctrl, ctx->dmesh, b, B.nx, B.ny, p, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
+    ctx->ghost_fresh = false;
     return HF_OK;
 }
 
@@ -622,6 +628,8 @@ int hf_apply_bcs(hf_ctx* ctx) {
     if (!ctx) return HF_ERR_ARG;
     if (ctx->next_block != 0) return fail(ctx, HF_ERR_STATE, "apply_bcs in the middle of a step");
     CK(hf::launch_bc_fill(ctx->dctrl, ctx->dmesh, ctx->side_len, ctx->nblocks, ctx->stream));
+    ctx->step_started = true;
+    ctx->ghost_fresh = false;
     return HF_OK;
 }
 
@@ -633,6 +641,8 @@ int hf_time_step(hf_ctx* ctx, double* dt) {
     // (a caller that fills the ghosts on the host uploads them and calls this directly)
     CK(hf::launch_step_begin(ctx->dctrl, ctx->stream));
     CK(hf::launch_ghost_cfl(ctx->dctrl, ctx->dmesh, ctx->hmesh.total_ghost, ctx->stream));
+    ctx->step_started = true;
+    ctx->ghost_fresh = true;
     if (dt) {
         CK(cudaMemcpyAsync(dt, &ctx->dctrl->dt_cfl, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
         CK(cudaStreamSynchronize(ctx->stream));
@@ -643,12 +653,20 @@ int hf_time_step(hf_ctx* ctx, double* dt) {
 int hf_advance_block(hf_ctx* ctx, int b, double dt) {
     if (!ctx || b < 0 || b >= ctx->nblocks) return HF_ERR_ARG;
     if (b != ctx->next_block) return fail(ctx, HF_ERR_STATE, "blocks must be advanced in order");
-    if (b == 0) CK(hf::launch_set_dt(ctx->dctrl, dt, ctx->stream));
+    if (b == 0) {
+        // a caller that gives dt itself may have skipped hf_time_step: start the step, and give
+        // the MUSCL-Hancock predictor's TimeStep call the ghost maxima of the current fields
+        if (!ctx->step_started) CK(hf::launch_step_begin(ctx->dctrl, ctx->stream));
+        if (ctx->scheme == 1 && !ctx->ghost_fresh)
+            CK(hf::launch_ghost_cfl(ctx->dctrl, ctx->dmesh, ctx->hmesh.total_ghost, ctx->stream, 0));
+        CK(hf::launch_set_dt(ctx->dctrl, dt, ctx->stream));
+    }
     CK(hf::launch_stencil(ctx->dctrl, ctx->dmesh, b, ctx->blocks[b].nx, ctx->blocks[b].ny,
                           ctx->scheme, ctx->limiter, &ctx->tmap[b][0], &ctx->tmap[b][1], ctx->stream));
     if (b == ctx->nblocks - 1) {
         CK(hf::launch_finalize(ctx->dctrl, ctx->stream));
         ctx->next_block = 0;
+        ctx->step_started = ctx->ghost_fresh = false;
     } else {
         ctx->next_block = b + 1;
     }
@@ -740,6 +758,7 @@ int hf_step_io(hf_ctx* ctx, const double* const* in, double* const* out, double*
                                   &ctx->tmap[b][0], &ctx->tmap[b][1], ctx->stream, out[b]));
         }
         CK(hf::launch_finalize(ctx->dctrl, ctx->stream));
+        ctx->step_started = ctx->ghost_fresh = false;
         if (dt) CK(cudaMemcpyAsync(dt, &ctx->dctrl->dt, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
         CK(cudaStreamSynchronize(ctx->stream));
         return strict_check(ctx);
@@ -768,6 +787,7 @@ int hf_step_io(hf_ctx* ctx, const double* const* in, double* const* out, double*
                              (size_t)B.tx * 8, (size_t)4 * B.ty, cudaMemcpyDeviceToHost, ctx->copy_stream));
     }
     CK(hf::launch_finalize(ctx->dctrl, ctx->stream));
+    ctx->step_started = ctx->ghost_fresh = false;
     if (dt) CK(cudaMemcpyAsync(dt, &ctx->dctrl->dt, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
     CK(cudaStreamSynchronize(ctx->copy_stream));
@@ -1086,6 +1106,7 @@ int hf_checkpoint_load(hf_ctx* ctx, const void* buf, size_t bytes) {
     C.err = 0;
     C.strict = cur.strict;
     ctx->drained = 0;
+    ctx->step_started = ctx->ghost_fresh = false;
     for (int b = 0; b < ctx->nblocks; ++b)
         for (int k = 0; k < 2; ++k) {
             size_t n = (size_t)4 * ctx->blocks[b].ty * ctx->blocks[b].pitch * sizeof(double);

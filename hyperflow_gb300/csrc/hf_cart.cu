@@ -126,8 +126,9 @@ __device__ __forceinline__ void ghost_cell_ij(const BlockDev& B, int g, long lon
 
 constexpr int kRedThreads = 256;
 
+// form_dt = 0: the ghost maxima only (for a predictor TimeStep in a step whose dt the caller gave)
 __global__ void __launch_bounds__(kRedThreads) ghost_cfl_kernel(Ctrl* __restrict__ c,
-                                                                const MeshDev* __restrict__ m) {
+                                                                const MeshDev* __restrict__ m, int form_dt) {
     if (c->done) return;
     const int p = (int)(c->step & 1);
     const double g = c->gamma, g1 = c->g1;
@@ -150,6 +151,7 @@ __global__ void __launch_bounds__(kRedThreads) ghost_cfl_kernel(Ctrl* __restrict
         block_max2_atomic<kRedThreads>(mx, my, &c->ghost_s[b][0], &c->ghost_s[b][1]);
         __syncthreads();
     }
+    if (!form_dt) return;
     // last CTA to finish forms the dt of this TimeStep call
     __shared__ bool last;
     __threadfence();
@@ -553,10 +555,10 @@ cudaError_t launch_bc_fill(Ctrl* c, const MeshDev* m, const int* side_len, int n
     return cudaGetLastError();
 }
 
-cudaError_t launch_ghost_cfl(Ctrl* c, const MeshDev* m, long long total_ghost, cudaStream_t s) {
+cudaError_t launch_ghost_cfl(Ctrl* c, const MeshDev* m, long long total_ghost, cudaStream_t s, int form_dt) {
     long long want = (total_ghost + kRedThreads - 1) / kRedThreads;
     int grid = (int)(want < 1 ? 1 : (want > 4 * 152 ? 4 * 152 : want));
-    ghost_cfl_kernel<<<grid, kRedThreads, 0, s>>>(c, m);
+    ghost_cfl_kernel<<<grid, kRedThreads, 0, s>>>(c, m, form_dt);
     return cudaGetLastError();
 }
 

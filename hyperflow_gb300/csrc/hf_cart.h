@@ -52,7 +52,10 @@ cudaError_t launch_bc_fill(Ctrl* c, const MeshDev* m, const int* side_len, int n
 // start of a step without a device ghost fill: stop flags, the ghost and next-state maxima and the
 // reduction ticket reset (launch_bc_fill does this first as well)
 cudaError_t launch_step_begin(Ctrl* c, cudaStream_t s);
-cudaError_t launch_ghost_cfl(Ctrl* c, const MeshDev* m, long long total_ghost, cudaStream_t s);
+// wave-speed maxima over the ghost cells; with form_dt the last CTA forms the step's dt (a
+// TimeStep call: counter, clamps, frame points)
+cudaError_t launch_ghost_cfl(Ctrl* c, const MeshDev* m, long long total_ghost, cudaStream_t s,
+                             int form_dt = 1);
 cudaError_t launch_interior_cfl(Ctrl* c, const MeshDev* m, int b, int nx, int ny, int parity,
                                 cudaStream_t s);
 cudaError_t launch_set_dt(Ctrl* c, double dt, cudaStream_t s);

@@ -78,7 +78,8 @@ int hf_time_step(hf_ctx* ctx, double* dt);
 /* ODESolver(Scheme(block b)) + set_fields for one block (simulation.cpp:106-110, fused
  * forward Euler of forward_euler.cpp:15-33).  Blocks must be advanced in order 0..B-1 within
  * a step; MUSCL-Hancock's predictor TimeStep call (muscl_hancock.cpp:246) happens on the
- * device against the partly advanced mesh, as in the reference. */
+ * device against the partly advanced mesh, as in the reference -- over all cells, ghosts
+ * included, also when the caller gives dt without calling hf_time_step in that step. */
 int hf_advance_block(hf_ctx* ctx, int block, double dt);
 /* all blocks in order with the same dt, then t += dt */
 int hf_advance(hf_ctx* ctx, double dt);

@@ -154,6 +154,38 @@ def test_gpu_adaptor_call_sequence_matches_oracle(limiter, port_lib):
         np.testing.assert_array_equal(host.U[b], ref.state(b))
 
 
+@pytest.mark.parametrize("scheme", ["Godunov", "MUSCLHancock"])
+@pytest.mark.parametrize("upload", [False, True])
+def test_gpu_fixed_dt_steps_without_time_step_match_oracle(scheme, upload, port_lib):
+    """A caller that gives dt itself and never calls TimeStep: ghost fill (on the device, or on
+    the host and uploaded), then every block advanced.  The MUSCL-Hancock predictor still makes
+    its own TimeStep call over all cells, ghosts included -- here the Dirichlet inflow ghosts are
+    the fastest cells (Mach 3 inflow into a slower start), so their maxima must be current."""
+    from hyperflow_gb300 import cases
+    from oracle.oracle import Oracle
+    case = cases.forward_facing_step_case(20, scheme=scheme) if scheme == "Godunov" else \
+        cases.forward_facing_step_case(20, limiter="VanLeer")
+    case["initial_condition"]["init_state"] = [1.4, 0.5, 0.0, 1.0]
+    o, host, s = Oracle(case), Oracle(case), _solver(case)
+    for k in range(10):
+        dt = 2e-3 if k < 5 else 4e-3
+        o.apply_bcs()
+        o.advance(dt)
+        if upload:
+            host.apply_bcs()
+            for b in range(s.nblocks):
+                s.set_state(b, host.U[b])
+        else:
+            s.apply_bcs()
+        s.advance(dt)
+        if upload:
+            for b in range(s.nblocks):
+                host.U[b][...] = s.state(b)
+    for b in range(s.nblocks):
+        np.testing.assert_array_equal(s.state(b), o.state(b))
+    assert s.time()[1] == o.calls
+
+
 def test_gpu_piecewise_api_equals_device_loop():
     """apply_bcs / calculate_time_step / advance_block driven from the host (the
     reference's Simulation::solve sequence) equals hf_run's device loop, with and
