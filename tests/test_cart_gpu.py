@@ -186,6 +186,40 @@ def test_gpu_fixed_dt_steps_without_time_step_match_oracle(scheme, upload, port_
     assert s.time()[1] == o.calls
 
 
+def test_gpu_interleaved_contexts_are_independent():
+    """Two contexts of different cases and schemes stepped in turn, in one process and on one
+    device (the device loop, the piecewise calls, the host-buffer step), each equal to the same
+    case run alone."""
+    import threading
+    from hyperflow_gb300 import cases
+    ca = cases.forward_facing_step_case(20, limiter="MinBee")
+    cb = cases.quadrant_case(64, scheme="Godunov")
+    a, b = _solver(ca), _solver(cb)
+    for k in range(6):
+        a.run(2)
+        b.apply_bcs()
+        b.advance(b.calculate_time_step())
+        host = [a.state(i) for i in range(a.nblocks)]
+        a.step_io(host)
+        b.run(1, graph=False)
+    a0, b0 = _solver(ca), _solver(cb)
+    a0.run(18)
+    b0.run(12)
+    for i in range(a.nblocks):
+        np.testing.assert_array_equal(a.state(i), a0.state(i))
+    np.testing.assert_array_equal(b.state(0), b0.state(0))
+    # two host threads, one context each
+    a1, b1 = _solver(ca), _solver(cb)
+    t = [threading.Thread(target=a1.run, args=(18,)), threading.Thread(target=b1.run, args=(12,))]
+    for x in t:
+        x.start()
+    for x in t:
+        x.join()
+    for i in range(a.nblocks):
+        np.testing.assert_array_equal(a1.state(i), a0.state(i))
+    np.testing.assert_array_equal(b1.state(0), b0.state(0))
+
+
 def test_gpu_piecewise_api_equals_device_loop():
     """apply_bcs / calculate_time_step / advance_block driven from the host (the
     reference's Simulation::solve sequence) equals hf_run's device loop, with and
