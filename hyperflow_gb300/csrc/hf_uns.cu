@@ -74,7 +74,7 @@ struct UnsMesh {
 __device__ __forceinline__ void rot(double c, double s, const double* f, double* o) {
     o[0] = f[0];
     o[1] = c * f[1] + s * f[2];
-    o[2] = -1.0 * s * f[1] + c * f[2];
+    o[2] = (-s) * f[1] + c * f[2];   // -1.0 * sin(..) * f[1] there; -1.0 * s is exactly -s
     o[3] = f[3];
 }
 
@@ -266,9 +266,13 @@ __global__ void __launch_bounds__(kUnsNT, MINB) uns_step_kernel(UnsCtrl* __restr
             double f[4];
             const int ed = m.pair_edge ? m.pair_edge[e] : -1;
             if (ed >= 0) {          // edge-based mode: the owner's flux, negated on the other side
-                const double sg = (double)m.pair_sign[e];
+                // (a sign flip, not a multiplication by -1.0: the same value, off the FP64 pipe)
+                const bool neg = m.pair_sign[e] < 0;
 #pragma unroll
-                for (int v = 0; v < 4; ++v) f[v] = sg * m.edge_flux[(size_t)v * m.nedges + ed];
+                for (int v = 0; v < 4; ++v) {
+                    const double x = m.edge_flux[(size_t)v * m.nedges + ed];
+                    f[v] = neg ? -x : x;
+                }
             } else if (pair_flux(m, U, N, g, g1, e, cv, f)) {
                 ++herr;
                 atomicMin(&c->first_bad, uns_key(c->step, i));
@@ -280,7 +284,7 @@ __global__ void __launch_bounds__(kUnsNT, MINB) uns_step_kernel(UnsCtrl* __restr
         double un[4];
 #pragma unroll
         for (int v = 0; v < 4; ++v) {
-            const double L = -1.0 * (inv * acc[v]);
+            const double L = -(inv * acc[v]);   // -1.0 * (...) of godunov.cpp, exactly
             un[v] = dt * L + cv[v];
             Un[v * N + i] = un[v];
         }
