@@ -293,6 +293,62 @@ def bench_quad256(args):
     s.close()
 
 
+def bench_learned(args):
+    """The learned coarse solver's step: 512^2 FP32 MUSCL-Hancock MinBee + HLLC with the MLP
+    face-flux correction (features -> 64 -> 64 -> 4, BF16 on the tensor cores, FP32
+    accumulation) on every face, random-init weights (throughput does not depend on them), the
+    change guard on.  Timed with CUDA events on the solver's stream, with and without the MLP;
+    the MLP path's throughput is its FLOPs over the time it adds to a step."""
+    import numpy as np
+    import torch
+    from hyperflow_gb300 import CartSolver, cases
+    from hyperflow_gb300.learned import LearnedSolver, init_params
+    n = 512
+    case = cases.quadrant_case(n, scheme="MUSCLHancock", limiter="MinBee", cfl=cases.CFL_2D)
+    s = CartSolver(case)
+    U0 = s.state(0)[:, 2:-2, 2:-2].astype(np.float32)
+    s.close()
+    ls = LearnedSolver(n, 1.0 / n, cfl=cases.CFL_2D)
+    ls.set_params(init_params(0))
+    ls.set_bound(0.5)
+    stream = torch.cuda.ExternalStream(ls.stream())
+
+    def timed(use_mlp):
+        ls.set_state(U0)
+        dt = ls.cfl_dt()
+        for _ in range(args.warmup):
+            ls.step(dt, use_mlp)
+        return timed_device(stream, lambda: [ls.step(dt, use_mlp) for _ in range(args.steps)])
+
+    with Clocks(0) as clk:
+        ms_mlp = timed(True)
+    ms_plain = timed(False)
+    cells = n * n
+    faces = 2 * n * (n + 1)
+    flop = 16896.0 * faces * args.steps            # 2 x (64x64 + 64x64 + 64x4) per face, x 2 (FMA)
+    extra_s = max(ms_mlp - ms_plain, 1e-9) / 1e3
+    achieved = flop / extra_s / 1e12
+    peak = 1947.2
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            peak = float(json.load(f).get("bf16_tflops", peak))
+    print(json.dumps({
+        "metric": "Mcell-updates/s", "value": cells * args.steps / (ms_mlp / 1e3) / 1e6, "unit": "Mcell-updates/s",
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_mlp / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32 + bf16 MLP",
+        "data": "synthetic (the 512^2 quadrant Riemann problem; random-init MLP weights)",
+        "config": {"workload": "learned_coarse_512x512_muscl_hancock_minbee_mlp_flux_correction", "cells": cells,
+                   "faces": faces, "mlp": "features->64->64->4 GELU, BF16 weights, FP32 accumulation"},
+        "plain_fp32_value": cells * args.steps / (ms_plain / 1e3) / 1e6,
+        "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved / peak, "traffic": None, "peak_kind": "measured",
+                     "kernel": "mlp_forward_kernel (tcgen05.mma kind::f16, TMEM accumulators); achieved = "
+                               "MLP FLOPs over the time the MLP path adds to a step"},
+        "cpu_baseline": None, "e2e": None, "gpu_launches": None, "clocks": clk.summary()}), flush=True)
+    ls.close()
+
+
 def bench_uns(args):
     """The unstructured workload: ~1M triangles of a jittered-lattice Delaunay mesh of
     [0,4]x[0,2] minus a disc, Mach 2 inflow, CFL 0.5, Godunov + HLLC, edge-based fluxes,
@@ -353,7 +409,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--limiter", default="MinBee", choices=["MinBee", "VanLeer"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="CPU-baseline sample budget")
-    ap.add_argument("--workload", default="ffs", choices=["ffs", "square", "batch", "uns", "quad256"],
+    ap.add_argument("--workload", default="ffs", choices=["ffs", "square", "batch", "uns", "quad256", "learned"],
                     help="ffs: the 3-block forward-facing step (default); square: one n x n block; "
                          "batch: 512 batched Riemann problems; uns: the 1M-triangle channel")
     ap.add_argument("--instances", type=int, default=512, help="batch workload: number of instances")
@@ -369,7 +425,7 @@ def main():
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
-    if args.workload in ("batch", "uns", "quad256"):
+    if args.workload in ("batch", "uns", "quad256", "learned"):
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "unavailable":
                               "the reference arm is timed on the forward-facing step and square workloads"}))
@@ -377,7 +433,7 @@ def main():
         import numpy as np  # noqa: F401
         import torch
         torch.cuda.set_device(0)
-        {"batch": bench_batch, "uns": bench_uns, "quad256": bench_quad256}[args.workload](args)
+        {"batch": bench_batch, "uns": bench_uns, "quad256": bench_quad256, "learned": bench_learned}[args.workload](args)
         return
 
     from hyperflow_gb300 import cases

@@ -117,6 +117,7 @@ SIGNATURES = {
     "hf_lc_step": (_i, [_p, _d, _i, C.POINTER(_i64)]),
     "hf_lc_run_to": (_i, [_p, _d, _i, C.POINTER(_i64), C.POINTER(_i64)]),
     "hf_lc_train_step": (_i, [_p, _p, _p, _p, _d, _d, C.POINTER(_d)]),
+    "hf_lc_features": (_i, [_p, _p, _p]),
     "hf_lc_mlp_forward": (_i, [_p, _p, _i, _p]),
     "hf_lc_mlp_backward": (_i, [_p, _p, _p, _i, _p]),
     "hf_lc_stream": (_i, [_p, C.POINTER(_p)]),

@@ -181,37 +181,73 @@ __global__ void plain_flux_kernel(const float* __restrict__ U, Grid G, float dt,
     }
 }
 
-// features (BF16 [nf][64]) and the correction scale of every face
-__global__ void features_kernel(const float* __restrict__ U, Grid G, __nv_bfloat16* __restrict__ X,
-                                float* __restrict__ scale /* [nf][2]: rho_ref, c_ref */) {
+// primitives of every cell, formed once: each is shared by the stencils of up to 16 faces
+__global__ void prims_kernel(const float* __restrict__ U, int n, float g1, float4* __restrict__ W) {
+    const size_t pl = (size_t)n * n;
+    for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < pl; k += (size_t)gridDim.x * blockDim.x) {
+        const float c[4] = {U[k], U[pl + k], U[2 * pl + k], U[3 * pl + k]};
+        const PrimF w = prim(g1, c);
+        W[k] = make_float4(w.r, w.u, w.v, w.p);
+    }
+}
+
+__device__ __forceinline__ float4 prim_at(const float4* __restrict__ W, int n, int i, int j) {
+    return W[(size_t)mir(j, n) * n + mir(i, n)];
+}
+
+constexpr int kFeatNT = 256;
+
+// features (BF16 [nf][64]) and the correction scale of every face.  Each thread forms one
+// face's 64 features in registers; a CTA's 256 faces (32 KB) go out through shared memory as
+// contiguous 16-byte stores (a face's row is 128 bytes, so per-element stores would touch a
+// different line in every lane).
+__global__ void __launch_bounds__(kFeatNT) features_kernel(const float4* __restrict__ W, Grid G,
+                                                          __nv_bfloat16* __restrict__ X,
+                                                          float* __restrict__ scale /* [nf][2] */) {
+    __shared__ uint4 stage[kFeatNT * 8];
     const int nf = 2 * (G.n + 1) * G.n;
-    for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < nf; f += gridDim.x * blockDim.x) {
-        int dir, i, j;
-        face_of(f, G.n, dir, i, j);
-        // lower cell (il, jl), normal unit (dn_i, dn_j), tangent (dt_i, dt_j)
-        const int il = dir == 0 ? i - 1 : i, jl = dir == 0 ? j : j - 1;
-        const int ni = dir == 0, nj = dir == 1, ti = dir == 1, tj = dir == 0;
-        float cl[4], cr[4];
-        load_cell(U, G.n, il, jl, cl);
-        load_cell(U, G.n, il + ni, jl + nj, cr);
-        PrimF wl = prim(G.g1, cl), wr = prim(G.g1, cr);
-        const float rr = 0.5f * (wl.r + wr.r), pr = 0.5f * (wl.p + wr.p);
-        const float cref = sqrtf(fmaxf(G.g * pr / rr, 1e-12f));
-        scale[2 * (size_t)f] = rr;
-        scale[2 * (size_t)f + 1] = cref;
-        __nv_bfloat16* x = X + (size_t)f * NIN;
-        int k = 0;
-        for (int a = -1; a <= 2; ++a)
-            for (int b = -1; b <= 2; ++b) {
-                float c[4];
-                load_cell(U, G.n, il + a * ni + b * ti, jl + a * nj + b * tj, c);
-                PrimF w = prim(G.g1, c);
-                const float un = dir == 0 ? w.u : w.v, ut = dir == 0 ? w.v : w.u;
-                x[k++] = __float2bfloat16_rn(w.r / rr - 1.0f);
-                x[k++] = __float2bfloat16_rn(un / cref);
-                x[k++] = __float2bfloat16_rn(ut / cref);
-                x[k++] = __float2bfloat16_rn(w.p / pr - 1.0f);
-            }
+    for (int base = blockIdx.x * kFeatNT; base < nf; base += gridDim.x * kFeatNT) {
+        const int f = base + threadIdx.x;
+        uint32_t pk[32] = {};
+        if (f < nf) {
+            int dir, i, j;
+            face_of(f, G.n, dir, i, j);
+            // lower cell (il, jl), normal unit (ni, nj), tangent (ti, tj)
+            const int il = dir == 0 ? i - 1 : i, jl = dir == 0 ? j : j - 1;
+            const int ni = dir == 0, nj = dir == 1, ti = dir == 1, tj = dir == 0;
+            const float4 wl = prim_at(W, G.n, il, jl), wr = prim_at(W, G.n, il + ni, jl + nj);
+            const float rr = 0.5f * (wl.x + wr.x), pr = 0.5f * (wl.w + wr.w);
+            const float cref = sqrtf(fmaxf(G.g * pr / rr, 1e-12f));
+            scale[2 * (size_t)f] = rr;
+            scale[2 * (size_t)f + 1] = cref;
+            int k = 0;
+#pragma unroll
+            for (int a = -1; a <= 2; ++a)
+#pragma unroll
+                for (int b = -1; b <= 2; ++b) {
+                    const float4 w = prim_at(W, G.n, il + a * ni + b * ti, jl + a * nj + b * tj);
+                    const float un = dir == 0 ? w.y : w.z, ut = dir == 0 ? w.z : w.y;
+                    const __nv_bfloat16 x0 = __float2bfloat16_rn(w.x / rr - 1.0f);
+                    const __nv_bfloat16 x1 = __float2bfloat16_rn(un / cref);
+                    const __nv_bfloat16 x2 = __float2bfloat16_rn(ut / cref);
+                    const __nv_bfloat16 x3 = __float2bfloat16_rn(w.w / pr - 1.0f);
+                    pk[k++] = (uint32_t)__bfloat16_as_ushort(x0) | ((uint32_t)__bfloat16_as_ushort(x1) << 16);
+                    pk[k++] = (uint32_t)__bfloat16_as_ushort(x2) | ((uint32_t)__bfloat16_as_ushort(x3) << 16);
+                }
+        }
+        // chunk q (16 bytes) of face t sits at t * 8 + (q ^ (t & 7)): conflict-free both ways
+#pragma unroll
+        for (int q = 0; q < 8; ++q)
+            stage[threadIdx.x * 8 + (q ^ (threadIdx.x & 7))] =
+                make_uint4(pk[4 * q], pk[4 * q + 1], pk[4 * q + 2], pk[4 * q + 3]);
+        __syncthreads();
+        const int nvalid = nf - base < kFeatNT ? nf - base : kFeatNT;
+        uint4* __restrict__ dst = reinterpret_cast<uint4*>(X + (size_t)base * NIN);
+        for (int L = threadIdx.x; L < nvalid * 8; L += kFeatNT) {
+            const int t = L >> 3, q = L & 7;
+            dst[L] = stage[t * 8 + (q ^ (t & 7))];
+        }
+        __syncthreads();
     }
 }
 
@@ -711,6 +747,7 @@ struct hf_lc {
     float *U[2] = {nullptr, nullptr}, *F = nullptr, *dF = nullptr, *scale = nullptr, *Y = nullptr;
     float *Z1 = nullptr, *Z2 = nullptr, *dY = nullptr, *T = nullptr, *wv = nullptr;
     __nv_bfloat16 *X = nullptr, *Wb = nullptr;
+    float4* Wp = nullptr;      // per-cell primitives (rho, u, v, p) for the feature stencils
     float *P = nullptr, *grad = nullptr, *m1 = nullptr, *m2 = nullptr, *maxs = nullptr;
     unsigned char* ok = nullptr;
     unsigned long long* rejected = nullptr;
@@ -774,12 +811,19 @@ int check_derr(hf_lc* L) {
 }
 
 // plain fluxes, and (use_mlp) features -> MLP -> corrections for state U[cur]
+void launch_features(hf_lc* L) {
+    hf::lc::Grid G = grid(L);
+    const int nf = nfaces(L);
+    prims_kernel<<<blocks_for(L->n * L->n, 256), 256, 0, L->stream>>>(L->U[L->cur], L->n, G.g1, L->Wp);
+    features_kernel<<<blocks_for(nf, hf::lc::kFeatNT), hf::lc::kFeatNT, 0, L->stream>>>(L->Wp, G, L->X, L->scale);
+}
+
 int fluxes(hf_lc* L, float dt, bool use_mlp, bool save_acts) {
     hf::lc::Grid G = grid(L);
     const int nf = nfaces(L);
     plain_flux_kernel<<<blocks_for(nf, 256), 256, 0, L->stream>>>(L->U[L->cur], G, dt, L->F);
     if (use_mlp) {
-        features_kernel<<<blocks_for(nf, 256), 256, 0, L->stream>>>(L->U[L->cur], G, L->X, L->scale);
+        launch_features(L);
         launch_forward(L, nf, save_acts);
         correction_kernel<<<blocks_for(nf, 256), 256, 0, L->stream>>>(L->Y, L->scale, L->n, L->dF);
     }
@@ -814,7 +858,8 @@ int hf_lc_create(int n, double dx, double gamma, double cfl, int limiter, hf_lc*
         (r = alloc(L, &L->Wb, (size_t)(H * NIN + H * H + NOUT * H))) || (r = alloc(L, &L->P, (size_t)NPARAM)) ||
         (r = alloc(L, &L->grad, (size_t)NPARAM)) || (r = alloc(L, &L->m1, (size_t)NPARAM)) ||
         (r = alloc(L, &L->m2, (size_t)NPARAM)) || (r = alloc(L, &L->maxs, 4)) || (r = alloc(L, &L->ok, nf)) ||
-        (r = alloc(L, &L->rejected, 1)) || (r = alloc(L, &L->loss, 1)) || (r = alloc(L, &L->derr, 1)))
+        (r = alloc(L, &L->rejected, 1)) || (r = alloc(L, &L->loss, 1)) || (r = alloc(L, &L->derr, 1)) ||
+        (r = alloc(L, &L->Wp, cells)))
         return r;
     return HF_OK;
 }
@@ -999,6 +1044,17 @@ int hf_lc_train_step(hf_lc* L, const float* U0, const float* T, const float* w, 
 }
 
 // ---- test entry points: the MLP alone on given inputs ----
+int hf_lc_features(hf_lc* L, uint16_t* x_bf16, float* scale) {
+    if (!L || !x_bf16 || !scale) return HF_ERR_ARG;
+    const size_t nf = nfaces(L);
+    launch_features(L);
+    LCK(cudaGetLastError());
+    LCK(cudaMemcpyAsync(x_bf16, L->X, nf * NIN * 2, cudaMemcpyDeviceToHost, L->stream));
+    LCK(cudaMemcpyAsync(scale, L->scale, nf * 2 * sizeof(float), cudaMemcpyDeviceToHost, L->stream));
+    LCK(cudaStreamSynchronize(L->stream));
+    return HF_OK;
+}
+
 int hf_lc_mlp_forward(hf_lc* L, const uint16_t* x_bf16, int nf, float* y) {
     if (!L || !x_bf16 || !y || nf < 1 || nf > nfaces(L)) return HF_ERR_ARG;
     LCK(cudaMemcpy(L->X, x_bf16, (size_t)nf * NIN * 2, cudaMemcpyHostToDevice));

@@ -129,6 +129,19 @@ class LearnedSolver:
         self._c(lib().hf_lc_train_step(self._h, ptr, T.ctypes.data, w.ctypes.data, dt, lr, C.byref(loss)))
         return loss.value
 
+    def stream(self) -> int:
+        s = C.c_void_p()
+        self._c(lib().hf_lc_stream(self._h, C.byref(s)))
+        return s.value or 0
+
+    def features(self):
+        """(BF16 bits [nf][64], scale [nf][2]) of the current state: the network's inputs."""
+        nf = 2 * self.n * (self.n + 1)
+        x = np.empty((nf, 64), np.uint16)
+        sc = np.empty((nf, 2), np.float32)
+        self._c(lib().hf_lc_features(self._h, x.ctypes.data, sc.ctypes.data))
+        return x, sc
+
     def mlp_forward(self, x_bits: np.ndarray) -> np.ndarray:
         x = np.ascontiguousarray(x_bits, dtype=np.uint16)
         nf = x.shape[0]

@@ -64,6 +64,9 @@ int hf_lc_train_step(hf_lc* L, const float* U0, const float* T, const float* w, 
 
 /* the MLP alone (for checking it): y[nf][4] = MLP(x) with x BF16 bit patterns [nf][64];
  * backward gives dL/dparams for dL/dy = dy (packed like the parameters) */
+/* the MLP's inputs of every face for the current state (BF16 bits [nf][64], faces x first) and
+ * the correction scale [nf][2] (rho_ref, c_ref): what the step feeds the network */
+int hf_lc_features(hf_lc* L, uint16_t* x_bf16, float* scale);
 int hf_lc_mlp_forward(hf_lc* L, const uint16_t* x_bf16, int nf, float* y);
 int hf_lc_mlp_backward(hf_lc* L, const uint16_t* x_bf16, const float* dy, int nf, float* grad);
 int hf_lc_stream(hf_lc* L, void** stream);

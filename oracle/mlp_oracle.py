@@ -92,3 +92,56 @@ def backward(params, x_bits, dy, rounding: bool = True):
     g[OFF_W1:OFF_B1] = (dz1.T @ x).ravel()
     g[OFF_B1:OFF_W2] = dz1.sum(0)
     return g
+
+
+def features(U, gamma: float):
+    """The MLP's inputs for every face, restating hf_learned.cu's feature kernel in float32
+    (same operations, same order, IEEE float32 rounding): faces x first ([n][n+1], face i of
+    row j between cells i-1 and i), then y; per face the 4x4 primitive stencil (normal offsets
+    -1..2 outer, tangential -1..2 inner; cells mirrored past the edges) as rho/rho_ref - 1,
+    u_n/c_ref, u_t/c_ref, p/p_ref - 1 with rho_ref, p_ref the two face cells' means and
+    c_ref = sqrt(max(gamma p_ref / rho_ref, 1e-12)).  Returns (BF16 bits [nf][64], scale
+    [nf][2] = rho_ref, c_ref)."""
+    U = np.asarray(U, np.float32)
+    n = U.shape[1]
+    g = np.float32(gamma)
+    g1 = np.float32(gamma - 1.0)
+    r, ru, rv, E = U[0], U[1], U[2], U[3]
+    with np.errstate(all="ignore"):
+        u = ru / r
+        v = rv / r
+        q = u * u + v * v
+        p = g1 * (E - np.float32(0.5) * r * q)
+    idx = np.arange(-3, n + 3)
+    m = np.where(idx < 0, -1 - idx, np.where(idx >= n, 2 * n - 1 - idx, idx))
+    m = np.clip(m, 0, n - 1)
+
+    def at(a, jj, ii):   # a[mir(j)][mir(i)] for index arrays
+        return a[m[jj + 3], m[ii + 3]]
+
+    out_x, out_s = [], []
+    for d in (0, 1):
+        if d == 0:
+            jj, ii = np.meshgrid(np.arange(n), np.arange(n + 1), indexing="ij")
+            il, jl = ii - 1, jj
+        else:
+            jj, ii = np.meshgrid(np.arange(n + 1), np.arange(n), indexing="ij")
+            il, jl = ii, jj - 1
+        il, jl = il.ravel(), jl.ravel()
+        ni, nj = (1, 0) if d == 0 else (0, 1)
+        ti, tj = (0, 1) if d == 0 else (1, 0)
+        with np.errstate(all="ignore"):
+            rr = np.float32(0.5) * (at(r, jl, il) + at(r, jl + nj, il + ni))
+            pr = np.float32(0.5) * (at(p, jl, il) + at(p, jl + nj, il + ni))
+            cref = np.sqrt(np.maximum(g * pr / rr, np.float32(1e-12)))
+            cols = []
+            for a in (-1, 0, 1, 2):
+                for b in (-1, 0, 1, 2):
+                    ci, cj = il + a * ni + b * ti, jl + a * nj + b * tj
+                    wr, wu, wv, wp = at(r, cj, ci), at(u, cj, ci), at(v, cj, ci), at(p, cj, ci)
+                    un, ut = (wu, wv) if d == 0 else (wv, wu)
+                    cols += [wr / rr - np.float32(1.0), un / cref, ut / cref, wp / pr - np.float32(1.0)]
+        out_x.append(np.stack(cols, axis=1))
+        out_s.append(np.stack([rr, cref], axis=1))
+    x = np.concatenate(out_x).astype(np.float32)
+    return bf16_bits(x), np.concatenate(out_s).astype(np.float32)

@@ -68,6 +68,27 @@ def test_mlp_forward_on_tensor_cores_matches_oracle():
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("n", [37, 48])
+def test_features_match_oracle_bit_for_bit(n):
+    """The network's inputs (4x4 primitive stencil per face, scaled, BF16) and the correction
+    scale: the GPU kernels against the oracle's float32 restatement, bit for bit, on a state
+    after a few plain steps of a four-quadrant problem (n = 37: a partial last CTA of faces)."""
+    from oracle import mlp_oracle as M
+    from hyperflow_gb300 import CartSolver, cases
+    from hyperflow_gb300.learned import LearnedSolver
+    c = cases.quadrant_case(n, scheme="MUSCLHancock", limiter="MinBee", cfl=cases.CFL_2D)
+    U = CartSolver(c).state(0)[:, 2:-2, 2:-2].astype(np.float32)
+    ls = LearnedSolver(n, 1.0 / n, cfl=cases.CFL_2D)
+    ls.set_state(U)
+    for _ in range(6):
+        ls.step(ls.cfl_dt(), False)
+    x, sc = ls.features()
+    xr, scr = M.features(ls.state(), 1.4)
+    np.testing.assert_array_equal(sc, scr)
+    np.testing.assert_array_equal(x, xr)
+
+
+@pytest.mark.gpu
 def test_mlp_backward_matches_oracle():
     from oracle import mlp_oracle as M
     from hyperflow_gb300.learned import LearnedSolver
