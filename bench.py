@@ -12,8 +12,15 @@ Prints one JSON line (rank 0).  `value` is device-resident throughput (state in 
 CUDA events on the solver's stream around K steps); `e2e` is the same metric through the
 C ABI with host buffers (per step, hf_step_io on pinned host memory: the kernels read every
 block from the host buffers, step, and the stencils store the updated cells straight back to
-them, so the download overlaps the updates).  With --gpus N under torchrun, every rank runs an independent
-replica (the path does not shard across GPUs) and `value` sums the replicas.
+them, so the download overlaps the updates).  With --gpus N under torchrun, every rank runs an
+independent replica (the path does not shard across GPUs) and `value` sums the replicas.
+
+Other workloads (`--workload`, one JSON line each, not the headline):
+    square    one N x N four-quadrant block (--n, --scheme, --limiter)
+    batch     512 batched Riemann problems in one persistent launch (autotuned)
+    uns       the ~1M-triangle channel, edge-based (or --uns-per-side) fluxes
+    quad256   the 256^2 Godunov problem as a batch of one (the whole run one launch)
+    learned   the 512^2 learned coarse step (FP32 + the tcgen05 MLP on every face)
 """
 from __future__ import annotations
 
