@@ -18,6 +18,7 @@
 
 #include "../../include/hyperflow_gb300.h"
 #include "hf_cart.h"
+#include "hf_trace.h"
 #include "hf_json.hpp"
 
 namespace {
@@ -399,13 +400,19 @@ void ev_record(hf_ctx* ctx, int kind, bool start) {
 // one step's kernels after the ghost fill: dt, then every block, then finalize
 int enqueue_step(hf_ctx* ctx, bool profiled) {
     if (profiled) ev_record(ctx, 1, true);
-    CK(hf::launch_bc_fill(ctx->dctrl, ctx->dmesh, ctx->side_len, ctx->nblocks, ctx->stream));
-    CK(hf::launch_ghost_cfl(ctx->dctrl, ctx->dmesh, ctx->hmesh.total_ghost, ctx->stream));
+    {
+        hf::TraceRange trace_("ghost fill + dt");
+        CK(hf::launch_bc_fill(ctx->dctrl, ctx->dmesh, ctx->side_len, ctx->nblocks, ctx->stream));
+        CK(hf::launch_ghost_cfl(ctx->dctrl, ctx->dmesh, ctx->hmesh.total_ghost, ctx->stream));
+    }
     if (profiled) { ev_record(ctx, 1, false); ev_record(ctx, 0, true); }
-    for (int b = 0; b < ctx->nblocks; ++b)
-        CK(hf::launch_stencil(ctx->dctrl, ctx->dmesh, b, ctx->blocks[b].nx, ctx->blocks[b].ny,
-                              ctx->scheme, ctx->limiter, &ctx->tmap[b][0], &ctx->tmap[b][1],
-                              ctx->stream));
+    {
+        hf::TraceRange trace_("block stencils");
+        for (int b = 0; b < ctx->nblocks; ++b)
+            CK(hf::launch_stencil(ctx->dctrl, ctx->dmesh, b, ctx->blocks[b].nx, ctx->blocks[b].ny,
+                                  ctx->scheme, ctx->limiter, &ctx->tmap[b][0], &ctx->tmap[b][1],
+                                  ctx->stream));
+    }
     if (profiled) ev_record(ctx, 0, false);
     if (ctx->ring_slots > 0) CK(hf::launch_frame_copy(ctx->dctrl, ctx->dmesh, ctx->ring, ctx->stream));
     CK(hf::launch_finalize(ctx->dctrl, ctx->stream));
@@ -567,6 +574,7 @@ int hf_block_dims(const hf_ctx* ctx, int b, int dims[5]) {
 }
 
 int hf_set_state(hf_ctx* ctx, int b, const double* cons, int layout) {
+    hf::TraceRange trace_("hf_set_state");
     if (!ctx || !cons || b < 0 || b >= ctx->nblocks) return HF_ERR_ARG;
     if (layout != HF_LAYOUT_SOA && layout != HF_LAYOUT_AOS_XY) return HF_ERR_ARG;
     if (ctx->next_block != 0) return fail(ctx, HF_ERR_STATE, "state upload in the middle of a step");
@@ -601,6 +609,7 @@ int hf_set_state(hf_ctx* ctx, int b, const double* cons, int layout) {
 }
 
 int hf_get_state(hf_ctx* ctx, int b, double* cons, int layout) {
+    hf::TraceRange trace_("hf_get_state");
     if (!ctx || !cons || b < 0 || b >= ctx->nblocks) return HF_ERR_ARG;
     if (layout != HF_LAYOUT_SOA && layout != HF_LAYOUT_AOS_XY) return HF_ERR_ARG;
     const BlockHost& B = ctx->blocks[b];
@@ -625,6 +634,7 @@ int hf_get_state(hf_ctx* ctx, int b, double* cons, int layout) {
 }
 
 int hf_apply_bcs(hf_ctx* ctx) {
+    hf::TraceRange trace_("hf_apply_bcs");
     if (!ctx) return HF_ERR_ARG;
     if (ctx->next_block != 0) return fail(ctx, HF_ERR_STATE, "apply_bcs in the middle of a step");
     CK(hf::launch_bc_fill(ctx->dctrl, ctx->dmesh, ctx->side_len, ctx->nblocks, ctx->stream));
@@ -634,6 +644,7 @@ int hf_apply_bcs(hf_ctx* ctx) {
 }
 
 int hf_time_step(hf_ctx* ctx, double* dt) {
+    hf::TraceRange trace_("hf_time_step");
     if (!ctx) return HF_ERR_ARG;
     int r = set_clamp(ctx, 0);
     if (r != HF_OK) return r;
@@ -651,6 +662,7 @@ int hf_time_step(hf_ctx* ctx, double* dt) {
 }
 
 int hf_advance_block(hf_ctx* ctx, int b, double dt) {
+    hf::TraceRange trace_("hf_advance_block");
     if (!ctx || b < 0 || b >= ctx->nblocks) return HF_ERR_ARG;
     if (b != ctx->next_block) return fail(ctx, HF_ERR_STATE, "blocks must be advanced in order");
     if (b == 0) {
@@ -724,6 +736,7 @@ int hf_host_mapped(const void* p, int* mapped) {
 }
 
 int hf_step_io(hf_ctx* ctx, const double* const* in, double* const* out, double* dt) {
+    hf::TraceRange trace_("hf_step_io");
     if (!ctx || !in || !out) return HF_ERR_ARG;
     for (int b = 0; b < ctx->nblocks; ++b)
         if (!in[b] || !out[b]) return HF_ERR_ARG;
@@ -795,6 +808,7 @@ int hf_step_io(hf_ctx* ctx, const double* const* in, double* const* out, double*
 }
 
 int hf_step(hf_ctx* ctx, double* dt) {
+    hf::TraceRange trace_("hf_step");
     if (!ctx) return HF_ERR_ARG;
     if (ctx->next_block != 0) return fail(ctx, HF_ERR_STATE, "step in the middle of a step");
     int r = set_clamp(ctx, 0);
@@ -810,6 +824,7 @@ int hf_step(hf_ctx* ctx, double* dt) {
 }
 
 int hf_run(hf_ctx* ctx, int64_t n, int clamp_t_end, int use_graph, int64_t* steps_done) {
+    hf::TraceRange trace_("hf_run");
     if (!ctx || n < 0) return HF_ERR_ARG;
     if (ctx->next_block != 0) return fail(ctx, HF_ERR_STATE, "run in the middle of a step");
     long long s0 = steps_done ? read_step(ctx) : 0;

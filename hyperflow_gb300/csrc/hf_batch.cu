@@ -33,6 +33,7 @@
 #include "../../include/hyperflow_gb300_batch.h"
 #include "hf_cart.h"
 #include "hf_device.cuh"
+#include "hf_trace.h"
 #include "hf_godunov_tile.cuh"
 #include "hf_mh_tile.cuh"
 
@@ -621,6 +622,7 @@ int hf_batch_set_config(hf_batch* b, int k) {
 }
 
 int hf_batch_run(hf_batch* b, int64_t nsteps, int use_graph) {
+    hf::TraceRange trace_("hf_batch_run");
     if (!b || nsteps < 0 || nsteps > (1 << 30)) return HF_ERR_ARG;
     if (nsteps == 0) return HF_OK;
     int r = ensure_tiles(b, b->config);

@@ -32,6 +32,7 @@
 
 #include "../../include/hyperflow_gb300_learned.h"
 #include "hf_device.cuh"
+#include "hf_trace.h"
 
 namespace hf {
 namespace lc {
@@ -923,6 +924,7 @@ int hf_lc_cfl_dt(hf_lc* L, double* dt) {
 
 // one coarse step with the given dt; use_mlp adds the guarded correction
 int hf_lc_step(hf_lc* L, double dt, int use_mlp, int64_t* rejected_cells) {
+    hf::TraceRange trace_("hf_lc_step");
     if (!L || dt <= 0) return HF_ERR_ARG;
     hf::lc::Grid G = grid(L);
     int r = fluxes(L, (float)dt, use_mlp != 0, false);
@@ -955,6 +957,7 @@ int hf_lc_step(hf_lc* L, double dt, int use_mlp, int64_t* rejected_cells) {
 
 // runs until t_end with CFL dt (host loop, one sync per step for dt); returns steps
 int hf_lc_run_to(hf_lc* L, double t_end, int use_mlp, int64_t* steps, int64_t* rejected_cells) {
+    hf::TraceRange trace_("hf_lc_run_to");
     if (!L) return HF_ERR_ARG;
     int64_t k = 0, rej = 0;
     while (L->t < t_end) {

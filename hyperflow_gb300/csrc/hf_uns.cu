@@ -28,6 +28,7 @@
 #include "../../include/hyperflow_gb300_uns.h"
 #include "hf_ctrl.h"
 #include "hf_device.cuh"
+#include "hf_trace.h"
 #include "hf_json.hpp"
 
 namespace hf {
@@ -814,6 +815,7 @@ int hf_uns_clear_error_cell(hf_uns* u) {
 }
 
 int hf_uns_time_step(hf_uns* u, double* dt) {
+    hf::TraceRange trace_("hf_uns_time_step");
     if (!u || !u->dctrl) return HF_ERR_ARG;
     int clamp = 0;
     UCK(cudaMemcpyAsync(&u->dctrl->clamp, &clamp, sizeof clamp, cudaMemcpyHostToDevice, u->stream));
@@ -828,12 +830,14 @@ int hf_uns_time_step(hf_uns* u, double* dt) {
 }
 
 int hf_uns_advance(hf_uns* u, double dt) {
+    hf::TraceRange trace_("hf_uns_advance");
     if (!u || !u->dctrl) return HF_ERR_ARG;
     hf::uns_set_dt_kernel<<<1, 1, 0, u->stream>>>(u->dctrl, dt);
     return enqueue_uns_step(u, false);
 }
 
 int hf_uns_run(hf_uns* u, int64_t n, int clamp_t_end, int use_graph, int64_t* steps_done) {
+    hf::TraceRange trace_("hf_uns_run");
     if (!u || !u->dctrl || n < 0) return HF_ERR_ARG;
     long long s0 = 0;
     int r = read_step(u, &s0);
