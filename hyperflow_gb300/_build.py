@@ -33,8 +33,8 @@ def nvcc() -> str:
     raise RuntimeError("nvcc not found")
 
 
-def _compile(src: str, extra: list[str]) -> str:
-    out = os.path.join(OBJ, os.path.splitext(src)[0] + ".o")
+def _compile(src: str, extra: list[str], obj: str = OBJ) -> str:
+    out = os.path.join(obj, os.path.splitext(src)[0] + ".o")
     srcp = os.path.join(CSRC, src)
     if os.path.exists(out) and os.path.getmtime(out) >= max(
             os.path.getmtime(srcp), *(os.path.getmtime(os.path.join(CSRC, h))
@@ -47,15 +47,24 @@ def _compile(src: str, extra: list[str]) -> str:
     return out
 
 
-def build(verbose: bool = False, extra: list[str] | None = None) -> str:
-    os.makedirs(OBJ, exist_ok=True)
+def build(verbose: bool = False, extra: list[str] | None = None, variant: str = "") -> str:
+    """variant "checked": the library with -DHF_CHECKS (every geometry- or mesh-dependent global
+    index range-checked into the error word), as libhyperflow_gb300_checked.so."""
+    obj = os.path.join(OBJ, variant) if variant else OBJ
+    lib_path = LIB if not variant else os.path.join(PKG, f"libhyperflow_gb300_{variant}.so")
+    flags = list(extra or []) + (["-DHF_CHECKS"] if variant == "checked" else [])
+    os.makedirs(obj, exist_ok=True)
     srcs = [s for s in SOURCES if os.path.exists(os.path.join(CSRC, s))]
     with ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
-        objs = list(ex.map(lambda s: _compile(s, extra or []), srcs))
-    cmd = [nvcc(), *ARCH, "-shared", "-o", LIB, *objs]
+        objs = list(ex.map(lambda s: _compile(s, flags, obj), srcs))
+    cmd = [nvcc(), *ARCH, "-shared", "-o", lib_path, *objs]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+    if variant:
+        if verbose:
+            print("built", lib_path)
+        return lib_path
     # the kernels' arithmetic built for the host (CPU tests of the device math)
     hm = _compile("hf_hostmath.cu", extra or [])
     r = subprocess.run([nvcc(), *ARCH, "-shared", "-o", HOSTMATH_LIB, hm], capture_output=True, text=True)

@@ -9,12 +9,16 @@ import ctypes as C
 import os
 
 PKG = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(PKG, "libhyperflow_gb300.so")
+# HF_LIB_VARIANT=checked loads the bounds-checked build (libhyperflow_gb300_checked.so, made by
+# _build.build(variant="checked")): same results, and an out-of-range index sets the error word
+_VARIANT = os.environ.get("HF_LIB_VARIANT", "")
+LIB_PATH = os.path.join(PKG, "libhyperflow_gb300%s.so" % ("_" + _VARIANT if _VARIANT else ""))
 
 HF_OK = 0
 STATUS = {0: "ok", 1: "bad argument", 2: "case file parse error", 3: "unsupported case",
           4: "CUDA error", 5: "device error word raised", 6: "call out of order",
-          7: "no CUDA device", 8: "problem exceeds the fixed-size working area"}
+          7: "no CUDA device", 8: "problem exceeds the fixed-size working area",
+          9: "strict mode: an HLLC zero-flux fallback occurred"}
 
 LAYOUT_SOA = 0
 LAYOUT_AOS_XY = 1
@@ -71,6 +75,7 @@ SIGNATURES = {
     "hf_uns_frames_enable": (_i, [_p, _i]),
     "hf_uns_frames_pending": (_i, [_p, C.POINTER(_i64)]),
     "hf_uns_frame_pop": (_i, [_p, _p, C.POINTER(_d), C.POINTER(_i64)]),
+    "hf_uns_sync": (_i, [_p]),
     "hf_uns_set_strict": (_i, [_p, _i]),
     "hf_uns_last_error_cell": (_i, [_p, C.POINTER(_i64), C.POINTER(_i64)]),
     "hf_uns_clear_error_cell": (_i, [_p]),

@@ -763,8 +763,8 @@ int hf_step_io(hf_ctx* ctx, const double* const* in, double* const* out, double*
         CK(hf::launch_bc_fill(ctx->dctrl, ctx->dmesh, ctx->side_len, ctx->nblocks, ctx->stream));
         CK(hf::launch_ghost_cfl(ctx->dctrl, ctx->dmesh, ctx->hmesh.total_ghost, ctx->stream));
         for (int b = 0; b < ctx->nblocks; ++b)
-            CK(hf::launch_ghost_store(ctx->dmesh, b, ctx->blocks[b].tx, ctx->blocks[b].ny, ctx->ghost, p,
-                                      out[b], ctx->stream));
+            CK(hf::launch_ghost_store(ctx->dctrl, ctx->dmesh, b, ctx->blocks[b].tx, ctx->blocks[b].ny, ctx->ghost,
+                                      p, out[b], ctx->stream));
         for (int b = 0; b < ctx->nblocks; ++b) {
             const BlockHost& B = ctx->blocks[b];
             CK(hf::launch_stencil(ctx->dctrl, ctx->dmesh, b, B.nx, B.ny, ctx->scheme, ctx->limiter,

@@ -29,7 +29,7 @@ constexpr unsigned kWaitLimit = 1u << 22;   // bounded mbarrier polls before giv
 // transmissive_boundary.cpp:25-104, reflective_boundary.cpp:25-120,
 // dirichlet_boundary.cpp:25-104, internal_boundary.cpp:27-108.  Layer k = 0..g-1 counts
 // outward from the interior; source indices are the reference's, written per layer.
-__device__ void fill_side(const MeshDev* __restrict__ m, int b, int side, int p) {
+__device__ void fill_side(const MeshDev* __restrict__ m, int b, int side, int p, int* err) {
     const BlockDev& B = m->b[b];
     const int g = m->ghost;
     const int kind = B.bc_type[side];
@@ -65,6 +65,9 @@ __device__ void fill_side(const MeshDev* __restrict__ m, int b, int side, int p)
             }
             const size_t dof = (size_t)dj * B.pitch + di;
             const size_t sof = (size_t)sj * E.pitch + si;
+            if (!hf_in((long long)dof, (long long)plane, err) ||
+                (kind != BC_DIRICHLET && !hf_in((long long)sof, (long long)eplane, err)))
+                continue;
 #pragma unroll
             for (int v = 0; v < 4; ++v) {
                 double val;
@@ -100,10 +103,10 @@ __global__ void step_begin_kernel(Ctrl* __restrict__ c) {
 
 // one side of one block; the sides run as consecutive launches in the reference order, so
 // a side sees every value the sides before it wrote
-__global__ void __launch_bounds__(256) bc_side_kernel(const Ctrl* __restrict__ c,
+__global__ void __launch_bounds__(256) bc_side_kernel(Ctrl* __restrict__ c,
                                                       const MeshDev* __restrict__ m, int b, int side) {
     if (c->done) return;
-    fill_side(m, b, side, (int)(c->step & 1));
+    fill_side(m, b, side, (int)(c->step & 1), &c->err);
 }
 
 // ------------------------------------------------------------------------------------
@@ -143,6 +146,7 @@ __global__ void __launch_bounds__(kRedThreads) ghost_cfl_kernel(Ctrl* __restrict
             int i, j;
             ghost_cell_ij(B, m->ghost, k, i, j);
             size_t o = (size_t)j * B.pitch + i;
+            if (!hf_in((long long)o, (long long)plane, &c->err)) continue;
             double sx, sy;
             wave_terms(g, g1, U[o], U[plane + o], U[2 * plane + o], U[3 * plane + o], sx, sy);
             mx = nmax(mx, sx);
@@ -231,6 +235,7 @@ __global__ void __launch_bounds__(kRedThreads) upload_kernel(Ctrl* __restrict__ 
          k += (long long)gridDim.x * blockDim.x) {
         const int i = (int)(k % B.tx), j = (int)(k / B.tx);
         const size_t o = (size_t)j * B.pitch + i;
+        if (!hf_in((long long)o, (long long)plane, &c->err)) continue;
         double u[4];
 #pragma unroll
         for (int v = 0; v < 4; ++v) u[v] = __ldcs(&hin[v * hplane + (size_t)k]);
@@ -251,8 +256,8 @@ __global__ void __launch_bounds__(kRedThreads) upload_kernel(Ctrl* __restrict__ 
 
 // The ghost cells of the updated buffer (filled this step, never written by the stencil) into
 // host memory the GPU maps: with the stencil's own host stores, the whole block downloaded.
-__global__ void __launch_bounds__(256) ghost_store_kernel(const MeshDev* __restrict__ m, int b, int parity,
-                                                          double* __restrict__ hout) {
+__global__ void __launch_bounds__(256) ghost_store_kernel(Ctrl* __restrict__ c, const MeshDev* __restrict__ m,
+                                                          int b, int parity, double* __restrict__ hout) {
     const BlockDev& B = m->b[b];
     const int g = m->ghost;
     const size_t plane = (size_t)B.ty * B.pitch, hplane = (size_t)B.ty * B.tx;
@@ -273,6 +278,8 @@ __global__ void __launch_bounds__(256) ghost_store_kernel(const MeshDev* __restr
             i = col < g ? col : B.tx - 2 * g + col;
         }
         const size_t o = (size_t)j * B.pitch + i, h = (size_t)j * B.tx + i;
+        if (!hf_in((long long)o, (long long)plane, &c->err) || !hf_in((long long)h, (long long)hplane, &c->err))
+            continue;
 #pragma unroll
         for (int v = 0; v < 4; ++v) __stcs(&hout[v * hplane + h], U[v * plane + o]);
     }
@@ -423,11 +430,15 @@ __global__ void __launch_bounds__(NT, 3) mh_kernel(Ctrl* __restrict__ c, const M
         if (gxx < B.nx && gyy < B.ny) {
             double un[4];
             const size_t o = (size_t)(gyy + 2) * B.pitch + (gxx + 2);
+            const size_t h = (size_t)(gyy + 2) * B.tx + gxx + 2;
+            if (!hf_in((long long)o, (long long)plane, &c->err) ||
+                !hf_in((long long)h, (long long)B.ty * B.tx, &c->err))
+                continue;
 #pragma unroll
             for (int v = 0; v < 4; ++v) {
                 un[v] = mh_update<TX, TY>(sU, sF, sG, v, ox, oy, dt, one_dx, one_dy);
                 out[v * plane + o] = un[v];
-                if (hout) __stcs(&hout[((size_t)v * B.ty + gyy + 2) * B.tx + gxx + 2], un[v]);
+                if (hout) __stcs(&hout[(size_t)v * B.ty * B.tx + h], un[v]);
             }
             double sx, sy;
             wave_terms(g, g1, un[0], un[1], un[2], un[3], sx, sy);
@@ -498,11 +509,15 @@ __global__ void __launch_bounds__(NT, 3) godunov_kernel(Ctrl* __restrict__ c,
         if (gxx < B.nx && gyy < B.ny) {
             double un[4];
             const size_t o = (size_t)(gyy + 1) * B.pitch + (gxx + 1);
+            const size_t h = (size_t)(gyy + 1) * B.tx + gxx + 1;
+            if (!hf_in((long long)o, (long long)plane, &c->err) ||
+                !hf_in((long long)h, (long long)B.ty * B.tx, &c->err))
+                continue;
 #pragma unroll
             for (int v = 0; v < 4; ++v) {
                 un[v] = go_update<TX, TY>(sU, sF, sG, v, ox, oy, dt, one_dx, one_dy);
                 out[v * plane + o] = un[v];
-                if (hout) __stcs(&hout[((size_t)v * B.ty + gyy + 1) * B.tx + gxx + 1], un[v]);
+                if (hout) __stcs(&hout[(size_t)v * B.ty * B.tx + h], un[v]);
             }
             double sx, sy;
             wave_terms(g, g1, un[0], un[1], un[2], un[3], sx, sy);
@@ -641,11 +656,11 @@ cudaError_t launch_upload(Ctrl* c, const MeshDev* m, int b, int tx, int ty, int 
     return cudaGetLastError();
 }
 
-cudaError_t launch_ghost_store(const MeshDev* m, int b, int tx, int ny, int ghost, int parity, double* hout,
-                               cudaStream_t s) {
+cudaError_t launch_ghost_store(Ctrl* c, const MeshDev* m, int b, int tx, int ny, int ghost, int parity,
+                               double* hout, cudaStream_t s) {
     long long n = 2LL * ghost * (tx + ny);
     int grid = (int)((n + 255) / 256);
-    ghost_store_kernel<<<grid < 1 ? 1 : grid, 256, 0, s>>>(m, b, parity, hout);
+    ghost_store_kernel<<<grid < 1 ? 1 : grid, 256, 0, s>>>(c, m, b, parity, hout);
     return cudaGetLastError();
 }
 

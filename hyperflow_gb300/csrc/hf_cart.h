@@ -75,8 +75,8 @@ cudaError_t launch_stencil(Ctrl* c, const MeshDev* m, int b, int nx, int ny, int
 // ghost fill, the updated buffer's ghost cells back out
 cudaError_t launch_upload(Ctrl* c, const MeshDev* m, int b, int tx, int ty, int parity, const double* hin,
                           cudaStream_t s);
-cudaError_t launch_ghost_store(const MeshDev* m, int b, int tx, int ny, int ghost, int parity, double* hout,
-                               cudaStream_t s);
+cudaError_t launch_ghost_store(Ctrl* c, const MeshDev* m, int b, int tx, int ny, int ghost, int parity,
+                               double* hout, cudaStream_t s);
 // TMA box of the stencil for the scheme
 StencilTiles stencil_tiles(int scheme);
 cudaError_t stencil_prepare();   // sets the large dynamic shared-memory opt-ins once

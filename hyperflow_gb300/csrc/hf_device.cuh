@@ -22,6 +22,19 @@ namespace hf {
 
 __device__ __forceinline__ void raise_error(Ctrl* c, int code) { atomicCAS(&c->err, 0, code); }
 
+// Checked builds (-DHF_CHECKS): a global-memory index outside its buffer sets the error word
+// (HF_DEV_BOUNDS, reported by the next synchronising call) and the caller skips the access --
+// no trap, no assert.  In normal builds the check compiles to `true`.
+#ifdef HF_CHECKS
+__device__ __forceinline__ bool hf_in(long long i, long long n, int* err) {
+    if (i >= 0 && i < n) return true;
+    atomicCAS(err, 0, (int)HF_DEV_BOUNDS);
+    return false;
+}
+#else
+__device__ __forceinline__ bool hf_in(long long, long long, int*) { return true; }
+#endif
+
 // ------------------------------------------------------------------------------
 // std::min / std::max exactly (NaN-order semantics of the C++ library)
 // ------------------------------------------------------------------------------

@@ -114,9 +114,15 @@ __device__ __forceinline__ unsigned long long uns_key(long long step, long long 
     return (s << 40) | ((unsigned long long)cell & 0xFFFFFFFFFFull);
 }
 
-// length x rotated-back HLLC flux of the pair (owner cell c, neighbour cell k)
+// length x rotated-back HLLC flux of the pair (owner cell c, neighbour cell k); in checked
+// builds a pair or neighbour index outside the mesh raises the error word and gives a zero flux
 __device__ __forceinline__ int pair_flux(const UnsMesh& m, const double* __restrict__ U, size_t N, double g,
-                                         double g1, int e, const double* cv, double* f) {
+                                         double g1, int e, const double* cv, double* f, int* err) {
+    if (!hf_in(e, m.npairs, err) || (m.nbr[e] >= 0 && !hf_in(m.nbr[e], m.ncells, err))) {
+#pragma unroll
+        for (int v = 0; v < 4; ++v) f[v] = 0.0;
+        return 0;
+    }
     const double ca = m.geo[e], sa = m.geo[m.npairs + e];
     const double cn = m.geo[2 * m.npairs + e], sn = m.geo[3 * m.npairs + e];
     const double len = m.geo[4 * m.npairs + e];
@@ -154,8 +160,9 @@ __global__ void __launch_bounds__(kUnsNT, 3) uns_edge_flux_kernel(UnsCtrl* __res
     int herr = 0;
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < m.nedges; e += gridDim.x * blockDim.x) {
         const int i = m.edge_cell[e];
+        if (!hf_in(i, m.ncells, &c->err)) continue;
         double cv[4] = {U[i], U[N + i], U[2 * N + i], U[3 * N + i]}, f[4];
-        if (pair_flux(m, U, N, g, g1, m.edge_pair[e], cv, f)) {
+        if (pair_flux(m, U, N, g, g1, m.edge_pair[e], cv, f, &c->err)) {
             ++herr;
             atomicMin(&c->first_bad, uns_key(c->step, i));
         }
@@ -265,8 +272,8 @@ __global__ void __launch_bounds__(kUnsNT, MINB) uns_step_kernel(UnsCtrl* __restr
         const int e0 = m.pair_start[i], e1 = m.pair_start[i + 1];
         for (int e = e0; e < e1; ++e) {
             double f[4];
-            const int ed = m.pair_edge ? m.pair_edge[e] : -1;
-            if (ed >= 0) {          // edge-based mode: the owner's flux, negated on the other side
+            const int ed = m.pair_edge && hf_in(e, m.npairs, &c->err) ? m.pair_edge[e] : -1;
+            if (ed >= 0 && hf_in(ed, m.nedges, &c->err)) {   // edge-based mode: the owner's flux, negated on the other side
                 // (a sign flip, not a multiplication by -1.0: the same value, off the FP64 pipe)
                 const bool neg = m.pair_sign[e] < 0;
 #pragma unroll
@@ -274,7 +281,7 @@ __global__ void __launch_bounds__(kUnsNT, MINB) uns_step_kernel(UnsCtrl* __restr
                     const double x = m.edge_flux[(size_t)v * m.nedges + ed];
                     f[v] = neg ? -x : x;
                 }
-            } else if (pair_flux(m, U, N, g, g1, e, cv, f)) {
+            } else if (pair_flux(m, U, N, g, g1, e, cv, f, &c->err)) {
                 ++herr;
                 atomicMin(&c->first_bad, uns_key(c->step, i));
             }
@@ -785,6 +792,15 @@ static int uns_strict_check(hf_uns* u) {
     return ufail(u, HF_ERR_NUMERIC,
                  "HLLC zero flux (all wave-speed branches failed) at step " + std::to_string(k >> 40) +
                      ", cell " + std::to_string(k & 0xFFFFFFFFFFull));
+}
+
+int hf_uns_sync(hf_uns* u) {
+    if (!u || !u->dctrl) return HF_ERR_ARG;
+    UCK(cudaStreamSynchronize(u->stream));
+    int e = 0;
+    UCK(cudaMemcpy(&e, &u->dctrl->err, sizeof e, cudaMemcpyDeviceToHost));
+    if (e != 0) return ufail(u, HF_ERR_DEVICE, "device error word " + std::to_string(e));
+    return uns_strict_check(u);
 }
 
 int hf_uns_set_strict(hf_uns* u, int on) {

@@ -164,6 +164,10 @@ class UnsSolver:
         self.frame_paths = paths
         return total
 
+    def sync(self):
+        """Waits for the solver's stream; raises if a kernel raised the device error word."""
+        check(lib().hf_uns_sync(self._h), self._h, _MSG)
+
     def set_strict(self, on: bool = True):
         """Strict mode: a zero-flux HLLC pair stops the loop and raises HyperFlowError."""
         check(lib().hf_uns_set_strict(self._h, int(bool(on))), self._h, _MSG)

@@ -85,6 +85,9 @@ int hf_uns_frame_pop(hf_uns* u, double* cons, double* t, int64_t* index);
  * owner cell -- or -1.  Strict mode (hf_uns_set_strict(u, 1)): once one is recorded the step
  * completes, later device-loop steps do nothing, and hf_uns_run / hf_uns_time_step return
  * HF_ERR_NUMERIC with the cell in hf_uns_last_error_message. */
+/* waits for the context's stream; HF_ERR_DEVICE if a kernel raised the error word (in the
+ * bounds-checked build: an index outside the mesh), HF_ERR_NUMERIC as hf_uns_run in strict mode */
+int hf_uns_sync(hf_uns* u);
 int hf_uns_set_strict(hf_uns* u, int on);
 int hf_uns_last_error_cell(hf_uns* u, int64_t* cell, int64_t* step);
 int hf_uns_clear_error_cell(hf_uns* u);
