@@ -184,3 +184,43 @@ def test_gpu_multiblock_frames_equal_oracle(scheme, tmp_path, port_lib):
             np.testing.assert_array_equal(a, b)
     for b in range(s.nblocks):
         np.testing.assert_array_equal(s.state(b), o.state(b))
+
+
+_CRASHER = r'''
+import os, sys
+sys.path.insert(0, ROOT)
+from hyperflow_gb300 import CartSolver, cases
+s = CartSolver(cases.forward_facing_step_case(20, limiter="VanLeer"))
+for k in range(1, 100):
+    s.run(5)
+    blob = s.checkpoint()                  # synchronises: no kernel is in flight after this
+    tmp = PATH + ".tmp"
+    with open(tmp, "wb") as f:
+        f.write(blob)
+    os.replace(tmp, PATH)                  # the checkpoint file is always a whole one
+    if k == 3:
+        os._exit(17)                       # the "rank" dies here, between steps, without cleanup
+'''
+
+
+def test_gpu_resume_after_a_process_dies_between_steps(tmp_path):
+    """A process that checkpoints every 5 steps dies abruptly (between steps, after its third
+    checkpoint, no cleanup); a new solver restored from the last checkpoint file and run on
+    equals an uninterrupted run bit for bit."""
+    import subprocess
+    import sys
+    from hyperflow_gb300 import CartSolver, cases
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    path = str(tmp_path / "ck.bin")
+    r = subprocess.run([sys.executable, "-c", "ROOT = %r\nPATH = %r\n" % (root, path) + _CRASHER],
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 17, r.stderr[-2000:]
+    case = cases.forward_facing_step_case(20, limiter="VanLeer")
+    b = CartSolver(case)
+    b.load_checkpoint(path)
+    b.run(25)
+    a = CartSolver(case)
+    a.run(40)
+    assert a.time() == b.time()
+    for k in range(a.nblocks):
+        np.testing.assert_array_equal(a.state(k), b.state(k))
