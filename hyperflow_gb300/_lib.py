@@ -18,7 +18,7 @@ HF_OK = 0
 STATUS = {0: "ok", 1: "bad argument", 2: "case file parse error", 3: "unsupported case",
           4: "CUDA error", 5: "device error word raised", 6: "call out of order",
           7: "no CUDA device", 8: "problem exceeds the fixed-size working area",
-          9: "strict mode: an HLLC zero-flux fallback occurred"}
+          9: "strict mode: an HLLC zero-flux fallback or a non-positive density or pressure occurred"}
 
 LAYOUT_SOA = 0
 LAYOUT_AOS_XY = 1
@@ -41,6 +41,7 @@ SIGNATURES = {
     "hf_host_mapped": (_i, [_p, C.POINTER(_i)]),
     "hf_set_strict": (_i, [_p, _i]),
     "hf_last_error_cell": (_i, [_p, C.POINTER(_i), C.POINTER(_i), C.POINTER(_i), C.POINTER(_i), C.POINTER(_i64)]),
+    "hf_last_nonpositive_cell": (_i, [_p, C.POINTER(_i), C.POINTER(_i), C.POINTER(_i), C.POINTER(_i64)]),
     "hf_clear_error_cell": (_i, [_p]),
     "hf_run": (_i, [_p, _i64, _i, _i, C.POINTER(_i64)]),
     "hf_get_time": (_i, [_p, C.POINTER(_d), C.POINTER(_i64), C.POINTER(_d)]),
@@ -78,6 +79,7 @@ SIGNATURES = {
     "hf_uns_sync": (_i, [_p]),
     "hf_uns_set_strict": (_i, [_p, _i]),
     "hf_uns_last_error_cell": (_i, [_p, C.POINTER(_i64), C.POINTER(_i64)]),
+    "hf_uns_last_nonpositive_cell": (_i, [_p, C.POINTER(_i64), C.POINTER(_i64)]),
     "hf_uns_clear_error_cell": (_i, [_p]),
     "hf_uns_checkpoint_size": (_i, [_p, C.POINTER(_sz)]),
     "hf_uns_checkpoint_save": (_i, [_p, _p, _sz]),

@@ -518,6 +518,7 @@ int hf_create(const char* case_json, size_t len, hf_ctx** out) {
     C.t = ctx->t_start;
     C.t_end = ctx->t_end;
     C.first_bad = ~0ull;
+    C.first_nonpos = ~0ull;
     CK(cudaMalloc(&ctx->dctrl, sizeof(hf::Ctrl)));
     CK(cudaMemcpyAsync(ctx->dctrl, &C, sizeof C, cudaMemcpyHostToDevice, ctx->stream));
     int r = make_tmaps(ctx);
@@ -694,23 +695,29 @@ int hf_advance(hf_ctx* ctx, double dt) {
     return HF_OK;
 }
 
-// One step with the state in host memory: every block uploaded (into both buffers, with the
-// interior TimeStep terms, as hf_set_state), one step (as hf_step), every block downloaded --
-// each block's download on a second stream as soon as its own update is done, so it overlaps
-// the updates of the blocks after it.  No synchronisation between the pieces.
-// strict mode, after a synchronisation: HF_ERR_NUMERIC once a zero-flux face is recorded
-static int strict_check(hf_ctx* ctx) {
-    if (!ctx->strict) return HF_OK;
-    unsigned long long k = ~0ull;
-    CK(cudaMemcpy(&k, &ctx->dctrl->first_bad, sizeof k, cudaMemcpyDeviceToHost));
-    if (k == ~0ull) return HF_OK;
+// the (step, block, direction, j, i) fields of a face_key
+static std::string key_text(unsigned long long k, bool face) {
     const long long step = (long long)(k >> 42);
     const int b = (int)((k >> 38) & 0xF), dir = (int)((k >> 37) & 1);
     const int j = (int)((k >> 19) & 0x3FFFF), i = (int)(k & 0x7FFFF);
-    return fail(ctx, HF_ERR_NUMERIC,
-                "HLLC zero flux (all wave-speed branches failed) at step " + std::to_string(step) + ", block " +
-                    std::to_string(b) + ", " + (dir ? "y" : "x") + " face (i " + std::to_string(i) + ", j " +
-                    std::to_string(j) + ")");
+    return "step " + std::to_string(step) + ", block " + std::to_string(b) + ", " +
+           (face ? std::string(dir ? "y face" : "x face") : std::string("cell")) + " (i " + std::to_string(i) +
+           ", j " + std::to_string(j) + ")";
+}
+
+// strict mode, after a synchronisation: HF_ERR_NUMERIC once a zero-flux face or a non-positive
+// cell is recorded
+static int strict_check(hf_ctx* ctx) {
+    if (!ctx->strict) return HF_OK;
+    unsigned long long k[2] = {~0ull, ~0ull};
+    CK(cudaMemcpy(&k[0], &ctx->dctrl->first_bad, sizeof k[0], cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(&k[1], &ctx->dctrl->first_nonpos, sizeof k[1], cudaMemcpyDeviceToHost));
+    // the record of the earlier step (a zero flux first within one step)
+    if (k[0] != ~0ull && (k[0] >> 42) <= (k[1] >> 42))
+        return fail(ctx, HF_ERR_NUMERIC, "HLLC zero flux (all wave-speed branches failed) at " + key_text(k[0], true));
+    if (k[1] != ~0ull)
+        return fail(ctx, HF_ERR_NUMERIC, "non-positive density or pressure at " + key_text(k[1], false));
+    return HF_OK;
 }
 
 // true when every pointer is 8-byte aligned host memory that kernels may address as it is
@@ -735,6 +742,10 @@ int hf_host_mapped(const void* p, int* mapped) {
     return HF_OK;
 }
 
+// One step with the state in host memory: every block uploaded (into both buffers, with the
+// interior TimeStep terms, as hf_set_state), one step (as hf_step), every block downloaded --
+// each block's download on a second stream as soon as its own update is done, so it overlaps
+// the updates of the blocks after it.  No synchronisation between the pieces.
 int hf_step_io(hf_ctx* ctx, const double* const* in, double* const* out, double* dt) {
     hf::TraceRange trace_("hf_step_io");
     if (!ctx || !in || !out) return HF_ERR_ARG;
@@ -907,10 +918,24 @@ int hf_last_error_cell(hf_ctx* ctx, int* block, int* i, int* j, int* dir, int64_
     return HF_OK;
 }
 
+int hf_last_nonpositive_cell(hf_ctx* ctx, int* block, int* i, int* j, int64_t* step) {
+    if (!ctx) return HF_ERR_ARG;
+    unsigned long long k = ~0ull;
+    CK(cudaStreamSynchronize(ctx->stream));
+    CK(cudaMemcpy(&k, &ctx->dctrl->first_nonpos, sizeof k, cudaMemcpyDeviceToHost));
+    const bool none = k == ~0ull;
+    if (block) *block = none ? -1 : (int)((k >> 38) & 0xF);
+    if (j) *j = none ? -1 : (int)((k >> 19) & 0x3FFFF);
+    if (i) *i = none ? -1 : (int)(k & 0x7FFFF);
+    if (step) *step = none ? -1 : (int64_t)(k >> 42);
+    return HF_OK;
+}
+
 int hf_clear_error_cell(hf_ctx* ctx) {
     if (!ctx) return HF_ERR_ARG;
     const unsigned long long none = ~0ull;
     CK(cudaMemcpyAsync(&ctx->dctrl->first_bad, &none, sizeof none, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(&ctx->dctrl->first_nonpos, &none, sizeof none, cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
     return HF_OK;
 }

@@ -88,7 +88,7 @@ __device__ void fill_side(const MeshDev* __restrict__ m, int b, int side, int p,
 __global__ void step_begin_kernel(Ctrl* __restrict__ c) {
     const int p = (int)(c->step & 1);
     int done = c->clamp && (c->t == c->t_end);
-    if (c->strict && c->first_bad != ~0ull) done = 1;   // strict mode: a zero flux stops the loop
+    if (c->strict && (c->first_bad != ~0ull || c->first_nonpos != ~0ull)) done = 1;   // strict mode
     // a step takes at most two frames: pause the loop while the ring lacks room for them
     if (c->clamp && c->frames && c->captured - c->drained > c->ring_slots - 2) done = 1;
     c->done = done;
@@ -441,7 +441,8 @@ __global__ void __launch_bounds__(NT, 3) mh_kernel(Ctrl* __restrict__ c, const M
                 if (hout) __stcs(&hout[(size_t)v * B.ty * B.tx + h], un[v]);
             }
             double sx, sy;
-            wave_terms(g, g1, un[0], un[1], un[2], un[3], sx, sy);
+            if (!wave_terms(g, g1, un[0], un[1], un[2], un[3], sx, sy))
+                atomicMin(&c->first_nonpos, face_key(c->step, b, 0, gyy, gxx));
             mx = nmax(mx, sx);
             my = nmax(my, sy);
         }
@@ -520,7 +521,8 @@ __global__ void __launch_bounds__(NT, 3) godunov_kernel(Ctrl* __restrict__ c,
                 if (hout) __stcs(&hout[(size_t)v * B.ty * B.tx + h], un[v]);
             }
             double sx, sy;
-            wave_terms(g, g1, un[0], un[1], un[2], un[3], sx, sy);
+            if (!wave_terms(g, g1, un[0], un[1], un[2], un[3], sx, sy))
+                atomicMin(&c->first_nonpos, face_key(c->step, b, 0, gyy, gxx));
             mx = nmax(mx, sx);
             my = nmax(my, sy);
         }

@@ -27,7 +27,9 @@ struct Ctrl {
     int err;                                // first error code raised on the device
     long long hllc_errors;                  // HLLC "should not get here" zero fluxes
     unsigned long long first_bad;           // least face_key of such a face, ~0 when none
-    int strict;                             // a recorded zero flux stops the loop
+    unsigned long long first_nonpos;        // least face_key (direction 0) of an updated interior cell
+                                            // whose density or pressure is not positive, ~0 when none
+    int strict;                             // a recorded zero flux or non-positive cell stops the loop
     // frame output with Simulation::solve's cadence (device loop only, i.e. clamp set)
     int frames;                             // frame clamp and capture on
     int ring_slots;                         // depth of the device frame ring

@@ -243,13 +243,14 @@ HF_HD double slope(double um, double u0, double up) {
 // dx / s over cells with std::min; fl(dx / s) is non-increasing in s, so that fold
 // equals fl(dx / max s) -- a max over s, which is exact in any order.  NaN terms are
 // skipped in both.
-HF_HD void wave_terms(double g, double g1, double r, double ru, double rv,
+HF_HD bool wave_terms(double g, double g1, double r, double ru, double rv,
                                            double E, double& sx, double& sy) {
     double u, v, p;
     to_prim_short(g1, r, ru, rv, E, u, v, p);
     double c = sound(g, r, p);
     sx = fabs(u) + c;
     sy = fabs(v) + c;
+    return gt0(r) && gt0(p);   // the state is physical: density and pressure positive, not NaN
 }
 
 // NaN-skipping max of non-negative values

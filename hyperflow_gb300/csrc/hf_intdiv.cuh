@@ -126,6 +126,10 @@ HF_HD bool ge0(double x) {            // 0.0 <= x
     const uint64_t u = f64_bits(x), m = u & kAbs;
     return m == 0 || (!(u >> 63) && m <= kInf);
 }
+HF_HD bool gt0(double x) {            // 0.0 < x: sign clear, not zero, not NaN
+    const uint64_t u = f64_bits(x);
+    return u != 0 && u <= kInf;
+}
 // |x| <= t for a positive finite t (false for NaN)
 HF_HD bool abs_le(double x, double t) { return (f64_bits(x) & kAbs) <= f64_bits(t); }
 

@@ -42,7 +42,9 @@ struct UnsCtrl {
     int err;
     long long hllc_errors;
     unsigned long long first_bad;   // least uns_key of a zero-flux pair, ~0 when none
-    int strict;                     // a recorded zero flux stops the loop
+    unsigned long long first_nonpos;// least uns_key of a cell a step left with density or
+                                    // pressure not positive, ~0 when none
+    int strict;                     // a recorded zero flux or non-positive cell stops the loop
     // frame output with Simulation::solve's cadence (device loop only, i.e. clamp set)
     int frames, ring_slots, snap_pre, snap_post;
     double frame_next, frame_interval, snap_t;
@@ -80,9 +82,10 @@ __device__ __forceinline__ void rot(double c, double s, const double* f, double*
 }
 
 // TimeStep term r_in / (|V| + c) of one cell (uns timestep.cpp:51-58)
-__device__ __forceinline__ double uns_dt_term(double g, double g1, double rin, const double* u) {
+__device__ __forceinline__ double uns_dt_term(double g, double g1, double rin, const double* u, bool& pos) {
     double uu, vv, p;
     to_prim_short(g1, u[0], u[1], u[2], u[3], uu, vv, p);
+    pos = gt0(u[0]) && gt0(p);   // density and pressure positive, not NaN
     double c = sound(g, u[0], p);
     return div_rn(rin, fabs(sqrt_rn(uu * uu + vv * vv)) + c);
 }
@@ -108,7 +111,8 @@ __device__ __forceinline__ void block_min_atomic(double v, unsigned long long* a
 
 constexpr int kUnsNT = 256;
 
-// key of a (cell, pair) whose HLLC took the zero flux: step (24 bits), then cell (40 bits)
+// key of a cell in the error records (a zero-flux pair's cell, a non-positive cell): step (24
+// bits), then cell (40 bits)
 __device__ __forceinline__ unsigned long long uns_key(long long step, long long cell) {
     const unsigned long long s = step > 0xFFFFFFll ? 0xFFFFFFull : (unsigned long long)step;
     return (s << 40) | ((unsigned long long)cell & 0xFFFFFFFFFFull);
@@ -177,7 +181,8 @@ __global__ void __launch_bounds__(kUnsNT) uns_cfl_kernel(UnsCtrl* __restrict__ c
     const double* U = m.U[parity];
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m.ncells; i += gridDim.x * blockDim.x) {
         double u[4] = {U[i], U[m.ncells + i], U[2 * (size_t)m.ncells + i], U[3 * (size_t)m.ncells + i]};
-        mn = nmin(mn, uns_dt_term(c->gamma, c->g1, m.rin[i], u));
+        bool pos;
+        mn = nmin(mn, uns_dt_term(c->gamma, c->g1, m.rin[i], u, pos));
     }
     block_min_atomic<kUnsNT>(mn, &c->min_dt[parity]);
 }
@@ -187,7 +192,7 @@ __global__ void uns_prep_kernel(UnsCtrl* c) {
     int p = (int)(c->step & 1);
     c->snap_pre = c->snap_post = 0;
     if (c->clamp && c->t == c->t_end) { c->done = 1; return; }
-    if (c->strict && c->first_bad != ~0ull) { c->done = 1; return; }   // strict mode
+    if (c->strict && (c->first_bad != ~0ull || c->first_nonpos != ~0ull)) { c->done = 1; return; }   // strict mode
     // a step takes at most two frames: pause the loop while the ring lacks room for them
     if (c->clamp && c->frames && c->captured - c->drained > c->ring_slots - 2) { c->done = 1; return; }
     c->done = 0;
@@ -296,7 +301,9 @@ __global__ void __launch_bounds__(kUnsNT, MINB) uns_step_kernel(UnsCtrl* __restr
             un[v] = dt * L + cv[v];
             Un[v * N + i] = un[v];
         }
-        mn = nmin(mn, uns_dt_term(g, g1, m.rin[i], un));
+        bool pos;
+        mn = nmin(mn, uns_dt_term(g, g1, m.rin[i], un, pos));
+        if (!pos) atomicMin(&c->first_nonpos, uns_key(c->step, i));
     }
     block_min_atomic<kUnsNT>(mn, &c->min_dt[p ^ 1]);
     if (herr) atomicAdd(reinterpret_cast<unsigned long long*>(&c->hllc_errors), (unsigned long long)herr);
@@ -608,6 +615,7 @@ int finish_create(hf_uns* u, const Json& cfg) {
     C.t = u->t_start;
     C.t_end = u->t_end;
     C.first_bad = ~0ull;
+    C.first_nonpos = ~0ull;
     UCK(cudaMalloc(&u->dctrl, sizeof C));
     UCK(cudaMemcpy(u->dctrl, &C, sizeof C, cudaMemcpyHostToDevice));
     return hf_uns_set_state(u, u->init.data());
@@ -783,15 +791,20 @@ int hf_uns_get_state(hf_uns* u, double* cons) {
     return HF_OK;
 }
 
-// strict mode, after a synchronisation: HF_ERR_NUMERIC once a zero-flux pair is recorded
+// strict mode, after a synchronisation: HF_ERR_NUMERIC once a zero-flux pair or a non-positive
+// cell is recorded (the record of the earlier step; a zero flux first within one step)
 static int uns_strict_check(hf_uns* u) {
     if (!u->strict) return HF_OK;
-    unsigned long long k = ~0ull;
-    UCK(cudaMemcpy(&k, &u->dctrl->first_bad, sizeof k, cudaMemcpyDeviceToHost));
-    if (k == ~0ull) return HF_OK;
-    return ufail(u, HF_ERR_NUMERIC,
-                 "HLLC zero flux (all wave-speed branches failed) at step " + std::to_string(k >> 40) +
-                     ", cell " + std::to_string(k & 0xFFFFFFFFFFull));
+    unsigned long long k[2] = {~0ull, ~0ull};
+    UCK(cudaMemcpy(&k[0], &u->dctrl->first_bad, sizeof k[0], cudaMemcpyDeviceToHost));
+    UCK(cudaMemcpy(&k[1], &u->dctrl->first_nonpos, sizeof k[1], cudaMemcpyDeviceToHost));
+    auto at = [](unsigned long long x) {
+        return "step " + std::to_string(x >> 40) + ", cell " + std::to_string(x & 0xFFFFFFFFFFull);
+    };
+    if (k[0] != ~0ull && (k[0] >> 40) <= (k[1] >> 40))
+        return ufail(u, HF_ERR_NUMERIC, "HLLC zero flux (all wave-speed branches failed) at " + at(k[0]));
+    if (k[1] != ~0ull) return ufail(u, HF_ERR_NUMERIC, "non-positive density or pressure at " + at(k[1]));
+    return HF_OK;
 }
 
 int hf_uns_sync(hf_uns* u) {
@@ -822,10 +835,22 @@ int hf_uns_last_error_cell(hf_uns* u, int64_t* cell, int64_t* step) {
     return HF_OK;
 }
 
+int hf_uns_last_nonpositive_cell(hf_uns* u, int64_t* cell, int64_t* step) {
+    if (!u || !u->dctrl) return HF_ERR_ARG;
+    unsigned long long k = ~0ull;
+    UCK(cudaStreamSynchronize(u->stream));
+    UCK(cudaMemcpy(&k, &u->dctrl->first_nonpos, sizeof k, cudaMemcpyDeviceToHost));
+    const bool none = k == ~0ull;
+    if (cell) *cell = none ? -1 : (int64_t)(k & 0xFFFFFFFFFFull);
+    if (step) *step = none ? -1 : (int64_t)(k >> 40);
+    return HF_OK;
+}
+
 int hf_uns_clear_error_cell(hf_uns* u) {
     if (!u || !u->dctrl) return HF_ERR_ARG;
     const unsigned long long none = ~0ull;
     UCK(cudaMemcpyAsync(&u->dctrl->first_bad, &none, sizeof none, cudaMemcpyHostToDevice, u->stream));
+    UCK(cudaMemcpyAsync(&u->dctrl->first_nonpos, &none, sizeof none, cudaMemcpyHostToDevice, u->stream));
     UCK(cudaStreamSynchronize(u->stream));
     return HF_OK;
 }

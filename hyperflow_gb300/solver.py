@@ -250,8 +250,9 @@ class CartSolver:
         return n.value
 
     def set_strict(self, on: bool = True):
-        """Strict mode: a zero-flux HLLC face stops the loop and raises HyperFlowError
-        (HF_ERR_NUMERIC); off (the default) the run continues as the reference's does."""
+        """Strict mode: a zero-flux HLLC face or a cell left with a non-positive density or
+        pressure stops the loop and raises HyperFlowError (HF_ERR_NUMERIC); off (the default)
+        the run continues as the reference's does."""
         check(lib().hf_set_strict(self._h, int(bool(on))), self._h)
 
     def last_error_cell(self):
@@ -263,7 +264,18 @@ class CartSolver:
             return None
         return {"step": st.value, "block": v[0].value, "i": v[1].value, "j": v[2].value, "dir": v[3].value}
 
+    def last_nonpositive_cell(self):
+        """The earliest interior cell a step left with density or pressure not positive (zero,
+        negative or NaN): dict(step, block, i, j), or None."""
+        v = [C.c_int() for _ in range(3)]
+        st = C.c_int64()
+        check(lib().hf_last_nonpositive_cell(self._h, *[C.byref(x) for x in v], C.byref(st)), self._h)
+        if v[0].value < 0:
+            return None
+        return {"step": st.value, "block": v[0].value, "i": v[1].value, "j": v[2].value}
+
     def clear_error_cell(self):
+        """Forgets both records (zero-flux face and non-positive cell)."""
         check(lib().hf_clear_error_cell(self._h), self._h)
 
     def stream(self) -> int:

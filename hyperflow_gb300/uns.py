@@ -169,7 +169,8 @@ class UnsSolver:
         check(lib().hf_uns_sync(self._h), self._h, _MSG)
 
     def set_strict(self, on: bool = True):
-        """Strict mode: a zero-flux HLLC pair stops the loop and raises HyperFlowError."""
+        """Strict mode: a zero-flux HLLC pair or a cell left with a non-positive density or
+        pressure stops the loop and raises HyperFlowError."""
         check(lib().hf_uns_set_strict(self._h, int(bool(on))), self._h, _MSG)
 
     def last_error_cell(self):
@@ -178,7 +179,15 @@ class UnsSolver:
         check(lib().hf_uns_last_error_cell(self._h, C.byref(cell), C.byref(st)), self._h, _MSG)
         return None if cell.value < 0 else {"step": st.value, "cell": cell.value}
 
+    def last_nonpositive_cell(self):
+        """The earliest cell a step left with density or pressure not positive (zero, negative
+        or NaN): dict(step, cell), or None."""
+        cell, st = C.c_int64(), C.c_int64()
+        check(lib().hf_uns_last_nonpositive_cell(self._h, C.byref(cell), C.byref(st)), self._h, _MSG)
+        return None if cell.value < 0 else {"step": st.value, "cell": cell.value}
+
     def clear_error_cell(self):
+        """Forgets both records (zero-flux pair and non-positive cell)."""
         check(lib().hf_uns_clear_error_cell(self._h), self._h, _MSG)
 
     # --- checkpoint / restart ---

@@ -35,7 +35,8 @@ enum {
     HF_ERR_STATE = 6,        /* call out of order (e.g. advancing block 2 before block 1) */
     HF_ERR_NO_DEVICE = 7,    /* no CUDA device is visible */
     HF_ERR_TOO_LARGE = 8,    /* the problem exceeds a fixed-size working area */
-    HF_ERR_NUMERIC = 9       /* strict mode: an HLLC zero-flux fallback occurred (hf_last_error_cell) */
+    HF_ERR_NUMERIC = 9       /* strict mode: an HLLC zero-flux fallback (hf_last_error_cell) or a
+                                non-positive density or pressure (hf_last_nonpositive_cell) occurred */
 };
 
 /* state layouts for hf_set_state / hf_get_state */
@@ -114,7 +115,7 @@ int hf_get_time(hf_ctx* ctx, double* t, int64_t* calls, double* last_dt);
 int hf_hllc_errors(hf_ctx* ctx, int64_t* count);
 
 /* waits for the context's stream; returns HF_ERR_DEVICE if a kernel raised its error word
- * (and HF_ERR_NUMERIC in strict mode once a zero-flux face is recorded) */
+ * (and HF_ERR_NUMERIC in strict mode once a zero-flux face or a non-positive cell is recorded) */
 int hf_sync(hf_ctx* ctx);
 
 /* Faces whose HLLC takes none of its four branches (riemann_hllc.cpp:199-211: NaN wave speeds,
@@ -124,11 +125,17 @@ int hf_sync(hf_ctx* ctx);
  * j, i), where direction 0 is the x face i between interior cells (i-1, j) and (i, j) and 1 the
  * y face j between (i, j-1) and (i, j); step counts the steps completed before it.  All outputs
  * are -1 when there is none; any pointer may be null.
- * hf_set_strict(ctx, 1): once such a face is recorded the step completes, later steps do
+ * hf_last_nonpositive_cell gives, the same way, the earliest (step, block, j, i) interior cell
+ * that a step left with a density or pressure (EulerIdealGasModel::cons_to_prim,
+ * euler_ideal_gas.cpp:76-92) that is not positive -- zero, negative or NaN.  The reference has no
+ * such check and carries the state on; so does this library outside strict mode.
+ * hf_set_strict(ctx, 1): once either is recorded the step completes, later steps do
  * nothing, and hf_step / hf_run (with steps_done) / hf_step_io / hf_sync return HF_ERR_NUMERIC
- * with the face in hf_last_error_message.  hf_clear_error_cell lets the run go on. */
+ * with the face or cell in hf_last_error_message.  hf_clear_error_cell clears both records and
+ * lets the run go on. */
 int hf_set_strict(hf_ctx* ctx, int on);
 int hf_last_error_cell(hf_ctx* ctx, int* block, int* i, int* j, int* dir, int64_t* step);
+int hf_last_nonpositive_cell(hf_ctx* ctx, int* block, int* i, int* j, int64_t* step);
 int hf_clear_error_cell(hf_ctx* ctx);
 
 /* the context's CUDA stream (a cudaStream_t), for callers that time or order work on it */

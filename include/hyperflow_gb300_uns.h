@@ -82,14 +82,19 @@ int hf_uns_frame_pop(hf_uns* u, double* cons, double* t, int64_t* index);
 /* Pairs whose HLLC takes the zero flux (NaN wave speeds) are counted by hf_uns_hllc_errors and
  * the run continues, as in the reference.  hf_uns_last_error_cell gives the earliest one since
  * creation or hf_uns_clear_error_cell: the least (step, cell) -- in edge-based mode the edge's
- * owner cell -- or -1.  Strict mode (hf_uns_set_strict(u, 1)): once one is recorded the step
+ * owner cell -- or -1.  hf_uns_last_nonpositive_cell gives the least (step, cell) of a cell that
+ * a step left with a density or pressure (cons_to_prim) that is not positive -- zero, negative or
+ * NaN -- or -1; the reference carries such a state on, and so does this library outside strict
+ * mode.  Strict mode (hf_uns_set_strict(u, 1)): once either is recorded the step
  * completes, later device-loop steps do nothing, and hf_uns_run / hf_uns_time_step return
- * HF_ERR_NUMERIC with the cell in hf_uns_last_error_message. */
+ * HF_ERR_NUMERIC with the cell in hf_uns_last_error_message.  hf_uns_clear_error_cell clears
+ * both records. */
 /* waits for the context's stream; HF_ERR_DEVICE if a kernel raised the error word (in the
  * bounds-checked build: an index outside the mesh), HF_ERR_NUMERIC as hf_uns_run in strict mode */
 int hf_uns_sync(hf_uns* u);
 int hf_uns_set_strict(hf_uns* u, int on);
 int hf_uns_last_error_cell(hf_uns* u, int64_t* cell, int64_t* step);
+int hf_uns_last_nonpositive_cell(hf_uns* u, int64_t* cell, int64_t* step);
 int hf_uns_clear_error_cell(hf_uns* u);
 
 /* Checkpoint / restart of the whole unstructured simulation state (both cell-state buffers and

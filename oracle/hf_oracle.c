@@ -386,12 +386,40 @@ double hfo_time_step(hfo_mesh *m) {
  * interior cells (i-1, j) and (i, j); 1: y face j between (i, j-1) and (i, j)), j, i; fields
  * saturate at 22, 4, 1, 18 and 19 bits.  Not in the reference, which prints a message
  * (riemann_hllc.cpp:199-211); the GPU records the same key. */
-static void note_bad(hfo_mesh *m, int b, int dir, int j, int i) {
+static uint64_t err_key(const hfo_mesh *m, int b, int dir, int j, int i) {
     uint64_t s = m->steps > 0x3FFFFF ? 0x3FFFFFu : (uint64_t)m->steps;
     uint64_t jj = j > 0x3FFFF ? 0x3FFFFu : (uint64_t)j, ii = i > 0x7FFFF ? 0x7FFFFu : (uint64_t)i;
-    uint64_t k = (s << 42) | ((uint64_t)(b & 0xF) << 38) | ((uint64_t)(dir & 1) << 37) | (jj << 19) | ii;
+    return (s << 42) | ((uint64_t)(b & 0xF) << 38) | ((uint64_t)(dir & 1) << 37) | (jj << 19) | ii;
+}
+
+static void note_bad(hfo_mesh *m, int b, int dir, int j, int i) {
+    uint64_t k = err_key(m, b, dir, j, i);
 #pragma omp critical(hfo_first_bad)
     if (k < m->first_bad) m->first_bad = k;
+}
+
+/* density and pressure (cons_to_prim) both positive; false for zero, negative and NaN.  Not in
+ * the reference, which carries such a state on; the GPU records the earliest cell that fails it. */
+static int physical(double g, const double *c) {
+    double w[4];
+    hfo_cons_to_prim(g, c, w);
+    return c[0] > 0.0 && w[3] > 0.0;
+}
+
+/* the earliest interior cell of block b's new state (layout of m->U[b]) that is not physical */
+static void note_nonpos(hfo_mesh *m, int b, const double *Unew) {
+    int tx = tot_x(m, b), ty = tot_y(m, b), gh = m->ghost;
+    size_t plane = (size_t)tx * ty;
+    for (int j = 0; j < m->ny[b]; ++j)
+        for (int i = 0; i < m->nx[b]; ++i) {
+            size_t o = (size_t)(j + gh) * tx + (i + gh);
+            double c[4] = {Unew[o], Unew[plane + o], Unew[2 * plane + o], Unew[3 * plane + o]};
+            if (!physical(m->gamma, c)) {
+                uint64_t k = err_key(m, b, 0, j, i);
+                if (k < m->first_nonpos) m->first_nonpos = k;
+                return;   /* row-major scan: the first one found is the least */
+            }
+        }
 }
 
 /* ---------------- Godunov block update, src/fvm_2d_cart/scheme/godunov/godunov.cpp:27-118,
@@ -559,6 +587,7 @@ void hfo_advance(hfo_mesh *m, double dt) {
             double dtp = hfo_time_step(m);
             mh_block(m, b, dt, dtp, Unew);
         }
+        note_nonpos(m, b, Unew);
         memcpy(m->U[b], Unew, n * sizeof(double));
         free(Unew);
     }
@@ -753,6 +782,17 @@ static void uns_update(double g, int ncells, const int *pair_start, const int *p
             Un[v * N + c] = dt * L + cv[v];
         }
     }
+}
+
+/* the least cell of an unstructured state [4][ncells] whose density or pressure is not
+ * positive (or NaN), -1 when none; the GPU records it per step */
+int64_t hfo_uns_first_nonpositive(double g, int ncells, const double *U) {
+    size_t N = (size_t)ncells;
+    for (int c = 0; c < ncells; ++c) {
+        double c4[4] = {U[c], U[N + c], U[2 * N + c], U[3 * N + c]};
+        if (!physical(g, c4)) return c;
+    }
+    return -1;
 }
 
 int hfo_uns_run(double g, double cfl, int64_t *calls, int ncells, const int *pair_start,

@@ -42,6 +42,8 @@ typedef struct {
     int64_t hllc_errors;               /* times the HLLC "should not get here" branch ran */
     int64_t steps;                     /* hfo_advance calls completed */
     uint64_t first_bad;                /* least key (step, block, direction, j, i) of such a face */
+    uint64_t first_nonpos;             /* least key (step, block, 0, j, i) of an interior cell a step
+                                          left with density or pressure not positive (or NaN) */
 } hfo_mesh;
 
 #ifdef __cplusplus
@@ -87,6 +89,8 @@ int hfo_uns_run(double gamma, double cfl, int64_t *calls, int ncells, const int 
                 const int *pair_nbr, const double *angle, const double *length,
                 const double *area, const double *rin, const double *inlet,
                 double *U, int n, double *dts, int nthreads);
+/* the least cell of a state [4][ncells] whose density or pressure is not positive, or -1 */
+int64_t hfo_uns_first_nonpositive(double gamma, int ncells, const double *U);
 /* the unstructured Simulation::solve with its t_end and frame clamps and frame cadence */
 int64_t hfo_uns_solve(double g, double cfl, int64_t *calls, int ncells, const int *pair_start,
                       const int *pair_nbr, const double *angle, const double *length,

@@ -40,7 +40,7 @@ class _Mesh(C.Structure):
         ("bc_type", (C.c_int * 4) * MAXB), ("bc_block", (C.c_int * 4) * MAXB),
         ("bc_state", ((C.c_double * 4) * 4) * MAXB),
         ("U", C.c_void_p * MAXB), ("nthreads", C.c_int), ("hllc_errors", C.c_int64),
-        ("steps", C.c_int64), ("first_bad", C.c_uint64),
+        ("steps", C.c_int64), ("first_bad", C.c_uint64), ("first_nonpos", C.c_uint64),
     ]
 
 
@@ -86,6 +86,8 @@ def port_lib():
                                       C.c_int64, p, i]
         lib.hfo_uns_run.restype = i
         lib.hfo_uns_run.argtypes = [d, d, p, i, p, p, p, p, p, p, p, p, i, p, i]
+        lib.hfo_uns_first_nonpositive.restype = C.c_int64
+        lib.hfo_uns_first_nonpositive.argtypes = [d, i, p]
         _port = lib
     return _port
 
@@ -136,6 +138,7 @@ class Oracle:
         m.t_end = float(case["simulation"]["t_end"])
         m.nthreads = nthreads
         m.first_bad = (1 << 64) - 1
+        m.first_nonpos = (1 << 64) - 1
         blocks = case["mesh"]["blocks"]
         m.nblocks = len(blocks)
         self.U = []
@@ -267,6 +270,15 @@ class Oracle:
             return None
         return {"step": k >> 42, "block": (k >> 38) & 0xF, "dir": (k >> 37) & 1,
                 "j": (k >> 19) & 0x3FFFF, "i": k & 0x7FFFF}
+
+    @property
+    def first_nonpos(self):
+        """The earliest interior cell a step left with density or pressure not positive
+        (step, block, i, j) as the GPU reports it, or None."""
+        k = self.m.first_nonpos
+        if k == (1 << 64) - 1:
+            return None
+        return {"step": k >> 42, "block": (k >> 38) & 0xF, "j": (k >> 19) & 0x3FFFF, "i": k & 0x7FFFF}
 
     def state(self, b: int = 0) -> np.ndarray:
         return self.U[b].copy()
@@ -485,6 +497,13 @@ def uns_solve(gamma, cfl, pair_start, pair_nbr, angle, length, area, rin, inlet,
                                  C.byref(nf), nthreads)
     m = min(nf.value, max_frames)
     return k, c.value, ft[:m], frames[:m]
+
+
+def uns_first_nonpositive(gamma, U):
+    """The least cell of U ([4][ncells]) whose density or pressure is not positive, or None."""
+    U = np.ascontiguousarray(U, dtype=np.float64)
+    k = port_lib().hfo_uns_first_nonpositive(gamma, U.shape[1], _ptr(U))
+    return None if k < 0 else int(k)
 
 
 def uns_run(gamma, cfl, calls, pair_start, pair_nbr, angle, length, area, rin, inlet, U, n,

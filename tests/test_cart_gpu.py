@@ -98,6 +98,47 @@ def test_gpu_negative_pressure_cell_matches_oracle(scheme, port_lib):
     bad = s.last_error_cell()
     assert bad == o.first_bad
     assert bad["step"] == 0 and bad["dir"] == 0 and abs(bad["i"] - 23) <= 3   # next to cell (23, 17)
+    assert s.last_nonpositive_cell() == o.first_nonpos
+    assert o.first_nonpos["step"] == 0
+
+
+def test_gpu_nonpositive_cell_matches_oracle():
+    """A physical start that loses positivity: the shock-bubble at 128^2 under MUSCL-Hancock at
+    CFL 0.8 (unstable for 2D flow) first leaves a cell with negative pressure at step 82, before
+    any zero-flux face.  The earliest non-positive cell, the later zero-flux face and the state
+    with its NaNs all match the oracle; clearing forgets both records."""
+    from oracle.oracle import Oracle
+    from hyperflow_gb300 import cases
+    case = cases.shock_bubble_case(128, cfl=0.8)
+    o, s = Oracle(case, nthreads=4), _solver(case)
+    o.run(82)
+    s.run(82)
+    assert o.first_nonpos is None and s.last_nonpositive_cell() is None
+    o.run(8)
+    s.run(8)
+    np.testing.assert_array_equal(s.state(0), o.state(0))
+    assert o.first_nonpos == {"step": 82, "block": 0, "j": 82, "i": 45}
+    assert s.last_nonpositive_cell() == o.first_nonpos
+    assert s.last_error_cell() == o.first_bad
+    s.clear_error_cell()
+    assert s.last_nonpositive_cell() is None and s.last_error_cell() is None
+
+
+def test_gpu_strict_mode_stops_at_the_nonpositive_step():
+    """Strict mode on the same run: the step that left the non-positive cell (step 82) completes
+    and the loop stops there, through the device loop and through the piecewise calls."""
+    from hyperflow_gb300 import HyperFlowError, cases
+    case = cases.shock_bubble_case(128, cfl=0.8)
+    s, ref = _solver(case), _solver(case)
+    ref.run(83)
+    s.set_strict(True)
+    with pytest.raises(HyperFlowError, match="non-positive density or pressure at step 82, block 0, cell"):
+        s.run(200)
+    assert s.time()[:2] == ref.time()[:2]
+    np.testing.assert_array_equal(s.state(0), ref.state(0))
+    with pytest.raises(HyperFlowError, match="non-positive"):
+        s.step()
+    assert s.time()[:2] == ref.time()[:2]
 
 
 def test_gpu_strict_mode_stops_at_the_zero_flux_step():

@@ -204,6 +204,13 @@ def test_uns_gpu_negative_pressure_cell_and_strict_mode():
     bad = s.last_error_cell()
     nbrs = {100} | {int(k) for k in m["nbr"][m["pair_start"][100]:m["pair_start"][101]] if k >= 0}
     assert bad["step"] == 0 and bad["cell"] in nbrs
+    # the earliest non-positive cell: the oracle's state after one step, scanned in cell order
+    W = U.copy()
+    oracle.uns_run(1.4, g["case"]["simulation"]["cfl"], 0, m["pair_start"], m["nbr"], m["angle"],
+                   m["length"], m["area"], m["rin"], _inlet(g["case"]), W, 1)
+    first = oracle.uns_first_nonpositive(1.4, W)
+    assert first is not None
+    assert s.last_nonpositive_cell() == {"step": 0, "cell": first}
     t = UnsSolver(g["case"], mesh_text=text)
     t.set_state(U)
     t.set_strict(True)
@@ -211,7 +218,7 @@ def test_uns_gpu_negative_pressure_cell_and_strict_mode():
         t.run(5)
     assert t.time()[1] == 1
     s.clear_error_cell()
-    assert s.last_error_cell() is None
+    assert s.last_error_cell() is None and s.last_nonpositive_cell() is None
 
 
 @pytest.mark.gpu
