@@ -105,6 +105,8 @@ SIGNATURES = {
     "hf_batch_set_state": (_i, [_p, _i, _p]),
     "hf_batch_instance_time": (_i, [_p, _i, C.POINTER(_d), C.POINTER(_d)]),
     "hf_batch_counters": (_i, [_p, C.POINTER(_i64), C.POINTER(_i64), C.POINTER(_i64)]),
+    "hf_batch_last_nonpositive_cell": (_i, [_p, C.POINTER(_i), C.POINTER(_i), C.POINTER(_i), C.POINTER(_i64)]),
+    "hf_batch_clear_error_cell": (_i, [_p]),
     "hf_batch_stream": (_i, [_p, C.POINTER(_p)]),
     # learned coarse solver (include/hyperflow_gb300_learned.h)
     "hf_lc_create": (_i, [_i, _d, _d, _d, _i, C.POINTER(_p)]),

@@ -97,6 +97,20 @@ class BatchSolver:
         check(lib().hf_batch_counters(self._h, C.byref(s), C.byref(c), C.byref(e)), self._h, _MSG)
         return {"steps": s.value, "calls": c.value, "hllc_errors": e.value}
 
+    def last_nonpositive_cell(self):
+        """The earliest cell a step left with density or pressure not positive (zero, negative
+        or NaN): dict(step, case, i, j), or None."""
+        v = [C.c_int() for _ in range(3)]
+        st = C.c_int64()
+        check(lib().hf_batch_last_nonpositive_cell(self._h, *[C.byref(x) for x in v], C.byref(st)),
+              self._h, _MSG)
+        if v[0].value < 0:
+            return None
+        return {"step": st.value, "case": v[0].value, "i": v[1].value, "j": v[2].value}
+
+    def clear_error_cell(self):
+        check(lib().hf_batch_clear_error_cell(self._h), self._h, _MSG)
+
     def stream(self) -> int:
         s = C.c_void_p()
         check(lib().hf_batch_stream(self._h, C.byref(s)), self._h, _MSG)

@@ -57,7 +57,17 @@ struct BatchCtrl {
     unsigned int bar_count;
     unsigned int bar_gen;
     long long hllc_errors;
+    unsigned long long first_nonpos;   // least batch_key of a cell a step left with density or
+                                       // pressure not positive, ~0 when none
 };
+
+// Key of a cell for the earliest non-positive record: the step (24 bits, saturating), then the
+// cell's offset in the batch state (40 bits: the case's offset + j * n + i), which orders by case,
+// row, column.
+__device__ __forceinline__ unsigned long long batch_key(long long step, long long off) {
+    const unsigned long long s = step > 0xFFFFFFll ? 0xFFFFFFull : (unsigned long long)step;
+    return (s << 40) | ((unsigned long long)off & 0xFFFFFFFFFFull);
+}
 
 struct BatchDev {
     BatchCtrl* ctrl;
@@ -248,7 +258,8 @@ __global__ void __launch_bounds__(NT, MINB) batch_kernel(BatchDev d, int nsteps)
                         out[v * plane + (size_t)gy * I.n + gx] = un[v];
                     }
                     double sx, sy;
-                    wave_terms(g, g1, un[0], un[1], un[2], un[3], sx, sy);
+                    if (!wave_terms(g, g1, un[0], un[1], un[2], un[3], sx, sy))
+                        atomicMin(&c->first_nonpos, batch_key(step, I.off + (long long)gy * I.n + gx));
                     mx = nmax(mx, sx);
                     my = nmax(my, sy);
                 }
@@ -569,6 +580,7 @@ int hf_batch_create(const char* manifest, size_t len, hf_batch** out) {
     C.limiter = b->limiter;
     C.scheme = b->scheme;
     C.ninst = (int)n;
+    C.first_nonpos = ~0ull;
     BCK(cudaMemcpy(b->dctrl, &C, sizeof C, cudaMemcpyHostToDevice));
     for (size_t i = 0; i < n; ++i)
         BCK(cudaMemcpy(b->U[0] + b->inst[i].off, init[i].data(), init[i].size() * sizeof(double), cudaMemcpyHostToDevice));
@@ -739,6 +751,42 @@ int hf_batch_counters(hf_batch* b, int64_t* steps, int64_t* calls, int64_t* hllc
     if (steps) *steps = C.step;
     if (calls) *calls = C.calls;
     if (hllc_errors) *hllc_errors = C.hllc_errors;
+    return HF_OK;
+}
+
+int hf_batch_last_nonpositive_cell(hf_batch* b, int* instance, int* i, int* j, int64_t* step) {
+    if (!b) return HF_ERR_ARG;
+    unsigned long long k = ~0ull;
+    BCK(cudaStreamSynchronize(b->stream));
+    BCK(cudaMemcpy(&k, &b->dctrl->first_nonpos, sizeof k, cudaMemcpyDeviceToHost));
+    int ci = -1, cj = -1, cx = -1;
+    long long st = -1;
+    if (k != ~0ull) {
+        const long long off = (long long)(k & 0xFFFFFFFFFFull);
+        // the case whose state holds that offset (offsets ascend with the case index)
+        size_t lo = 0, hi = b->inst.size();
+        while (hi - lo > 1) {
+            const size_t mid = (lo + hi) / 2;
+            (b->inst[mid].off <= off ? lo : hi) = mid;
+        }
+        const long long rem = off - b->inst[lo].off;
+        cx = (int)lo;
+        cj = (int)(rem / b->inst[lo].n);
+        ci = (int)(rem % b->inst[lo].n);
+        st = (long long)(k >> 40);
+    }
+    if (instance) *instance = cx;
+    if (i) *i = ci;
+    if (j) *j = cj;
+    if (step) *step = st;
+    return HF_OK;
+}
+
+int hf_batch_clear_error_cell(hf_batch* b) {
+    if (!b) return HF_ERR_ARG;
+    const unsigned long long none = ~0ull;
+    BCK(cudaMemcpyAsync(&b->dctrl->first_nonpos, &none, sizeof none, cudaMemcpyHostToDevice, b->stream));
+    BCK(cudaStreamSynchronize(b->stream));
     return HF_OK;
 }
 

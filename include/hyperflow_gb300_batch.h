@@ -55,6 +55,12 @@ int hf_batch_get_state(hf_batch* b, int i, double* out);
 int hf_batch_set_state(hf_batch* b, int i, const double* in);
 int hf_batch_instance_time(hf_batch* b, int i, double* t, double* last_dt);
 int hf_batch_counters(hf_batch* b, int64_t* steps, int64_t* calls, int64_t* hllc_errors);
+/* the earliest cell a step left with a density or pressure (cons_to_prim) that is not positive --
+ * zero, negative or NaN -- since creation or hf_batch_clear_error_cell: the least (step, case,
+ * j, i), step counting the steps completed before it; all -1 when there is none.  The run
+ * continues, as the reference's does; there is no strict mode in a batch. */
+int hf_batch_last_nonpositive_cell(hf_batch* b, int* instance, int* i, int* j, int64_t* step);
+int hf_batch_clear_error_cell(hf_batch* b);
 int hf_batch_stream(hf_batch* b, void** stream);
 
 #ifdef __cplusplus

@@ -135,3 +135,34 @@ def test_batch_of_one_runs_the_256_godunov_workload(port_lib):
     s.run(200)
     np.testing.assert_array_equal(b.state(0), s.state(0)[:, 1:-1, 1:-1])
     assert b.instance_time(0)[0] == s.time()[0]
+
+
+@pytest.mark.gpu
+def test_batch_records_the_earliest_nonpositive_cell(port_lib):
+    """Eight small Riemann problems at CFL 0.8 (unstable for 2D flow): cases 7 and 2 leave a cell
+    with non-positive pressure at steps 29 and 31.  The batch records the least (step, case, j, i),
+    equal to the oracle's per-case records, runs on as the reference does (every state equals the
+    oracle's, NaNs included), and clearing forgets the record."""
+    from oracle.oracle import Oracle
+    from hyperflow_gb300 import BatchSolver, cases
+    m = cases.batch_manifest(8, seed=4, side_min=48, side_max=80, cfl=0.8)
+    steps = 40
+    recs, ref = [], []
+    for k, c in enumerate(m["cases"]):
+        o = Oracle(c, nthreads=4)
+        o.run(steps)
+        ref.append(o.state(0)[:, 2:-2, 2:-2])
+        if o.first_nonpos is not None:
+            r = o.first_nonpos
+            recs.append((r["step"], k, r["j"], r["i"]))
+    assert [(s, k) for s, k, _, _ in sorted(recs)] == [(29, 7), (31, 2)]
+    b = BatchSolver(m)
+    b.run(28)
+    assert b.last_nonpositive_cell() is None
+    b.run(steps - 28)
+    s, k, j, i = min(recs)
+    assert b.last_nonpositive_cell() == {"step": s, "case": k, "j": j, "i": i}
+    for n in range(b.ninstances):
+        np.testing.assert_array_equal(b.state(n), ref[n], err_msg=f"case {n}")
+    b.clear_error_cell()
+    assert b.last_nonpositive_cell() is None
