@@ -17,6 +17,7 @@
 // order, so the sum matches the reference bit for bit.
 #include <cmath>
 #include <cstdio>
+#include <cstdint>
 #include <cstring>
 #include <fstream>
 #include <memory>
@@ -403,6 +404,48 @@ int parse_mesh(hf_uns* u, const std::string& text) {
     return HF_OK;
 }
 
+// The binary mesh format: the text format's content in a fixed little-endian layout, read
+// without number parsing.
+//   bytes 0..7    "HFMESHB1"
+//   bytes 8..15   ncells, int64
+//   bytes 16..23  npairs (the cells' vertex counts summed: one (cell, edge) pair per vertex), int64
+//   ncells int32  vertices per cell, 3 or 4
+//   npairs int32  boundary code per pair, in the text format's EDGES order
+//   zero padding to a multiple of 8 bytes
+//   npairs x 2 float64  the cells' vertices (x, y) in order
+constexpr char kMeshMagic[8] = {'H', 'F', 'M', 'E', 'S', 'H', 'B', '1'};
+
+bool is_binary_mesh(const std::string& data) {
+    return data.size() >= 8 && std::memcmp(data.data(), kMeshMagic, 8) == 0;
+}
+
+int parse_mesh_binary(hf_uns* u, const std::string& data) {
+    const size_t size = data.size();
+    if (size < 24) return ufail(u, HF_ERR_PARSE, "binary mesh: truncated header");
+    int64_t n = 0, np = 0;
+    std::memcpy(&n, data.data() + 8, 8);
+    std::memcpy(&np, data.data() + 16, 8);
+    if (n < 1 || n > INT32_MAX / 4 || np < 3 * n || np > 4 * n)
+        return ufail(u, HF_ERR_PARSE, "binary mesh: bad cell or pair count");
+    const size_t ints = 24 + 4 * (size_t)(n + np);
+    const size_t vo = (ints + 7) / 8 * 8;
+    if (size != vo + 16 * (size_t)np) return ufail(u, HF_ERR_PARSE, "binary mesh: size does not match the counts");
+    u->nverts.resize(n);
+    std::memcpy(u->nverts.data(), data.data() + 24, 4 * (size_t)n);
+    int64_t sum = 0;
+    for (int v : u->nverts) {
+        if (v != 3 && v != 4) return ufail(u, HF_ERR_PARSE, "binary mesh: a cell needs 3 or 4 vertices");
+        sum += v;
+    }
+    if (sum != np) return ufail(u, HF_ERR_PARSE, "binary mesh: vertex counts do not sum to the pair count");
+    u->codes.resize(np);
+    std::memcpy(u->codes.data(), data.data() + 24 + 4 * (size_t)n, 4 * (size_t)np);
+    u->verts.resize(2 * (size_t)np);
+    std::memcpy(u->verts.data(), data.data() + vo, 16 * (size_t)np);
+    u->ncells = (int)n;
+    return HF_OK;
+}
+
 struct EdgeKey {
     uint64_t a, b, c, d;
     bool operator==(const EdgeKey& o) const { return a == o.a && b == o.b && c == o.c && d == o.d; }
@@ -674,13 +717,13 @@ int create_common(const char* case_json, size_t len, const std::string* mesh_tex
         if (mesh_text) {
             text = *mesh_text;
         } else {
-            std::ifstream f(cfg["mesh"]["file"].string());
+            std::ifstream f(cfg["mesh"]["file"].string(), std::ios::binary);
             if (!f) return ufail(u, HF_ERR_ARG, "unable to open mesh file " + cfg["mesh"]["file"].string());
             std::stringstream ss;
             ss << f.rdbuf();
             text = ss.str();
         }
-        int r = parse_mesh(u, text);
+        int r = is_binary_mesh(text) ? parse_mesh_binary(u, text) : parse_mesh(u, text);
         if (r != HF_OK) return r;
         return finish_create(u, cfg);
     } catch (const std::exception& e) {

@@ -15,6 +15,17 @@ where the int is the boundary code used when the edge has no neighbour
 -3 Inlet).  The same format carries triangles here: a cell line with 6 numbers is a
 triangle.  Coordinates are written with repr(), so they read back bit-exactly.
 
+The binary format holds the same content in a fixed little-endian layout that loads without
+number parsing (``hmshb_bytes``; the loader tells the two apart by its magic):
+
+    bytes 0..7    b"HFMESHB1"
+    bytes 8..15   cell count, int64
+    bytes 16..23  pair count (the cells' vertex counts summed), int64
+    int32 x cells vertices per cell (3 or 4)
+    int32 x pairs boundary code per (cell, edge) pair, in the EDGES order
+    zero padding to a multiple of 8 bytes
+    float64 x 2 x pairs  the cells' vertices (x, y), in order
+
 ``jittered_hole_mesh`` builds the circular-hole channel of the 1M-cell workload: a
 seeded jittered lattice (jitter 0.3 h) over [0,4]x[0,2], points on the circle of radius
 0.25 at (1,1), Delaunay triangulation, triangles inside the hole removed, every triangle
@@ -134,6 +145,64 @@ def hmsh_text(verts, codes) -> str:
     lines += ["EDGES", str(sum(len(c) for c in codes))]
     lines += [str(int(c)) for row in codes for c in row]
     return "\n".join(lines) + "\n"
+
+
+MESHB_MAGIC = b"HFMESHB1"
+
+
+def hmshb_bytes(verts, codes) -> bytes:
+    """The binary mesh format of cells (3 or 4 vertices each) and their per-edge codes."""
+    nv = np.array([len(c) for c in verts], dtype="<i4")
+    flat_codes = np.array([int(c) for row in codes for c in row], dtype="<i4")
+    xy = np.array([float(z) for cell in verts for pt in cell for z in pt], dtype="<f8")
+    if len(flat_codes) != int(nv.sum()) or len(xy) != 2 * int(nv.sum()):
+        raise ValueError("one code and one vertex per (cell, edge) pair")
+    head = MESHB_MAGIC + np.array([len(nv), int(nv.sum())], dtype="<i8").tobytes()
+    ints = nv.tobytes() + flat_codes.tobytes()
+    pad = b"\0" * ((-(len(head) + len(ints))) % 8)
+    return head + ints + pad + xy.tobytes()
+
+
+def write_hmshb(path: str, verts, codes) -> None:
+    with open(path, "wb") as f:
+        f.write(hmshb_bytes(verts, codes))
+
+
+def read_hmshb(data: bytes):
+    """(verts, codes) from the binary format: per cell a list of (x, y) and a list of codes."""
+    if data[:8] != MESHB_MAGIC:
+        raise ValueError("not a binary mesh")
+    n, npairs = (int(x) for x in np.frombuffer(data, "<i8", 2, 8))
+    nv = np.frombuffer(data, "<i4", n, 24)
+    codes = np.frombuffer(data, "<i4", npairs, 24 + 4 * n)
+    off = 24 + 4 * (n + npairs)
+    off += (-off) % 8
+    xy = np.frombuffer(data, "<f8", 2 * npairs, off).reshape(-1, 2)
+    if off + 16 * npairs != len(data) or int(nv.sum()) != npairs:
+        raise ValueError("binary mesh: size does not match the counts")
+    starts = np.concatenate([[0], np.cumsum(nv)])
+    verts = [[tuple(p) for p in xy[starts[c]:starts[c + 1]].tolist()] for c in range(n)]
+    return verts, [codes[starts[c]:starts[c + 1]].tolist() for c in range(n)]
+
+
+def read_hmsh(text: str):
+    """(verts, codes) from the text format."""
+    lines = text.split("\n")
+    if not lines[0].startswith("CELLS"):
+        raise ValueError("expected CELLS header")
+    n = int(lines[1])
+    verts = []
+    for line in lines[2:2 + n]:
+        z = [float(t) for t in line.split()]
+        verts.append([(z[2 * k], z[2 * k + 1]) for k in range(len(z) // 2)])
+    if not lines[2 + n].startswith("EDGES"):
+        raise ValueError("expected EDGES header")
+    flat = [int(t) for t in lines[4 + n:] if t.strip()]
+    codes, k = [], 0
+    for cell in verts:
+        codes.append(flat[k:k + len(cell)])
+        k += len(cell)
+    return verts, codes
 
 
 def match_neighbours(verts, codes):

@@ -18,7 +18,10 @@ _MSG = "hf_uns_last_error_message"
 
 
 class UnsSolver:
-    def __init__(self, case, mesh_text: str | None = None):
+    def __init__(self, case, mesh_text: str | bytes | None = None):
+        """mesh_text: the mesh in memory instead of the case's mesh.file -- the text format
+        (str) or the binary format's bytes (``meshgen.hmshb_bytes``); a mesh.file may hold
+        either, told apart by the binary format's magic."""
         text = case if isinstance(case, str) else json.dumps(case)
         self.case = json.loads(text)
         raw = text.encode()
@@ -27,7 +30,7 @@ class UnsSolver:
         if mesh_text is None:
             st = L.hf_uns_create(raw, len(raw), C.byref(h))
         else:
-            mt = mesh_text.encode()
+            mt = mesh_text if isinstance(mesh_text, bytes) else mesh_text.encode()
             st = L.hf_uns_create_mesh(raw, len(raw), mt, len(mt), C.byref(h))
         self._h = h
         if st != 0:

@@ -27,9 +27,14 @@ typedef struct hf_uns hf_uns;
  * mesh.file.  Replaces JSONParser::generate_mesh + LoadStructuredMesh
  * (src/fvm_2d_uns/mesh/mesh_structured/mesh_structured.cpp:23-122): same text format, cells
  * of 3 or 4 vertices, neighbours found by hashing edge endpoints instead of the O(E^2) scan.
+ * mesh.file may instead hold the binary format, recognised by its first 8 bytes "HFMESHB1":
+ * int64 cell count, int64 pair count (the vertex counts summed), int32 vertices per cell,
+ * int32 boundary code per (cell, edge) pair, zero padding to a multiple of 8 bytes, then
+ * float64 (x, y) per vertex, cell by cell, all little-endian -- the text format's content,
+ * read without number parsing.
  * On failure *out may still be set (for hf_uns_last_error_message); destroy it. */
 int hf_uns_create(const char* case_json, size_t len, hf_uns** out);
-/* same, with the mesh text passed in memory instead of read from mesh.file */
+/* same, with the mesh (text or binary format) passed in memory instead of read from mesh.file */
 int hf_uns_create_mesh(const char* case_json, size_t len, const char* mesh_text, size_t mesh_len,
                        hf_uns** out);
 void hf_uns_destroy(hf_uns* u);

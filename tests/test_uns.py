@@ -57,6 +57,21 @@ def test_mesh_text_round_trip():
     np.testing.assert_array_equal(back, V)
 
 
+def test_mesh_binary_round_trip():
+    """The binary mesh format holds exactly the text format's content."""
+    from hyperflow_gb300 import meshgen
+    V, codes = meshgen.jittered_hole_mesh(500, seed=9)
+    data = meshgen.hmshb_bytes(V, codes)
+    assert data[:8] == b"HFMESHB1" and len(data) % 8 == 0
+    v2, c2 = meshgen.read_hmshb(data)
+    np.testing.assert_array_equal(np.array(v2), V)
+    np.testing.assert_array_equal(np.array(c2), codes)
+    v3, c3 = meshgen.read_hmsh(meshgen.hmsh_text(V, codes))
+    assert v3 == v2 and c3 == c2
+    with pytest.raises(ValueError):
+        meshgen.read_hmshb(data[:-8])
+
+
 def test_generator_is_canonical():
     from hyperflow_gb300 import meshgen
     a = meshgen.jittered_hole_mesh(2000, seed=5)
@@ -86,6 +101,37 @@ def test_uns_gpu_matches_reference_fixture(name):
         s.advance(dts[-1])
     np.testing.assert_array_equal(np.array(dts), g["dts"])
     np.testing.assert_array_equal(s.state(), g["U"])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", uns_names())
+def test_uns_gpu_binary_mesh_equals_text(name, tmp_path):
+    """The same mesh in the binary format, in memory and as mesh.file, loads to the same pairs,
+    neighbours, geometry and centroids and steps to the same states; malformed binary meshes
+    are refused before any device work."""
+    from hyperflow_gb300 import HyperFlowError, UnsSolver, meshgen
+    g = load(name)
+    text = meshgen.hmsh_text(g["verts"], g["codes"])
+    data = meshgen.hmshb_bytes(g["verts"], g["codes"])
+    path = tmp_path / "mesh.hmshb"
+    path.write_bytes(data)
+    case = json.loads(json.dumps(g["case"]))
+    case["mesh"]["file"] = str(path)
+    a, b, c = UnsSolver(g["case"], mesh_text=text), UnsSolver(g["case"], mesh_text=data), UnsSolver(case)
+    ma = a.mesh_arrays()
+    for s in (b, c):
+        m = s.mesh_arrays()
+        for k in ma:
+            np.testing.assert_array_equal(m[k], ma[k], err_msg=k)
+        np.testing.assert_array_equal(s.centroids(), a.centroids())
+    for s in (a, b, c):
+        s.run(int(g["steps"]))
+    np.testing.assert_array_equal(b.state(), g["U"])
+    np.testing.assert_array_equal(c.state(), g["U"])
+    bad_count = data[:24] + np.array([5], "<i4").tobytes() + data[28:]   # first cell: 5 vertices
+    for broken in (data[:-8], data[:20], bad_count):
+        with pytest.raises(HyperFlowError):
+            UnsSolver(g["case"], mesh_text=broken)
 
 
 @pytest.mark.gpu
