@@ -105,3 +105,82 @@ def test_blocks_narrower_than_two_ghosts_are_refused():
         if h:
             L.hf_destroy(h)
         assert st == 3 and "2*ghost" in msg
+
+
+def test_block_count_limits():
+    """No blocks, and more than the 16 a context holds, are refused before any device work."""
+    from hyperflow_gb300 import cases
+    c = cases.quadrant_case(16)
+    c["mesh"]["blocks"] = []
+    st, msg = _create(json.dumps(c))
+    assert st == 3 and "between 1 and 16" in msg
+    c = cases.quadrant_case(16)
+    c["mesh"]["blocks"] = [json.loads(json.dumps(c["mesh"]["blocks"][0])) for _ in range(17)]
+    st, msg = _create(json.dumps(c))
+    assert st == 3 and "between 1 and 16" in msg
+
+
+def test_boundary_errors():
+    """An unknown boundary type, an Internal side naming a missing block, and an Internal side
+    between blocks whose shared extents differ are refused with their reasons."""
+    from hyperflow_gb300 import cases
+    c = cases.quadrant_case(16)
+    c["mesh"]["blocks"][0]["boundaries"]["left"] = {"type": "Periodic"}
+    st, msg = _create(json.dumps(c))
+    assert st == 3 and "Periodic" in msg
+    c = cases.quadrant_case(16)
+    c["mesh"]["blocks"][0]["boundaries"]["right"] = {"type": "Internal", "block": 3}
+    st, msg = _create(json.dumps(c))
+    assert st == 1 and "missing block" in msg
+    ffs = cases.forward_facing_step_case(cells_per_unit=20)
+    blocks = ffs["mesh"]["blocks"]
+    for b, blk in enumerate(blocks):
+        for side, bc in blk["boundaries"].items():
+            if bc["type"] == "Internal":
+                other = blocks[bc["block"]]
+                key = "x_cells" if side in ("bottom", "top") else "y_cells"
+                other[key] = other[key] + 1            # the shared side no longer matches
+                st, msg = _create(json.dumps(ffs))
+                assert st == 3 and "unequal extent" in msg
+                return
+    pytest.fail("the forward-facing step has no Internal side")
+
+
+def _uns_create(case, mesh: bytes):
+    from hyperflow_gb300 import _lib
+    L = _lib.lib()
+    h = C.c_void_p()
+    raw = json.dumps(case).encode()
+    st = L.hf_uns_create_mesh(raw, len(raw), mesh, len(mesh), C.byref(h))
+    msg = L.hf_uns_last_error_message(h).decode() if h else ""
+    if h:
+        L.hf_uns_destroy(h)
+    return st, msg
+
+
+def test_uns_mesh_parse_errors_need_no_device():
+    """Malformed text and binary meshes are parse errors found before any device work; a valid
+    mesh of either format gets as far as the device (no GPU here: HF_ERR_NO_DEVICE)."""
+    import numpy as np
+    import torch
+    from hyperflow_gb300 import meshgen
+    V, codes = meshgen.jittered_hole_mesh(300, seed=2)
+    case = meshgen.channel_case("unused.hmsh")
+    text = meshgen.hmsh_text(V, codes).encode()
+    data = meshgen.hmshb_bytes(V, codes)
+    lines = text.split(b"\n")
+    bad = {
+        "binary truncated": data[:-8],
+        "binary header only": data[:20],
+        "binary 5-vertex cell": data[:24] + np.array([5], "<i4").tobytes() + data[28:],
+        "binary pair count": data[:16] + np.array([len(V) * 3 + 1], "<i8").tobytes() + data[24:],
+        "text header": text.replace(b"CELLS", b"CELS", 1),
+        "text cell count": text.replace(str(len(V)).encode(), str(len(V) + 1).encode(), 1),
+        "text 2-vertex cell": b"\n".join(lines[:2] + [b"0.0 0.0 1.0 1.0"] + lines[3:]),
+    }
+    for what, mesh in bad.items():
+        st, msg = _uns_create(case, mesh)
+        assert st == 2 and "mesh" in msg, (what, st, msg)
+    if not torch.cuda.is_available():
+        for mesh in (text, data):
+            assert _uns_create(case, mesh)[0] == 7
