@@ -290,8 +290,13 @@ int parse_case(hf_ctx* ctx, const Json& cfg) {
         B.xr = ex["x_right"].number();
         B.yb = ex["y_bottom"].number();
         B.yt = ex["y_top"].number();
-        B.nx = (int)jb["x_cells"].number();
-        B.ny = (int)jb["y_cells"].number();
+        const double cx = jb["x_cells"].number(), cy = jb["y_cells"].number();
+        // cell counts are whole numbers; above 2^24 per side no state fits in device memory
+        if (!(cx >= 0.0 && cx <= 16777216.0 && cy >= 0.0 && cy <= 16777216.0) || cx != (double)(long long)cx ||
+            cy != (double)(long long)cy)
+            return fail(ctx, HF_ERR_UNSUPPORTED, "x_cells and y_cells must be whole numbers up to 2^24");
+        B.nx = (int)cx;
+        B.ny = (int)cy;
         if (B.nx < 2 * ctx->ghost || B.ny < 2 * ctx->ghost)
             return fail(ctx, HF_ERR_UNSUPPORTED, "a block needs at least 2*ghost cells per axis");
         B.tx = B.nx + 2 * ctx->ghost;

@@ -120,6 +120,17 @@ def test_block_count_limits():
     assert st == 3 and "between 1 and 16" in msg
 
 
+def test_cell_counts_must_be_whole_and_bounded():
+    from hyperflow_gb300 import cases
+    for nx in (16.5, -4, 3e9, float("inf")):
+        c = cases.quadrant_case(16)
+        c["mesh"]["blocks"][0]["x_cells"] = nx
+        st, msg = _create(json.dumps(c).replace("Infinity", "1e400"))
+        assert st in (2, 3), (nx, st, msg)
+        if st == 3:
+            assert "whole numbers" in msg
+
+
 def test_boundary_errors():
     """An unknown boundary type, an Internal side naming a missing block, and an Internal side
     between blocks whose shared extents differ are refused with their reasons."""
