@@ -23,7 +23,6 @@
 #include <memory>
 #include <sstream>
 #include <string>
-#include <unordered_map>
 #include <vector>
 
 #include "../../include/hyperflow_gb300_uns.h"
@@ -446,19 +445,6 @@ int parse_mesh_binary(hf_uns* u, const std::string& data) {
     return HF_OK;
 }
 
-struct EdgeKey {
-    uint64_t a, b, c, d;
-    bool operator==(const EdgeKey& o) const { return a == o.a && b == o.b && c == o.c && d == o.d; }
-};
-struct EdgeHash {
-    size_t operator()(const EdgeKey& k) const {
-        uint64_t h = k.a * 0x9E3779B97F4A7C15ull;
-        h ^= k.b + 0x7F4A7C159E3779B9ull + (h << 6) + (h >> 2);
-        h ^= k.c + 0x94D049BB133111EBull + (h << 6) + (h >> 2);
-        h ^= k.d + 0xBF58476D1CE4E5B9ull + (h << 6) + (h >> 2);
-        return (size_t)h;
-    }
-};
 uint64_t bitsof(double x) {
     if (x == 0.0) x = 0.0;   // -0.0 and +0.0 name the same point
     uint64_t b;
@@ -466,37 +452,76 @@ uint64_t bitsof(double x) {
     return b;
 }
 
+// 64-bit finaliser of MurmurHash3 (Appleby): every input bit affects every output bit
+inline uint64_t fmix64(uint64_t x) {
+    x ^= x >> 33;
+    x *= 0xFF51AFD7ED558CCDull;
+    x ^= x >> 33;
+    x *= 0xC4CEB9FE1A85EC53ull;
+    x ^= x >> 33;
+    return x;
+}
+
 // Neighbour search of mesh_structured.cpp:92-114 (a pair's neighbour is the cell holding
 // the same edge reversed; unmatched pairs keep their boundary code), by hashing the
 // exact endpoint coordinates instead of the O(E^2) scan.  For meshes whose shared
 // vertices are written identically -- every mesh the generators produce -- this is the
-// same match the reference finds with its 1e-12 tolerance.
+// same match the reference finds with its 1e-12 tolerance.  Pair p runs from vertex p to
+// vertex nxt[p] (the cells' vertices are stored pair by pair).  The table is open-addressed
+// over pair indices with a 32-bit fingerprint per slot; a directed edge that appears twice
+// keeps the later pair.
 void build_pairs(hf_uns* u) {
-    int n = u->ncells;
+    const int n = u->ncells;
     u->pair_start.assign(n + 1, 0);
     for (int c = 0; c < n; ++c) u->pair_start[c + 1] = u->pair_start[c] + u->nverts[c];
-    std::unordered_map<EdgeKey, int, EdgeHash> table;
-    table.reserve((size_t)u->pair_start[n] * 2);
-    std::vector<size_t> voff(n + 1, 0);
-    for (int c = 0; c < n; ++c) voff[c + 1] = voff[c] + u->nverts[c];
+    const size_t np = (size_t)u->pair_start[n];
+    std::vector<uint64_t> bx(np), by(np);
+    std::vector<int> nxt(np), cell(np);
+    for (size_t q = 0; q < np; ++q) {
+        bx[q] = bitsof(u->verts[2 * q]);
+        by[q] = bitsof(u->verts[2 * q + 1]);
+    }
     for (int c = 0; c < n; ++c) {
-        const double* V = &u->verts[2 * voff[c]];
-        int nv = u->nverts[c];
-        for (int k = 0; k < nv; ++k) {
-            int k1 = (k == nv - 1) ? 0 : k + 1;
-            table[EdgeKey{bitsof(V[2 * k]), bitsof(V[2 * k + 1]), bitsof(V[2 * k1]), bitsof(V[2 * k1 + 1])}] = c;
+        const int s = u->pair_start[c], e = u->pair_start[c + 1];
+        for (int q = s; q < e; ++q) {
+            nxt[q] = (q == e - 1) ? s : q + 1;
+            cell[q] = c;
         }
     }
-    u->nbr.resize(u->pair_start[n]);
-    for (int c = 0; c < n; ++c) {
-        const double* V = &u->verts[2 * voff[c]];
-        int nv = u->nverts[c];
-        for (int k = 0; k < nv; ++k) {
-            int k1 = (k == nv - 1) ? 0 : k + 1;
-            auto it = table.find(EdgeKey{bitsof(V[2 * k1]), bitsof(V[2 * k1 + 1]), bitsof(V[2 * k]), bitsof(V[2 * k + 1])});
-            int pr = u->pair_start[c] + k;
-            u->nbr[pr] = it != table.end() ? it->second : u->codes[pr];
+    size_t cap = 16;
+    while (cap < 2 * np) cap <<= 1;
+    const size_t mask = cap - 1;
+    std::vector<uint64_t> slot(cap, 0);   // (fingerprint << 32) | (pair + 1); 0 is empty
+    // the directed edge from vertex a to vertex b
+    auto hash = [&](size_t a, size_t b) { return fmix64(bx[a] ^ fmix64(by[a] ^ fmix64(bx[b] ^ fmix64(by[b])))); };
+    auto same = [&](size_t q, size_t a, size_t b) {
+        return bx[q] == bx[a] && by[q] == by[a] && bx[nxt[q]] == bx[b] && by[nxt[q]] == by[b];
+    };
+    for (size_t q = 0; q < np; ++q) {
+        const uint64_t h = hash(q, nxt[q]), fp = h >> 32, entry = (fp << 32) | (uint64_t)(q + 1);
+        for (size_t i = h & mask;; i = (i + 1) & mask) {
+            const uint64_t sv = slot[i];
+            if (sv == 0 || ((sv >> 32) == fp && same((size_t)(sv & 0xFFFFFFFFull) - 1, q, nxt[q]))) {
+                slot[i] = entry;
+                break;
+            }
         }
+    }
+    u->nbr.resize(np);
+    for (size_t q = 0; q < np; ++q) {
+        const size_t a = nxt[q], b = q;   // the same edge reversed
+        const uint64_t h = hash(a, b), fp = h >> 32;
+        int found = -1;
+        for (size_t i = h & mask;; i = (i + 1) & mask) {
+            const uint64_t sv = slot[i];
+            if (sv == 0) break;
+            const size_t r = (size_t)(sv & 0xFFFFFFFFull) - 1;
+            if ((sv >> 32) == fp && same(r, a, b)) {
+                found = cell[r];
+                break;
+            }
+        }
+        u->nbr[q] = found >= 0 ? found : u->codes[q];
     }
 }
 
@@ -601,8 +626,6 @@ int finish_create(hf_uns* u, const Json& cfg) {
     {
         std::vector<int> pe(np, -1), ep, ec;
         std::vector<signed char> sg(np, 0);
-        std::unordered_map<uint64_t, int> owner;   // (cell, nbr) -> owner pair
-        owner.reserve(np);
         for (int c = 0; c < n; ++c)
             for (int q = u->pair_start[c]; q < u->pair_start[c + 1]; ++q) {
                 const int k = u->nbr[q];
@@ -612,16 +635,19 @@ int finish_create(hf_uns* u, const Json& cfg) {
                     sg[q] = 1;
                     ep.push_back(q);
                     ec.push_back(c);
-                    owner[((uint64_t)c << 32) | (uint32_t)k] = q;
                 }
             }
+        // the partner side: the owner cell's pair facing this cell (its last such pair, should a
+        // degenerate mesh hold two)
         for (int c = 0; c < n; ++c)
             for (int q = u->pair_start[c]; q < u->pair_start[c + 1]; ++q) {
                 const int k = u->nbr[q];
                 if (k < 0 || c < k) continue;
-                auto it = owner.find(((uint64_t)k << 32) | (uint32_t)c);
-                if (it == owner.end()) continue;        // unmatched: keep the per-side flux
-                pe[q] = pe[it->second];
+                int own = -1;
+                for (int o = u->pair_start[k + 1] - 1; o >= u->pair_start[k] && own < 0; --o)
+                    if (u->nbr[o] == c) own = o;
+                if (own < 0) continue;                  // unmatched: keep the per-side flux
+                pe[q] = pe[own];
                 sg[q] = -1;
             }
         int* d_pe; signed char* d_sg; int* d_ep; int* d_ec; double* d_ef;
