@@ -426,7 +426,10 @@ int enqueue_step(hf_ctx* ctx, bool profiled) {
 }
 
 int set_clamp(hf_ctx* ctx, int clamp) {
-    CK(cudaMemcpyAsync(&ctx->dctrl->clamp, &clamp, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+    if (clamp == 0)   // the common case needs no host memory
+        CK(cudaMemsetAsync(&ctx->dctrl->clamp, 0, sizeof(int), ctx->stream));
+    else
+        CK(cudaMemcpyAsync(&ctx->dctrl->clamp, &clamp, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
     return HF_OK;
 }
 
@@ -769,13 +772,15 @@ int hf_step_io(hf_ctx* ctx, const double* const* in, double* const* out, double*
         // pass uploads each block into both buffers with its TimeStep terms, and every stencil
         // stores its updated cells to the host as it goes, so no download trails the last
         // block's update
+        // every block's interior TimeStep maxima (int_s[p][b], contiguous over b) start at 0
+        CK(cudaMemsetAsync(&ctx->dctrl->int_s[p][0][0], 0, (size_t)ctx->nblocks * 2 * sizeof(unsigned long long),
+                           ctx->stream));
         for (int b = 0; b < ctx->nblocks; ++b) {
             const BlockHost& B = ctx->blocks[b];
-            CK(cudaMemsetAsync(&ctx->dctrl->int_s[p][b][0], 0, 2 * sizeof(unsigned long long), ctx->stream));
             CK(hf::launch_upload(ctx->dctrl, ctx->dmesh, b, B.tx, B.ty, p, in[b], ctx->stream));
         }
-        int clamp = 0;
-        CK(cudaMemcpyAsync(&ctx->dctrl->clamp, &clamp, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+        int r = set_clamp(ctx, 0);
+        if (r != HF_OK) return r;
         CK(hf::launch_bc_fill(ctx->dctrl, ctx->dmesh, ctx->side_len, ctx->nblocks, ctx->stream));
         CK(hf::launch_ghost_cfl(ctx->dctrl, ctx->dmesh, ctx->hmesh.total_ghost, ctx->stream));
         for (int b = 0; b < ctx->nblocks; ++b)
@@ -802,8 +807,8 @@ int hf_step_io(hf_ctx* ctx, const double* const* in, double* const* out, double*
         CK(cudaMemsetAsync(&ctx->dctrl->int_s[p][b][0], 0, 2 * sizeof(unsigned long long), ctx->stream));
         CK(hf::launch_interior_cfl(ctx->dctrl, ctx->dmesh, b, B.nx, B.ny, p, ctx->stream));
     }
-    int clamp = 0;
-    CK(cudaMemcpyAsync(&ctx->dctrl->clamp, &clamp, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+    int r = set_clamp(ctx, 0);
+    if (r != HF_OK) return r;
     CK(hf::launch_bc_fill(ctx->dctrl, ctx->dmesh, ctx->side_len, ctx->nblocks, ctx->stream));
     CK(hf::launch_ghost_cfl(ctx->dctrl, ctx->dmesh, ctx->hmesh.total_ghost, ctx->stream));
     for (int b = 0; b < ctx->nblocks; ++b) {
