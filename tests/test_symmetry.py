@@ -1,0 +1,63 @@
+"""Reflection symmetry of the restated algorithm (the oracle, which the CUDA path equals bit for
+bit in the GPU parity tests).
+
+Godunov: mirrored initial data give the mirrored solution to rounding (the reference's HLLC
+forms the star speed from left and right terms in a fixed order, so a mirror image is not
+bit-exact; a sign or side mix-up would show at O(1)).
+
+MUSCL-Hancock is not mirror-symmetric, in the reference's own formulation: the slope is
+xi(r) * (dl + dr) / 2 with r = dl / dr (muscl_hancock.cpp:137-206), and its limiters do not
+satisfy xi(1/r) = xi(r) (MinBee, minbee.cpp:29-38: xi(2) = 2/3, xi(1/2) = 1/2), so a
+mirrored stencil gets a slope of another magnitude.  The test pins that property too: a
+"symmetric" restatement would no longer equal the reference."""
+import numpy as np
+import pytest
+
+
+def _mirror_run(scheme, limiter, axis, n=96, steps=60):
+    from hyperflow_gb300 import cases
+    from oracle.oracle import Oracle
+    # primitive (rho, u, v, p); quadrants NE, NW, SW, SE mirrored about x = 0.5 (or y = 0.5)
+    a, b = [1.0, 0.3, 0.1, 1.0], [0.5, 0.2, -0.1, 0.4]
+    if axis == "x":   # the east states are a (NE) and b (SE); the west ones their mirror images
+        st = (a, [a[0], -a[1], a[2], a[3]], [b[0], -b[1], b[2], b[3]], b)
+    else:             # the south states are a (SE) and b (SW); the north ones their mirror images
+        st = ([a[0], a[1], -a[2], a[3]], [b[0], b[1], -b[2], b[3]], b, a)
+    o = Oracle(cases.quadrant_case(n, scheme=scheme, limiter=limiter, states=st), nthreads=4)
+    g = o.m.ghost
+    U0 = o.state(0)[:, g:-g, g:-g]
+    o.run(steps)
+    U = o.state(0)[:, g:-g, g:-g]
+
+    def mirrored(V):
+        if axis == "x":
+            M = V[:, :, ::-1].copy()
+            M[1] = -M[1]
+        else:
+            M = V[:, ::-1, :].copy()
+            M[2] = -M[2]
+        return M
+
+    return U0, mirrored(U0), U, mirrored(U)
+
+
+@pytest.mark.parametrize("axis", ["x", "y"])
+def test_godunov_mirror_symmetry(axis, port_lib):
+    U0, M0, U, M = _mirror_run("Godunov", None, axis)
+    np.testing.assert_array_equal(U0, M0)
+    np.testing.assert_allclose(U, M, rtol=1e-7, atol=1e-7)   # rounding: 1e-10 (x), 1e-8 (y) after 60 steps
+    assert np.abs(U - U0).max() > 0.1          # the flow has moved
+
+
+@pytest.mark.parametrize("limiter", ["MinBee", "VanLeer"])
+@pytest.mark.parametrize("axis", ["x", "y"])
+def test_muscl_hancock_is_not_mirror_symmetric(limiter, axis, port_lib):
+    U0, M0, U, M = _mirror_run("MUSCLHancock", limiter, axis)
+    np.testing.assert_array_equal(U0, M0)
+    assert np.abs(U - M).max() > 0.1            # O(1) after 60 steps, against 1e-8 for Godunov
+
+
+def test_minbee_limiter_is_not_reciprocal_symmetric(port_lib):
+    from oracle.oracle import port_lib as lib
+    L = lib()
+    assert L.hfo_limiter(0, 2.0) == 2.0 / 3.0 and L.hfo_limiter(0, 0.5) == 0.5
