@@ -49,12 +49,16 @@ def test_godunov_mirror_symmetry(axis, port_lib):
     assert np.abs(U - U0).max() > 0.1          # the flow has moved
 
 
-@pytest.mark.parametrize("limiter", ["MinBee", "VanLeer"])
+@pytest.mark.parametrize("limiter, least", [("MinBee", 0.1), ("VanLeer", 1e-4)])
 @pytest.mark.parametrize("axis", ["x", "y"])
-def test_muscl_hancock_is_not_mirror_symmetric(limiter, axis, port_lib):
+def test_muscl_hancock_is_not_mirror_symmetric(limiter, least, axis, port_lib):
+    """MinBee: O(1) after 60 steps.  Van Leer's xi does satisfy xi(1/r) = xi(r); what breaks its
+    mirror is the clamp of near-zero differences (|d| <= 1e-6 -> +-1e-6, and a zero difference to
+    +1e-6 whatever its side, muscl_hancock.cpp:78-84): 1e-3 after 60 steps, still far above the
+    1e-8 of Godunov's rounding."""
     U0, M0, U, M = _mirror_run("MUSCLHancock", limiter, axis)
     np.testing.assert_array_equal(U0, M0)
-    assert np.abs(U - M).max() > 0.1            # O(1) after 60 steps, against 1e-8 for Godunov
+    assert np.abs(U - M).max() > least
 
 
 def test_minbee_limiter_is_not_reciprocal_symmetric(port_lib):
