@@ -193,5 +193,6 @@ def test_uns_mesh_parse_errors_need_no_device():
         st, msg = _uns_create(case, mesh)
         assert st == 2 and "mesh" in msg, (what, st, msg)
     if not torch.cuda.is_available():
-        for mesh in (text, data):
+        # CRLF line endings and a missing final newline are read like the plain text
+        for mesh in (text, data, text.replace(b"\n", b"\r\n"), text.rstrip(b"\n")):
             assert _uns_create(case, mesh)[0] == 7
