@@ -523,9 +523,10 @@ int hf_batch_create(const char* manifest, size_t len, hf_batch** out) {
             for (const char* side : {"bottom", "right", "top", "left"})
                 if (blk["boundaries"][side]["type"].string() != "Transmissive")
                     return bfail(b, HF_ERR_UNSUPPORTED, "batched cases are transmissive on every side");
-            int nx = (int)blk["x_cells"].number(), ny = (int)blk["y_cells"].number();
-            if (nx != ny || nx < 4 || nx > 65535)
+            const double cx = blk["x_cells"].number(), cy = blk["y_cells"].number();
+            if (!(cx >= 4.0 && cx <= 65535.0) || cx != cy || cx != (double)(int)cx)
                 return bfail(b, HF_ERR_UNSUPPORTED, "batched cases are square, 4..65535 cells per side");
+            const int nx = (int)cx, ny = (int)cy;
             const Json& ex = blk["extents"];
             double xl = ex["x_left"].number(), xr = ex["x_right"].number();
             double yb = ex["y_bottom"].number(), yt = ex["y_top"].number();

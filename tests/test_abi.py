@@ -196,3 +196,20 @@ def test_uns_mesh_parse_errors_need_no_device():
         # CRLF line endings and a missing final newline are read like the plain text
         for mesh in (text, data, text.replace(b"\n", b"\r\n"), text.rstrip(b"\n")):
             assert _uns_create(case, mesh)[0] == 7
+
+
+def test_batch_manifest_cell_counts_are_checked_before_any_device_work():
+    """Non-square, fractional, too small or too large batched cases are refused."""
+    from hyperflow_gb300 import _lib, cases
+    L = _lib.lib()
+    for nx, ny in ((64, 65), (64.5, 64.5), (3, 3), (70000, 70000), (1e12, 1e12)):
+        m = cases.batch_manifest(2, seed=0, side_min=64, side_max=80)
+        blk = m["cases"][1]["mesh"]["blocks"][0]
+        blk["x_cells"], blk["y_cells"] = nx, ny
+        raw = json.dumps(m).encode()
+        h = C.c_void_p()
+        st = L.hf_batch_create(raw, len(raw), C.byref(h))
+        msg = L.hf_batch_last_error_message(h).decode() if h else ""
+        if h:
+            L.hf_batch_destroy(h)
+        assert st == 3 and "square" in msg, (nx, ny, st, msg)
