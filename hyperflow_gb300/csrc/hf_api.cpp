@@ -321,7 +321,8 @@ int parse_case(hf_ctx* ctx, const Json& cfg) {
                 }
             } else if (kind == "Internal") {
                 B.bc_type[s] = hf::BC_INTERNAL;
-                B.bc_block[s] = (int)bc["block"].number();
+                const double nb = bc["block"].number();   // a block index: checked below
+                B.bc_block[s] = (nb >= 0.0 && nb < (double)HF_MAXB && nb == (double)(int)nb) ? (int)nb : -1;
             } else {
                 return fail(ctx, HF_ERR_UNSUPPORTED, "boundary '" + kind + "' not recognised");
             }

@@ -140,9 +140,10 @@ def test_boundary_errors():
     st, msg = _create(json.dumps(c))
     assert st == 3 and "Periodic" in msg
     c = cases.quadrant_case(16)
-    c["mesh"]["blocks"][0]["boundaries"]["right"] = {"type": "Internal", "block": 3}
-    st, msg = _create(json.dumps(c))
-    assert st == 1 and "missing block" in msg
+    for blk in (3, -1, 0.5, 1e12):
+        c["mesh"]["blocks"][0]["boundaries"]["right"] = {"type": "Internal", "block": blk}
+        st, msg = _create(json.dumps(c))
+        assert st == 1 and "missing block" in msg, blk
     ffs = cases.forward_facing_step_case(cells_per_unit=20)
     blocks = ffs["mesh"]["blocks"]
     for b, blk in enumerate(blocks):
