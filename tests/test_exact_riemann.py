@@ -108,3 +108,95 @@ def test_gpu_toro1_error_equals_oracle_and_converges(scheme, port_lib):
         assert errs[1600] < 0.001
     else:
         assert errs[1600] < 0.0035
+
+
+def _tri_strip(nx, ny=4, length=1.0, height=0.05):
+    """Toro test 1's tube as triangles: an nx x ny grid of squares, each cut along a diagonal
+    (alternating), counter-clockwise; ends transmissive, sides reflective."""
+    from hyperflow_gb300 import meshgen
+    xs, ys = np.linspace(0.0, length, nx + 1), np.linspace(0.0, height, ny + 1)
+    verts, codes = [], []
+    for i in range(nx):
+        for j in range(ny):
+            p00, p10 = (xs[i], ys[j]), (xs[i + 1], ys[j])
+            p01, p11 = (xs[i], ys[j + 1]), (xs[i + 1], ys[j + 1])
+            tris = [(p00, p10, p11), (p00, p11, p01)] if (i + j) % 2 == 0 else [(p00, p10, p01), (p10, p11, p01)]
+            for t in tris:
+                verts.append(t)
+                cc = []
+                for k in range(3):
+                    a, b = t[k], t[(k + 1) % 3]
+                    if a[1] == b[1] and a[1] in (ys[0], ys[-1]):
+                        cc.append(meshgen.REFLECTIVE)
+                    elif a[0] == b[0] and a[0] in (xs[0], xs[-1]):
+                        cc.append(meshgen.TRANSMISSIVE)
+                    else:
+                        cc.append(0)
+                codes.append(cc)
+    return np.array(verts), np.array(codes)
+
+
+def _uns_toro_state(verts):
+    from oracle.oracle import prim_to_cons
+    cx = verts[:, :, 0].mean(axis=1)
+    left = prim_to_cons([WL[0], WL[1], 0.0, WL[2]])
+    right = prim_to_cons([WR[0], WR[1], 0.0, WR[2]])
+    return np.where(cx[None, :] <= X0, left[:, None], right[:, None]).astype(np.float64)
+
+
+def _uns_l1(U, verts, t):
+    """L1 density error over the strip, cell by cell against the exact solution at the
+    centroid x (area-weighted: every triangle of the strip has the same area)."""
+    from oracle.exact_riemann import sample
+    cx = verts[:, :, 0].mean(axis=1)
+    return float(np.mean(np.abs(U[0] - sample(WL, WR, (cx - X0) / t)[0])))
+
+
+def _uns_case():
+    from hyperflow_gb300 import meshgen
+    case = meshgen.channel_case("unused.hmsh", cfl=0.5)
+    case["simulation"]["t_end"] = 0.2
+    return case
+
+
+def _uns_oracle(nx):
+    """The oracle's Godunov run on the strip (ny = nx / 20, right-angled triangles of equal
+    area) up to the first step that ends at or past t = 0.2."""
+    from hyperflow_gb300 import meshgen
+    from oracle import oracle
+    verts, codes = _tri_strip(nx, ny=nx // 20)
+    nbr = meshgen.match_neighbours(list(verts), list(codes))
+    nv = np.full(len(verts), 3, np.int32)
+    ang, ln, area, rin = oracle.uns_geometry(nv, verts.reshape(-1))
+    ps = np.concatenate([[0], np.cumsum(nv)]).astype(np.int32)
+    U = _uns_toro_state(verts)
+    t, calls, steps = 0.0, 0, 0
+    while t < 0.2:
+        dts, calls = oracle.uns_run(1.4, 0.5, calls, ps, nbr, ang, ln, area, rin, np.zeros(4), U, 1)
+        t += dts[0]
+        steps += 1
+    return verts, codes, U, t, steps
+
+
+def test_uns_oracle_converges_to_the_exact_toro1_solution(port_lib):
+    """Toro test 1 through the unstructured Godunov scheme (rotations, edge normals, the
+    reflective sides and transmissive ends) on triangles: the L1 density error at the cell
+    centroids falls under refinement."""
+    e = {}
+    for nx in (80, 160, 320):
+        verts, _, U, t, _ = _uns_oracle(nx)
+        e[nx] = _uns_l1(U, verts, t)
+    assert e[80] < 0.03 and e[80] / e[160] > 1.4 and e[160] / e[320] > 1.4, e
+
+
+@pytest.mark.gpu
+def test_uns_gpu_toro1_equals_oracle(port_lib):
+    """The CUDA unstructured path (per-pair mode) on the same strip and steps: bit-exact to
+    the oracle, so its error against the exact solution is the oracle's."""
+    from hyperflow_gb300 import UnsSolver, meshgen
+    verts, codes, U, t, steps = _uns_oracle(160)
+    s = UnsSolver(_uns_case(), mesh_text=meshgen.hmshb_bytes(verts, codes))
+    s.set_state(_uns_toro_state(verts))
+    s.run(steps)
+    np.testing.assert_array_equal(s.state(), U)
+    assert s.time()[0] == t
