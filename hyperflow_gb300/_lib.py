@@ -67,6 +67,9 @@ SIGNATURES = {
     "hf_uns_last_error_message": (C.c_char_p, [_p]),
     "hf_uns_sizes": (_i, [_p, C.POINTER(_i64), C.POINTER(_i64)]),
     "hf_uns_mesh_arrays": (_i, [_p, _p, _p, _p, _p, _p, _p]),
+    "hf_uns_unmatched_pairs": (_i, [_p, C.POINTER(_i64), C.POINTER(_i64)]),
+    "hf_uns_mesh_neighbours": (_i, [C.c_char_p, _sz, C.POINTER(_i64), C.POINTER(_i64), _p, _i64,
+                                    C.POINTER(_i64), C.POINTER(_i64)]),
     "hf_uns_set_state": (_i, [_p, _p]),
     "hf_uns_get_state": (_i, [_p, _p]),
     "hf_uns_time_step": (_i, [_p, C.POINTER(_d)]),

@@ -20,8 +20,9 @@
 //     whose kernels overlap on the GPU (different streams, or different host threads
 //     without ordering) race on the array and give wrong results;
 //   * the first call on a device looks up the array's device address with
-//     cudaGetSymbolAddress (once per device, with that device current).  Make that first
-//     call before any stream capture that includes this entry point.
+//     cudaGetSymbolAddress (with that device current) and keeps it once the lookup succeeds;
+//     a lookup that fails returns HF_ERR_CUDA and is retried by the next call.  Make that
+//     first call before any stream capture that includes this entry point.
 #include <cstdint>
 #include <mutex>
 
@@ -40,9 +41,8 @@ constexpr long long kNoAllocMaxCells = (long long)kNoAllocMaxCtas * kNoAllocCell
 static __device__ __align__(256) double g_noalloc_scratch[2 * kNoAllocMaxCtas + 32];
 
 constexpr int kMaxDevices = 64;
-static void* g_scratch_addr[kMaxDevices];
-static std::once_flag g_scratch_once[kMaxDevices];
-static cudaError_t g_scratch_err[kMaxDevices];
+static void* g_scratch_addr[kMaxDevices];   // set once a lookup on that device has succeeded
+static std::mutex g_scratch_mutex;
 
 // TimeStep::operator() (src/fvm_2d_cart/scheme/timestep/timestep.cpp:29-68) over every cell
 // of one block, ghosts included.  Each CTA writes its two partial maxima; the last CTA to
@@ -116,12 +116,22 @@ extern "C" int hf_time_step_noalloc(const double* d_cons, int total_x, int total
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return HF_ERR_NO_DEVICE;
     if (dev < 0 || dev >= kMaxDevices) return HF_ERR_ARG;
-    // once per device, with that device current: the array's device address
-    std::call_once(g_scratch_once[dev], [dev] {
-        g_scratch_err[dev] = cudaGetSymbolAddress(&g_scratch_addr[dev], g_noalloc_scratch);
-    });
-    if (g_scratch_err[dev] != cudaSuccess || !g_scratch_addr[dev]) return HF_ERR_CUDA;
-    double* scratch = static_cast<double*>(g_scratch_addr[dev]);
+    // the array's device address, looked up with this device current and kept once the lookup
+    // has succeeded; a failed lookup (say, made inside a stream capture) is not kept, so a
+    // later call retries it
+    double* scratch;
+    {
+        std::lock_guard<std::mutex> lock(g_scratch_mutex);
+        if (!g_scratch_addr[dev]) {
+            void* addr = nullptr;
+            if (cudaGetSymbolAddress(&addr, g_noalloc_scratch) != cudaSuccess || !addr) {
+                (void)cudaGetLastError();   // clear the failed call's error state
+                return HF_ERR_CUDA;
+            }
+            g_scratch_addr[dev] = addr;
+        }
+        scratch = static_cast<double*>(g_scratch_addr[dev]);
+    }
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     if (cudaMemsetAsync(scratch + 2 * kNoAllocMaxCtas, 0, sizeof(unsigned int), s) != cudaSuccess)
         return HF_ERR_CUDA;

@@ -325,6 +325,8 @@ struct hf_uns {
     std::vector<double> verts;          // per cell vertex, x y
     std::vector<int> codes;             // per pair boundary code from the mesh file
     std::vector<int> pair_start, nbr;
+    long long unmatched = 0;            // pairs with a cell-index code (0: interior) and no match
+    long long first_unmatched = -1;     // the first of them, or -1
     std::vector<double> angle, length, area, rin;
     std::vector<double> init;           // initial SoA state
     hf::UnsMesh dm{};
@@ -363,6 +365,28 @@ void prim_to_cons(double gamma, const double* w, double* c) {
     c[1] = rho * uu;
     c[2] = rho * v;
     c[3] = p / (gamma - 1.0) + 0.5 * rho * (uu * uu + v * v);
+}
+
+// The boundary codes of the mesh file must be one per (cell, edge) pair, and each a boundary
+// type of src/fvm_2d_uns/scheme/boundary/boundary.h:12 (-1 reflective, -2 transmissive,
+// -3 inlet) or a cell index (0 marks an interior edge; an unmatched pair takes its code as its
+// neighbour, mesh_structured.cpp:96-109).  The reference reads past its vectors (or prints
+// "not supported" and continues with an empty state) otherwise; here such a mesh is refused
+// before any device work.
+int validate_codes(hf_uns* u, const std::vector<long>* raw = nullptr) {
+    int64_t np = 0;
+    for (int v : u->nverts) np += v;
+    const size_t nc = raw ? raw->size() : u->codes.size();
+    if ((int64_t)nc != np)
+        return ufail(u, HF_ERR_PARSE, "mesh: " + std::to_string(nc) + " boundary codes for " + std::to_string(np) +
+                                          " (cell, edge) pairs");
+    for (size_t q = 0; q < nc; ++q) {
+        const long k = raw ? (*raw)[q] : (long)u->codes[q];
+        if (k < -3 || k >= (long)u->ncells)
+            return ufail(u, HF_ERR_PARSE, "mesh: boundary code " + std::to_string(k) + " of pair " +
+                                              std::to_string(q) + " is neither -1, -2, -3 nor a cell index");
+    }
+    return HF_OK;
 }
 
 // the mesh text format of generate_block_mesh.py:217-246, cells of 3 or 4 vertices; parsed in
@@ -414,15 +438,19 @@ int parse_mesh(hf_uns* u, const std::string& text) {
     if ((long)u->nverts.size() != n) return ufail(u, HF_ERR_PARSE, "mesh: cell count mismatch");
     if (!edges || !next_line(b, e)) return ufail(u, HF_ERR_PARSE, "mesh: missing edge count");
     const long ne = std::strtol(b, nullptr, 0);
-    if (ne >= 0) u->codes.reserve(ne);
+    std::vector<long> raw;
+    if (ne >= 0 && ne <= 4 * n) raw.reserve(ne);
     while (next_line(b, e)) {
         const char* s = b;
         while (s < e && (*s == ' ' || *s == '\t' || *s == '\r')) ++s;
         if (s == e) continue;
-        u->codes.push_back((int)std::strtol(s, nullptr, 0));
+        raw.push_back(std::strtol(s, nullptr, 0));
     }
-    if ((long)u->codes.size() != ne) return ufail(u, HF_ERR_PARSE, "mesh: edge count mismatch");
+    if ((long)raw.size() != ne) return ufail(u, HF_ERR_PARSE, "mesh: edge count mismatch");
     u->ncells = (int)n;
+    const int r = validate_codes(u, &raw);
+    if (r != HF_OK) return r;
+    u->codes.assign(raw.begin(), raw.end());
     return HF_OK;
 }
 
@@ -465,14 +493,7 @@ int parse_mesh_binary(hf_uns* u, const std::string& data) {
     u->verts.resize(2 * (size_t)np);
     std::memcpy(u->verts.data(), data.data() + vo, 16 * (size_t)np);
     u->ncells = (int)n;
-    return HF_OK;
-}
-
-uint64_t bitsof(double x) {
-    if (x == 0.0) x = 0.0;   // -0.0 and +0.0 name the same point
-    uint64_t b;
-    std::memcpy(&b, &x, 8);
-    return b;
+    return validate_codes(u);
 }
 
 // 64-bit finaliser of MurmurHash3 (Appleby): every input bit affects every output bit
@@ -485,25 +506,56 @@ inline uint64_t fmix64(uint64_t x) {
     return x;
 }
 
-// Neighbour search of mesh_structured.cpp:92-114 (a pair's neighbour is the cell holding
-// the same edge reversed; unmatched pairs keep their boundary code), by hashing the
-// exact endpoint coordinates instead of the O(E^2) scan.  For meshes whose shared
-// vertices are written identically -- every mesh the generators produce -- this is the
-// same match the reference finds with its 1e-12 tolerance.  Pair p runs from vertex p to
-// vertex nxt[p] (the cells' vertices are stored pair by pair).  The table is open-addressed
-// over pair indices with a 32-bit fingerprint per slot; a directed edge that appears twice
-// keeps the later pair.
+// The tolerance of Edge::opposite_edges_equal: the Edge constructor's default _tol
+// (src/fvm_2d_uns/geometry/edge/edge.h:21), which the loader's cells use.
+constexpr double kEdgeTol = 1e-12;
+
+// Grid key of one coordinate for the neighbour search: floor(x * 2^30), i.e. grid cells of
+// 2^-30 (9.3e-10, far wider than the tolerance), for |x| < 2^32, where the product is exact and
+// the key fits in 62 bits.  Beyond 2^32 one ulp exceeds 1e-12, so two coordinates within the
+// tolerance are equal and the key is the bit pattern (tagged so it cannot meet a grid key).
+// -0.0 and +0.0 both give key 0.
+inline int64_t grid_key(double x) {
+    if (std::fabs(x) < 4294967296.0) return (int64_t)std::floor(x * 1073741824.0);
+    uint64_t b;
+    std::memcpy(&b, &x, 8);
+    return (int64_t)((b >> 2) | 0x8000000000000000ull) - 1;   // below every grid key
+}
+
+// Grid keys a coordinate within the tolerance of x can have: [lo, hi], one or two keys.
+// The margin of 4 tolerances covers the rounding of x -/+ 4e-12 and of the test's own
+// difference; the exact test below decides.
+inline void grid_range(double x, int64_t& lo, int64_t& hi) {
+    if (std::fabs(x) < 4294967296.0) {
+        lo = grid_key(x - 4 * kEdgeTol);
+        hi = grid_key(x + 4 * kEdgeTol);
+        if (lo > hi || hi - lo > 2) lo = hi = grid_key(x);   // cannot happen below 2^32
+    } else {
+        lo = hi = grid_key(x);
+    }
+}
+
+// Neighbour search of LoadStructuredMesh (mesh_structured.cpp:92-114): for pair q (the edge
+// from vertex A to vertex B of its cell) every pair r of the mesh is tested with
+// Edge::opposite_edges_equal (edge.cpp:59-71) -- |start_r - B| < 1e-12 and |end_r - A| < 1e-12,
+// coordinate by coordinate, as fabs of the difference -- and the last matching r in the scan
+// order (cell by cell, edge by edge: the pair index) gives the neighbour cell; a pair with no
+// match keeps its code from the mesh file (a boundary type, or a cell index -- 0 for an interior
+// edge, so an unmatched interior pair reads cell 0 exactly as in the reference; such pairs are
+// counted and reported).  Instead of the O(E^2) scan, pairs are bucketed by the grid keys of
+// their start vertex, and a query visits only the buckets a start within the tolerance of B can
+// fall in (one, or two near a grid line per axis); every candidate there is tested with the
+// reference's own comparison, so the result is the reference's, including the last-match rule,
+// self-matches of degenerate edges and coordinates that differ in their last bits between two
+// cells.  Non-finite coordinates never compare as within the tolerance and are not bucketed.
+// Pair p runs from vertex p to vertex nxt[p] (the cells' vertices are stored pair by pair).
 void build_pairs(hf_uns* u) {
     const int n = u->ncells;
     u->pair_start.assign(n + 1, 0);
     for (int c = 0; c < n; ++c) u->pair_start[c + 1] = u->pair_start[c] + u->nverts[c];
     const size_t np = (size_t)u->pair_start[n];
-    std::vector<uint64_t> bx(np), by(np);
+    const double* V = u->verts.data();
     std::vector<int> nxt(np), cell(np);
-    for (size_t q = 0; q < np; ++q) {
-        bx[q] = bitsof(u->verts[2 * q]);
-        by[q] = bitsof(u->verts[2 * q + 1]);
-    }
     for (int c = 0; c < n; ++c) {
         const int s = u->pair_start[c], e = u->pair_start[c + 1];
         for (int q = s; q < e; ++q) {
@@ -511,40 +563,73 @@ void build_pairs(hf_uns* u) {
             cell[q] = c;
         }
     }
+    // buckets: open-addressed over distinct (kx, ky) start keys; each holds the head of a chain
+    // through chain[] in decreasing pair order (pairs are inserted in increasing order)
     size_t cap = 16;
     while (cap < 2 * np) cap <<= 1;
     const size_t mask = cap - 1;
-    std::vector<uint64_t> slot(cap, 0);   // (fingerprint << 32) | (pair + 1); 0 is empty
-    // the directed edge from vertex a to vertex b
-    auto hash = [&](size_t a, size_t b) { return fmix64(bx[a] ^ fmix64(by[a] ^ fmix64(bx[b] ^ fmix64(by[b])))); };
-    auto same = [&](size_t q, size_t a, size_t b) {
-        return bx[q] == bx[a] && by[q] == by[a] && bx[nxt[q]] == bx[b] && by[nxt[q]] == by[b];
+    std::vector<int64_t> kxs(cap), kys(cap);
+    std::vector<int> head(cap, -1), chain(np, -1);
+    auto bucket_hash = [](int64_t kx, int64_t ky) {
+        return fmix64((uint64_t)kx ^ fmix64((uint64_t)ky + 0x9E3779B97F4A7C15ull));
     };
-    for (size_t q = 0; q < np; ++q) {
-        const uint64_t h = hash(q, nxt[q]), fp = h >> 32, entry = (fp << 32) | (uint64_t)(q + 1);
-        for (size_t i = h & mask;; i = (i + 1) & mask) {
-            const uint64_t sv = slot[i];
-            if (sv == 0 || ((sv >> 32) == fp && same((size_t)(sv & 0xFFFFFFFFull) - 1, q, nxt[q]))) {
-                slot[i] = entry;
+    for (size_t r = 0; r < np; ++r) {
+        const double x = V[2 * r], y = V[2 * r + 1];
+        if (!std::isfinite(x) || !std::isfinite(y)) continue;
+        const int64_t kx = grid_key(x), ky = grid_key(y);
+        for (size_t i = bucket_hash(kx, ky) & mask;; i = (i + 1) & mask) {
+            if (head[i] < 0) {
+                kxs[i] = kx;
+                kys[i] = ky;
+                head[i] = (int)r;
+                break;
+            }
+            if (kxs[i] == kx && kys[i] == ky) {
+                chain[r] = head[i];
+                head[i] = (int)r;
                 break;
             }
         }
     }
+    auto find_bucket = [&](int64_t kx, int64_t ky) {
+        for (size_t i = bucket_hash(kx, ky) & mask;; i = (i + 1) & mask) {
+            if (head[i] < 0) return -1;
+            if (kxs[i] == kx && kys[i] == ky) return head[i];
+        }
+    };
     u->nbr.resize(np);
+    u->unmatched = 0;
+    u->first_unmatched = -1;
     for (size_t q = 0; q < np; ++q) {
-        const size_t a = nxt[q], b = q;   // the same edge reversed
-        const uint64_t h = hash(a, b), fp = h >> 32;
-        int found = -1;
-        for (size_t i = h & mask;; i = (i + 1) & mask) {
-            const uint64_t sv = slot[i];
-            if (sv == 0) break;
-            const size_t r = (size_t)(sv & 0xFFFFFFFFull) - 1;
-            if ((sv >> 32) == fp && same(r, a, b)) {
-                found = cell[r];
-                break;
+        const double ax = V[2 * q], ay = V[2 * q + 1];              // this edge's start
+        const double bx = V[2 * nxt[q]], by = V[2 * nxt[q] + 1];    // and end
+        long long best = -1;
+        if (std::isfinite(bx) && std::isfinite(by)) {
+            int64_t xlo, xhi, ylo, yhi;
+            grid_range(bx, xlo, xhi);
+            grid_range(by, ylo, yhi);
+            for (int64_t kx = xlo; kx <= xhi; ++kx)
+                for (int64_t ky = ylo; ky <= yhi; ++ky)
+                    for (int r = find_bucket(kx, ky); r > best; r = chain[r]) {
+                        // rhs = pair r, this = pair q, as in edge.cpp:65-68
+                        const double rsx = V[2 * (size_t)r], rsy = V[2 * (size_t)r + 1];
+                        const double rex = V[2 * (size_t)nxt[r]], rey = V[2 * (size_t)nxt[r] + 1];
+                        if ((std::fabs(rsx - bx) < kEdgeTol) && (std::fabs(rsy - by) < kEdgeTol) &&
+                            (std::fabs(rex - ax) < kEdgeTol) && (std::fabs(rey - ay) < kEdgeTol)) {
+                            best = r;   // the chain runs in decreasing order: the bucket's last match
+                            break;
+                        }
+                    }
+        }
+        if (best >= 0) {
+            u->nbr[q] = cell[best];
+        } else {
+            u->nbr[q] = u->codes[q];
+            if (u->codes[q] >= 0) {
+                if (u->unmatched == 0) u->first_unmatched = (long long)q;
+                ++u->unmatched;
             }
         }
-        u->nbr[q] = found >= 0 ? found : u->codes[q];
     }
 }
 
@@ -815,6 +900,37 @@ int hf_uns_sizes(const hf_uns* u, int64_t* ncells, int64_t* npairs) {
     if (!u) return HF_ERR_ARG;
     if (ncells) *ncells = u->ncells;
     if (npairs) *npairs = u->pair_start.empty() ? 0 : u->pair_start.back();
+    return HF_OK;
+}
+
+int hf_uns_unmatched_pairs(const hf_uns* u, int64_t* count, int64_t* first_pair) {
+    if (!u) return HF_ERR_ARG;
+    if (count) *count = u->unmatched;
+    if (first_pair) *first_pair = u->first_unmatched;
+    return HF_OK;
+}
+
+int hf_uns_mesh_neighbours(const char* mesh, size_t mesh_len, int64_t* ncells, int64_t* npairs,
+                           int32_t* nbr, int64_t max_pairs, int64_t* unmatched, int64_t* first_unmatched) {
+    if (!mesh) return HF_ERR_ARG;
+    hf_uns u;
+    try {
+        const std::string text(mesh, mesh_len);
+        const int r = is_binary_mesh(text) ? parse_mesh_binary(&u, text) : parse_mesh(&u, text);
+        if (r != HF_OK) return r;
+        build_pairs(&u);
+    } catch (const std::exception&) {
+        return HF_ERR_PARSE;
+    }
+    const int64_t np = u.pair_start.back();
+    if (ncells) *ncells = u.ncells;
+    if (npairs) *npairs = np;
+    if (unmatched) *unmatched = u.unmatched;
+    if (first_unmatched) *first_unmatched = u.first_unmatched;
+    if (nbr) {
+        if (max_pairs < np) return HF_ERR_ARG;
+        std::memcpy(nbr, u.nbr.data(), (size_t)np * sizeof(int32_t));
+    }
     return HF_OK;
 }
 

@@ -205,29 +205,6 @@ def read_hmsh(text: str):
     return verts, codes
 
 
-def match_neighbours(verts, codes):
-    """Neighbour of every (cell, edge) pair: the cell holding the same edge in the
-    opposite direction, else the edge's boundary code -- the result of the reference
-    loader's search (mesh_structured.cpp:92-114), found by hashing exact coordinates."""
-    ncell = len(verts)
-    nv = np.array([len(c) for c in verts])
-    starts = np.concatenate([[0], np.cumsum(nv)])
-    table = {}
-    for c in range(ncell):
-        V = verts[c]
-        for k in range(nv[c]):
-            a, b = V[k], V[(k + 1) % nv[c]]
-            table[(float(a[0]), float(a[1]), float(b[0]), float(b[1]))] = c
-    nbr = np.empty(starts[-1], dtype=np.int32)
-    for c in range(ncell):
-        V = verts[c]
-        for k in range(nv[c]):
-            a, b = V[k], V[(k + 1) % nv[c]]
-            m = table.get((float(b[0]), float(b[1]), float(a[0]), float(a[1])))
-            nbr[starts[c] + k] = m if m is not None else codes[c][k]
-    return nbr
-
-
 def channel_case(mesh_file: str, cfl: float = 0.5, inflow=(1.4, 2.0, 0.0, 1.0),
                  t_end: float = 1.0e9) -> dict:
     """Case file of the reference's unstructured solver (parser keys of

@@ -9,12 +9,30 @@ from __future__ import annotations
 
 import ctypes as C
 import json
+import warnings
 
 import numpy as np
 
 from ._lib import check, lib
 
 _MSG = "hf_uns_last_error_message"
+
+
+class MeshWarning(UserWarning):
+    """A mesh loaded with interior pairs that have no partner edge."""
+
+
+def mesh_neighbours(mesh: str | bytes):
+    """The loader's neighbour search alone, on the host (no GPU): (nbr per pair, unmatched
+    count, first unmatched pair or -1) for a mesh in the text or binary format."""
+    raw = mesh if isinstance(mesh, bytes) else mesh.encode()
+    L = lib()
+    nc, npair, un, first = C.c_int64(), C.c_int64(), C.c_int64(), C.c_int64()
+    check(L.hf_uns_mesh_neighbours(raw, len(raw), C.byref(nc), C.byref(npair), None, 0, None, None))
+    nbr = np.empty(npair.value, np.int32)
+    check(L.hf_uns_mesh_neighbours(raw, len(raw), C.byref(nc), C.byref(npair), nbr.ctypes.data, nbr.size,
+                                   C.byref(un), C.byref(first)))
+    return nbr, un.value, first.value
 
 
 class UnsSolver:
@@ -43,6 +61,11 @@ class UnsSolver:
         nc, npair = C.c_int64(), C.c_int64()
         check(L.hf_uns_sizes(self._h, C.byref(nc), C.byref(npair)), self._h, _MSG)
         self.ncells, self.npairs = nc.value, npair.value
+        n_unmatched, first = self.unmatched_pairs()
+        if n_unmatched:
+            warnings.warn(f"mesh: {n_unmatched} interior (cell-coded) pairs match no edge within 1e-12 and "
+                          f"take their code as the neighbour cell, as the reference does (first: pair {first})",
+                          MeshWarning, stacklevel=2)
 
     def close(self):
         if getattr(self, "_h", None):
@@ -54,6 +77,14 @@ class UnsSolver:
             self.close()
         except Exception:
             pass
+
+    def unmatched_pairs(self):
+        """(count, first pair index or -1) of the pairs whose code names a cell (0: an interior
+        edge) but that found no partner; they take the code as their neighbour, as in the
+        reference's loader."""
+        n, first = C.c_int64(), C.c_int64()
+        check(lib().hf_uns_unmatched_pairs(self._h, C.byref(n), C.byref(first)), self._h, _MSG)
+        return n.value, first.value
 
     def mesh_arrays(self):
         ps = np.empty(self.ncells + 1, np.int32)

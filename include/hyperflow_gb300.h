@@ -197,8 +197,9 @@ int hf_checkpoint_load(hf_ctx* ctx, const void* buf, size_t bytes);
  * d_dt on `stream` (a cudaStream_t; 0 = default stream).  It allocates nothing: its only
  * working memory is a 64 KiB static device array, so it handles at most 16,777,216 cells
  * (larger blocks return HF_ERR_TOO_LARGE).  Calls that overlap on the GPU share that array
- * and race.  The first call on each device looks up the array's address; make it before
- * any stream capture. */
+ * and race.  The first call on each device looks up the array's address (kept once found;
+ * a failed lookup returns HF_ERR_CUDA and the next call retries it); make it before any
+ * stream capture. */
 int hf_time_step_noalloc(const double* d_cons, int total_x, int total_y, int pitch, double dx,
                          double dy, double gamma, double cfl, int64_t call_index, double* d_dt,
                          void* stream);

@@ -26,7 +26,12 @@ typedef struct hf_uns hf_uns;
  * model, mesh.{type,file,boundaries.inlet}, initial_condition, scheme, simulation) and loads
  * mesh.file.  Replaces JSONParser::generate_mesh + LoadStructuredMesh
  * (src/fvm_2d_uns/mesh/mesh_structured/mesh_structured.cpp:23-122): same text format, cells
- * of 3 or 4 vertices, neighbours found by hashing edge endpoints instead of the O(E^2) scan.
+ * of 3 or 4 vertices, and the same neighbours -- a pair's neighbour is the cell of the last
+ * pair (in cell, edge order) whose edge equals it reversed within 1e-12 per coordinate
+ * (Edge::opposite_edges_equal, src/fvm_2d_uns/geometry/edge/edge.cpp:59-71), else the pair's
+ * code -- found through a grid hash of the edge start points in O(E) instead of the O(E^2) scan.
+ * A mesh whose code count differs from its (cell, edge) pair count, or with a code that is
+ * neither -1, -2, -3 nor a cell index, is refused with HF_ERR_PARSE before any device work.
  * mesh.file may instead hold the binary format, recognised by its first 8 bytes "HFMESHB1":
  * int64 cell count, int64 pair count (the vertex counts summed), int32 vertices per cell,
  * int32 boundary code per (cell, edge) pair, zero padding to a multiple of 8 bytes, then
@@ -48,6 +53,24 @@ int hf_uns_sizes(const hf_uns* u, int64_t* ncells, int64_t* npairs);
  * Polygon signed area and incircle radius, polygon.cpp:72-186).  Null outputs are skipped. */
 int hf_uns_mesh_arrays(const hf_uns* u, int32_t* pair_start, int32_t* nbr, double* angle,
                        double* length, double* area, double* rin);
+
+/* Pairs whose code names a cell (0 for an interior edge) but that match no pair of the mesh.
+ * The reference then takes the code itself as the neighbour -- an interior edge reads cell 0 --
+ * without a message (mesh_structured.cpp:96-109); this library does the same for parity and
+ * counts them here: the count and the first such pair index (-1 when none).  No counterpart in
+ * the reference. */
+int hf_uns_unmatched_pairs(const hf_uns* u, int64_t* count, int64_t* first_pair);
+
+/* The mesh loader alone, on the host: parses a mesh (text or binary format), validates its
+ * codes and runs the neighbour search of hf_uns_create, with no device work and no case file --
+ * for tools that inspect meshes and for checking the search on machines without a GPU.  Gives
+ * the cell and pair counts, the neighbour of every pair (as hf_uns_mesh_arrays; skipped when
+ * nbr is null, HF_ERR_ARG when max_pairs is below the pair count) and the unmatched-pair
+ * diagnostics of hf_uns_unmatched_pairs.  Replaces LoadStructuredMesh::load_structured_mesh
+ * (mesh_structured.cpp:23-122) up to its cell_edge_indices. */
+int hf_uns_mesh_neighbours(const char* mesh, size_t mesh_len, int64_t* ncells, int64_t* npairs,
+                           int32_t* nbr, int64_t max_pairs, int64_t* unmatched,
+                           int64_t* first_unmatched);
 
 /* cell centroids [2][ncells] as Polygon::calculate_centroid computes them
  * (src/fvm_2d_uns/geometry/polygon/polygon.cpp:188-212); host-side, no device work */

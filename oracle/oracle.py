@@ -404,6 +404,10 @@ def ref_uns_lib():
         lib.hfref_uns_solve.restype = i
         lib.hfref_uns_solve.argtypes = [p, C.c_char_p]
         lib.hfref_uns_centroids.argtypes = [p, p]
+        lib.hfref_uns_create_file.restype = p
+        lib.hfref_uns_create_file.argtypes = [C.c_char_p]
+        lib.hfref_uns_cell_edge_indices.restype = C.c_long
+        lib.hfref_uns_cell_edge_indices.argtypes = [p, p, C.c_long]
         _refu = lib
     return _refu
 
@@ -422,6 +426,46 @@ class RefUns:
                                                       _ptr(self.nverts), _ptr(self.verts),
                                                       _ptr(self.nbr)))
         self.nsteps = 0
+
+    @classmethod
+    def from_file(cls, case: dict, quiet: bool = True):
+        """The reference's own loader (JSONParser::generate_mesh -> LoadStructuredMesh, an O(E^2)
+        scan over quadrilaterals) on the case's mesh.file.  quiet: its per-cell progress lines,
+        printed to stdout, are dropped."""
+        self = cls.__new__(cls)
+        self.lib = ref_uns_lib()
+        raw = json.dumps(case).encode()
+        if quiet:
+            import sys
+            sys.stdout.flush()
+            saved = os.dup(1)
+            devnull = os.open(os.devnull, os.O_WRONLY)
+            os.dup2(devnull, 1)
+            try:
+                h = self.lib.hfref_uns_create_file(raw)
+            finally:
+                os.dup2(saved, 1)
+                os.close(saved)
+                os.close(devnull)
+        else:
+            h = self.lib.hfref_uns_create_file(raw)
+        if not h:
+            raise ValueError("the reference loader refused the mesh")
+        self.h = C.c_void_p(h)
+        cei = self.cell_edge_indices()
+        self.npairs = len(cei)
+        self.ncells = int(cei[:, 0].max()) + 1 if self.npairs else 0
+        self.nverts = np.bincount(cei[:, 0], minlength=self.ncells).astype(np.int32)
+        self.nbr = np.ascontiguousarray(cei[:, 1])
+        self.nsteps = 0
+        return self
+
+    def cell_edge_indices(self) -> np.ndarray:
+        """The mesh's cell_edge_indices, [npairs][3] = (cell, neighbour or code, edge index)."""
+        n = self.lib.hfref_uns_cell_edge_indices(self.h, None, 0)
+        out = np.zeros((n, 3), np.int32)
+        self.lib.hfref_uns_cell_edge_indices(self.h, _ptr(out), n)
+        return out
 
     def __del__(self):
         try:
@@ -464,6 +508,51 @@ class RefUns:
         rin = np.zeros(self.ncells)
         self.lib.hfref_uns_geometry(self.h, _ptr(ang), _ptr(ln), _ptr(area), _ptr(rin))
         return ang, ln, area, rin
+
+
+EDGE_TOL = 1e-12   # Edge's default tolerance, src/fvm_2d_uns/geometry/edge/edge.h:21
+
+
+def ref_neighbours(verts, codes, tol: float = EDGE_TOL):
+    """The neighbour of every (cell, edge) pair by the reference loader's rule
+    (src/fvm_2d_uns/mesh/mesh_structured/mesh_structured.cpp:92-114): pair q (edge A -> B of its
+    cell) takes the cell of the LAST pair r, in pair order, for which
+    Edge::opposite_edges_equal holds (src/fvm_2d_uns/geometry/edge/edge.cpp:59-71):
+    fabs(start_r - B) < tol and fabs(end_r - A) < tol in x and in y; with no such r it keeps its
+    code.  Candidates come from a k-d tree over the start points (a radius of 4 tol in the max
+    norm), every one is decided by the reference's own comparison.  verts: per cell a sequence
+    of (x, y) vertices; codes: per cell its codes.  Returns (nbr int32 per pair, unmatched pairs
+    whose code is a cell index)."""
+    from scipy.spatial import cKDTree
+    S = np.array([p for cell in verts for p in cell], dtype=np.float64).reshape(-1, 2)
+    nv = np.array([len(cell) for cell in verts])
+    starts = np.concatenate([[0], np.cumsum(nv)])
+    nxt = np.arange(len(S)) + 1
+    nxt[starts[1:] - 1] = starts[:-1]
+    cell = np.repeat(np.arange(len(verts)), nv)
+    E = S[nxt]
+    flat = np.array([k for cc in codes for k in cc], dtype=np.int64)
+    finite = np.isfinite(S).all(axis=1)
+    idx = np.nonzero(finite)[0]
+    tree = cKDTree(S[idx])
+    nbr = np.empty(len(S), np.int32)
+    unmatched = 0
+    qok = np.isfinite(E).all(axis=1)
+    cands = tree.query_ball_point(np.where(qok[:, None], E, 0.0), r=4 * tol, p=np.inf)
+    for q in range(len(S)):
+        best = -1
+        if qok[q]:
+            for r in sorted((int(idx[j]) for j in cands[q]), reverse=True):
+                if (abs(S[r, 0] - E[q, 0]) < tol and abs(S[r, 1] - E[q, 1]) < tol and
+                        abs(E[r, 0] - S[q, 0]) < tol and abs(E[r, 1] - S[q, 1]) < tol):
+                    best = r
+                    break
+        if best >= 0:
+            nbr[q] = cell[best]
+        else:
+            nbr[q] = flat[q]
+            unmatched += int(flat[q] >= 0)
+    return nbr, unmatched
 
 
 def uns_geometry(nverts: np.ndarray, verts: np.ndarray):

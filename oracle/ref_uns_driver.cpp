@@ -3,7 +3,9 @@
 //
 // The reference loads meshes only through LoadStructuredMesh
 // (src/fvm_2d_uns/mesh/mesh_structured/mesh_structured.cpp:23-122), which reads
-// quadrilaterals and matches neighbours in O(E^2).  This driver instead builds
+// quadrilaterals and matches neighbours in O(E^2); hfref_uns_create_file runs exactly that
+// on a mesh file, for quadrilateral meshes small enough for its scan.  For triangle meshes,
+// which that loader cannot read, hfref_uns_create builds
 // Mesh(edges, cells, cell_edge_indices) directly (src/fvm_2d_uns/mesh/mesh/mesh.cpp:17-24)
 // with the same cell_edge_indices layout as mesh_structured.cpp:93-115:
 //   one entry per (cell, own edge) in cell order, [cell, neighbour-or-bc, pair index],
@@ -45,9 +47,49 @@ struct RefUns {
     std::vector<double> dts;
 };
 
+// the objects JSONParser makes after the mesh, as Simulation's caller does (main.cpp)
+void finish_setup(RefUns* r) {
+    r->initcon = r->parser->generate_initial_condition();
+    r->riemann = r->parser->generate_riemann_solver();
+    std::shared_ptr<TimeStep> unused = r->parser->generate_time_step();
+    r->scheme = r->parser->generate_spatial_scheme(r->model, r->riemann, unused, r->mesh);
+    r->ode = r->parser->generate_ode_solver();
+    r->mesh->initialise_field_values(r->initcon);
+    r->time_step.reset(new TimeStep(r->model, r->parser->get_cfl()));
+}
+
 }  // namespace
 
 extern "C" {
+
+// The reference's own loader end to end: JSONParser::generate_mesh (parser.cpp:141-158) with
+// LoadStructuredMesh on the case's mesh.file (mesh_structured.cpp:23-122: quadrilaterals, the
+// O(E^2) neighbour search with Edge::opposite_edges_equal), then the solver objects.
+void* hfref_uns_create_file(const char* case_json) {
+    RefUns* r = new RefUns();
+    r->config = json::parse(case_json);
+    r->parser.reset(new JSONParser(r->config));
+    r->t = r->parser->get_t_start();
+    r->model = r->parser->generate_model();
+    r->mesh = r->parser->generate_mesh();
+    if (!r->mesh) {
+        delete r;
+        return nullptr;
+    }
+    finish_setup(r);
+    return r;
+}
+
+// the mesh's cell_edge_indices (mesh.h:43), [npairs][3] = (cell, neighbour or code, edge index);
+// returns the pair count (the rows written only when it is at most cap)
+long hfref_uns_cell_edge_indices(void* h, int* out, long cap) {
+    auto& cei = static_cast<RefUns*>(h)->mesh->get_cell_edge_indices();
+    const long n = (long)cei.size();
+    if (out && n <= cap)
+        for (long k = 0; k < n; ++k)
+            for (int j = 0; j < 3; ++j) out[3 * k + j] = cei[k][j];
+    return n;
+}
 
 void* hfref_uns_create(const char* case_json, int ncells, const int* nverts,
                        const double* verts, const int* pair_nbr) {
@@ -82,13 +124,7 @@ void* hfref_uns_create(const char* case_json, int ncells, const int* nverts,
         }
     }
     r->mesh = std::make_shared<Mesh>(edges, cells, cei);
-    r->initcon = r->parser->generate_initial_condition();
-    r->riemann = r->parser->generate_riemann_solver();
-    std::shared_ptr<TimeStep> unused = r->parser->generate_time_step();
-    r->scheme = r->parser->generate_spatial_scheme(r->model, r->riemann, unused, r->mesh);
-    r->ode = r->parser->generate_ode_solver();
-    r->mesh->initialise_field_values(r->initcon);
-    r->time_step.reset(new TimeStep(r->model, r->parser->get_cfl()));
+    finish_setup(r);
     return r;
 }
 

@@ -28,9 +28,9 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 
 from hyperflow_gb300 import cases  # noqa: E402
-from oracle import oracle  # noqa: E402
+from oracle import oracle, reference_root  # noqa: E402
 
-REF_CASES = "/root/reference/cases/fvm_2d_cart"
+REF_CASES = os.path.join(reference_root(), "cases", "fvm_2d_cart")
 
 # (ne, nw, sw, se) primitive states of two rarefactions moving apart at speed 2 / 3
 VACUUM2 = ([1.0, 2.0, 0.0, 0.4], [1.0, -2.0, 0.0, 0.4], [1.0, -2.0, 0.0, 0.4], [1.0, 2.0, 0.0, 0.4])
@@ -58,6 +58,9 @@ def cart_cases():
             30, ny=26, scheme="MUSCLHancock", limiter="VanLeer", states=VACUUM3), 20, False, True),
         # the 256x256 Godunov workload at full length
         ("godunov_quad_256_200", cases.quadrant_case(256), 200, False, False),
+        # the forward-facing step to its end time t = 4 (about 800 steps) at dx = 1/40
+        ("ffs_minbee_dx1_40_t4", cases.forward_facing_step_case(40, limiter="MinBee"), 10**6, True, True),
+        ("ffs_vanleer_dx1_40_t4", cases.forward_facing_step_case(40, limiter="VanLeer"), 10**6, True, True),
     ]
     for rel, steps in [("shock_tubes/toro/toro_shock_tube_01_godunov_hllc_100x5.json", 400),
                        ("shock_tubes/toro/toro_shock_tube_01_muscl_hancock_vanleer_hllc_100x5.json", 400),
@@ -75,8 +78,10 @@ def sample_idx(shape, n=2000, seed=7):
     return np.stack([rng.integers(0, s, n) for s in shape[1:]], axis=0)
 
 
-def make_cart():
+def make_cart(only=None):
     for name, case, steps, clamp, full in cart_cases():
+        if only and name not in only:
+            continue
         ref = oracle.RefCart(case)
         taken = ref.run(steps, clamp)
         blocks = [ref.state(b) for b in range(ref.nblocks())]
@@ -132,7 +137,7 @@ def make_uns_frames():
     sets = [("quad_channel_240", *quad_channel(), 0.05, 20.0),
             ("tri_hole_3k", *meshgen.jittered_hole_mesh(3000, seed=3), 0.02, 10.0)]
     for name, verts, codes, t_end, fps in sets:
-        nbr = meshgen.match_neighbours(verts, codes)
+        nbr = oracle.ref_neighbours(verts, codes)[0]
         case = meshgen.channel_case("mesh.hmsh", cfl=0.5, t_end=t_end)
         case["simulation"]["animation"] = {"duration": 1.0, "fps": fps}
         nverts = np.full(len(verts), verts.shape[1], np.int32)
@@ -213,15 +218,70 @@ def quad_channel(nx=24, ny=10, seed=4):
     return np.array(verts, dtype=np.float64), np.array(codes, dtype=np.int32)
 
 
-def make_uns():
+def _ref_uns(case, verts, codes, tmpdir):
+    """The reference's unstructured solver on this mesh, and the neighbours it used.  Quad
+    meshes go through the reference's own loader (the mesh written to a file, read by
+    LoadStructuredMesh with its O(E^2) tolerance search); triangle meshes, which that loader
+    cannot read, take the oracle's restatement of the same search (pinned against the loader on
+    the quad meshes)."""
     from hyperflow_gb300 import meshgen
-    sets = [("tri_hole_3k", *meshgen.jittered_hole_mesh(3000, seed=3), 40, 0.5),
-            ("quad_channel_240", *quad_channel(), 60, 0.5)]
-    for name, verts, codes, steps, cfl in sets:
-        nbr = meshgen.match_neighbours(verts, codes)
-        case = meshgen.channel_case("mesh.hmsh", cfl=cfl)
-        nverts = np.full(len(verts), verts.shape[1], np.int32)
-        ref = oracle.RefUns(case, nverts, verts.reshape(-1, 2), nbr)
+    if verts.shape[1] == 4:
+        path = os.path.join(tmpdir, "mesh.hmsh")
+        with open(path, "w") as f:
+            f.write(meshgen.hmsh_text(verts, codes))
+        fcase = json.loads(json.dumps(case))
+        fcase["mesh"]["file"] = path
+        fcase["mesh"]["type"] = "hyperflow_structured"   # the one type parser.cpp:146 reads
+        ref = oracle.RefUns.from_file(fcase)
+        return ref, ref.nbr.copy()
+    nbr = oracle.ref_neighbours(verts, codes)[0]
+    nverts = np.full(len(verts), verts.shape[1], np.int32)
+    return oracle.RefUns(case, nverts, verts.reshape(-1, 2), nbr), nbr
+
+
+def scramjet(reduction: int):
+    """The reference's own scramjet case (cases/fvm_2d_uns/scramjet_kumar): its block spec
+    (scramjet_kumar_coarse_mesh.json, 17 blocks, 22,960 quads) with every block's cell counts
+    divided by `reduction` (at least one cell), meshed by the reference's own
+    src/mesh_generation/generate_block_mesh.py, and its case file
+    (scramjet_kumar_godunov_hllc.json: Godunov + HLLC, CFL 0.5, Mach 5 inlet).  Blocks of that
+    generator meet with vertex coordinates that differ in their last bits, so its neighbour
+    search needs the reference loader's 1e-12 tolerance.  Returns (verts, codes, case)."""
+    import importlib.util
+    import tempfile
+    from hyperflow_gb300 import meshgen
+    ref = reference_root()
+    spec = importlib.util.spec_from_file_location(
+        "ref_generate_block_mesh", os.path.join(ref, "src", "mesh_generation", "generate_block_mesh.py"))
+    gen = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(gen)
+    sdir = os.path.join(ref, "cases", "fvm_2d_uns", "scramjet_kumar")
+    with open(os.path.join(sdir, "scramjet_kumar_coarse_mesh.json")) as f:
+        blocks = json.load(f)
+    for b in blocks:
+        b["cells"] = [max(1, b["cells"][0] // reduction), max(1, b["cells"][1] // reduction)]
+    with tempfile.TemporaryDirectory() as d:
+        sp, mp = os.path.join(d, "blocks.json"), os.path.join(d, "mesh.hmsh")
+        with open(sp, "w") as f:
+            json.dump(blocks, f)
+        gen.BlockStructuredMeshGenerator(sp).generate_mesh(mp)
+        with open(mp) as f:
+            verts, codes = meshgen.read_hmsh(f.read())
+    with open(os.path.join(sdir, "scramjet_kumar_godunov_hllc.json")) as f:
+        case = json.load(f)
+    case["mesh"]["file"] = "mesh.hmsh"
+    return np.array(verts, dtype=np.float64), np.array(codes, dtype=np.int32), case
+
+
+def make_uns():
+    import tempfile
+    from hyperflow_gb300 import meshgen
+    sets = [("tri_hole_3k", *meshgen.jittered_hole_mesh(3000, seed=3), meshgen.channel_case("mesh.hmsh", cfl=0.5), 40),
+            ("quad_channel_240", *quad_channel(), meshgen.channel_case("mesh.hmsh", cfl=0.5), 60),
+            ("scramjet_reduced4", *scramjet(4), 300)]
+    for name, verts, codes, case, steps in sets:
+        with tempfile.TemporaryDirectory() as d:
+            ref, nbr = _ref_uns(case, verts, codes, d)
         ang, ln, area, rin = ref.geometry()
         ref.run(steps)
         np.savez_compressed(os.path.join(HERE, f"uns_{name}.npz"), case=json.dumps(case),
@@ -230,16 +290,33 @@ def make_uns():
         print("uns", name, len(verts), "cells", steps, "steps")
 
 
+def make_loader():
+    """The reference loader's neighbours on the full scramjet coarse mesh (22,960 quads,
+    91,840 pairs; its O(E^2) scan takes about ten minutes)."""
+    import tempfile
+    verts, codes, case = scramjet(1)
+    with tempfile.TemporaryDirectory() as d:
+        ref, nbr = _ref_uns(case, verts, codes, d)
+    np.savez_compressed(os.path.join(HERE, "loader_scramjet_coarse.npz"), verts=verts,
+                        codes=codes.astype(np.int8), nbr=nbr)
+    print("loader scramjet coarse", len(verts), "cells", len(nbr), "pairs")
+
+
 if __name__ == "__main__":
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref"], check=True)
-    which = sys.argv[1:] or ["units", "cart", "uns", "frames", "unsframes"]
+    which = sys.argv[1:] or ["units", "cart", "uns", "frames", "unsframes", "loader"]
     if "units" in which:
         make_units()
     if "cart" in which:
         make_cart()
+    for w in which:
+        if w.startswith("cart:"):      # cart:<fixture name>[,<name>...]
+            make_cart(w[5:].split(","))
     if "uns" in which:
         make_uns()
     if "frames" in which:
         make_frames()
     if "unsframes" in which:
         make_uns_frames()
+    if "loader" in which:
+        make_loader()

@@ -14,7 +14,10 @@ import types
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = "/root/reference/src/visualisation/euler/euler_2d.py"
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+from oracle import reference_root  # noqa: E402
+
+REF = os.path.join(reference_root(), "src", "visualisation", "euler", "euler_2d.py")
 
 
 def load_reference():

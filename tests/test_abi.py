@@ -170,6 +170,27 @@ def _uns_create(case, mesh: bytes):
     return st, msg
 
 
+def _drop_last_code(text: bytes) -> bytes:
+    """the text mesh with its last boundary code removed and the EDGES count lowered to match"""
+    lines = text.rstrip(b"\n").split(b"\n")
+    k = lines.index(b"EDGES")
+    lines[k + 1] = str(int(lines[k + 1]) - 1).encode()
+    return b"\n".join(lines[:-1]) + b"\n"
+
+
+def _set_first_code(text: bytes, code: int) -> bytes:
+    lines = text.rstrip(b"\n").split(b"\n")
+    k = lines.index(b"EDGES")
+    lines[k + 2] = str(code).encode()
+    return b"\n".join(lines) + b"\n"
+
+
+def _set_binary_code(data: bytes, ncells: int, code: int) -> bytes:
+    import numpy as np
+    off = 24 + 4 * ncells
+    return data[:off] + np.array([code], "<i4").tobytes() + data[off + 4:]
+
+
 def test_uns_mesh_parse_errors_need_no_device():
     """Malformed text and binary meshes are parse errors found before any device work; a valid
     mesh of either format gets as far as the device (no GPU here: HF_ERR_NO_DEVICE)."""
@@ -189,6 +210,12 @@ def test_uns_mesh_parse_errors_need_no_device():
         "text header": text.replace(b"CELLS", b"CELS", 1),
         "text cell count": text.replace(str(len(V)).encode(), str(len(V) + 1).encode(), 1),
         "text 2-vertex cell": b"\n".join(lines[:2] + [b"0.0 0.0 1.0 1.0"] + lines[3:]),
+        # boundary codes: one per (cell, edge) pair, each -1, -2, -3 or a cell index
+        "text fewer codes than pairs": _drop_last_code(text),
+        "text code below -3": _set_first_code(text, -4),
+        "text code past the cells": _set_first_code(text, len(V)),
+        "binary code below -3": _set_binary_code(data, len(V), -4),
+        "binary code past the cells": _set_binary_code(data, len(V), len(V)),
     }
     for what, mesh in bad.items():
         st, msg = _uns_create(case, mesh)

@@ -82,20 +82,34 @@ def test_batch_autotune_restores_state(port_lib):
 
 @pytest.mark.gpu
 def test_batch_full_workload_sample_matches_oracle(port_lib):
-    """The 512-case workload (sides 64..1024), 3 steps; a seeded sample of cases plus the
-    smallest and largest checked against the oracle."""
+    """The 512-case workload (sides 64..1024) to its 500 steps in one graph-captured persistent
+    launch; 16 seeded cases plus the smallest and the largest (side 1010) checked against the
+    oracle run on each case alone, bit for bit, with each case's own time."""
+    import os
+    from concurrent.futures import ThreadPoolExecutor
     from hyperflow_gb300 import BatchSolver, cases
+    from oracle.oracle import Oracle
+    steps = 500
     m = cases.batch_manifest(512, seed=0)
     b = BatchSolver(m)
     assert b.ninstances == 512
-    b.run(3, graph=True)
+    b.run(steps, graph=True)
     b.sync()
     sides = np.array(b.sides)
+    assert sides.max() == 1010 and sides.min() == 64     # this seed's extremes (the range is 64..1024)
     rng = np.random.default_rng(1)
-    pick = set(rng.choice(512, 12, replace=False).tolist()) | {int(sides.argmin()), int(sides.argmax())}
-    for i in sorted(pick):
-        ref, t = _oracle_interior(m["cases"][i], 3)
-        np.testing.assert_array_equal(b.state(i), ref, err_msg=f"case {i} side {sides[i]}")
+    pick = sorted(set(rng.choice(512, 16, replace=False).tolist()) | {int(sides.argmin()), int(sides.argmax())})
+    threads = max(1, (os.cpu_count() or 4) // 4)
+
+    def oracle_run(i):
+        o = Oracle(m["cases"][i], nthreads=threads)
+        o.run(steps)
+        return i, o.state(0)[:, 2:-2, 2:-2], o.t
+
+    with ThreadPoolExecutor(max_workers=4) as ex:
+        for i, ref, t in ex.map(oracle_run, pick):
+            np.testing.assert_array_equal(b.state(i), ref, err_msg=f"case {i} side {sides[i]}")
+            assert b.instance_time(i)[0] == t
 
 
 @pytest.mark.gpu

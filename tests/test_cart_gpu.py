@@ -312,16 +312,22 @@ def test_gpu_set_state_then_step_matches_oracle(port_lib):
     np.testing.assert_array_equal(s.state(0), o.state(0))
 
 
-@pytest.mark.parametrize("which", ["godunov_256", "mh_minbee_ffs_full", "mh_vanleer_4096"])
+@pytest.mark.parametrize("which", ["godunov_256", "mh_minbee_ffs_full", "mh_vanleer_ffs_full", "mh_vanleer_4096"])
 def test_gpu_full_size_matches_oracle(which, port_lib):
-    """The full benchmark sizes, a few steps, against the oracle on all host cores."""
+    """The full benchmark sizes against the oracle on all host cores: the 256^2 Godunov workload
+    to its 200 steps; the 4.7M-cell forward-facing step (dx = 1/1365, the benchmark's workload)
+    for 200 steps with each limiter -- ten times the benchmark's timed steps, past the start-up
+    factor's 10 TimeStep calls; its full run to t = 4 at dx = 1/40 is the reference's own
+    fixture (cart_ffs_*_dx1_40_t4); and 4096^2 MUSCL-Hancock for 2 steps."""
     import os
     from hyperflow_gb300 import cases
     from oracle.oracle import Oracle
     if which == "godunov_256":
         case, steps = cases.quadrant_case(256), 200
     elif which == "mh_minbee_ffs_full":
-        case, steps = cases.forward_facing_step_case(1365, limiter="MinBee"), 4
+        case, steps = cases.forward_facing_step_case(1365, limiter="MinBee"), 200
+    elif which == "mh_vanleer_ffs_full":
+        case, steps = cases.forward_facing_step_case(1365, limiter="VanLeer"), 200
     else:
         case, steps = cases.quadrant_case(4096, scheme="MUSCLHancock", limiter="VanLeer"), 2
     o = Oracle(case, nthreads=os.cpu_count() or 4)

@@ -165,7 +165,7 @@ def _uns_oracle(nx):
     from hyperflow_gb300 import meshgen
     from oracle import oracle
     verts, codes = _tri_strip(nx, ny=nx // 20)
-    nbr = meshgen.match_neighbours(list(verts), list(codes))
+    nbr = oracle.ref_neighbours(list(verts), list(codes))[0]
     nv = np.full(len(verts), 3, np.int32)
     ang, ln, area, rin = oracle.uns_geometry(nv, verts.reshape(-1))
     ps = np.concatenate([[0], np.cumsum(nv)]).astype(np.int32)
