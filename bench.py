@@ -157,6 +157,31 @@ def cpu_run(case, steps: int, nthreads: int):
     return time.perf_counter() - t0
 
 
+def reference_cpu_baseline(limiter: str, seconds: float = 10.0):
+    """The reference's own solver -- its sources compiled serially (oracle/_ref, from the reference
+    tree or its staged copy) -- on one host core, timed on the forward-facing step at a reduced
+    spacing (dx = 1/200: 100,800 cells; at the benchmark's spacing its per-cell allocations need
+    about 4 GB and minutes per step): a bounded sample of whole steps, after one untimed step."""
+    from hyperflow_gb300 import cases
+    from oracle import oracle
+    if not oracle.ref_available():
+        return None
+    case = cases.forward_facing_step_case(200, limiter=limiter, cfl=0.8, t_end=4.0)
+    cells = sum(b["x_cells"] * b["y_cells"] for b in case["mesh"]["blocks"])
+    ref = oracle.RefCart(case)
+    ref.run(1)
+    t0 = time.perf_counter()
+    ref.run(1)
+    probe = time.perf_counter() - t0
+    n = int(max(1, min(100, seconds / max(probe, 1e-3))))
+    t0 = time.perf_counter()
+    ref.run(n)
+    el = time.perf_counter() - t0
+    return {"value": cells * n / el / 1e6, "unit": "Mcell-updates/s", "cores": 1, "kind": "reference",
+            "sample": f"{n} steps of the forward-facing step at dx = 1/200 ({cells} cells), "
+                      f"{limiter}, after 2 steps; the reference's sources compiled serially (-O3)"}
+
+
 def reference_arm(args, cells):
     ws, rank, _ = dist_env()
     if rank != 0:
@@ -570,6 +595,10 @@ def main():
                "kind": "port",
                "sample": f"first {n_cpu} steps of the same workload (all {cells} cells)"}
 
+    cpu_ref = None
+    if rank == 0 and ws == 1 and args.workload == "ffs" and args.cpu_seconds > 0:
+        cpu_ref = reference_cpu_baseline(args.limiter)
+
     # step start, one ghost-fill launch per block side, ghost CFL + dt, one stencil per block, finalize
     launches_per_step = 3 + 5 * nb
     if rank == 0:
@@ -584,6 +613,7 @@ def main():
                        "parallelism": "replicas" if ws > 1 else "single GPU"},
             "roofline": roof,
             "cpu_baseline": cpu,
+            "cpu_baseline_reference": cpu_ref,
             "e2e": {"value": e2e_value, "unit": "Mcell-updates/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": h2d, "steps": e2e_steps,
                     "path": "kernels read and write pinned host buffers" if direct else "copies"},

@@ -6,12 +6,14 @@
 // A maintainer copies this header into the reference tree (e.g. src/fvm_2d_uns/scheme/gpu/),
 // compiles with -I src/fvm_2d_uns -I <this repo>/include, links libhyperflow_gb300.so, and has
 // the parser return GpuUnsScheme / GpuUnsForwardEuler / GpuUnsTimeStep sharing one
-// GpuUnsContext.  Simulation::solve builds a local TimeStep (simulation.cpp:61); that one line
-// becomes the injected time step.  Per step:
+// GpuUnsContext.  Simulation::solve builds a local TimeStep (simulation.cpp:61); with that one
+// line made the injected time step, per step:
 //   * GpuUnsTimeStep uploads the cells' values (Mesh::get_cells_flow_values) and returns
 //     TimeStep's dt computed on the device, counter included;
 //   * GpuUnsForwardEuler advances every cell on the device and returns the new values, which
 //     Simulation::solve stores with set_cells_flow_values.
+// Left unmodified, Simulation::solve forms dt with its local (CPU) TimeStep and the ODE adaptor
+// uploads the values it is handed before advancing them; the results are the same.
 // The GPU context reads the same case file and mesh file (its loader keeps the reference's cell
 // and edge order), so cell i is the same cell on both sides.  Results equal the reference's bit
 // for bit (per-(cell, edge) flux mode, the default).
@@ -55,9 +57,19 @@ class GpuUnsContext {
             throw std::runtime_error(std::string(hf_status_string(status)) + ": " + hf_uns_last_error_message(u));
     }
 
+    // the cells' values into the device state
+    void upload(const Vec2D& vals) {
+        const size_t n = (size_t)ncells;
+        for (size_t c = 0; c < n; ++c)
+            for (unsigned v = 0; v < 4; ++v) soa[v * n + c] = vals[c][v];
+        check(hf_uns_set_state(u, soa.data()));
+        uploaded = true;
+    }
+
     hf_uns* u = nullptr;
     int64_t ncells = 0;
     std::vector<double> soa;   // [4][ncells] staging
+    bool uploaded = false;     // the device holds the values of this step
 };
 
 class GpuUnsTimeStep : public TimeStep {   // replaces the local TimeStep of Simulation::solve
@@ -65,11 +77,7 @@ class GpuUnsTimeStep : public TimeStep {   // replaces the local TimeStep of Sim
     explicit GpuUnsTimeStep(std::shared_ptr<GpuUnsContext> g) : gpu(std::move(g)) {}
 
     double operator()(const std::shared_ptr<Mesh>& mesh) override {
-        const Vec2D vals = mesh->get_cells_flow_values();
-        const size_t n = (size_t)gpu->ncells;
-        for (size_t c = 0; c < n; ++c)
-            for (unsigned v = 0; v < 4; ++v) gpu->soa[v * n + c] = vals[c][v];
-        gpu->check(hf_uns_set_state(gpu->u, gpu->soa.data()));
+        gpu->upload(mesh->get_cells_flow_values());
         double dt = 0.0;
         gpu->check(hf_uns_time_step(gpu->u, &dt));   // TimeStep::operator(), counter advanced
         return dt;
@@ -88,7 +96,12 @@ class GpuUnsForwardEuler : public ODESolver {   // replaces ForwardEulerODESolve
   public:
     explicit GpuUnsForwardEuler(std::shared_ptr<GpuUnsContext> g) : gpu(std::move(g)) {}
 
-    Vec2D operator()(const std::function<Vec2D()>&, const Vec2D&, const double dt) override {
+    // `values` are the cells' values Simulation::solve passes (get_cells_flow_values): uploaded
+    // here unless GpuUnsTimeStep did so this step, so the adaptor also runs under the
+    // reference's unmodified Simulation::solve, whose own TimeStep then forms dt on the host
+    Vec2D operator()(const std::function<Vec2D()>&, const Vec2D& values, const double dt) override {
+        if (!gpu->uploaded) gpu->upload(values);
+        gpu->uploaded = false;
         gpu->check(hf_uns_advance(gpu->u, dt));
         gpu->check(hf_uns_get_state(gpu->u, gpu->soa.data()));
         const size_t n = (size_t)gpu->ncells;
