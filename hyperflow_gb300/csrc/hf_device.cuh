@@ -51,15 +51,26 @@ struct Prim {
     double Et;           // prim_total_energy (40-46), recomputed from the primitives
 };
 
-HF_HD Prim to_prim(double g1, double r, double ru, double rv, double E) {
+// the primitives without the total energy (Et left unset)
+HF_HD Prim to_prim_noE(double g1, double r, double ru, double rv, double E) {
     Prim w;
     w.r = r;
     w.u = div_rn(ru, r);
     w.v = div_rn(rv, r);
     w.q = w.u * w.u + w.v * w.v;
     w.p = g1 * (E - half(r) * w.q);
-    double e = div_rn(w.p, w.r * g1);      // prim_internal_energy (32-36)
-    w.Et = w.r * (half(w.q) + e);
+    return w;
+}
+
+// prim_total_energy (40-46) of the primitives, with prim_internal_energy (32-36)
+HF_HD double prim_energy(double g1, const Prim& w) {
+    double e = div_rn(w.p, w.r * g1);
+    return w.r * (half(w.q) + e);
+}
+
+HF_HD Prim to_prim(double g1, double r, double ru, double rv, double E) {
+    Prim w = to_prim_noE(g1, r, ru, rv, E);
+    w.Et = prim_energy(g1, w);
     return w;
 }
 
@@ -120,75 +131,76 @@ HF_HD void star_flux(const double* UK, const Prim& wK, double SK, double Ss,
 // test every branch uses one side only, so that side's state, flux and wave speed are selected
 // first and one flux / one star state is formed: a warp whose faces take different branches
 // runs the star-state arithmetic once, not once per branch.  LAZY forms the side's flux from its
-// primitives (the MUSCL-Hancock and unstructured faces); otherwise FL / FR are given.
+// primitives (the MUSCL-Hancock and unstructured faces) and its total energy, which nothing else
+// uses, for the selected side only (wL.Et / wR.Et are not read), after the branches have joined,
+// so a warp whose faces take different branches forms one energy and one flux per face;
+// otherwise FL / FR and the energies are given.
 template <int DIR, bool LAZY>
-HF_HD int hllc_sel(const double* UL, const Prim& wL, double aL, const double* FL,
+HF_HD int hllc_sel(double g1, const double* UL, const Prim& wL, double aL, const double* FL,
                    const double* UR, const Prim& wR, double aR, const double* FR, double* F) {
     double velL = DIR == 0 ? wL.u : wL.v;
     double velR = DIR == 0 ? wR.u : wR.v;
     double SL = smin(velL - aL, velR - aR);
     double SR = smax(velL + aL, velR + aR);
-    if (ge0(SL)) {
-        if (LAZY) {
-            flux<DIR>(wL, F);
-        } else {
+    bool left = true, star = false;   // the side whose state and flux the result uses; star region?
+    double Ss = 0.0;
+    if (!ge0(SL)) {
+        double num = wR.p - wL.p + wL.r * velL * (SL - velL) - wR.r * velR * (SR - velR);
+        double den = wL.r * (SL - velL) - wR.r * (SR - velR);
+        Ss = div_rn(num, den);
+        const bool star_l = le0(SL) && ge0(Ss);
+        const bool star_r = !star_l && le0(Ss) && ge0(SR);
+        const bool right = !star_l && !star_r && le0(SR);
+        if (!(star_l || star_r || right)) {
 #pragma unroll
-            for (int i = 0; i < 4; ++i) F[i] = FL[i];
+            for (int i = 0; i < 4; ++i) F[i] = 0.0;
+            return 1;
         }
-        return 0;
-    }
-    double num = wR.p - wL.p + wL.r * velL * (SL - velL) - wR.r * velR * (SR - velR);
-    double den = wL.r * (SL - velL) - wR.r * (SR - velR);
-    double Ss = div_rn(num, den);
-    const bool star_l = le0(SL) && ge0(Ss);
-    const bool star_r = !star_l && le0(Ss) && ge0(SR);
-    const bool right = !star_l && !star_r && le0(SR);
-    if (!(star_l || star_r || right)) {
-#pragma unroll
-        for (int i = 0; i < 4; ++i) F[i] = 0.0;
-        return 1;
+        left = star_l;
+        star = !right;
     }
     Prim w;
-    w.r = star_l ? wL.r : wR.r;
-    w.u = star_l ? wL.u : wR.u;
-    w.v = star_l ? wL.v : wR.v;
-    w.p = star_l ? wL.p : wR.p;
-    w.q = star_l ? wL.q : wR.q;
-    w.Et = star_l ? wL.Et : wR.Et;
-    double UK[4], FK[4];
-#pragma unroll
-    for (int i = 0; i < 4; ++i) UK[i] = star_l ? UL[i] : UR[i];
+    w.r = left ? wL.r : wR.r;
+    w.u = left ? wL.u : wR.u;
+    w.v = left ? wL.v : wR.v;
+    w.p = left ? wL.p : wR.p;
+    w.q = left ? wL.q : wR.q;
+    w.Et = LAZY ? prim_energy(g1, w) : (left ? wL.Et : wR.Et);
+    double FK[4];
     if (LAZY) {
         flux<DIR>(w, FK);
     } else {
 #pragma unroll
-        for (int i = 0; i < 4; ++i) FK[i] = star_l ? FL[i] : FR[i];
+        for (int i = 0; i < 4; ++i) FK[i] = left ? FL[i] : FR[i];
     }
-    if (right) {
+    if (!star) {   // supersonic left (riemann_hllc.cpp:179-181) or right (203-205)
 #pragma unroll
         for (int i = 0; i < 4; ++i) F[i] = FK[i];
         return 0;
     }
-    star_flux<DIR>(UK, w, star_l ? SL : SR, Ss, FK, F);
+    double UK[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) UK[i] = left ? UL[i] : UR[i];
+    star_flux<DIR>(UK, w, left ? SL : SR, Ss, FK, F);
     return 0;
 }
 
 template <int DIR>
 HF_HD int hllc(const double* UL, const Prim& wL, double aL, const double* FL,
                const double* UR, const Prim& wR, double aR, const double* FR, double* F) {
-    return hllc_sel<DIR, false>(UL, wL, aL, FL, UR, wR, aR, FR, F);
+    return hllc_sel<DIR, false>(0.0, UL, wL, aL, FL, UR, wR, aR, FR, F);
 }
 
 // HLLC from two conservative states (computes primitives, sound speeds, the used flux)
 template <int DIR>
 HF_HD int hllc_cons(double g, double g1, const double* UL, const double* UR,
                                          double* F) {
-    Prim wL = to_prim(g1, UL[0], UL[1], UL[2], UL[3]);
-    Prim wR = to_prim(g1, UR[0], UR[1], UR[2], UR[3]);
+    Prim wL = to_prim_noE(g1, UL[0], UL[1], UL[2], UL[3]);
+    Prim wR = to_prim_noE(g1, UR[0], UR[1], UR[2], UR[3]);
     // calc_wave_speeds_direct_min_max (127-150): sqrt(gamma * p / rho)
     double aL = sound(g, wL.r, wL.p);
     double aR = sound(g, wR.r, wR.p);
-    return hllc_sel<DIR, true>(UL, wL, aL, nullptr, UR, wR, aR, nullptr, F);
+    return hllc_sel<DIR, true>(g1, UL, wL, aL, nullptr, UR, wR, aR, nullptr, F);
 }
 
 // ------------------------------------------------------------------------------
