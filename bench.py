@@ -452,6 +452,8 @@ def main():
     ap.add_argument("--n", type=int, default=4096, help="side of the square workload")
     ap.add_argument("--scheme", default="MUSCLHancock", choices=["MUSCLHancock", "Godunov"],
                     help="scheme of the square workload")
+    ap.add_argument("--per-block-launches", action="store_true",
+                    help="ffs/square workloads: one stencil launch per block instead of the all-blocks launch")
     ap.add_argument("--quick", action="store_true",
                     help="device-resident timing only (no graph pass, e2e or CPU baseline)")
     args = ap.parse_args()
@@ -495,6 +497,7 @@ def main():
     from hyperflow_gb300 import CartSolver
     s = CartSolver(case)
     nb = s.nblocks
+    s.set_block_launches(args.per_block_launches)
     stream = torch.cuda.ExternalStream(s.stream())
 
     # ---- device-resident timed region ----
@@ -515,13 +518,15 @@ def main():
     s.profile(False)
     value, t_max = replica_value(ms, ws, cells, args.steps, pg)
     hllc_fallbacks = s.hllc_errors()
+    reruns = s.blocks_rerun()
 
     if args.quick:
         if rank == 0:
             print(json.dumps({"metric": "Mcell-updates/s", "value": value, "unit": "Mcell-updates/s",
                               "steps": args.steps, "ms_per_step": t_max / args.steps,
                               "config": {"workload": workload_name(args), "cells": cells},
-                              "stencil_ms_per_step": stencil_ms / args.steps}), flush=True)
+                              "stencil_ms_per_step": stencil_ms / args.steps,
+                              "blocks_rerun": reruns}), flush=True)
         s.close()
         return
 
@@ -621,6 +626,7 @@ def main():
             "clocks": clk.summary(),
             "graph_value": graph_value,
             "hllc_zero_flux_fallbacks": hllc_fallbacks,
+            "blocks_rerun": reruns,
         }
         print(json.dumps(line), flush=True)
     s.close()

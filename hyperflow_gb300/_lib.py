@@ -59,6 +59,8 @@ SIGNATURES = {
     "hf_checkpoint_save": (_i, [_p, _p, _sz]),
     "hf_checkpoint_load": (_i, [_p, _p, _sz]),
     "hf_status_string": (C.c_char_p, [_i]),
+    "hf_set_block_launches": (_i, [_p, _i]),
+    "hf_blocks_rerun": (_i, [_p, C.POINTER(_i64)]),
     "hf_time_step_noalloc": (_i, [_p, _i, _i, _i, _d, _d, _d, _d, _i64, _p, _p]),
     # unstructured (include/hyperflow_gb300_uns.h)
     "hf_uns_create": (_i, [C.c_char_p, _sz, C.POINTER(_p)]),

@@ -81,6 +81,8 @@ struct hf_ctx {
     hf::MeshDev* dmesh = nullptr;
     hf::Ctrl* dctrl = nullptr;
     CUtensorMap tmap[HF_MAXB][2];
+    hf::StepPlan plan{};        // the all-blocks MUSCL-Hancock launch (plan.nb = 0: not usable)
+    bool block_launches = false;   // hf_set_block_launches: one stencil launch per block instead
     std::vector<double*> allocs;
     double* pinned = nullptr;   // staging for layout conversion
     size_t pinned_n = 0;
@@ -346,6 +348,20 @@ int parse_case(hf_ctx* ctx, const Json& cfg) {
     return HF_OK;
 }
 
+// every block of a MUSCL-Hancock step in one launch, where the mesh has few enough blocks
+bool step_kernel(const hf_ctx* ctx) { return ctx->scheme == 1 && ctx->plan.nb > 0 && !ctx->block_launches; }
+
+void make_plan(hf_ctx* ctx) {
+    ctx->plan = hf::StepPlan{};
+    if (ctx->scheme != 1 || ctx->nblocks > hf::kStepMaxBlocks) return;
+    for (int b = 0; b < ctx->nblocks; ++b) {
+        ctx->plan.tm[b][0] = ctx->tmap[b][0];
+        ctx->plan.tm[b][1] = ctx->tmap[b][1];
+        hf::step_plan_tiles(ctx->plan, b, ctx->blocks[b].nx, ctx->blocks[b].ny);
+    }
+    ctx->plan.nb = ctx->nblocks;
+}
+
 int make_tmaps(hf_ctx* ctx) {
     PFN_encodeTiled enc = get_encode();
     if (!enc) return fail(ctx, HF_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
@@ -414,10 +430,14 @@ int enqueue_step(hf_ctx* ctx, bool profiled) {
     if (profiled) { ev_record(ctx, 1, false); ev_record(ctx, 0, true); }
     {
         hf::TraceRange trace_("block stencils");
-        for (int b = 0; b < ctx->nblocks; ++b)
-            CK(hf::launch_stencil(ctx->dctrl, ctx->dmesh, b, ctx->blocks[b].nx, ctx->blocks[b].ny,
-                                  ctx->scheme, ctx->limiter, &ctx->tmap[b][0], &ctx->tmap[b][1],
-                                  ctx->stream));
+        if (step_kernel(ctx)) {
+            CK(hf::launch_mh_step(ctx->dctrl, ctx->dmesh, ctx->plan, ctx->limiter, ctx->stream));
+        } else {
+            for (int b = 0; b < ctx->nblocks; ++b)
+                CK(hf::launch_stencil(ctx->dctrl, ctx->dmesh, b, ctx->blocks[b].nx, ctx->blocks[b].ny,
+                                      ctx->scheme, ctx->limiter, &ctx->tmap[b][0], &ctx->tmap[b][1],
+                                      ctx->stream));
+        }
     }
     if (profiled) ev_record(ctx, 0, false);
     if (ctx->ring_slots > 0) CK(hf::launch_frame_copy(ctx->dctrl, ctx->dmesh, ctx->ring, ctx->stream));
@@ -532,6 +552,7 @@ int hf_create(const char* case_json, size_t len, hf_ctx** out) {
     CK(cudaMemcpyAsync(ctx->dctrl, &C, sizeof C, cudaMemcpyHostToDevice, ctx->stream));
     int r = make_tmaps(ctx);
     if (r != HF_OK) return r;
+    make_plan(ctx);
     // initial condition, uploaded into both buffers (ghosts zero until the first fill)
     try {
         for (int b = 0; b < ctx->nblocks; ++b) {
@@ -787,10 +808,16 @@ int hf_step_io(hf_ctx* ctx, const double* const* in, double* const* out, double*
         for (int b = 0; b < ctx->nblocks; ++b)
             CK(hf::launch_ghost_store(ctx->dctrl, ctx->dmesh, b, ctx->blocks[b].tx, ctx->blocks[b].ny, ctx->ghost,
                                       p, out[b], ctx->stream));
-        for (int b = 0; b < ctx->nblocks; ++b) {
-            const BlockHost& B = ctx->blocks[b];
-            CK(hf::launch_stencil(ctx->dctrl, ctx->dmesh, b, B.nx, B.ny, ctx->scheme, ctx->limiter,
-                                  &ctx->tmap[b][0], &ctx->tmap[b][1], ctx->stream, out[b]));
+        if (step_kernel(ctx)) {
+            hf::StepPlan plan = ctx->plan;
+            for (int b = 0; b < ctx->nblocks; ++b) plan.hout[b] = out[b];
+            CK(hf::launch_mh_step(ctx->dctrl, ctx->dmesh, plan, ctx->limiter, ctx->stream));
+        } else {
+            for (int b = 0; b < ctx->nblocks; ++b) {
+                const BlockHost& B = ctx->blocks[b];
+                CK(hf::launch_stencil(ctx->dctrl, ctx->dmesh, b, B.nx, B.ny, ctx->scheme, ctx->limiter,
+                                      &ctx->tmap[b][0], &ctx->tmap[b][1], ctx->stream, out[b]));
+            }
         }
         CK(hf::launch_finalize(ctx->dctrl, ctx->stream));
         ctx->step_started = ctx->ghost_fresh = false;
@@ -1165,6 +1192,30 @@ int hf_checkpoint_load(hf_ctx* ctx, const void* buf, size_t bytes) {
             p += n;
         }
     CK(cudaMemcpy(ctx->dctrl, &C, sizeof C, cudaMemcpyHostToDevice));
+    return HF_OK;
+}
+
+int hf_set_block_launches(hf_ctx* ctx, int per_block) {
+    if (!ctx) return HF_ERR_ARG;
+    if (ctx->next_block != 0) return fail(ctx, HF_ERR_STATE, "launch mode changed in the middle of a step");
+    if (ctx->block_launches != (per_block != 0)) {
+        CK(cudaStreamSynchronize(ctx->stream));
+        for (int k = 0; k < 2; ++k)   // the captured steps hold the other launch mode
+            if (ctx->graph[k]) {
+                cudaGraphExecDestroy(ctx->graph[k]);
+                ctx->graph[k] = nullptr;
+            }
+    }
+    ctx->block_launches = per_block != 0;
+    return HF_OK;
+}
+
+int hf_blocks_rerun(hf_ctx* ctx, int64_t* count) {
+    if (!ctx || !count) return HF_ERR_ARG;
+    long long n = 0;
+    CK(cudaStreamSynchronize(ctx->stream));
+    CK(cudaMemcpy(&n, &ctx->dctrl->blocks_rerun, sizeof n, cudaMemcpyDeviceToHost));
+    *count = n;
     return HF_OK;
 }
 

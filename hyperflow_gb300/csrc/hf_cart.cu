@@ -97,8 +97,12 @@ __global__ void step_begin_kernel(Ctrl* __restrict__ c) {
     for (int b = 0; b < HF_MAXB; ++b) {
         c->ghost_s[b][0] = c->ghost_s[b][1] = 0ull;
         c->int_s[p ^ 1][b][0] = c->int_s[p ^ 1][b][1] = 0ull;
+        c->step_hllc[b] = 0;
+        c->step_bad[b] = c->step_nonpos[b] = ~0ull;
     }
     c->ticket = 0u;
+    c->tile_ctr = 0u;
+    c->bar_count = 0u;
 }
 
 // one side of one block; the sides run as consecutive launches in the reference order, so
@@ -164,19 +168,8 @@ __global__ void __launch_bounds__(kRedThreads) ghost_cfl_kernel(Ctrl* __restrict
     if (!last || threadIdx.x != 0) return;
     __threadfence();
     volatile Ctrl* vc = c;
-    Ctrl snap;
-    snap.nblocks = vc->nblocks;
-    snap.cfl = vc->cfl;
-    for (int b = 0; b < snap.nblocks; ++b) {
-        snap.dx[b] = vc->dx[b];
-        snap.dy[b] = vc->dy[b];
-        snap.ghost_s[b][0] = vc->ghost_s[b][0];
-        snap.ghost_s[b][1] = vc->ghost_s[b][1];
-        snap.int_s[p][b][0] = vc->int_s[p][b][0];
-        snap.int_s[p][b][1] = vc->int_s[p][b][1];
-    }
     long long call = vc->calls;
-    double dt = cfl_dt(&snap, call, 0, p, p);
+    double dt = cfl_dt_fresh(c, call, 0, p, p);
     c->dt_cfl = dt;
     const double t = c->t;
     if (c->clamp && t + dt > c->t_end) dt = c->t_end - t;        // simulation.cpp:88-90
@@ -452,6 +445,207 @@ __global__ void __launch_bounds__(NT, 3) mh_kernel(Ctrl* __restrict__ c, const M
 }
 
 // ------------------------------------------------------------------------------------
+// MUSCL-Hancock, every block of a step in one persistent launch
+// ------------------------------------------------------------------------------------
+// The reference updates the blocks one after the other, and block b's half-step predictor takes
+// its dt from a TimeStep call over a mesh whose blocks < b are already updated
+// (muscl_hancock.cpp:246, called from simulation.cpp:106-110).  One launch per block leaves a
+// partly filled last wave of CTAs at the end of every block.  Here one cooperative launch (all
+// CTAs resident) walks the tiles of all blocks, in block order, from a shared counter, so one
+// block's tail overlaps the next block's start, and runs every block with the predictor dt of a
+// TimeStep call over the step's starting state.  For block 0 that is the reference's value.  For
+// block b > 0 it is the reference's value whenever updating blocks 0..b-1 leaves the largest wave
+// speed TimeStep sees unchanged, the usual case.  After all tiles, block by block: a grid barrier,
+// then every CTA forms block b's true predictor dt (the reference's call: blocks < b from their
+// updated state) from the same data; where its bits differ from the value used, the grid runs
+// block b again with it.  A step never writes a block's input buffer, so the second run gives
+// exactly the sequential result; a block's wave-speed maxima and numerical-failure records are
+// kept per block and folded into the totals only when every block is final, so a discarded run
+// leaves nothing behind.
+// grid-wide barrier with a bounded wait (10 s of the global timer); false after a timeout or
+// once another CTA raised the error word
+__device__ bool step_grid_barrier(Ctrl* c) {
+    __shared__ int ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned int* gen = &c->bar_gen;
+        const unsigned int g0 = *gen;
+        __threadfence();
+        const unsigned int arrived = atomicAdd(&c->bar_count, 1u) + 1u;
+        if (arrived == gridDim.x) {
+            c->bar_count = 0u;
+            __threadfence();
+            atomicAdd(&c->bar_gen, 1u);
+            ok = 1;
+        } else {
+            ok = 0;
+            unsigned long long t0;
+            asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+            for (;;) {
+                if (*gen != g0) { ok = 1; break; }
+                if (*(volatile int*)&c->err != 0) break;
+                unsigned long long t1;
+                asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t1));
+                if (t1 - t0 > 10000000000ull) {
+                    raise_error(c, HF_DEV_TIMEOUT);
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    return ok != 0;
+}
+
+// this launch's predictor scalars per block: 0.5 dtp / dx, 0.5 dtp / dy, 1 / dx, 1 / dy, and dtp
+__shared__ double s_step_sc[kStepMaxBlocks][5];
+
+// One tile of block b (local tile index `local`): its TMA load (mbarrier phase `phase`), the
+// fused fluxes with the block's predictor scalars, the update and the block's records.  False if
+// the load's bounded wait gave up.  Out of line: the tile loop and the re-run loop share one copy.
+template <int TX, int TY, int LIM, int NT>
+__device__ __noinline__ bool mh_step_tile(Ctrl* __restrict__ c, const MeshDev* __restrict__ m,
+                                          const StepPlan& plan, int b, int local, int p, uint32_t phase) {
+    using L = MhLayout<TX, TY>;
+    extern __shared__ __align__(1024) double smem[];
+    double* sU = smem + L::U_OFF;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + L::END);
+    const BlockDev& B = m->b[b];
+    const int x0 = (local % plan.tiles_x[b]) * TX, y0 = (local / plan.tiles_x[b]) * TY;
+    if (threadIdx.x == 0) {
+        // the previous tile's reads of sU (generic proxy) are ordered before this copy's writes
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        mbar_expect_tx(bar, L::TMA_BYTES);
+        tma_load_3d(sU, &plan.tm[b][p], bar, x0, y0, 0);
+    }
+    const bool ok = mbar_wait_bounded(bar, phase, kWaitLimit);
+    if (__syncthreads_or(!ok)) {
+        if (threadIdx.x == 0) {
+            raise_error(c, HF_DEV_TIMEOUT);
+            mbar_wait_bounded(bar, phase, kWaitLimit);   // let an in-flight copy land before exit
+        }
+        __syncthreads();
+        return false;
+    }
+    const double g = c->gamma, g1 = c->g1;
+    const int herr = mh_tile_fluxes<TX, TY, NT, LIM>(sU, smem + L::A_OFF, smem + L::F_OFF, smem + L::G_OFF, g, g1,
+                                                     s_step_sc[b][0], s_step_sc[b][1], x0, y0, B.nx, B.ny,
+                                                     &c->step_bad[b], face_key(c->step, b, 0, 0, 0));
+    const double* sF = smem + L::F_OFF;
+    const double* sG = smem + L::G_OFF;
+    const double dt = c->dt, one_dx = s_step_sc[b][2], one_dy = s_step_sc[b][3];
+    double* __restrict__ out = B.buf[p ^ 1];
+    double* __restrict__ hout = plan.hout[b];
+    const size_t plane = (size_t)B.ty * B.pitch;
+    double mx = 0.0, my = 0.0;
+    for (int it = threadIdx.x; it < TX * TY; it += NT) {
+        const int ox = it % TX, oy = it / TX;
+        const int gxx = x0 + ox, gyy = y0 + oy;
+        if (gxx < B.nx && gyy < B.ny) {
+            double un[4];
+            const size_t o = (size_t)(gyy + 2) * B.pitch + (gxx + 2);
+            const size_t h = (size_t)(gyy + 2) * B.tx + gxx + 2;
+            if (!hf_in((long long)o, (long long)plane, &c->err) ||
+                !hf_in((long long)h, (long long)B.ty * B.tx, &c->err))
+                continue;
+#pragma unroll
+            for (int v = 0; v < 4; ++v) {
+                un[v] = mh_update<TX, TY>(sU, sF, sG, v, ox, oy, dt, one_dx, one_dy);
+                out[v * plane + o] = un[v];
+                if (hout) __stcs(&hout[(size_t)v * B.ty * B.tx + h], un[v]);
+            }
+            double sx, sy;
+            if (!wave_terms(g, g1, un[0], un[1], un[2], un[3], sx, sy))
+                atomicMin(&c->step_nonpos[b], face_key(c->step, b, 0, gyy, gxx));
+            mx = nmax(mx, sx);
+            my = nmax(my, sy);
+        }
+    }
+    block_max2_atomic<NT>(mx, my, &c->int_s[p ^ 1][b][0], &c->int_s[p ^ 1][b][1]);
+    if (herr) atomicAdd(reinterpret_cast<unsigned long long*>(&c->step_hllc[b]), (unsigned long long)herr);
+    return true;
+}
+
+// the predictor scalars of block b from its predictor dt (muscl_hancock.cpp:248-249, 352-353)
+__device__ __forceinline__ void step_scalars(const Ctrl* c, int b, double dtp) {
+    s_step_sc[b][0] = 0.5 * dtp / c->dx[b];
+    s_step_sc[b][1] = 0.5 * dtp / c->dy[b];
+    s_step_sc[b][2] = 1.0 / c->dx[b];
+    s_step_sc[b][3] = 1.0 / c->dy[b];
+    s_step_sc[b][4] = dtp;
+}
+
+template <int TX, int TY, int LIM, int NT>
+__global__ void __launch_bounds__(NT, 3) mh_step_kernel(Ctrl* __restrict__ c, const MeshDev* __restrict__ m,
+                                                     const __grid_constant__ StepPlan plan) {
+    using L = MhLayout<TX, TY>;
+    extern __shared__ __align__(1024) double smem[];
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + L::END);
+    if (c->done) return;   // set before this launch: every CTA leaves, no barrier is entered
+
+    const int p = (int)(c->step & 1);
+    const int nb = plan.nb;
+    const long long calls = c->calls;
+    __shared__ int s_tile, s_redo;
+    if (threadIdx.x == 0) {
+        for (int b = 0; b < nb; ++b) step_scalars(c, b, cfl_dt(c, calls + b, 0, p, p ^ 1));   // starting state
+        mbar_init(bar, 1);
+    }
+    __syncthreads();
+    uint32_t phase = 0u;
+    const int total = plan.tile_start[nb];
+    for (;;) {
+        if (threadIdx.x == 0) s_tile = (int)atomicAdd(&c->tile_ctr, 1u);
+        __syncthreads();
+        const int t = s_tile;
+        if (t >= total) break;
+        int b = 0;
+        while (t >= plan.tile_start[b + 1]) ++b;
+        if (!mh_step_tile<TX, TY, LIM, NT>(c, m, plan, b, t - plan.tile_start[b], p, phase)) return;
+        phase ^= 1u;
+    }
+    for (int b = 1; b < nb; ++b) {
+        if (!step_grid_barrier(c)) return;   // blocks < b final
+        if (threadIdx.x == 0) {
+            const double dtp = cfl_dt_fresh(c, calls + b, b, p, p ^ 1);
+            s_redo = f64_bits(dtp) != f64_bits(s_step_sc[b][4]);
+            if (s_redo) {
+                step_scalars(c, b, dtp);
+                if (blockIdx.x == 0) {   // forget the first run's records of block b
+                    c->int_s[p ^ 1][b][0] = c->int_s[p ^ 1][b][1] = 0ull;
+                    c->step_hllc[b] = 0;
+                    c->step_bad[b] = c->step_nonpos[b] = ~0ull;
+                    c->blocks_rerun = c->blocks_rerun + 1;
+                }
+            }
+        }
+        __syncthreads();
+        if (!s_redo) continue;
+        if (!step_grid_barrier(c)) return;   // the cleared records are in place before the re-run
+        const int ntiles = plan.tile_start[b + 1] - plan.tile_start[b];
+        for (int local = blockIdx.x; local < ntiles; local += gridDim.x) {
+            if (!mh_step_tile<TX, TY, LIM, NT>(c, m, plan, b, local, p, phase)) return;
+            phase ^= 1u;
+        }
+    }
+    if (!step_grid_barrier(c)) return;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {   // every block final: fold this step's records
+        const volatile Ctrl* vc = c;
+        long long herr = 0;
+        for (int b = 0; b < nb; ++b) {
+            herr += vc->step_hllc[b];
+            const unsigned long long fb = vc->step_bad[b], fn = vc->step_nonpos[b];
+            if (fb < c->first_bad) c->first_bad = fb;
+            if (fn < c->first_nonpos) c->first_nonpos = fn;
+            c->dt_pred[b] = s_step_sc[b][4];
+        }
+        c->hllc_errors = c->hllc_errors + herr;
+    }
+}
+
+// ------------------------------------------------------------------------------------
 // Godunov, fused: per-cell primitives/fluxes once, then x/y HLLC, then update
 // ------------------------------------------------------------------------------------
 template <int TX, int TY>
@@ -541,8 +735,57 @@ StencilTiles stencil_tiles(int scheme) {
     return scheme == 0 ? StencilTiles{kGoTX + 2, kGoTY + 2} : StencilTiles{kMhTX + 4, kMhTY + 4};
 }
 
+void step_plan_tiles(StepPlan& plan, int b, int nx, int ny) {
+    plan.tiles_x[b] = (nx + kMhTX - 1) / kMhTX;
+    plan.tile_start[b + 1] = plan.tile_start[b] + plan.tiles_x[b] * ((ny + kMhTY - 1) / kMhTY);
+}
+
+// CTAs of the all-blocks launch: as many as are resident at once (the grid barrier needs every
+// CTA running), found once per limiter and device
+static int g_step_grid[2][64];
+
+template <int LIM>
+static cudaError_t launch_mh_step_lim(Ctrl* c, const MeshDev* m, const StepPlan& plan, cudaStream_t s) {
+    auto k = mh_step_kernel<kMhTX, kMhTY, LIM, kMhNT>;
+    const size_t smem = MhLayout<kMhTX, kMhTY>::BYTES;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+    int& grid = g_step_grid[LIM][dev];
+    if (grid == 0) {
+        int per_sm = 0, sms = 0;
+        if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kMhNT, smem)) != cudaSuccess) return e;
+        if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+        if (per_sm < 1) return cudaErrorInvalidConfiguration;
+        grid = per_sm * sms;
+    }
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3(kMhNT);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;   // all CTAs resident: the grid barrier is safe
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k, c, m, plan);
+}
+
+cudaError_t launch_mh_step(Ctrl* c, const MeshDev* m, const StepPlan& plan, int limiter, cudaStream_t s) {
+    if (plan.nb < 1 || plan.nb > kStepMaxBlocks) return cudaErrorInvalidValue;
+    return limiter == 0 ? launch_mh_step_lim<0>(c, m, plan, s) : launch_mh_step_lim<1>(c, m, plan, s);
+}
+
 cudaError_t stencil_prepare() {
     cudaError_t e;
+    e = cudaFuncSetAttribute(mh_step_kernel<kMhTX, kMhTY, 0, kMhNT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)MhLayout<kMhTX, kMhTY>::BYTES);
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(mh_step_kernel<kMhTX, kMhTY, 1, kMhNT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)MhLayout<kMhTX, kMhTY>::BYTES);
+    if (e != cudaSuccess) return e;
     e = cudaFuncSetAttribute(mh_kernel<kMhTX, kMhTY, 0, kMhNT>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)MhLayout<kMhTX, kMhTY>::BYTES);

@@ -77,6 +77,22 @@ cudaError_t launch_upload(Ctrl* c, const MeshDev* m, int b, int tx, int ty, int 
                           cudaStream_t s);
 cudaError_t launch_ghost_store(Ctrl* c, const MeshDev* m, int b, int tx, int ny, int ghost, int parity,
                                double* hout, cudaStream_t s);
+// Every block of a MUSCL-Hancock step in one cooperative launch (mh_step_kernel in hf_cart.cu:
+// the blocks' tiles from one counter, each block's predictor dt verified against the reference's
+// TimeStep call and the block run again where it differs), for meshes of at most
+// kStepMaxBlocks blocks.
+constexpr int kStepMaxBlocks = 4;
+struct StepPlan {
+    CUtensorMap tm[kStepMaxBlocks][2];   // per block, per state parity
+    double* hout[kStepMaxBlocks];        // host-buffer stores of the updated cells, or null
+    int tiles_x[kStepMaxBlocks];
+    int tile_start[kStepMaxBlocks + 1];  // prefix sums of the blocks' tile counts
+    int nb;
+};
+// the tile grid of block b (nx x ny interior cells) in the plan
+void step_plan_tiles(StepPlan& plan, int b, int nx, int ny);
+cudaError_t launch_mh_step(Ctrl* c, const MeshDev* m, const StepPlan& plan, int limiter, cudaStream_t s);
+
 // TMA box of the stencil for the scheme
 StencilTiles stencil_tiles(int scheme);
 cudaError_t stencil_prepare();   // sets the large dynamic shared-memory opt-ins once

@@ -41,6 +41,14 @@ struct Ctrl {
     long long captured, drained;            // frames put into / taken out of the ring
     double ring_t[HF_MAXRING];              // time label per ring slot
     long long ring_idx[HF_MAXRING];         // frame index per ring slot
+    // the all-blocks MUSCL-Hancock step launch (mh_step_kernel): its tile counter and grid
+    // barrier, and this step's per-block records, folded into the totals above when the step's
+    // blocks are final (a block run again discards its first run's records)
+    unsigned int tile_ctr;
+    unsigned int bar_count, bar_gen;
+    long long step_hllc[HF_MAXB];
+    unsigned long long step_bad[HF_MAXB], step_nonpos[HF_MAXB];
+    long long blocks_rerun;                 // blocks run again because their predictor dt changed
 };
 
 enum : int {

@@ -281,18 +281,28 @@ __device__ __forceinline__ double bitsd(unsigned long long x) {
 
 // dt of TimeStep call number `call` (0-based) over all blocks; blocks < new_upto take
 // their interior maximum from parity `pn` (already advanced this step), the others
-// from parity `po`.
-__device__ __forceinline__ double cfl_dt(const Ctrl* c, long long call, int new_upto, int po, int pn) {
+// from parity `po`.  CP: const Ctrl*, or const volatile Ctrl* to read values other CTAs of the
+// same launch wrote (past the L1 cache).
+template <class CP>
+__device__ __forceinline__ double cfl_dt_t(CP c, long long call, int new_upto, int po, int pn) {
     double dtx = 1e16, dty = 1e16;
-    for (int b = 0; b < c->nblocks; ++b) {
+    const int nb = c->nblocks;
+    for (int b = 0; b < nb; ++b) {
         int pp = b < new_upto ? pn : po;
         double mx = smax(bitsd(c->ghost_s[b][0]), bitsd(c->int_s[pp][b][0]));
         double my = smax(bitsd(c->ghost_s[b][1]), bitsd(c->int_s[pp][b][1]));
         dtx = smin(dtx, c->dx[b] / mx);
         dty = smin(dty, c->dy[b] / my);
     }
-    double final_cfl = (call + 1 <= 10) ? 0.2 * c->cfl : c->cfl;
+    const double cfl = c->cfl;
+    double final_cfl = (call + 1 <= 10) ? 0.2 * cfl : cfl;
     return final_cfl * smin(dtx, dty);
+}
+__device__ __forceinline__ double cfl_dt(const Ctrl* c, long long call, int new_upto, int po, int pn) {
+    return cfl_dt_t<const Ctrl*>(c, call, new_upto, po, pn);
+}
+__device__ __forceinline__ double cfl_dt_fresh(const Ctrl* c, long long call, int new_upto, int po, int pn) {
+    return cfl_dt_t<const volatile Ctrl*>(c, call, new_upto, po, pn);
 }
 
 // block-wide max of two values, one atomicMax per CTA

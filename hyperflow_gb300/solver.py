@@ -283,6 +283,18 @@ class CartSolver:
         check(lib().hf_stream(self._h, C.byref(s)), self._h)
         return s.value or 0
 
+    def set_block_launches(self, per_block: bool):
+        """True: one stencil launch per block, in order.  False (default): a MUSCL-Hancock step
+        of up to 4 blocks is one launch that checks each block's predictor dt against the
+        reference's and runs a block again where it differs; the results are identical."""
+        check(lib().hf_set_block_launches(self._h, int(bool(per_block))), self._h)
+
+    def blocks_rerun(self) -> int:
+        """block updates run a second time because their predictor dt changed (all-blocks launch)"""
+        n = C.c_int64()
+        check(lib().hf_blocks_rerun(self._h, C.byref(n)), self._h)
+        return n.value
+
     def profile(self, enable: bool = True):
         check(lib().hf_profile(self._h, int(enable)), self._h)
 

@@ -141,9 +141,23 @@ int hf_clear_error_cell(hf_ctx* ctx);
 /* the context's CUDA stream (a cudaStream_t), for callers that time or order work on it */
 int hf_stream(hf_ctx* ctx, void** stream);
 
-/* per-kernel timing: when enabled, every stencil launch is bracketed by CUDA events on the
- * context's stream; hf_kernel_time returns the summed milliseconds and launch count since
- * the last reset.  kind 0 = stencil (Godunov/MUSCL-Hancock), 1 = ghost fill + CFL. */
+/* How a step's MUSCL-Hancock block updates are launched.  No counterpart in the reference,
+ * whose Simulation::solve updates the blocks in order (simulation.cpp:106-110).  By default a
+ * mesh of at most 4 blocks is updated by one cooperative launch that takes the blocks' tiles in
+ * order from one counter (no partly filled last wave per block) and runs every block with the
+ * predictor dt of a TimeStep call over the step's starting state; each block b > 0 is then
+ * checked against the predictor dt the reference forms (muscl_hancock.cpp:246: blocks < b
+ * already updated) and run again where the two differ, so results are the reference's bit for
+ * bit either way.  per_block = 1 selects one launch per block in order instead (also used for
+ * Godunov, for meshes of more blocks and by hf_advance_block).  hf_blocks_rerun counts the
+ * block runs redone since creation. */
+int hf_set_block_launches(hf_ctx* ctx, int per_block);
+int hf_blocks_rerun(hf_ctx* ctx, int64_t* count);
+
+/* per-kernel timing: when enabled, every step's stencil launches are bracketed by CUDA events on
+ * the context's stream; hf_kernel_time returns the summed milliseconds and the number of
+ * bracketed steps since the last reset.  kind 0 = stencil (Godunov/MUSCL-Hancock), 1 = ghost
+ * fill + CFL. */
 int hf_profile(hf_ctx* ctx, int enable);
 int hf_kernel_time(hf_ctx* ctx, int kind, double* ms, int64_t* launches);
 

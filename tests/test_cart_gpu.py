@@ -456,3 +456,63 @@ def test_gpu_tiny_and_ragged_grids_match_oracle(scheme, limiter, nx, ny, port_li
     np.testing.assert_array_equal(np.array(dts), dts_o)
     np.testing.assert_array_equal(s.state(0), o.state(0))
     assert s.hllc_errors() == o.hllc_errors
+
+
+def _fast_block0(case, seed=3):
+    """the forward-facing step with block 0's interior replaced by a seeded field whose waves
+    are the fastest of the mesh and change every step"""
+    from oracle.oracle import Oracle
+    o = Oracle(case)
+    U = o.state(0)
+    rng = np.random.default_rng(seed)
+    g = 2
+    inner = (slice(None), slice(g, -g), slice(g, -g))
+    shape = U[inner][0].shape
+    rho = rng.uniform(0.5, 2.0, shape)
+    u = rng.uniform(2.0, 6.0, shape)
+    v = rng.uniform(-1.0, 1.0, shape)
+    p = rng.uniform(0.5, 3.0, shape)
+    W = np.stack([rho, rho * u, rho * v, p / 0.4 + 0.5 * rho * (u * u + v * v)])
+    U[inner] = W
+    return U
+
+
+@pytest.mark.parametrize("limiter", ["MinBee", "VanLeer"])
+def test_gpu_all_blocks_launch_reruns_a_block_whose_predictor_dt_changed(limiter, port_lib):
+    """The all-blocks launch runs every block with the predictor dt of the step's starting state
+    and runs block b again when the reference's predictor dt (blocks < b updated) differs.  Here
+    block 0 holds the fastest waves and they change every step, so blocks 1 and 2 are run twice
+    in most steps: the results equal the oracle's bit for bit, as do those of the one-launch-per-
+    block mode, and the re-run count is positive."""
+    from hyperflow_gb300 import cases
+    from oracle.oracle import Oracle
+    case = cases.forward_facing_step_case(40, limiter=limiter)
+    U0 = _fast_block0(case)
+    o = Oracle(case)
+    o.set_state(0, U0)
+    o.run(12)
+    for per_block in (False, True):
+        s = _solver(case)
+        s.set_block_launches(per_block)
+        s.set_state(0, U0)
+        s.run(7, graph=False)
+        s.run(5, graph=True)
+        for b in range(3):
+            np.testing.assert_array_equal(s.state(b), o.state(b), err_msg=f"block {b}, per_block={per_block}")
+        assert s.time()[1] == o.calls
+        assert (s.blocks_rerun() > 0) == (not per_block)
+
+
+def test_gpu_all_blocks_launch_equals_per_block_launches_on_the_benchmark_step(port_lib):
+    """The 4.7M-cell forward-facing step for 30 steps in both launch modes: identical states,
+    time and TimeStep calls."""
+    from hyperflow_gb300 import cases
+    case = cases.forward_facing_step_case(1365, limiter="MinBee")
+    a, b = _solver(case), _solver(case)
+    b.set_block_launches(True)
+    a.run(30)
+    b.run(30)
+    assert a.time() == b.time()
+    for k in range(3):
+        np.testing.assert_array_equal(a.state(k), b.state(k))
+    assert a.hllc_errors() == b.hllc_errors() == 0
