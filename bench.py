@@ -568,13 +568,17 @@ def main():
     achieved = BYTES_PER_CELL * cells * args.steps / (stencil_ms / 1e3) / 1e9
     traffic = None
     tr = ncu_traffic()
+    all_blocks = args.scheme == "MUSCLHancock" and nb <= 4 and not args.per_block_launches
+    per_launch = 1 if all_blocks else nb           # stencil launches per step
     if tr and tr.get("workload") == workload_name(args):
-        traffic = tr["dram_bytes_per_cell_update"] * cells / nb
+        traffic = tr["dram_bytes_per_cell_update"] * cells / per_launch
     roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
             "frac": achieved / hbm, "traffic": traffic, "peak_kind": peak_kind,
-            "algorithmic_bytes_per_launch": BYTES_PER_CELL * cells / nb,
-            "avg_launch_ms": stencil_ms / max(stencil_launches * nb, 1),
-            "kernel": "mh_kernel (fused MUSCL-Hancock + HLLC + forward Euler + CFL epilogue)"}
+            "algorithmic_bytes_per_launch": BYTES_PER_CELL * cells / per_launch,
+            "avg_launch_ms": stencil_ms / max(stencil_launches * per_launch, 1),
+            "kernel": ("mh_step_kernel (every block of the step in one launch: fused MUSCL-Hancock + HLLC + "
+                       "forward Euler + CFL epilogue)") if all_blocks else
+                      "mh_kernel (fused MUSCL-Hancock + HLLC + forward Euler + CFL epilogue)"}
     # the bound that binds on this part: FP64 issue (2 lanes per SM per clock)
     if tr and tr.get("workload") == workload_name(args) and tr.get("fp64_ops_per_cell_update"):
         sm_mhz = 2070.0
@@ -604,8 +608,9 @@ def main():
     if rank == 0 and ws == 1 and args.workload == "ffs" and args.cpu_seconds > 0:
         cpu_ref = reference_cpu_baseline(args.limiter)
 
-    # step start, one ghost-fill launch per block side, ghost CFL + dt, one stencil per block, finalize
-    launches_per_step = 3 + 5 * nb
+    # step start, the ghost fill + ghost CFL + dt, the stencils (one launch for every block of a
+    # MUSCL-Hancock mesh of up to 4 blocks, else one per block), finalize
+    launches_per_step = 3 + per_launch
     if rank == 0:
         line = {
             "metric": "Mcell-updates/s", "value": value, "unit": "Mcell-updates/s",

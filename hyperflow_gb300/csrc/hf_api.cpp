@@ -11,6 +11,7 @@
 #include <cstring>
 #include <memory>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include <cuda.h>
@@ -86,7 +87,6 @@ struct hf_ctx {
     std::vector<double*> allocs;
     double* pinned = nullptr;   // staging for layout conversion
     size_t pinned_n = 0;
-    int side_len[2 * HF_MAXB] = {};   // total_x, total_y per block (ghost-fill launch sizes)
     // frame output: simulation.animation of the case and the device frame ring
     bool has_anim = false;
     double anim_duration = 0.0, anim_fps = 0.0;
@@ -348,6 +348,102 @@ int parse_case(hf_ctx* ctx, const Json& cfg) {
     return HF_OK;
 }
 
+// Mesh::apply_bcs (mesh.cpp:31-39) replayed on the host in the reference's order -- blocks in
+// case order; per block the bottom, right, top and left sides; per side position by position,
+// layer by layer (transmissive_boundary.cpp, reflective_boundary.cpp: the normal momentum negated,
+// dirichlet_boundary.cpp, internal_boundary.cpp: the neighbour block's cells) -- tracking, for
+// every ghost cell written, where its value comes from: a cell's value before the fill (an
+// interior cell, or a ghost cell not yet written in this fill, whose value is the previous
+// fill's) or a Dirichlet side's state, with the sign changes of the reflective sides met on the
+// way.  The result is one FillOp per ghost cell, in the ghost enumeration of the CFL pass; the
+// device applies them all at once.  Every ghost cell is written by some side.
+int build_fill_program(hf_ctx* ctx, std::vector<hf::FillOp>& ops) {
+    const int g = ctx->ghost;
+    const hf::MeshDev& M = ctx->hmesh;
+    auto key = [](int b, long long off) { return ((long long)b << 44) | off; };
+    std::unordered_map<long long, hf::FillOp> cur;   // ghost cells written so far: their values
+    cur.reserve((size_t)M.total_ghost * 2);
+    auto is_ghost = [g](const hf::BlockDev& B, int i, int j) {
+        return i < g || i >= B.tx - g || j < g || j >= B.ty - g;
+    };
+    for (int b = 0; b < M.nblocks; ++b) {
+        const hf::BlockDev& B = M.b[b];
+        for (int side = 0; side < 4; ++side) {
+            const int kind = B.bc_type[side];
+            const int eb = kind == hf::BC_INTERNAL ? B.bc_block[side] : b;
+            if (eb < 0 || eb >= M.nblocks) return fail(ctx, HF_ERR_PARSE, "internal boundary names no block");
+            const hf::BlockDev& E = M.b[eb];
+            const bool along_x = (side == hf::SIDE_BOTTOM || side == hf::SIDE_TOP);
+            const int n = along_x ? B.tx : B.ty;
+            const unsigned char neg = along_x ? 2 : 1;   // reflective: rho*v across y sides, rho*u across x
+            for (int pos = 0; pos < n; ++pos)
+                for (int k = 0; k < g; ++k) {
+                    int di, dj, si = 0, sj = 0;
+                    switch (side) {
+                        case hf::SIDE_BOTTOM:
+                            di = pos; dj = g - 1 - k;
+                            si = pos; sj = kind == hf::BC_INTERNAL ? E.ty - g - 1 - k : g + k;
+                            break;
+                        case hf::SIDE_TOP:
+                            di = pos; dj = B.ty - g + k;
+                            si = pos; sj = kind == hf::BC_INTERNAL ? g + k : B.ty - g - 1 - k;
+                            break;
+                        case hf::SIDE_LEFT:
+                            dj = pos; di = g - 1 - k;
+                            sj = pos; si = kind == hf::BC_INTERNAL ? E.tx - g - 1 - k : g + k;
+                            break;
+                        default:  // right
+                            dj = pos; di = B.tx - g + k;
+                            sj = pos; si = kind == hf::BC_INTERNAL ? g + k : B.tx - g - 1 - k;
+                            break;
+                    }
+                    hf::FillOp v{};
+                    if (kind == hf::BC_DIRICHLET) {
+                        v.kind = 2;
+                        v.block = b;
+                        v.side = (unsigned char)side;
+                    } else {
+                        if (si < 0 || si >= E.tx || sj < 0 || sj >= E.ty)
+                            return fail(ctx, HF_ERR_UNSUPPORTED, "a ghost fill source lies outside its block");
+                        const long long so = (long long)sj * E.pitch + si;
+                        auto it = cur.find(key(eb, so));
+                        if (it != cur.end()) {
+                            v = it->second;
+                        } else {
+                            v.kind = is_ghost(E, si, sj) ? 1 : 0;
+                            v.block = eb;
+                            v.src = so;
+                        }
+                        if (kind == hf::BC_REFLECTIVE) v.neg ^= neg;
+                    }
+                    cur[key(b, (long long)dj * B.pitch + di)] = v;
+                }
+        }
+    }
+    ops.resize((size_t)M.total_ghost);
+    for (int b = 0; b < M.nblocks; ++b) {
+        const hf::BlockDev& B = M.b[b];
+        const long long rows = (long long)g * B.tx;
+        for (long long k = 0; k < B.ghost_count; ++k) {
+            int i, j;   // the ghost enumeration of the CFL pass (hf_cart.cu ghost_cell_ij)
+            if (k < rows) {
+                j = (int)(k / B.tx); i = (int)(k % B.tx);
+            } else if (k < 2 * rows) {
+                j = B.ty - g + (int)((k - rows) / B.tx); i = (int)((k - rows) % B.tx);
+            } else {
+                const long long r = k - 2 * rows;
+                j = g + (int)(r / (2 * g));
+                const int c = (int)(r % (2 * g));
+                i = c < g ? c : B.tx - 2 * g + c;
+            }
+            auto it = cur.find(key(b, (long long)j * B.pitch + i));
+            if (it == cur.end()) return fail(ctx, HF_ERR_UNSUPPORTED, "a ghost cell no side fills");
+            ops[(size_t)(B.ghost_off + k)] = it->second;
+        }
+    }
+    return HF_OK;
+}
+
 // every block of a MUSCL-Hancock step in one launch, where the mesh has few enough blocks
 bool step_kernel(const hf_ctx* ctx) { return ctx->scheme == 1 && ctx->plan.nb > 0 && !ctx->block_launches; }
 
@@ -424,8 +520,8 @@ int enqueue_step(hf_ctx* ctx, bool profiled) {
     if (profiled) ev_record(ctx, 1, true);
     {
         hf::TraceRange trace_("ghost fill + dt");
-        CK(hf::launch_bc_fill(ctx->dctrl, ctx->dmesh, ctx->side_len, ctx->nblocks, ctx->stream));
-        CK(hf::launch_ghost_cfl(ctx->dctrl, ctx->dmesh, ctx->hmesh.total_ghost, ctx->stream));
+        CK(hf::launch_step_begin(ctx->dctrl, ctx->stream));
+        CK(hf::launch_fill_cfl(ctx->dctrl, ctx->dmesh, ctx->hmesh.total_ghost, ctx->stream));
     }
     if (profiled) { ev_record(ctx, 1, false); ev_record(ctx, 0, true); }
     {
@@ -523,13 +619,21 @@ int hf_create(const char* case_json, size_t len, hf_ctx** out) {
             CK(cudaMemsetAsync(p, 0, n * sizeof(double), ctx->stream));
             D.buf[k] = p;
         }
-        ctx->side_len[2 * b] = B.tx;
-        ctx->side_len[2 * b + 1] = B.ty;
         D.ghost_off = goff;
         D.ghost_count = B.tx * B.ty - B.nx * B.ny;
         goff += D.ghost_count;
     }
     M.total_ghost = goff;
+    {
+        std::vector<hf::FillOp> ops;
+        int r = build_fill_program(ctx, ops);
+        if (r != HF_OK) return r;
+        hf::FillOp* d = nullptr;
+        CK(cudaMalloc(&d, ops.size() * sizeof(hf::FillOp)));
+        ctx->allocs.push_back(reinterpret_cast<double*>(d));
+        CK(cudaMemcpyAsync(d, ops.data(), ops.size() * sizeof(hf::FillOp), cudaMemcpyHostToDevice, ctx->stream));
+        M.fill = d;
+    }
     CK(cudaMalloc(&ctx->dmesh, sizeof(hf::MeshDev)));
     CK(cudaMemcpyAsync(ctx->dmesh, &M, sizeof M, cudaMemcpyHostToDevice, ctx->stream));
     hf::Ctrl C{};
@@ -668,7 +772,9 @@ int hf_apply_bcs(hf_ctx* ctx) {
     hf::TraceRange trace_("hf_apply_bcs");
     if (!ctx) return HF_ERR_ARG;
     if (ctx->next_block != 0) return fail(ctx, HF_ERR_STATE, "apply_bcs in the middle of a step");
-    CK(hf::launch_bc_fill(ctx->dctrl, ctx->dmesh, ctx->side_len, ctx->nblocks, ctx->stream));
+    CK(hf::launch_step_begin(ctx->dctrl, ctx->stream));
+    CK(hf::launch_fill_cfl(ctx->dctrl, ctx->dmesh, ctx->hmesh.total_ghost, ctx->stream, 0));
+    CK(hf::launch_ghost_mirror(ctx->dctrl, ctx->dmesh, ctx->hmesh.total_ghost, ctx->stream));
     ctx->step_started = true;
     ctx->ghost_fresh = false;
     return HF_OK;
@@ -803,8 +909,8 @@ int hf_step_io(hf_ctx* ctx, const double* const* in, double* const* out, double*
         }
         int r = set_clamp(ctx, 0);
         if (r != HF_OK) return r;
-        CK(hf::launch_bc_fill(ctx->dctrl, ctx->dmesh, ctx->side_len, ctx->nblocks, ctx->stream));
-        CK(hf::launch_ghost_cfl(ctx->dctrl, ctx->dmesh, ctx->hmesh.total_ghost, ctx->stream));
+        CK(hf::launch_step_begin(ctx->dctrl, ctx->stream));
+        CK(hf::launch_fill_cfl(ctx->dctrl, ctx->dmesh, ctx->hmesh.total_ghost, ctx->stream));
         for (int b = 0; b < ctx->nblocks; ++b)
             CK(hf::launch_ghost_store(ctx->dctrl, ctx->dmesh, b, ctx->blocks[b].tx, ctx->blocks[b].ny, ctx->ghost,
                                       p, out[b], ctx->stream));
@@ -837,8 +943,8 @@ int hf_step_io(hf_ctx* ctx, const double* const* in, double* const* out, double*
     }
     int r = set_clamp(ctx, 0);
     if (r != HF_OK) return r;
-    CK(hf::launch_bc_fill(ctx->dctrl, ctx->dmesh, ctx->side_len, ctx->nblocks, ctx->stream));
-    CK(hf::launch_ghost_cfl(ctx->dctrl, ctx->dmesh, ctx->hmesh.total_ghost, ctx->stream));
+    CK(hf::launch_step_begin(ctx->dctrl, ctx->stream));
+    CK(hf::launch_fill_cfl(ctx->dctrl, ctx->dmesh, ctx->hmesh.total_ghost, ctx->stream));
     for (int b = 0; b < ctx->nblocks; ++b) {
         const BlockHost& B = ctx->blocks[b];
         CK(hf::launch_stencil(ctx->dctrl, ctx->dmesh, b, B.nx, B.ny, ctx->scheme, ctx->limiter,

@@ -23,67 +23,6 @@ namespace hf {
 
 constexpr unsigned kWaitLimit = 1u << 22;   // bounded mbarrier polls before giving up
 
-// ------------------------------------------------------------------------------------
-// ghost fill (one CTA; sides strictly in the reference order)
-// ------------------------------------------------------------------------------------
-// transmissive_boundary.cpp:25-104, reflective_boundary.cpp:25-120,
-// dirichlet_boundary.cpp:25-104, internal_boundary.cpp:27-108.  Layer k = 0..g-1 counts
-// outward from the interior; source indices are the reference's, written per layer.
-__device__ void fill_side(const MeshDev* __restrict__ m, int b, int side, int p, int* err) {
-    const BlockDev& B = m->b[b];
-    const int g = m->ghost;
-    const int kind = B.bc_type[side];
-    const int e = B.bc_block[side];
-    const BlockDev& E = m->b[kind == BC_INTERNAL ? e : b];
-    const bool along_x = (side == SIDE_BOTTOM || side == SIDE_TOP);
-    const int n = along_x ? B.tx : B.ty;
-    const int neg_comp = along_x ? 2 : 1;
-    const size_t plane = (size_t)B.ty * B.pitch, eplane = (size_t)E.ty * E.pitch;
-    double* __restrict__ d0 = B.buf[p];
-    double* __restrict__ d1 = B.buf[p ^ 1];
-    const double* __restrict__ src = E.buf[p];
-    for (int pos = blockIdx.x * blockDim.x + threadIdx.x; pos < n; pos += gridDim.x * blockDim.x) {
-        for (int k = 0; k < g; ++k) {
-            int di, dj, si = 0, sj = 0;
-            switch (side) {
-                case SIDE_BOTTOM:
-                    di = pos; dj = g - 1 - k;
-                    si = pos; sj = kind == BC_INTERNAL ? E.ty - g - 1 - k : g + k;
-                    break;
-                case SIDE_TOP:
-                    di = pos; dj = B.ty - g + k;
-                    si = pos; sj = kind == BC_INTERNAL ? g + k : B.ty - g - 1 - k;
-                    break;
-                case SIDE_LEFT:
-                    dj = pos; di = g - 1 - k;
-                    sj = pos; si = kind == BC_INTERNAL ? E.tx - g - 1 - k : g + k;
-                    break;
-                default:  // right
-                    dj = pos; di = B.tx - g + k;
-                    sj = pos; si = kind == BC_INTERNAL ? g + k : B.tx - g - 1 - k;
-                    break;
-            }
-            const size_t dof = (size_t)dj * B.pitch + di;
-            const size_t sof = (size_t)sj * E.pitch + si;
-            if (!hf_in((long long)dof, (long long)plane, err) ||
-                (kind != BC_DIRICHLET && !hf_in((long long)sof, (long long)eplane, err)))
-                continue;
-#pragma unroll
-            for (int v = 0; v < 4; ++v) {
-                double val;
-                if (kind == BC_DIRICHLET) {
-                    val = B.bc_state[side][v];
-                } else {
-                    val = src[v * eplane + sof];
-                    if (kind == BC_REFLECTIVE && v == neg_comp) val = -1.0 * val;
-                }
-                d0[v * plane + dof] = val;
-                d1[v * plane + dof] = val;
-            }
-        }
-    }
-}
-
 // start of a step: stop at t_end (device loop), clear this step's accumulators
 __global__ void step_begin_kernel(Ctrl* __restrict__ c) {
     const int p = (int)(c->step & 1);
@@ -105,14 +44,6 @@ __global__ void step_begin_kernel(Ctrl* __restrict__ c) {
     c->bar_count = 0u;
 }
 
-// one side of one block; the sides run as consecutive launches in the reference order, so
-// a side sees every value the sides before it wrote
-__global__ void __launch_bounds__(256) bc_side_kernel(Ctrl* __restrict__ c,
-                                                      const MeshDev* __restrict__ m, int b, int side) {
-    if (c->done) return;
-    fill_side(m, b, side, (int)(c->step & 1), &c->err);
-}
-
 // ------------------------------------------------------------------------------------
 // TimeStep over the ghost cells; the last CTA forms the step dt
 // ------------------------------------------------------------------------------------
@@ -132,6 +63,8 @@ __device__ __forceinline__ void ghost_cell_ij(const BlockDev& B, int g, long lon
 }
 
 constexpr int kRedThreads = 256;
+
+__device__ void form_step_dt(Ctrl* __restrict__ c, int p);
 
 // form_dt = 0: the ghost maxima only (for a predictor TimeStep in a step whose dt the caller gave)
 __global__ void __launch_bounds__(kRedThreads) ghost_cfl_kernel(Ctrl* __restrict__ c,
@@ -159,8 +92,12 @@ __global__ void __launch_bounds__(kRedThreads) ghost_cfl_kernel(Ctrl* __restrict
         block_max2_atomic<kRedThreads>(mx, my, &c->ghost_s[b][0], &c->ghost_s[b][1]);
         __syncthreads();
     }
-    if (!form_dt) return;
-    // last CTA to finish forms the dt of this TimeStep call
+    if (form_dt) form_step_dt(c, p);
+}
+
+// The last CTA of a ghost-maxima launch to finish forms the step's dt: TimeStep call number
+// `calls` over every block (timestep.cpp:29-68), then Simulation::solve's clamps and frame points.
+__device__ void form_step_dt(Ctrl* __restrict__ c, int p) {
     __shared__ bool last;
     __threadfence();
     if (threadIdx.x == 0) last = (atomicAdd(&c->ticket, 1u) == gridDim.x - 1);
@@ -186,6 +123,88 @@ __global__ void __launch_bounds__(kRedThreads) ghost_cfl_kernel(Ctrl* __restrict
     c->dt = dt;
     c->calls = call + 1;
     c->ticket = 0u;
+}
+
+// the block of ghost cell k of the all-blocks enumeration
+__device__ __forceinline__ int ghost_block(const MeshDev* __restrict__ m, long long k) {
+    int b = 0;
+    while (b + 1 < m->nblocks && k >= m->b[b + 1].ghost_off) ++b;
+    return b;
+}
+
+// Mesh::apply_bcs (mesh.cpp:31-39) for every block in one launch: ghost cell k takes its final
+// value from the fill program (a copy of one cell's pre-fill value or of a Dirichlet side's state,
+// with the reflective sides' negations: transmissive_boundary.cpp, reflective_boundary.cpp,
+// dirichlet_boundary.cpp, internal_boundary.cpp replayed in the reference's order on the host),
+// then its TimeStep terms feed the block's ghost maxima.
+__global__ void __launch_bounds__(kRedThreads) fill_cfl_kernel(Ctrl* __restrict__ c, const MeshDev* __restrict__ m,
+                                                               int form_dt) {
+    if (c->done) return;
+    const int p = (int)(c->step & 1);
+    const double g = c->gamma, g1 = c->g1;
+    const int gh = m->ghost;
+    const long long total = m->total_ghost;
+    const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long k0 = (long long)blockIdx.x * blockDim.x;
+    const long long k1 = (k0 + blockDim.x < total ? k0 + blockDim.x : total) - 1;
+    int b = -1;
+    double sx = 0.0, sy = 0.0;
+    if (k < total) {
+        b = ghost_block(m, k);
+        const BlockDev& B = m->b[b];
+        int i, j;
+        ghost_cell_ij(B, gh, k - B.ghost_off, i, j);
+        const FillOp op = m->fill[k];
+        double u[4];
+        if (op.kind == 2) {
+            const BlockDev& S = m->b[op.block];
+#pragma unroll
+            for (int v = 0; v < 4; ++v) u[v] = S.bc_state[op.side][v];
+        } else {
+            const BlockDev& S = m->b[op.block];
+            const size_t splane = (size_t)S.ty * S.pitch;
+            const double* __restrict__ src = S.buf[op.kind == 0 ? p : p ^ 1];
+            if (hf_in(op.src, (long long)splane, &c->err)) {
+#pragma unroll
+                for (int v = 0; v < 4; ++v) u[v] = src[v * splane + op.src];
+            } else {
+#pragma unroll
+                for (int v = 0; v < 4; ++v) u[v] = 0.0;
+            }
+        }
+        if (op.neg & 1) u[1] = -1.0 * u[1];
+        if (op.neg & 2) u[2] = -1.0 * u[2];
+        const size_t plane = (size_t)B.ty * B.pitch, o = (size_t)j * B.pitch + i;
+        if (hf_in((long long)o, (long long)plane, &c->err)) {
+            double* __restrict__ dst = B.buf[p];
+#pragma unroll
+            for (int v = 0; v < 4; ++v) dst[v * plane + o] = u[v];
+        }
+        double tx_, ty_;
+        wave_terms(g, g1, u[0], u[1], u[2], u[3], tx_, ty_);
+        sx = nmax(0.0, tx_);   // NaN terms are skipped, as TimeStep's std::min skips them
+        sy = nmax(0.0, ty_);
+    }
+    // one atomic pair per block this CTA touched (its cells are consecutive in block order)
+    const int b0 = ghost_block(m, k0), b1 = ghost_block(m, k1);
+    for (int bb = b0; bb <= b1; ++bb)
+        block_max2_atomic<kRedThreads>(b == bb ? sx : 0.0, b == bb ? sy : 0.0, &c->ghost_s[bb][0],
+                                       &c->ghost_s[bb][1]);
+    if (form_dt) form_step_dt(c, p);
+}
+
+// the current buffer's ghost cells into the other buffer (after a fill no stencil follows)
+__global__ void __launch_bounds__(256) ghost_mirror_kernel(const Ctrl* __restrict__ c, const MeshDev* __restrict__ m) {
+    const int p = (int)(c->step & 1);
+    const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= m->total_ghost) return;
+    const int b = ghost_block(m, k);
+    const BlockDev& B = m->b[b];
+    int i, j;
+    ghost_cell_ij(B, m->ghost, k - B.ghost_off, i, j);
+    const size_t plane = (size_t)B.ty * B.pitch, o = (size_t)j * B.pitch + i;
+#pragma unroll
+    for (int v = 0; v < 4; ++v) B.buf[p ^ 1][v * plane + o] = B.buf[p][v * plane + o];
 }
 
 // TimeStep terms over one block's interior (after an upload of new state)
@@ -247,14 +266,14 @@ __global__ void __launch_bounds__(kRedThreads) upload_kernel(Ctrl* __restrict__ 
     block_max2_atomic<kRedThreads>(mx, my, &c->int_s[parity][b][0], &c->int_s[parity][b][1]);
 }
 
-// The ghost cells of the updated buffer (filled this step, never written by the stencil) into
-// host memory the GPU maps: with the stencil's own host stores, the whole block downloaded.
+// The ghost cells filled this step into host memory the GPU maps: with the stencil's own host
+// stores of the updated cells, the whole block downloaded.
 __global__ void __launch_bounds__(256) ghost_store_kernel(Ctrl* __restrict__ c, const MeshDev* __restrict__ m,
                                                           int b, int parity, double* __restrict__ hout) {
     const BlockDev& B = m->b[b];
     const int g = m->ghost;
     const size_t plane = (size_t)B.ty * B.pitch, hplane = (size_t)B.ty * B.tx;
-    const double* __restrict__ U = B.buf[parity ^ 1];
+    const double* __restrict__ U = B.buf[parity];    // filled this step; the stencil copies them later
     const long long rows = (long long)g * B.tx;          // cells in the g bottom (or top) rows
     const long long n = 2 * rows + 2LL * g * B.ny;       // + g columns each side of the interior rows
     for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n;
@@ -356,6 +375,32 @@ __device__ __forceinline__ bool load_tile(double* sU, uint64_t* bar, const CUten
     return true;
 }
 
+// The ghost cells in a tile's halo (loaded after this step's fill), from shared memory into the
+// step's output buffer, so the updated state carries the ghost values the reference's mesh holds
+// after the step (its update leaves ghost cells as filled) and the next fill finds this fill's
+// values in its other buffer.  Each ghost cell is stored by the one tile holding its nearest
+// interior cell; only tiles on the block's edge hold any.  sU is [4][TY + 2G][TX + 2G].
+template <int TX, int TY, int G, int NT>
+__device__ __forceinline__ void store_ghosts(const double* __restrict__ sU, const BlockDev& B, int x0, int y0,
+                                             double* __restrict__ out, int* err) {
+    if (x0 > 0 && y0 > 0 && x0 + TX < B.nx && y0 + TY < B.ny) return;
+    constexpr int UX = TX + 2 * G, UY = TY + 2 * G;
+    const size_t plane = (size_t)B.ty * B.pitch;
+    for (int it = threadIdx.x; it < UX * UY; it += NT) {
+        const int lx = it % UX, ly = it / UX;
+        const int x = x0 - G + lx, y = y0 - G + ly;   // interior coordinates
+        if (x < -G || y < -G || x >= B.nx + G || y >= B.ny + G) continue;
+        if (x >= 0 && y >= 0 && x < B.nx && y < B.ny) continue;
+        const int cx = x < 0 ? 0 : (x >= B.nx ? B.nx - 1 : x);
+        const int cy = y < 0 ? 0 : (y >= B.ny ? B.ny - 1 : y);
+        if (cx < x0 || cx >= x0 + TX || cy < y0 || cy >= y0 + TY) continue;
+        const size_t o = (size_t)(y + G) * B.pitch + (x + G);
+        if (!hf_in((long long)o, (long long)plane, err)) continue;
+#pragma unroll
+        for (int v = 0; v < 4; ++v) out[v * plane + o] = sU[(v * UY + ly) * UX + lx];
+    }
+}
+
 // ------------------------------------------------------------------------------------
 // MUSCL-Hancock, fused
 // ------------------------------------------------------------------------------------
@@ -440,6 +485,7 @@ __global__ void __launch_bounds__(NT, 3) mh_kernel(Ctrl* __restrict__ c, const M
             my = nmax(my, sy);
         }
     }
+    store_ghosts<TX, TY, 2, NT>(sU, B, x0, y0, out, &c->err);
     block_max2_atomic<NT>(mx, my, &c->int_s[p ^ 1][b][0], &c->int_s[p ^ 1][b][1]);
     if (herr) atomicAdd(reinterpret_cast<unsigned long long*>(&c->hllc_errors), (unsigned long long)herr);
 }
@@ -563,6 +609,7 @@ __device__ __noinline__ bool mh_step_tile(Ctrl* __restrict__ c, const MeshDev* _
             my = nmax(my, sy);
         }
     }
+    store_ghosts<TX, TY, 2, NT>(sU, B, x0, y0, out, &c->err);
     block_max2_atomic<NT>(mx, my, &c->int_s[p ^ 1][b][0], &c->int_s[p ^ 1][b][1]);
     if (herr) atomicAdd(reinterpret_cast<unsigned long long*>(&c->step_hllc[b]), (unsigned long long)herr);
     return true;
@@ -721,6 +768,7 @@ __global__ void __launch_bounds__(NT, 3) godunov_kernel(Ctrl* __restrict__ c,
             my = nmax(my, sy);
         }
     }
+    store_ghosts<TX, TY, 1, NT>(sU, B, x0, y0, out, &c->err);
     block_max2_atomic<NT>(mx, my, &c->int_s[p ^ 1][b][0], &c->int_s[p ^ 1][b][1]);
     if (herr) atomicAdd(reinterpret_cast<unsigned long long*>(&c->hllc_errors), (unsigned long long)herr);
 }
@@ -804,14 +852,15 @@ cudaError_t launch_step_begin(Ctrl* c, cudaStream_t s) {
     return cudaGetLastError();
 }
 
-cudaError_t launch_bc_fill(Ctrl* c, const MeshDev* m, const int* side_len, int nblocks, cudaStream_t s) {
-    step_begin_kernel<<<1, 1, 0, s>>>(c);
-    for (int b = 0; b < nblocks; ++b)
-        for (int side = 0; side < 4; ++side) {
-            const int n = side_len[2 * b + (side == SIDE_BOTTOM || side == SIDE_TOP ? 0 : 1)];
-            int grid = (n + 255) / 256;
-            bc_side_kernel<<<grid < 1 ? 1 : grid, 256, 0, s>>>(c, m, b, side);
-        }
+cudaError_t launch_fill_cfl(Ctrl* c, const MeshDev* m, long long total_ghost, cudaStream_t s, int form_dt) {
+    long long grid = (total_ghost + kRedThreads - 1) / kRedThreads;
+    fill_cfl_kernel<<<(unsigned)(grid < 1 ? 1 : grid), kRedThreads, 0, s>>>(c, m, form_dt);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_ghost_mirror(Ctrl* c, const MeshDev* m, long long total_ghost, cudaStream_t s) {
+    long long grid = (total_ghost + 255) / 256;
+    ghost_mirror_kernel<<<(unsigned)(grid < 1 ? 1 : grid), 256, 0, s>>>(c, m);
     return cudaGetLastError();
 }
 

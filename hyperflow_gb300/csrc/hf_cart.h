@@ -28,10 +28,25 @@ struct BlockDev {
     int ghost_count;
 };
 
+// One ghost cell's value after the whole ghost fill of Mesh::apply_bcs (all blocks, all sides, in
+// the reference's order), found by replaying that fill on the host once: a copy of one cell's
+// value from before the fill, or of a side's Dirichlet state, with the reflective sides' sign
+// changes.  Cells are listed in the ghost-cell enumeration of the CFL pass (ghost_off order).
+struct FillOp {
+    long long src;          // kinds 0, 1: offset of the source cell in its block's buffer plane
+    int block;              // kinds 0, 1: the source block; kind 2: the block whose side is used
+    unsigned char kind;     // 0: an interior cell (current buffer); 1: a ghost cell's value before
+                            // the fill (held by the other buffer); 2: a Dirichlet side's state
+    unsigned char neg;      // bit 0: negate rho*u, bit 1: negate rho*v
+    unsigned char side;     // kind 2: the side
+    unsigned char pad;
+};
+
 struct MeshDev {
     int nblocks, ghost;
     long long total_ghost;
     BlockDev b[HF_MAXB];
+    const FillOp* fill;     // total_ghost entries
 };
 
 // the device frame ring: slots of slot_len doubles; block b's interior at off[b] in a slot
@@ -46,11 +61,18 @@ struct StencilTiles {
 };
 
 // launchers (all asynchronous on `s`)
-// ghost fill: one launch per (block, side) in the reference order; side_len[2b] = total_x,
-// side_len[2b+1] = total_y of block b
-cudaError_t launch_bc_fill(Ctrl* c, const MeshDev* m, const int* side_len, int nblocks, cudaStream_t s);
-// start of a step without a device ghost fill: stop flags, the ghost and next-state maxima and the
-// reduction ticket reset (launch_bc_fill does this first as well)
+// The ghost fill of every block in one launch from the fill program (m->fill), written into the
+// current buffer only, with the ghost cells' TimeStep terms; with form_dt the last CTA forms the
+// step's dt (a TimeStep call: counter, clamps, frame points).  Its ghost-cell sources are read
+// from the other buffer, whose ghost cells equal the current buffer's before the fill: every
+// stencil stores the ghost cells it loaded into its output buffer, and launch_ghost_mirror does
+// the same after a fill that no stencil follows.  Launch after launch_step_begin.
+cudaError_t launch_fill_cfl(Ctrl* c, const MeshDev* m, long long total_ghost, cudaStream_t s, int form_dt = 1);
+// the current buffer's ghost cells into the other buffer
+cudaError_t launch_ghost_mirror(Ctrl* c, const MeshDev* m, long long total_ghost, cudaStream_t s);
+// start of a step (before its ghost fill, or before a TimeStep call when the caller filled the
+// ghosts): stop flags; the ghost and next-state maxima, the reduction ticket and the all-blocks
+// launch's counters and records reset
 cudaError_t launch_step_begin(Ctrl* c, cudaStream_t s);
 // wave-speed maxima over the ghost cells; with form_dt the last CTA forms the step's dt (a
 // TimeStep call: counter, clamps, frame points)
