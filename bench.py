@@ -67,7 +67,7 @@ def peaks():
 
 def ncu_traffic():
     """DRAM bytes per cell update of the stencil kernel from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "mh_kernel_traffic.json")
+    path = os.path.join(ROOT, "profiles", "mh_step_kernel_ffs_traffic.json")
     if os.path.exists(path):
         with open(path) as f:
             return json.load(f)
