@@ -15,6 +15,7 @@
 // cos/sin of the rotation angles precomputed on the host with the same libm calls the
 // reference makes every step.  One thread owns one cell and accumulates its pairs in
 // order, so the sum matches the reference bit for bit.
+#include <algorithm>
 #include <charconv>
 #include <cmath>
 #include <cstdio>
@@ -69,8 +70,13 @@ struct UnsMesh {
     const signed char* __restrict__ pair_sign;
     const int* __restrict__ edge_pair;      // per unique edge: the owning pair
     const int* __restrict__ edge_cell;      // per unique edge: the owning cell
+    const int* __restrict__ edge_nbr;       // per unique edge: the other cell
+    const double* __restrict__ edge_geo;    // [5][nedges]: the owning pair's geo, edge by edge
     double* edge_flux;                      // [4][nedges]: length x rotated-back HLLC flux
     int nedges;
+    // cells are held in a locality order (Morton order of their vertex centroids); orig[i] is
+    // the mesh file's index of device cell i, used in the failure records' keys
+    const int* __restrict__ orig;
 };
 
 // rotate_flow_values (euler_ideal_gas.cpp:152-165) with precomputed cos/sin
@@ -154,6 +160,31 @@ __device__ __forceinline__ int pair_flux(const UnsMesh& m, const double* __restr
     return bad;
 }
 
+// pair_flux of an interior edge's owning pair from the per-edge arrays (the same arithmetic):
+// the edge kernel reads its geometry once, contiguously, instead of through the pair lists
+__device__ __forceinline__ int edge_flux(const UnsMesh& m, const double* __restrict__ U, size_t N, double g,
+                                         double g1, int e, const double* cv, double* f, int* err) {
+    const int k = m.edge_nbr[e];
+    if (!hf_in(k, m.ncells, err)) {
+#pragma unroll
+        for (int v = 0; v < 4; ++v) f[v] = 0.0;
+        return 0;
+    }
+    const size_t E = (size_t)m.nedges;
+    const double ca = m.edge_geo[e], sa = m.edge_geo[E + e];
+    const double cn = m.edge_geo[2 * E + e], sn = m.edge_geo[3 * E + e];
+    const double len = m.edge_geo[4 * E + e];
+    double rc[4], rn[4], nb[4] = {U[k], U[N + k], U[2 * N + k], U[3 * N + k]};
+    rot(ca, sa, cv, rc);
+    rot(ca, sa, nb, rn);
+    double rf[4], fr[4];
+    const int bad = hllc_cons<0>(g, g1, rc, rn, rf);
+    rot(cn, sn, rf, fr);
+#pragma unroll
+    for (int v = 0; v < 4; ++v) f[v] = len * fr[v];
+    return bad;
+}
+
 // edge-based mode, pass 1: one flux per unique interior edge, from its owner's side
 __global__ void __launch_bounds__(kUnsNT, 3) uns_edge_flux_kernel(UnsCtrl* __restrict__ c, UnsMesh m) {
     if (c->done) return;
@@ -166,9 +197,9 @@ __global__ void __launch_bounds__(kUnsNT, 3) uns_edge_flux_kernel(UnsCtrl* __res
         const int i = m.edge_cell[e];
         if (!hf_in(i, m.ncells, &c->err)) continue;
         double cv[4] = {U[i], U[N + i], U[2 * N + i], U[3 * N + i]}, f[4];
-        if (pair_flux(m, U, N, g, g1, m.edge_pair[e], cv, f, &c->err)) {
+        if (edge_flux(m, U, N, g, g1, e, cv, f, &c->err)) {
             ++herr;
-            atomicMin(&c->first_bad, uns_key(c->step, i));
+            atomicMin(&c->first_bad, uns_key(c->step, m.orig[i]));
         }
 #pragma unroll
         for (int v = 0; v < 4; ++v) m.edge_flux[(size_t)v * m.nedges + e] = f[v];
@@ -288,7 +319,7 @@ __global__ void __launch_bounds__(kUnsNT, MINB) uns_step_kernel(UnsCtrl* __restr
                 }
             } else if (pair_flux(m, U, N, g, g1, e, cv, f, &c->err)) {
                 ++herr;
-                atomicMin(&c->first_bad, uns_key(c->step, i));
+                atomicMin(&c->first_bad, uns_key(c->step, m.orig[i]));
             }
 #pragma unroll
             for (int v = 0; v < 4; ++v) acc[v] = acc[v] + f[v];
@@ -303,7 +334,7 @@ __global__ void __launch_bounds__(kUnsNT, MINB) uns_step_kernel(UnsCtrl* __restr
         }
         bool pos;
         mn = nmin(mn, uns_dt_term(g, g1, m.rin[i], un, pos));
-        if (!pos) atomicMin(&c->first_nonpos, uns_key(c->step, i));
+        if (!pos) atomicMin(&c->first_nonpos, uns_key(c->step, m.orig[i]));
     }
     block_min_atomic<kUnsNT>(mn, &c->min_dt[p ^ 1]);
     if (herr) atomicAdd(reinterpret_cast<unsigned long long*>(&c->hllc_errors), (unsigned long long)herr);
@@ -325,6 +356,10 @@ struct hf_uns {
     std::vector<double> verts;          // per cell vertex, x y
     std::vector<int> codes;             // per pair boundary code from the mesh file
     std::vector<int> pair_start, nbr;
+    // the device holds cells in a locality order: perm[d] = file index of device cell d,
+    // iperm[f] = device index of file cell f; stage: a [4][ncells] host buffer for reordering
+    std::vector<int> perm, iperm;
+    std::vector<double> stage;
     long long unmatched = 0;            // pairs with a cell-index code (0: interior) and no match
     long long first_unmatched = -1;     // the first of them, or -1
     std::vector<double> angle, length, area, rin;
@@ -682,6 +717,18 @@ void build_geometry(hf_uns* u) {
     }
 }
 
+// a [4][ncells] state in the mesh file's cell order into u->stage in device order, and back
+void to_device_order(hf_uns* u, const double* cons) {
+    const size_t n = (size_t)u->ncells;
+    for (int v = 0; v < 4; ++v)
+        for (size_t d = 0; d < n; ++d) u->stage[v * n + d] = cons[v * n + (size_t)u->perm[d]];
+}
+void to_file_order(const hf_uns* u, double* cons) {
+    const size_t n = (size_t)u->ncells;
+    for (int v = 0; v < 4; ++v)
+        for (size_t d = 0; d < n; ++d) cons[v * n + (size_t)u->perm[d]] = u->stage[v * n + d];
+}
+
 template <class T>
 int upload(hf_uns* u, T** dst, const std::vector<T>& src) {
     UCK(cudaMalloc(dst, src.size() * sizeof(T) + 16));
@@ -714,63 +761,131 @@ int finish_create(hf_uns* u, const Json& cfg) {
         return ufail(u, HF_ERR_NO_DEVICE, "no CUDA device visible");
     UCK(cudaStreamCreateWithFlags(&u->stream, cudaStreamNonBlocking));
     size_t np = u->pair_start[n];
-    std::vector<double> geo(5 * np), inv(n);
+    // Device cell order: the Morton (Z-order) code of each cell's vertex mean on a 2^16 x 2^16
+    // grid over the mesh's bounding box, ties in file order.  Neighbouring cells then sit close
+    // in memory, so the flux kernels' gathers of neighbour states and edge fluxes hit the caches.
+    // The arithmetic is unchanged: each cell still sums its own pairs in the file's order.
+    {
+        std::vector<double> cx(n), cy(n);
+        double x0 = INFINITY, x1 = -INFINITY, y0 = INFINITY, y1 = -INFINITY;
+        size_t vo = 0;
+        for (int c = 0; c < n; ++c) {
+            double sx = 0.0, sy = 0.0;
+            for (int k = 0; k < u->nverts[c]; ++k) {
+                sx += u->verts[2 * (vo + k)];
+                sy += u->verts[2 * (vo + k) + 1];
+            }
+            vo += u->nverts[c];
+            cx[c] = std::isfinite(sx) ? sx / u->nverts[c] : 0.0;
+            cy[c] = std::isfinite(sy) ? sy / u->nverts[c] : 0.0;
+            x0 = std::min(x0, cx[c]); x1 = std::max(x1, cx[c]);
+            y0 = std::min(y0, cy[c]); y1 = std::max(y1, cy[c]);
+        }
+        auto spread = [](uint32_t v) {   // the 16 bits of v to the even bit positions
+            v &= 0xFFFFu;
+            v = (v | (v << 8)) & 0x00FF00FFu;
+            v = (v | (v << 4)) & 0x0F0F0F0Fu;
+            v = (v | (v << 2)) & 0x33333333u;
+            v = (v | (v << 1)) & 0x55555555u;
+            return v;
+        };
+        const double sxr = x1 > x0 ? 65535.0 / (x1 - x0) : 0.0, syr = y1 > y0 ? 65535.0 / (y1 - y0) : 0.0;
+        std::vector<uint64_t> key(n);
+        for (int c = 0; c < n; ++c) {
+            const uint32_t qx = (uint32_t)((cx[c] - x0) * sxr), qy = (uint32_t)((cy[c] - y0) * syr);
+            key[c] = ((uint64_t)(spread(qx) | (spread(qy) << 1)) << 32) | (uint32_t)c;
+        }
+        std::sort(key.begin(), key.end());
+        u->perm.resize(n);
+        u->iperm.resize(n);
+        for (int d = 0; d < n; ++d) {
+            u->perm[d] = (int)(key[d] & 0xFFFFFFFFu);
+            u->iperm[u->perm[d]] = d;
+        }
+        u->stage.resize((size_t)4 * n);
+    }
+    const std::vector<int>& perm = u->perm;
+    const std::vector<int>& iperm = u->iperm;
+    // pairs in device order: device cell d holds the pairs of file cell perm[d], in their order
+    std::vector<int> dps(n + 1, 0), qmap(np);   // qmap[device pair] = file pair
+    for (int d = 0; d < n; ++d) {
+        const int f = perm[d];
+        dps[d + 1] = dps[d] + u->nverts[f];
+        for (int k = 0; k < u->nverts[f]; ++k) qmap[(size_t)dps[d] + k] = u->pair_start[f] + k;
+    }
+    std::vector<int> dnbr(np);
+    std::vector<double> geo(5 * np), inv(n), drin(n);
     for (size_t e = 0; e < np; ++e) {
-        double a = u->angle[e] * (M_PI / 180.0);
-        double an = (-1.0 * u->angle[e]) * (M_PI / 180.0);
+        const size_t q = (size_t)qmap[e];
+        const int k = u->nbr[q];
+        dnbr[e] = k >= 0 ? iperm[k] : k;
+        double a = u->angle[q] * (M_PI / 180.0);
+        double an = (-1.0 * u->angle[q]) * (M_PI / 180.0);
         geo[e] = std::cos(a);
         geo[np + e] = std::sin(a);
         geo[2 * np + e] = std::cos(an);
         geo[3 * np + e] = std::sin(an);
-        geo[4 * np + e] = u->length[e];
+        geo[4 * np + e] = u->length[q];
     }
-    for (int c = 0; c < n; ++c) inv[c] = 1.0 / u->area[c];
+    for (int d = 0; d < n; ++d) {
+        inv[d] = 1.0 / u->area[perm[d]];
+        drin[d] = u->rin[perm[d]];
+    }
     int r;
-    int* ps; int* nb; double* g; double* ia; double* ri;
-    if ((r = upload(u, &ps, u->pair_start)) || (r = upload(u, &nb, u->nbr)) || (r = upload(u, &g, geo)) ||
-        (r = upload(u, &ia, inv)) || (r = upload(u, &ri, u->rin)))
+    int* ps; int* nb; double* g; double* ia; double* ri; int* org;
+    if ((r = upload(u, &ps, dps)) || (r = upload(u, &nb, dnbr)) || (r = upload(u, &g, geo)) ||
+        (r = upload(u, &ia, inv)) || (r = upload(u, &ri, drin)) || (r = upload(u, &org, perm)))
         return r;
-    // unique interior edges, owned by the lower-indexed cell (edge-based mode)
+    // unique interior edges (edge-based mode), owned by the cell with the lower file index, listed
+    // in device order of their owners; each with its owner pair's geometry, contiguous by edge
     {
-        std::vector<int> pe(np, -1), ep, ec;
+        std::vector<int> pe(np, -1), ep, ec, en;
         std::vector<signed char> sg(np, 0);
-        for (int c = 0; c < n; ++c)
-            for (int q = u->pair_start[c]; q < u->pair_start[c + 1]; ++q) {
-                const int k = u->nbr[q];
+        for (int d = 0; d < n; ++d)
+            for (int q = dps[d]; q < dps[d + 1]; ++q) {
+                const int k = dnbr[q];
                 if (k < 0) continue;
-                if (c < k) {
+                if (perm[d] < perm[k]) {
                     pe[q] = (int)ep.size();
                     sg[q] = 1;
                     ep.push_back(q);
-                    ec.push_back(c);
+                    ec.push_back(d);
+                    en.push_back(k);
                 }
             }
         // the partner side: the owner cell's pair facing this cell (its last such pair, should a
         // degenerate mesh hold two)
-        for (int c = 0; c < n; ++c)
-            for (int q = u->pair_start[c]; q < u->pair_start[c + 1]; ++q) {
-                const int k = u->nbr[q];
-                if (k < 0 || c < k) continue;
+        for (int d = 0; d < n; ++d)
+            for (int q = dps[d]; q < dps[d + 1]; ++q) {
+                const int k = dnbr[q];
+                if (k < 0 || perm[d] < perm[k]) continue;
                 int own = -1;
-                for (int o = u->pair_start[k + 1] - 1; o >= u->pair_start[k] && own < 0; --o)
-                    if (u->nbr[o] == c) own = o;
+                for (int o = dps[k + 1] - 1; o >= dps[k] && own < 0; --o)
+                    if (dnbr[o] == d) own = o;
                 if (own < 0) continue;                  // unmatched: keep the per-side flux
                 pe[q] = pe[own];
                 sg[q] = -1;
             }
-        int* d_pe; signed char* d_sg; int* d_ep; int* d_ec; double* d_ef;
+        const size_t ne = ep.size();
+        std::vector<double> eg(5 * ne);
+        for (size_t e = 0; e < ne; ++e)
+            for (int j = 0; j < 5; ++j) eg[j * ne + e] = geo[(size_t)j * np + ep[e]];
+        int* d_pe; signed char* d_sg; int* d_ep; int* d_ec; int* d_en; double* d_eg; double* d_ef;
         if ((r = upload(u, &d_pe, pe)) || (r = upload(u, &d_sg, sg)) || (r = upload(u, &d_ep, ep)) ||
-            (r = upload(u, &d_ec, ec)))
+            (r = upload(u, &d_ec, ec)) || (r = upload(u, &d_en, en)) || (r = upload(u, &d_eg, eg)))
             return r;
-        UCK(cudaMalloc(&d_ef, 4 * (ep.size() + 1) * sizeof(double)));
+        UCK(cudaMalloc(&d_ef, 4 * (ne + 1) * sizeof(double)));
         u->allocs.push_back(d_ef);
         u->d_pair_edge = d_pe;
         u->d_pair_sign = d_sg;
         u->dm.edge_pair = d_ep;
         u->dm.edge_cell = d_ec;
+        u->dm.edge_nbr = d_en;
+        u->dm.edge_geo = d_eg;
         u->dm.edge_flux = d_ef;
-        u->dm.nedges = (int)ep.size();
+        u->dm.nedges = (int)ne;
     }
+    u->dm.orig = org;
     u->dm.ncells = n;
     u->dm.pair_start = ps;
     u->dm.nbr = nb;
@@ -979,7 +1094,8 @@ int hf_uns_set_state(hf_uns* u, const double* cons) {
     if (r) return r;
     int p = (int)(s & 1);
     size_t bytes = (size_t)4 * u->ncells * sizeof(double);
-    UCK(cudaMemcpyAsync(u->dm.U[p], cons, bytes, cudaMemcpyHostToDevice, u->stream));
+    to_device_order(u, cons);
+    UCK(cudaMemcpyAsync(u->dm.U[p], u->stage.data(), bytes, cudaMemcpyHostToDevice, u->stream));
     unsigned long long init = 0;
     double big = 1e16;
     std::memcpy(&init, &big, 8);
@@ -997,7 +1113,8 @@ int hf_uns_get_state(hf_uns* u, double* cons) {
     long long s;
     int r = read_step(u, &s);
     if (r) return r;
-    UCK(cudaMemcpy(cons, u->dm.U[s & 1], (size_t)4 * u->ncells * sizeof(double), cudaMemcpyDeviceToHost));
+    UCK(cudaMemcpy(u->stage.data(), u->dm.U[s & 1], (size_t)4 * u->ncells * sizeof(double), cudaMemcpyDeviceToHost));
+    to_file_order(u, cons);
     return HF_OK;
 }
 
@@ -1272,7 +1389,10 @@ int hf_uns_frame_pop(hf_uns* u, double* cons, double* t, int64_t* index) {
     UCK(cudaMemcpy(&C, u->dctrl, sizeof C, cudaMemcpyDeviceToHost));
     if (C.captured == u->drained) return ufail(u, HF_ERR_STATE, "no frame pending");
     const long long slot = u->drained % u->ring_slots, len = 4LL * u->ncells;
-    if (cons) UCK(cudaMemcpy(cons, u->ring + slot * len, (size_t)len * sizeof(double), cudaMemcpyDeviceToHost));
+    if (cons) {
+        UCK(cudaMemcpy(u->stage.data(), u->ring + slot * len, (size_t)len * sizeof(double), cudaMemcpyDeviceToHost));
+        to_file_order(u, cons);
+    }
     if (t) *t = C.ring_t[slot];
     if (index) *index = C.ring_idx[slot];
     u->drained += 1;
