@@ -237,14 +237,22 @@ HF_HD double limiter(double r) {
     }
 }
 
+// The difference clamp of calculate_slope_limiters (muscl_hancock.cpp:78-84): |d| <= tol gives
+// tol for d = +-0 and tol * sgn(d) otherwise, i.e. tol with d's sign (NaN fails |d| <= tol).  On
+// the bit pattern: the FP64 compares, the conversion and the multiplication of the literal form
+// would all run on the FP64 pipe, and the clamp fires in every uniform region.
+HF_HD double clamp_tol(double d) {
+    const uint64_t b = f64_bits(d);
+    if ((b & kAbs) > f64_bits(kTol)) return d;
+    if ((b & kAbs) == 0) return kTol;
+    return f64_from(f64_bits(kTol) | (b & ~kAbs));
+}
+
 // limited slope of one variable from the three cell averages (um, u0, up)
 template <int LIM>
 HF_HD double slope(double um, double u0, double up) {
     double dl = u0 - um, dr = up - u0;
-    double dlc = dl, drc = dr;
-    if (abs_le(dlc, kTol)) dlc = (dlc == 0.0) ? kTol : kTol * sgn(dlc);
-    if (abs_le(drc, kTol)) drc = (drc == 0.0) ? kTol : kTol * sgn(drc);
-    double xi = limiter<LIM>(div_rn(dlc, drc));
+    double xi = limiter<LIM>(div_rn(clamp_tol(dl), clamp_tol(dr)));
     return xi * (half(dl) + half(dr));
 }
 

@@ -44,14 +44,21 @@ constexpr int NOUT = 4;
 constexpr int OFF_W1 = 0, OFF_B1 = OFF_W1 + H * NIN, OFF_W2 = OFF_B1 + H, OFF_B2 = OFF_W2 + H * H,
               OFF_W3 = OFF_B2 + H, OFF_B3 = OFF_W3 + NOUT * H, NPARAM = OFF_B3 + NOUT;
 
+// the hardware's approximate tanh (one MUFU instruction, absolute error about 2^-11): GELU's
+// epilogue cost, which bounds the MLP kernels, falls by half against the accurate tanhf
+__device__ __forceinline__ float tanh_fast(float x) {
+    float y;
+    asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
 __device__ __forceinline__ float gelu(float z) {
     const float k = 0.7978845608028654f;   // sqrt(2/pi)
-    return 0.5f * z * (1.0f + tanhf(k * (z + 0.044715f * z * z * z)));
+    return 0.5f * z * (1.0f + tanh_fast(k * (z + 0.044715f * z * z * z)));
 }
 __device__ __forceinline__ float gelu_grad(float z) {
     const float k = 0.7978845608028654f;
     const float u = k * (z + 0.044715f * z * z * z);
-    const float t = tanhf(u);
+    const float t = tanh_fast(u);
     return 0.5f * (1.0f + t) + 0.5f * z * (1.0f - t * t) * k * (1.0f + 3.0f * 0.044715f * z * z);
 }
 
@@ -796,9 +803,25 @@ hf::lc::Grid grid(const hf_lc* L) {
 int nfaces(const hf_lc* L) { return 2 * (L->n + 1) * L->n; }
 int blocks_for(long long n, int t) { long long b = (n + t - 1) / t; return (int)(b > 4096 ? 4096 : (b < 1 ? 1 : b)); }
 
+// CTAs of the MLP forward: 4 per SM.  Each loads the weights once and then walks its tiles;
+// measured on the 512^2 learned step, 2 / 3 / 4 / 5 / 6 CTAs per SM gave 1175 / 1238 / 1257 /
+// 1243 / 987 Mcell-updates/s (shared memory would allow 6).
+int forward_grid_cap() {
+    static int cap = 0;
+    if (cap == 0) {
+        int sms = 0, dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1)
+            return 4 * 152;
+        cap = 4 * sms;
+    }
+    return cap;
+}
+
 void launch_forward(hf_lc* L, int nf, bool save_acts) {
     const int tiles = (nf + hf::lc::kTcRows - 1) / hf::lc::kTcRows;
-    const int grid = tiles < 4 * 152 ? tiles : 4 * 152;
+    const int cap = forward_grid_cap();
+    const int grid = tiles < cap ? tiles : cap;
     hf::lc::mlp_forward_kernel<<<grid, hf::lc::kTcRows, hf::lc::mlp_forward_smem(), L->stream>>>(
         L->X, nf, L->Wb, L->P, L->Y, save_acts ? L->Z1 : nullptr, save_acts ? L->Z2 : nullptr, L->derr);
 }

@@ -62,8 +62,10 @@ def test_mlp_forward_on_tensor_cores_matches_oracle():
         ls.set_params(p)
         y = ls.mlp_forward(x)
         ref, _ = M.forward(p, x)
-        # FP32 accumulation order and tanhf vs tanh: BF16-level agreement
-        np.testing.assert_allclose(y, ref, rtol=2e-2, atol=2e-3)
+        # FP32 accumulation order, and GELU's tanh taken from the hardware approximation
+        # (absolute error about 2^-11) where the oracle has numpy's: now and then an activation
+        # rounds to the neighbouring BF16 value -- BF16-level agreement, and a small mean
+        np.testing.assert_allclose(y, ref, rtol=2e-2, atol=4e-3)
         assert np.abs(y - ref).mean() < 1e-3
 
 
@@ -209,3 +211,50 @@ def test_coarsen_on_device_equals_box_filter():
     got = s.coarsen(0, 4)
     assert got.dtype == np.float32 and got.shape == (4, 32, 32)
     np.testing.assert_allclose(got, want, rtol=2e-7, atol=1e-12)
+
+
+@pytest.mark.gpu
+def test_learned_solver_lowers_the_end_time_error_in_both_families():
+    """What the trained network gains where it counts: the error at the end of a run.  Trained on
+    4x box-filtered 256^2 FP64 runs of the plain solver (8 seeded four-quadrant Riemann problems, 8
+    shock-bubble flows), the learned 64^2 solver (change guard, bound 2) ends with a lower L1
+    density error against the filtered 256^2 solution than the plain coarse solver on held-out
+    cases of both families: two Riemann seeds and two bubble placements it was not trained on.
+    (Seen across training seeds: learned / plain error 0.65-0.90 on these four cases.)"""
+    from hyperflow_gb300 import cases
+    from hyperflow_gb300.learned import (LearnedSolver, change_weights, evaluate_learned, evaluate_plain,
+                                         fine_sequence, init_params, train)
+    nf, f = 256, 4
+
+    def rp(seed):
+        return lambda n: cases.random_quadrant_case(n, seed)
+
+    def sb(b, r):
+        return lambda n: cases.shock_bubble_case(n, bubble=b, radius=r, t_end=1.0)
+
+    rng = np.random.default_rng(1)
+    train_sets = [(rp(100 + k), None) for k in range(8)]
+    for _ in range(8):
+        b = (float(rng.uniform(0.35, 0.5)), float(rng.uniform(0.4, 0.6)))
+        train_sets.append((sb(b, float(rng.uniform(0.15, 0.22))), 0.25))
+    pairs = []
+    for fn, t_end in train_sets:
+        c = fn(nf)
+        st, dts = fine_sequence(c, t_end if t_end is not None else c["simulation"]["t_end"], factor=f)
+        pairs += [(st[k], st[k + 1], dts[k]) for k in range(len(dts))]
+    ls = LearnedSolver(nf // f, f / nf)
+    ls.set_params(init_params(0))
+    losses, _ = train(ls, pairs, 6000, lr=2e-3, seed=0, w=change_weights(pairs))
+    params = ls.params()
+    ls.close()
+    assert np.isfinite(losses).all()
+    held = {"riemann_200": (rp(200), rp(200)(nf)["simulation"]["t_end"]),
+            "riemann_201": (rp(201), rp(201)(nf)["simulation"]["t_end"]),
+            "bubble_a": (sb((0.42, 0.55), 0.2), 0.2), "bubble_b": (sb((0.38, 0.45), 0.17), 0.2)}
+    ratios = {}
+    for name, (fn, t_end) in held.items():
+        res, ref, U0 = evaluate_plain(fn, nf, t_end, factor=f)
+        learned = evaluate_learned(t_end, params, ref, U0, bound=2.0)
+        ratios[name] = learned["l1_rho"] / res["fp32_plain"]["l1_rho"]
+    assert all(r < 0.97 for r in ratios.values()), ratios
+    assert np.mean(list(ratios.values())) < 0.9, ratios
