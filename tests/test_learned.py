@@ -229,8 +229,8 @@ def test_learned_solver_lowers_the_end_time_error_in_both_families():
     def rp(seed):
         return lambda n: cases.random_quadrant_case(n, seed)
 
-    def sb(b, r):
-        return lambda n: cases.shock_bubble_case(n, bubble=b, radius=r, t_end=1.0)
+    def sb(b, r, t_end=1.0):
+        return lambda n: cases.shock_bubble_case(n, bubble=b, radius=r, t_end=t_end)
 
     rng = np.random.default_rng(1)
     train_sets = [(rp(100 + k), None) for k in range(8)]
@@ -250,7 +250,7 @@ def test_learned_solver_lowers_the_end_time_error_in_both_families():
     assert np.isfinite(losses).all()
     held = {"riemann_200": (rp(200), rp(200)(nf)["simulation"]["t_end"]),
             "riemann_201": (rp(201), rp(201)(nf)["simulation"]["t_end"]),
-            "bubble_a": (sb((0.42, 0.55), 0.2), 0.2), "bubble_b": (sb((0.38, 0.45), 0.17), 0.2)}
+            "bubble_a": (sb((0.42, 0.55), 0.2, 0.2), 0.2), "bubble_b": (sb((0.38, 0.45), 0.17, 0.2), 0.2)}
     ratios = {}
     for name, (fn, t_end) in held.items():
         res, ref, U0 = evaluate_plain(fn, nf, t_end, factor=f)
