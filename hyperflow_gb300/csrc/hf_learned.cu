@@ -271,7 +271,8 @@ __global__ void __launch_bounds__(kFeatNT) features_kernel(const float4* __restr
 // rounded to BF16 and stored as the next layer's A operand.  The output layer runs with
 // N = 16 (rows 4..15 of its weight tile are zero).
 constexpr int kTcRows = 128;       // faces per tile = threads per CTA = TMEM lanes
-constexpr int kTcCols = 64;        // TMEM columns held by a CTA (one layer's accumulator)
+constexpr int kTcTiles = 2;        // tiles in flight per CTA: one's MMA overlaps the other's epilogue
+constexpr int kTcCols = 64 * kTcTiles;   // TMEM columns held by a CTA (one accumulator per tile)
 constexpr uint32_t kTcWaitLimit = 1u << 22;
 
 __device__ __forceinline__ uint32_t canon_off(int r, int k) {   // bytes; K = 64 BF16 per row
@@ -338,16 +339,19 @@ __device__ __forceinline__ void put8(unsigned char* tile, int r, int k0, const f
 }
 
 struct __align__(1024) TcSmem {
-    unsigned char a[kTcRows * 64 * 2];     // activations of the tile (A operand)
+    unsigned char a[kTcTiles][kTcRows * 64 * 2];   // activations of each tile (A operands)
     unsigned char w1[64 * 64 * 2], w2[64 * 64 * 2], w3[16 * 64 * 2];
     float b1[64], b2[64], b3[4];
-    uint64_t bar;
+    uint64_t bar[kTcTiles];
     uint32_t taddr;
 };
 
 // Y[nf][4] = MLP(X).  When Z1/Z2 are given (training), the hidden pre-activations are saved.
-// A bounded wait that gives up sets *err, waits (bounded) for the CTA's MMAs in flight,
-// frees the TMEM columns and returns.
+// A CTA takes its tiles two at a time (tiles blockIdx.x + k gridDim.x, k = 2i and 2i + 1), each
+// with its own operand buffer, TMEM accumulator (64 columns) and mbarrier, and alternates between
+// them: while the tensor cores run one tile's layer, the CTA's threads run the other tile's
+// epilogue.  A bounded wait that gives up sets *err, waits (bounded) for the CTA's MMAs in
+// flight, frees the TMEM columns and returns.
 __global__ void __launch_bounds__(kTcRows)
 mlp_forward_kernel(const __nv_bfloat16* __restrict__ X, int nf, const __nv_bfloat16* __restrict__ Wb,
                    const float* __restrict__ P, float* __restrict__ Y, float* __restrict__ Z1,
@@ -371,7 +375,8 @@ mlp_forward_kernel(const __nv_bfloat16* __restrict__ X, int nf, const __nv_bfloa
     }
     for (int k = tid; k < H; k += kTcRows) { S.b1[k] = P[OFF_B1 + k]; S.b2[k] = P[OFF_B2 + k]; }
     if (tid < NOUT) S.b3[tid] = P[OFF_B3 + tid];
-    if (tid == 0) mbar_init(&S.bar, 1);
+    if (tid == 0)
+        for (int k = 0; k < kTcTiles; ++k) mbar_init(&S.bar[k], 1);
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&S.taddr)),
                      "r"(kTcCols)
@@ -384,74 +389,103 @@ mlp_forward_kernel(const __nv_bfloat16* __restrict__ X, int nf, const __nv_bfloa
     tc_after_sync();
     const uint32_t tm = S.taddr;
     const uint32_t tm_row = tm + ((uint32_t)(warp * 32) << 16);   // this warp's lane quarter
-    const uint32_t sa = smem_u32(S.a), sw1 = smem_u32(S.w1), sw2 = smem_u32(S.w2), sw3 = smem_u32(S.w3);
-    uint32_t phase = 0;
+    const uint32_t sw1 = smem_u32(S.w1), sw2 = smem_u32(S.w2), sw3 = smem_u32(S.w3);
+    uint32_t phase[kTcTiles] = {0u, 0u};
+    int pending[kTcTiles] = {0, 0};   // MMA groups committed and not yet waited for
     bool failed = false;
+    const int ntiles = (nf + kTcRows - 1) / kTcRows;
 
-    for (int base = blockIdx.x * kTcRows; base < nf && !failed; base += gridDim.x * kTcRows) {
-        const int face = base + tid;
-        const bool valid = face < nf;
-        // features -> A
-        {
-            const uint4* x = reinterpret_cast<const uint4*>(X + (size_t)(valid ? face : 0) * NIN);
+    // one layer's 4 MMAs of tile k (thread 0), committed to the tile's mbarrier
+    auto issue = [&](int k, int layer) {
+        if (tid == 0) {
+            tc_after_sync();
+            const uint32_t wb = layer == 0 ? sw1 : (layer == 1 ? sw2 : sw3);
+            const uint32_t id = idesc_bf16(layer == 2 ? 16 : 64);
+            const uint32_t sa = smem_u32(S.a[k]);
+#pragma unroll
+            for (int kk = 0; kk < 4; ++kk)
+                tc_mma(tm + (uint32_t)(k * 64), smem_desc(sa + kk * 256), smem_desc(wb + kk * 256), id, kk);
+            tc_commit(&S.bar[k]);
+        }
+        ++pending[k];
+    };
+    // the writes of the tiles' operands are visible to the tensor cores before the next issue
+    auto publish = [&]() {
+        async_smem_fence();
+        tc_before_sync();
+        __syncthreads();
+    };
+
+    for (int t0 = blockIdx.x; t0 < ntiles && !failed; t0 += kTcTiles * gridDim.x) {
+        int face[kTcTiles];
+        bool valid[kTcTiles];
+        // features -> A; a tile past the last is computed on zeros and not stored
+#pragma unroll
+        for (int k = 0; k < kTcTiles; ++k) {
+            const int t = t0 + k * gridDim.x;
+            face[k] = t * kTcRows + tid;
+            valid[k] = t < ntiles && face[k] < nf;
+            const uint4* x = reinterpret_cast<const uint4*>(X + (size_t)(valid[k] ? face[k] : 0) * NIN);
 #pragma unroll
             for (int kb = 0; kb < 8; ++kb)
-                *reinterpret_cast<uint4*>(S.a + canon_off(tid, kb * 8)) = valid ? x[kb] : make_uint4(0u, 0u, 0u, 0u);
+                *reinterpret_cast<uint4*>(S.a[k] + canon_off(tid, kb * 8)) = valid[k] ? x[kb] : make_uint4(0u, 0u, 0u, 0u);
         }
+        publish();
+        for (int k = 0; k < kTcTiles; ++k) issue(k, 0);
 #pragma unroll 1
-        for (int layer = 0; layer < 3; ++layer) {
-            async_smem_fence();
-            tc_before_sync();
-            __syncthreads();
-            if (tid == 0) {
+        for (int layer = 0; layer < 3 && !failed; ++layer) {
+#pragma unroll 1
+            for (int k = 0; k < kTcTiles; ++k) {
+                const bool ok = mbar_wait_bounded(&S.bar[k], phase[k], kTcWaitLimit);
+                if (__syncthreads_or(!ok)) {
+                    failed = true;
+                    break;
+                }
+                phase[k] ^= 1u;
+                --pending[k];
                 tc_after_sync();
-                const uint32_t wb = layer == 0 ? sw1 : (layer == 1 ? sw2 : sw3);
-                const uint32_t id = idesc_bf16(layer == 2 ? 16 : 64);
-#pragma unroll
-                for (int kk = 0; kk < 4; ++kk)
-                    tc_mma(tm, smem_desc(sa + kk * 256), smem_desc(wb + kk * 256), id, kk);
-                tc_commit(&S.bar);
-            }
-            const bool ok = mbar_wait_bounded(&S.bar, phase, kTcWaitLimit);
-            phase ^= 1u;
-            if (__syncthreads_or(!ok)) {
-                if (tid == 0) {
-                    atomicExch(err, 1);
-                    mbar_wait_bounded(&S.bar, phase ^ 1u, kTcWaitLimit);   // let the MMAs land
-                }
-                failed = true;
-                break;
-            }
-            tc_after_sync();
-            if (layer < 2) {
-                const float* b = layer == 0 ? S.b1 : S.b2;
-                float* Zs = layer == 0 ? Z1 : Z2;
+                const uint32_t tcol = tm_row + (uint32_t)(k * 64);
+                if (layer < 2) {
+                    const float* b = layer == 0 ? S.b1 : S.b2;
+                    float* Zs = layer == 0 ? Z1 : Z2;
 #pragma unroll 1
-                for (int q = 0; q < 4; ++q) {
-                    float z[16];
-                    tc_ld16(tm_row + q * 16, z);
-                    float h[16];
+                    for (int q = 0; q < 4; ++q) {
+                        float z[16];
+                        tc_ld16(tcol + q * 16, z);
+                        float h[16];
 #pragma unroll
-                    for (int k = 0; k < 16; ++k) {
-                        z[k] += b[q * 16 + k];
-                        h[k] = gelu(z[k]);
-                    }
-                    if (Zs && valid) {
-                        float4* zo = reinterpret_cast<float4*>(Zs + (size_t)face * H + q * 16);
+                        for (int j = 0; j < 16; ++j) {
+                            z[j] += b[q * 16 + j];
+                            h[j] = gelu(z[j]);
+                        }
+                        if (Zs && valid[k]) {
+                            float4* zo = reinterpret_cast<float4*>(Zs + (size_t)face[k] * H + q * 16);
 #pragma unroll
-                        for (int k = 0; k < 4; ++k) zo[k] = make_float4(z[4 * k], z[4 * k + 1], z[4 * k + 2], z[4 * k + 3]);
+                            for (int j = 0; j < 4; ++j)
+                                zo[j] = make_float4(z[4 * j], z[4 * j + 1], z[4 * j + 2], z[4 * j + 3]);
+                        }
+                        put8(S.a[k], tid, q * 16, h);
+                        put8(S.a[k], tid, q * 16 + 8, h + 8);
                     }
-                    put8(S.a, tid, q * 16, h);
-                    put8(S.a, tid, q * 16 + 8, h + 8);
+                    publish();
+                    issue(k, layer + 1);
+                } else {
+                    float y[16];
+                    tc_ld16(tcol, y);
+                    if (valid[k])
+                        *reinterpret_cast<float4*>(Y + (size_t)face[k] * 4) =
+                            make_float4(y[0] + S.b3[0], y[1] + S.b3[1], y[2] + S.b3[2], y[3] + S.b3[3]);
                 }
-            } else {
-                float y[16];
-                tc_ld16(tm_row, y);
-                if (valid)
-                    *reinterpret_cast<float4*>(Y + (size_t)face * 4) =
-                        make_float4(y[0] + S.b3[0], y[1] + S.b3[1], y[2] + S.b3[2], y[3] + S.b3[3]);
             }
         }
+    }
+    if (failed && tid == 0) {
+        atomicExch(err, 1);
+        for (int k = 0; k < kTcTiles; ++k)   // let the MMAs in flight land
+            for (; pending[k] > 0; --pending[k]) {
+                mbar_wait_bounded(&S.bar[k], phase[k], kTcWaitLimit);
+                phase[k] ^= 1u;
+            }
     }
     tc_before_sync();
     __syncthreads();
@@ -873,6 +907,9 @@ int hf_lc_create(int n, double dx, double gamma, double cfl, int limiter, hf_lc*
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return lfail(L, HF_ERR_NO_DEVICE, "no CUDA device");
     L->n = n; L->dx = dx; L->gamma = gamma; L->cfl = cfl; L->lim = limiter;
     LCK(cudaStreamCreateWithFlags(&L->stream, cudaStreamNonBlocking));
+    // the MLP kernel's two operand buffers take it past the 48 KB default
+    LCK(cudaFuncSetAttribute(hf::lc::mlp_forward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)hf::lc::mlp_forward_smem()));
     const size_t cells = (size_t)n * n, nf = nfaces(L);
     int r;
     if ((r = alloc(L, &L->U[0], 4 * cells)) || (r = alloc(L, &L->U[1], 4 * cells)) || (r = alloc(L, &L->F, 4 * nf)) ||

@@ -56,8 +56,10 @@ def test_mlp_forward_on_tensor_cores_matches_oracle():
     from oracle import mlp_oracle as M
     from hyperflow_gb300.learned import LearnedSolver
     rng = np.random.default_rng(4)
-    ls = LearnedSolver(64, 1 / 64)
-    for nf in (1000, 17, 2 * 65 * 64):          # partial tiles and a full grid's faces
+    ls = LearnedSolver(300, 1 / 300)   # room for 180,600 faces
+    # partial tiles, a full grid's faces, and more 128-face tiles than the kernel has CTAs (4 per
+    # SM), so that CTAs run two tiles at a time, the second of a pair partial or absent
+    for nf in (1000, 17, 2 * 65 * 64, 160_000 + 77):
         p, x = _rand_case(rng, nf)
         ls.set_params(p)
         y = ls.mlp_forward(x)
