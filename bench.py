@@ -568,7 +568,9 @@ def main():
     achieved = BYTES_PER_CELL * cells * args.steps / (stencil_ms / 1e3) / 1e9
     traffic = None
     tr = ncu_traffic()
-    all_blocks = args.scheme == "MUSCLHancock" and nb <= 4 and not args.per_block_launches
+    tiles = sum(-(-b["x_cells"] // 32) * -(-b["y_cells"] // 12) for b in case["mesh"]["blocks"])
+    all_blocks = (args.scheme == "MUSCLHancock" and nb <= 4 and not args.per_block_launches
+                  and (nb > 1 or tiles >= 1024))
     per_launch = 1 if all_blocks else nb           # stencil launches per step
     if tr and tr.get("workload") == workload_name(args):
         traffic = tr["dram_bytes_per_cell_update"] * cells / per_launch

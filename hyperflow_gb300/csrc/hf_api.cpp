@@ -26,23 +26,8 @@ namespace {
 
 using hf::Json;
 
-typedef CUresult (*PFN_encodeTiled)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
-                                    const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
-                                    const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
-                                    CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-
-PFN_encodeTiled get_encode() {
-    static PFN_encodeTiled fn = nullptr;
-    if (!fn) {
-        void* p = nullptr;
-        cudaDriverEntryPointQueryResult q;
-        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
-                                             &q) == cudaSuccess &&
-            q == cudaDriverEntryPointSuccess)
-            fn = reinterpret_cast<PFN_encodeTiled>(p);
-    }
-    return fn;
-}
+typedef hf::EncodeTiledFn PFN_encodeTiled;
+PFN_encodeTiled get_encode() { return hf::tensor_map_encoder(); }
 
 struct BlockHost {
     int nx, ny, tx, ty, pitch;
@@ -447,15 +432,24 @@ int build_fill_program(hf_ctx* ctx, std::vector<hf::FillOp>& ops) {
 // every block of a MUSCL-Hancock step in one launch, where the mesh has few enough blocks
 bool step_kernel(const hf_ctx* ctx) { return ctx->scheme == 1 && ctx->plan.nb > 0 && !ctx->block_launches; }
 
+// The all-blocks launch pays a grid barrier per block and the start-up of every resident CTA; a
+// mesh of one block gains nothing from it unless the block fills many waves (measured: a 264^2
+// block 341 Mcell-updates/s against 448 with one launch per block, 1010^2 999 against 986, 4096^2
+// 1173 against 1163).
+constexpr int kStepMinTilesOneBlock = 1024;
+
 void make_plan(hf_ctx* ctx) {
     ctx->plan = hf::StepPlan{};
     if (ctx->scheme != 1 || ctx->nblocks > hf::kStepMaxBlocks) return;
+    hf::StepPlan plan{};
     for (int b = 0; b < ctx->nblocks; ++b) {
-        ctx->plan.tm[b][0] = ctx->tmap[b][0];
-        ctx->plan.tm[b][1] = ctx->tmap[b][1];
-        hf::step_plan_tiles(ctx->plan, b, ctx->blocks[b].nx, ctx->blocks[b].ny);
+        plan.tm[b][0] = ctx->tmap[b][0];
+        plan.tm[b][1] = ctx->tmap[b][1];
+        hf::step_plan_tiles(plan, b, ctx->blocks[b].nx, ctx->blocks[b].ny);
     }
-    ctx->plan.nb = ctx->nblocks;
+    plan.nb = ctx->nblocks;
+    if (ctx->nblocks == 1 && plan.tile_start[1] < kStepMinTilesOneBlock) return;
+    ctx->plan = plan;
 }
 
 int make_tmaps(hf_ctx* ctx) {
@@ -1340,3 +1334,18 @@ int hf_kernel_time(hf_ctx* ctx, int kind, double* ms, int64_t* launches) {
 }
 
 }  // extern "C"
+
+namespace hf {
+EncodeTiledFn tensor_map_encoder() {
+    static EncodeTiledFn fn = nullptr;
+    if (!fn) {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFn>(p);
+    }
+    return fn;
+}
+}  // namespace hf

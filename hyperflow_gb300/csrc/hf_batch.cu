@@ -41,8 +41,8 @@ namespace hf {
 
 struct BatchInst {
     int n;                 // cells per side
-    int tiles;             // unused on device
-    long long off;         // offset (doubles) of the case's [4][n][n] state
+    int pitch;             // doubles per row: n rounded up to even (a TMA row stride is a multiple of 16 bytes)
+    long long off;         // offset (doubles) of the case's [4][n][pitch] state
     double dx, dy;
 };
 
@@ -72,6 +72,8 @@ __device__ __forceinline__ unsigned long long batch_key(long long step, long lon
 struct BatchDev {
     BatchCtrl* ctrl;
     const BatchInst* inst;
+    const CUtensorMap* maps;       // MUSCL-Hancock: per state parity, per case, [2][ninst]
+    int ninst;
     const int* tile_inst;
     const int* tile_xy;            // x0 | (y0 << 16), interior cells
     long long ntiles;
@@ -125,6 +127,8 @@ __device__ __forceinline__ int mirror(int x, int n) {
     return x < 0 ? 0 : (x >= n ? n - 1 : x);   // positions past the 2-cell halo are never used
 }
 
+constexpr unsigned kBatchWaitLimit = 1u << 22;   // bounded mbarrier polls before giving up
+
 __device__ __forceinline__ void cp_async8(void* dst, const void* src) {
     asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
 }
@@ -158,15 +162,52 @@ __device__ __forceinline__ void stage_tile(const BatchDev& d, const double* __re
     const int x0 = xy & 0xffff, y0 = xy >> 16;
     const BatchInst I = d.inst[inst];
     const double* __restrict__ base = U + I.off;
-    const size_t plane = (size_t)I.n * I.n;
+    const size_t plane = (size_t)I.pitch * I.n;
     for (int k = threadIdx.x; k < T::U_SIZE; k += NT) {
         const int v = k / (T::UY * T::UX);
         const int r = k - v * (T::UY * T::UX);
         const int ly = r / T::UX, lx = r - ly * T::UX;
         const int gx = mirror(x0 + lx - T::H, I.n), gy = mirror(y0 + ly - T::H, I.n);
-        cp_async8(sU + k, base + v * plane + (size_t)gy * I.n + gx);
+        cp_async8(sU + k, base + v * plane + (size_t)gy * I.pitch + gx);
     }
     cp_async_commit();
+}
+
+// MUSCL-Hancock tiles by TMA: one 3-D box (the tile and its 2-cell halo, all four variables) of
+// the case's state per tile, issued by thread 0 on `bar`; positions outside the case arrive as
+// zeros and mirror_halo then writes the transmissive ghosts there.  (The box's x start, x0 - 2, is
+// even, as a TMA copy of FP64 needs; Godunov's 1-cell halo would start at an odd x, so Godunov
+// batches keep the element-wise loader.)
+template <int TX, int TY>
+__device__ __forceinline__ void tma_tile(const BatchDev& d, int p, long long t, double* sU, uint64_t* bar) {
+    using T = BatchTile<1, TX, TY>;
+    const int inst = d.tile_inst[t];
+    const int xy = d.tile_xy[t];
+    const int x0 = xy & 0xffff, y0 = xy >> 16;
+    // the previous tile's reads and writes of this buffer (generic proxy) come before the copy
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    mbar_expect_tx(bar, T::U_SIZE * 8);
+    tma_load_3d(sU, &d.maps[(size_t)p * d.ninst + inst], bar, x0 - T::H, y0 - T::H, 0);
+}
+
+// The halo positions outside the case (within 2 cells of it) take the mirrored interior values,
+// the transmissive ghosts (transmissive_boundary.cpp:25-104; corners mirrored in x and in y).
+// Every source is an interior cell inside the same box.  Positions further out are never read.
+template <int TX, int TY, int NT>
+__device__ __forceinline__ void mirror_halo(double* sU, int x0, int y0, int n) {
+    using T = BatchTile<1, TX, TY>;
+    constexpr int H = T::H;
+    if (x0 >= H && y0 >= H && x0 + TX + H <= n && y0 + TY + H <= n) return;   // the box lies inside the case
+    for (int k = threadIdx.x; k < T::U_SIZE; k += NT) {
+        const int v = k / (T::UY * T::UX);
+        const int r = k - v * (T::UY * T::UX);
+        const int ly = r / T::UX, lx = r - ly * T::UX;
+        const int gx = x0 + lx - H, gy = y0 + ly - H;
+        if (gx >= 0 && gx < n && gy >= 0 && gy < n) continue;
+        if (gx < -H || gy < -H || gx >= n + H || gy >= n + H) continue;
+        const int sx = mirror(gx, n) - x0 + H, sy = mirror(gy, n) - y0 + H;
+        sU[k] = sU[(v * T::UY + sy) * T::UX + sx];
+    }
 }
 
 template <int SCHEME, int TX, int TY, int NT, int STAGES, int MINB>
@@ -187,6 +228,17 @@ __global__ void __launch_bounds__(NT, MINB) batch_kernel(BatchDev d, int nsteps)
     const double g = c->gamma, g1 = c->g1, cfl = c->cfl;
     const int lim = c->limiter, ninst = c->ninst;
     int herr = 0;
+    // MUSCL-Hancock: one mbarrier per staging buffer for the TMA loads, and its phase
+    __shared__ uint64_t tbar[2];
+    uint32_t tph[2] = {0u, 0u};
+    bool failed = false;
+    if (SCHEME == 1) {
+        if (threadIdx.x == 0) {
+            mbar_init(&tbar[0], 1);
+            mbar_init(&tbar[1], 1);
+        }
+        __syncthreads();
+    }
 
     for (int s = 0; s < nsteps; ++s) {
         const long long step = step0 + s;
@@ -200,11 +252,29 @@ __global__ void __launch_bounds__(NT, MINB) batch_kernel(BatchDev d, int nsteps)
         const double* __restrict__ U = d.U[p];
         double* __restrict__ Un = d.U[p ^ 1];
         long long t = blockIdx.x;
-        if (STAGES == 2 && t < d.ntiles) stage_tile<SCHEME, TX, TY, NT>(d, U, t, sUb[0]);
+        if (STAGES == 2 && t < d.ntiles) {
+            if (SCHEME == 1) {
+                if (threadIdx.x == 0) tma_tile<TX, TY>(d, p, t, sUb[0], &tbar[0]);
+            } else {
+                stage_tile<SCHEME, TX, TY, NT>(d, U, t, sUb[0]);
+            }
+        }
         int buf = 0;
         for (; t < d.ntiles; t += gridDim.x) {
             double* sU = sUb[STAGES == 2 ? buf : 0];
-            if (STAGES == 1) {
+            const int sb = STAGES == 2 ? buf : 0;   // this tile's staging buffer and mbarrier
+            if (SCHEME == 1) {
+                if (threadIdx.x == 0) {
+                    if (STAGES == 1) tma_tile<TX, TY>(d, p, t, sU, &tbar[0]);
+                    else if (t + gridDim.x < d.ntiles) tma_tile<TX, TY>(d, p, t + gridDim.x, sUb[buf ^ 1], &tbar[buf ^ 1]);
+                }
+                const bool ok = mbar_wait_bounded(&tbar[sb], tph[sb], kBatchWaitLimit);
+                if (__syncthreads_or(!ok)) {
+                    failed = true;
+                    break;
+                }
+                tph[sb] ^= 1u;
+            } else if (STAGES == 1) {
                 stage_tile<SCHEME, TX, TY, NT>(d, U, t, sU);
                 cp_async_wait<0>();
             } else {
@@ -216,24 +286,27 @@ __global__ void __launch_bounds__(NT, MINB) batch_kernel(BatchDev d, int nsteps)
                     cp_async_wait<0>();
                 }
             }
-            __syncthreads();
             const int inst = d.tile_inst[t];
             const int xy = d.tile_xy[t];
             const int x0 = xy & 0xffff, y0 = xy >> 16;
             const BatchInst I = d.inst[inst];
+            if (SCHEME == 1) mirror_halo<TX, TY, NT>(sU, x0, y0, I.n);
+            __syncthreads();
             if (threadIdx.x == 0) {
                 // TimeStep::operator() for this case (timestep.cpp:29-68) from last step's maxima
                 const unsigned long long* a = d.acc + ((size_t)ar * ninst + inst) * 2;
-                const double dtx = smin(1e16, I.dx / bitsd(a[0]));
-                const double dty = smin(1e16, I.dy / bitsd(a[1]));
+                // (divisions on the integer pipes: the same correctly rounded quotients, without
+                // the FP64 pipe's Newton sequences on one thread while the CTA waits)
+                const double dtx = smin(1e16, div_rn(I.dx, bitsd(a[0])));
+                const double dty = smin(1e16, div_rn(I.dy, bitsd(a[1])));
                 sdt[0] = m0 * smin(dtx, dty);
                 if (SCHEME == 1) {
                     const double dtp = m1 * smin(dtx, dty);
-                    sdt[1] = 0.5 * dtp / I.dx;   // muscl_hancock.cpp:248-249
-                    sdt[2] = 0.5 * dtp / I.dy;
+                    sdt[1] = div_rn(0.5 * dtp, I.dx);   // muscl_hancock.cpp:248-249
+                    sdt[2] = div_rn(0.5 * dtp, I.dy);
                 }
-                sdt[3] = 1.0 / I.dx;             // muscl_hancock.cpp:352-353, godunov.cpp:97-98
-                sdt[4] = 1.0 / I.dy;
+                sdt[3] = div_rn(1.0, I.dx);             // muscl_hancock.cpp:352-353, godunov.cpp:97-98
+                sdt[4] = div_rn(1.0, I.dy);
             }
             __syncthreads();
             const double dt = sdt[0], hdx = sdt[1], hdy = sdt[2], one_dx = sdt[3], one_dy = sdt[4];
@@ -245,7 +318,7 @@ __global__ void __launch_bounds__(NT, MINB) batch_kernel(BatchDev d, int nsteps)
                 herr += mh_tile_fluxes<TX, TY, NT, 1>(sU, sW, sF, sG, g, g1, hdx, hdy, x0, y0, I.n, I.n);
             double mx = 0.0, my = 0.0;
             double* __restrict__ out = Un + I.off;
-            const size_t plane = (size_t)I.n * I.n;
+            const size_t plane = (size_t)I.pitch * I.n;
             for (int it = threadIdx.x; it < TX * TY; it += NT) {
                 const int ox = it % TX, oy = it / TX;
                 const int gx = x0 + ox, gy = y0 + oy;
@@ -255,11 +328,11 @@ __global__ void __launch_bounds__(NT, MINB) batch_kernel(BatchDev d, int nsteps)
                     for (int v = 0; v < 4; ++v) {
                         un[v] = SCHEME == 0 ? go_update<TX, TY>(sU, sF, sG, v, ox, oy, dt, one_dx, one_dy)
                                             : mh_update<TX, TY>(sU, sF, sG, v, ox, oy, dt, one_dx, one_dy);
-                        out[v * plane + (size_t)gy * I.n + gx] = un[v];
+                        out[v * plane + (size_t)gy * I.pitch + gx] = un[v];
                     }
                     double sx, sy;
                     if (!wave_terms(g, g1, un[0], un[1], un[2], un[3], sx, sy))
-                        atomicMin(&c->first_nonpos, batch_key(step, I.off + (long long)gy * I.n + gx));
+                        atomicMin(&c->first_nonpos, batch_key(step, I.off + (long long)gy * I.pitch + gx));
                     mx = nmax(mx, sx);
                     my = nmax(my, sy);
                 }
@@ -272,6 +345,15 @@ __global__ void __launch_bounds__(NT, MINB) batch_kernel(BatchDev d, int nsteps)
             }
             __syncthreads();   // smem reuse by the next tile
             buf ^= 1;
+        }
+        if (failed) {
+            if (threadIdx.x == 0) {
+                atomicCAS(&c->err, 0, (int)HF_DEV_TIMEOUT);
+                // let the copies in flight land before the CTA's shared memory goes
+                for (int k = 0; k < 2; ++k) mbar_wait_bounded(&tbar[k], tph[k], kBatchWaitLimit);
+            }
+            __syncthreads();
+            break;
         }
         if (!grid_barrier(c)) break;
     }
@@ -294,12 +376,12 @@ __global__ void __launch_bounds__(NT) batch_cfl_kernel(BatchDev d) {
     const int x0 = xy & 0xffff, y0 = xy >> 16;
     const BatchInst I = d.inst[inst];
     const double* U = d.U[p] + I.off;
-    const size_t plane = (size_t)I.n * I.n;
+    const size_t plane = (size_t)I.pitch * I.n;
     double mx = 0.0, my = 0.0;
     for (int it = threadIdx.x; it < TX * TY; it += NT) {
         const int gx = x0 + it % TX, gy = y0 + it / TX;
         if (gx < I.n && gy < I.n) {
-            const size_t o = (size_t)gy * I.n + gx;
+            const size_t o = (size_t)gy * I.pitch + gx;
             double sx, sy;
             wave_terms(c->gamma, c->g1, U[o], U[plane + o], U[2 * plane + o], U[3 * plane + o], sx, sy);
             mx = nmax(mx, sx);
@@ -387,6 +469,7 @@ struct hf_batch {
     int scheme = 1;             // 0 Godunov, 1 MUSCL-Hancock
     std::vector<hf::BatchInst> inst;
     long long total_cells = 0;
+    long long total_doubles = 0;   // the state buffer: every case's [4][n][pitch]
     std::vector<void*> allocs;
     hf::BatchCtrl* dctrl = nullptr;
     hf::BatchInst* dinst = nullptr;
@@ -398,6 +481,7 @@ struct hf_batch {
     int* tile_inst[hf::kNumConfigs] = {};
     int* tile_xy[hf::kNumConfigs] = {};
     long long ntiles[hf::kNumConfigs] = {};
+    CUtensorMap* maps[hf::kNumConfigs] = {};   // MUSCL-Hancock: the TMA maps of the config's tile box
     int config = 0;
     // graphs: key = (config, nsteps)
     struct G { int config; long long nsteps; cudaGraphExec_t exec; };
@@ -441,10 +525,40 @@ int ensure_tiles(hf_batch* b, int k) {
     return HF_OK;
 }
 
+// The TMA maps of configuration k (MUSCL-Hancock batches): per state parity and case, the case's
+// [4][n][pitch] state as a 3-D tensor {n, n, 4} with the box of the config's tile and its 2-cell halo.
+int ensure_maps(hf_batch* b, int k) {
+    if (b->scheme != 1 || b->maps[k]) return HF_OK;
+    const hf::BatchConfig C = hf::kConfigs[k];
+    hf::EncodeTiledFn enc = hf::tensor_map_encoder();
+    if (!enc) return bfail(b, HF_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
+    const size_t n = b->inst.size();
+    std::vector<CUtensorMap> maps(2 * n);
+    for (int par = 0; par < 2; ++par)
+        for (size_t i = 0; i < n; ++i) {
+            const hf::BatchInst& I = b->inst[i];
+            cuuint64_t dims[3] = {(cuuint64_t)I.n, (cuuint64_t)I.n, 4};
+            cuuint64_t strides[2] = {(cuuint64_t)I.pitch * 8, (cuuint64_t)I.pitch * I.n * 8};
+            cuuint32_t box[3] = {(cuuint32_t)(C.tx + 4), (cuuint32_t)(C.ty + 4), 4};
+            cuuint32_t es[3] = {1, 1, 1};
+            CUresult r = enc(&maps[par * n + i], CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3, b->U[par] + I.off, dims, strides,
+                             box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                             CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+            if (r != CUDA_SUCCESS)
+                return bfail(b, HF_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
+        }
+    BCK(cudaMalloc(&b->maps[k], maps.size() * sizeof(CUtensorMap)));
+    b->allocs.push_back(b->maps[k]);
+    BCK(cudaMemcpy(b->maps[k], maps.data(), maps.size() * sizeof(CUtensorMap), cudaMemcpyHostToDevice));
+    return HF_OK;
+}
+
 hf::BatchDev devview(hf_batch* b, int k) {
     hf::BatchDev d{};
     d.ctrl = b->dctrl;
     d.inst = b->dinst;
+    d.maps = b->maps[k];
+    d.ninst = (int)b->inst.size();
     d.tile_inst = b->tile_inst[k];
     d.tile_xy = b->tile_xy[k];
     d.ntiles = b->ntiles[k];
@@ -532,7 +646,9 @@ int hf_batch_create(const char* manifest, size_t len, hf_batch** out) {
             double yb = ex["y_bottom"].number(), yt = ex["y_top"].number();
             hf::BatchInst I{};
             I.n = nx;
-            I.off = b->total_cells * 4;
+            I.pitch = nx + (nx & 1);
+            I.off = b->total_doubles;
+            b->total_doubles += 4LL * I.pitch * nx;
             I.dx = (xr - xl) / nx;   // mesh_block.cpp:227-236
             I.dy = (yt - yb) / ny;
             b->inst.push_back(I);
@@ -561,7 +677,8 @@ int hf_batch_create(const char* manifest, size_t len, hf_batch** out) {
     BCK(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
     const size_t n = b->inst.size();
     for (int k = 0; k < 2; ++k) {
-        BCK(cudaMalloc(&b->U[k], (size_t)b->total_cells * 4 * sizeof(double)));
+        BCK(cudaMalloc(&b->U[k], (size_t)b->total_doubles * sizeof(double)));
+        BCK(cudaMemset(b->U[k], 0, (size_t)b->total_doubles * sizeof(double)));
         b->allocs.push_back(b->U[k]);
     }
     BCK(cudaMalloc(&b->acc, 3 * 2 * n * sizeof(unsigned long long)));
@@ -583,8 +700,11 @@ int hf_batch_create(const char* manifest, size_t len, hf_batch** out) {
     C.ninst = (int)n;
     C.first_nonpos = ~0ull;
     BCK(cudaMemcpy(b->dctrl, &C, sizeof C, cudaMemcpyHostToDevice));
-    for (size_t i = 0; i < n; ++i)
-        BCK(cudaMemcpy(b->U[0] + b->inst[i].off, init[i].data(), init[i].size() * sizeof(double), cudaMemcpyHostToDevice));
+    for (size_t i = 0; i < n; ++i) {
+        const hf::BatchInst& I = b->inst[i];
+        BCK(cudaMemcpy2D(b->U[0] + I.off, (size_t)I.pitch * 8, init[i].data(), (size_t)I.n * 8, (size_t)I.n * 8,
+                         (size_t)4 * I.n, cudaMemcpyHostToDevice));
+    }
     return refresh_cfl(b);
 }
 
@@ -639,6 +759,7 @@ int hf_batch_run(hf_batch* b, int64_t nsteps, int use_graph) {
     if (!b || nsteps < 0 || nsteps > (1 << 30)) return HF_ERR_ARG;
     if (nsteps == 0) return HF_OK;
     int r = ensure_tiles(b, b->config);
+    if (!r) r = ensure_maps(b, b->config);
     if (r) return r;
     hf::BatchDev d = devview(b, b->config);
     if (!use_graph) {
@@ -671,7 +792,7 @@ int hf_batch_sync(hf_batch* b) {
 int hf_batch_autotune(hf_batch* b, int steps_per_trial, int* best, double* ms_per_step) {
     if (!b || steps_per_trial < 1) return HF_ERR_ARG;
     // trials advance a copy: save the live state, time each configuration, restore
-    const size_t bytes = (size_t)b->total_cells * 4 * sizeof(double);
+    const size_t bytes = (size_t)b->total_doubles * sizeof(double);
     long long step = read_step(b);
     int p = (int)(step & 1);
     double* save = nullptr;
@@ -691,6 +812,7 @@ int hf_batch_autotune(hf_batch* b, int steps_per_trial, int* best, double* ms_pe
     double bestms = 1e300;
     for (int k = 0; k < hf::kNumConfigs; ++k) {
         int r = ensure_tiles(b, k);
+        if (!r) r = ensure_maps(b, k);
         if (r) return r;
         hf::BatchDev d = devview(b, k);
         // warm (first launch pays the shared-memory opt-in), then time
@@ -724,7 +846,8 @@ int hf_batch_get_state(hf_batch* b, int i, double* out) {
     if (!b || !out || i < 0 || i >= (int)b->inst.size()) return HF_ERR_ARG;
     long long step = read_step(b);
     const hf::BatchInst& I = b->inst[i];
-    BCK(cudaMemcpy(out, b->U[step & 1] + I.off, (size_t)4 * I.n * I.n * sizeof(double), cudaMemcpyDeviceToHost));
+    BCK(cudaMemcpy2D(out, (size_t)I.n * 8, b->U[step & 1] + I.off, (size_t)I.pitch * 8, (size_t)I.n * 8,
+                     (size_t)4 * I.n, cudaMemcpyDeviceToHost));
     return HF_OK;
 }
 
@@ -732,7 +855,8 @@ int hf_batch_set_state(hf_batch* b, int i, const double* in) {
     if (!b || !in || i < 0 || i >= (int)b->inst.size()) return HF_ERR_ARG;
     long long step = read_step(b);
     const hf::BatchInst& I = b->inst[i];
-    BCK(cudaMemcpy(b->U[step & 1] + I.off, in, (size_t)4 * I.n * I.n * sizeof(double), cudaMemcpyHostToDevice));
+    BCK(cudaMemcpy2D(b->U[step & 1] + I.off, (size_t)I.pitch * 8, in, (size_t)I.n * 8, (size_t)I.n * 8,
+                     (size_t)4 * I.n, cudaMemcpyHostToDevice));
     return refresh_cfl(b);
 }
 
@@ -772,8 +896,8 @@ int hf_batch_last_nonpositive_cell(hf_batch* b, int* instance, int* i, int* j, i
         }
         const long long rem = off - b->inst[lo].off;
         cx = (int)lo;
-        cj = (int)(rem / b->inst[lo].n);
-        ci = (int)(rem % b->inst[lo].n);
+        cj = (int)(rem / b->inst[lo].pitch);
+        ci = (int)(rem % b->inst[lo].pitch);
         st = (long long)(k >> 40);
     }
     if (instance) *instance = cx;

@@ -617,10 +617,10 @@ __device__ __noinline__ bool mh_step_tile(Ctrl* __restrict__ c, const MeshDev* _
 
 // the predictor scalars of block b from its predictor dt (muscl_hancock.cpp:248-249, 352-353)
 __device__ __forceinline__ void step_scalars(const Ctrl* c, int b, double dtp) {
-    s_step_sc[b][0] = 0.5 * dtp / c->dx[b];
-    s_step_sc[b][1] = 0.5 * dtp / c->dy[b];
-    s_step_sc[b][2] = 1.0 / c->dx[b];
-    s_step_sc[b][3] = 1.0 / c->dy[b];
+    s_step_sc[b][0] = div_rn(0.5 * dtp, c->dx[b]);
+    s_step_sc[b][1] = div_rn(0.5 * dtp, c->dy[b]);
+    s_step_sc[b][2] = div_rn(1.0, c->dx[b]);
+    s_step_sc[b][3] = div_rn(1.0, c->dy[b]);
     s_step_sc[b][4] = dtp;
 }
 

@@ -115,6 +115,12 @@ struct StepPlan {
 void step_plan_tiles(StepPlan& plan, int b, int nx, int ny);
 cudaError_t launch_mh_step(Ctrl* c, const MeshDev* m, const StepPlan& plan, int limiter, cudaStream_t s);
 
+// the driver's cuTensorMapEncodeTiled, or null where the driver lacks it
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+EncodeTiledFn tensor_map_encoder();
+
 // TMA box of the stencil for the scheme
 StencilTiles stencil_tiles(int scheme);
 cudaError_t stencil_prepare();   // sets the large dynamic shared-memory opt-ins once

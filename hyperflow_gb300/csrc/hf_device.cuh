@@ -299,8 +299,8 @@ __device__ __forceinline__ double cfl_dt_t(CP c, long long call, int new_upto, i
         int pp = b < new_upto ? pn : po;
         double mx = smax(bitsd(c->ghost_s[b][0]), bitsd(c->int_s[pp][b][0]));
         double my = smax(bitsd(c->ghost_s[b][1]), bitsd(c->int_s[pp][b][1]));
-        dtx = smin(dtx, c->dx[b] / mx);
-        dty = smin(dty, c->dy[b] / my);
+        dtx = smin(dtx, div_rn(c->dx[b], mx));   // exact, on the integer pipes
+        dty = smin(dty, div_rn(c->dy[b], my));
     }
     const double cfl = c->cfl;
     double final_cfl = (call + 1 <= 10) ? 0.2 * cfl : cfl;

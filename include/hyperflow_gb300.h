@@ -143,7 +143,8 @@ int hf_stream(hf_ctx* ctx, void** stream);
 
 /* How a step's MUSCL-Hancock block updates are launched.  No counterpart in the reference,
  * whose Simulation::solve updates the blocks in order (simulation.cpp:106-110).  By default a
- * mesh of at most 4 blocks is updated by one cooperative launch that takes the blocks' tiles in
+ * mesh of 2 to 4 blocks (or one block of at least 1024 tiles of 32 x 12 cells) is updated by one
+ * cooperative launch that takes the blocks' tiles in
  * order from one counter (no partly filled last wave per block) and runs every block with the
  * predictor dt of a TimeStep call over the step's starting state; each block b > 0 is then
  * checked against the predictor dt the reference forms (muscl_hancock.cpp:246: blocks < b
