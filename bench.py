@@ -329,8 +329,10 @@ def bench_learned(args):
     """The learned coarse solver's step: 512^2 FP32 MUSCL-Hancock MinBee + HLLC with the MLP
     face-flux correction (features -> 64 -> 64 -> 4, BF16 on the tensor cores, FP32
     accumulation) on every face, random-init weights (throughput does not depend on them), the
-    change guard on.  Timed with CUDA events on the solver's stream, with and without the MLP;
-    the MLP path's throughput is its FLOPs over the time it adds to a step."""
+    change guard on.  Steps are enqueued without reading back the rejection count and timed
+    with CUDA events on the solver's stream: with the fused face kernel (the line's value), with
+    the plain flux fused in as well, with the separate kernels, and without the MLP; the MLP
+    path's throughput is its FLOPs over the time it adds to a step."""
     import numpy as np
     import torch
     from hyperflow_gb300 import CartSolver, cases
@@ -345,16 +347,19 @@ def bench_learned(args):
     ls.set_bound(0.5)
     stream = torch.cuda.ExternalStream(ls.stream())
 
-    def timed(use_mlp):
+    def timed(use_mlp, fused=1):
+        ls.set_fused(fused)
         ls.set_state(U0)
         dt = ls.cfl_dt()
         for _ in range(args.warmup):
-            ls.step(dt, use_mlp)
-        return timed_device(stream, lambda: [ls.step(dt, use_mlp) for _ in range(args.steps)])
+            ls.step(dt, use_mlp, count_rejected=False)
+        return timed_device(stream, lambda: [ls.step(dt, use_mlp, count_rejected=False) for _ in range(args.steps)])
 
     with Clocks(0) as clk:
         ms_mlp = timed(True)
     ms_plain = timed(False)
+    ms_unfused = timed(True, fused=0)
+    ms_flux_fused = timed(True, fused=2)
     cells = n * n
     faces = 2 * n * (n + 1)
     flop = 16896.0 * faces * args.steps            # 2 x (64x64 + 64x64 + 64x4) per face, x 2 (FMA)
@@ -373,10 +378,13 @@ def bench_learned(args):
         "config": {"workload": "learned_coarse_512x512_muscl_hancock_minbee_mlp_flux_correction", "cells": cells,
                    "faces": faces, "mlp": "features->64->64->4 GELU, BF16 weights, FP32 accumulation"},
         "plain_fp32_value": cells * args.steps / (ms_plain / 1e3) / 1e6,
+        "unfused_value": cells * args.steps / (ms_unfused / 1e3) / 1e6,
+        "flux_fused_value": cells * args.steps / (ms_flux_fused / 1e3) / 1e6,
         "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak, "traffic": None, "peak_kind": "measured",
-                     "kernel": "mlp_forward_kernel (tcgen05.mma kind::f16, TMEM accumulators); achieved = "
-                               "MLP FLOPs over the time the MLP path adds to a step"},
+                     "kernel": "face_kernel (per 128-face tile: features, the tcgen05.mma kind::f16 MLP with "
+                               "TMEM accumulators, the corrections); achieved = MLP FLOPs over the time the MLP "
+                               "path adds to a step"},
         "cpu_baseline": None, "e2e": None, "gpu_launches": None, "clocks": clk.summary()}), flush=True)
     ls.close()
 

@@ -123,6 +123,7 @@ SIGNATURES = {
     "hf_lc_set_bound": (_i, [_p, _d]),
     "hf_lc_set_guard_mode": (_i, [_p, _i]),
     "hf_lc_set_train_guard": (_i, [_p, _i]),
+    "hf_lc_set_fused": (_i, [_p, _i, _i]),
     "hf_lc_set_state": (_i, [_p, _p]),
     "hf_lc_get_state": (_i, [_p, _p]),
     "hf_lc_set_time": (_i, [_p, _d]),

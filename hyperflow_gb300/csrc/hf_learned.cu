@@ -51,9 +51,14 @@ __device__ __forceinline__ float tanh_fast(float x) {
     asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
     return y;
 }
+// GELU, tanh form: 0.5 z (1 + tanh(k (z + 0.044715 z^3))), k = sqrt(2/pi), formed as h + h t
+// with h = z / 2 and t = tanh(z (k + 0.044715 k z^2)) -- half of what the MLP kernels' packed
+// gelu2x computes, exactly, so the backward's recomputed activations equal the forward's
 __device__ __forceinline__ float gelu(float z) {
-    const float k = 0.7978845608028654f;   // sqrt(2/pi)
-    return 0.5f * z * (1.0f + tanh_fast(k * (z + 0.044715f * z * z * z)));
+    const float k = 0.7978845608028654f, c = 0.7978845608028654f * 0.044715f;
+    const float t = tanh_fast(z * fmaf(z * z, c, k));
+    const float h = z * 0.5f;
+    return fmaf(h, t, h);
 }
 __device__ __forceinline__ float gelu_grad(float z) {
     const float k = 0.7978845608028654f;
@@ -168,23 +173,30 @@ __device__ __forceinline__ void face_of(int f, int n, int& dir, int& i, int& j) 
     else { f -= nxf; dir = 1; j = f / n; i = f % n; }
 }
 
+// plain MUSCL-Hancock HLLC flux of face f (FP32); hdt = dt / (2 dx)
+__device__ __forceinline__ void plain_face_flux(const float* __restrict__ U, const Grid& G, float hdt, int f,
+                                                float* out) {
+    int dir, i, j;
+    face_of(f, G.n, dir, i, j);
+    float a0[4], a1[4], b0[4], b1[4];
+    if (dir == 0) {
+        evolved_pair<0>(U, G, hdt, i - 1, j, a0, a1);
+        evolved_pair<0>(U, G, hdt, i, j, b0, b1);
+        hllcf<0>(G.g, G.g1, a1, b0, out);
+    } else {
+        evolved_pair<1>(U, G, hdt, i, j - 1, a0, a1);
+        evolved_pair<1>(U, G, hdt, i, j, b0, b1);
+        hllcf<1>(G.g, G.g1, a1, b0, out);
+    }
+}
+
 // plain MUSCL-Hancock HLLC flux of every face (FP32)
 __global__ void plain_flux_kernel(const float* __restrict__ U, Grid G, float dt, float* __restrict__ F) {
     const int nf = 2 * (G.n + 1) * G.n;
     const float hdt = 0.5f * dt / G.dx;
     for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < nf; f += gridDim.x * blockDim.x) {
-        int dir, i, j;
-        face_of(f, G.n, dir, i, j);
-        float a0[4], a1[4], b0[4], b1[4], out[4];
-        if (dir == 0) {
-            evolved_pair<0>(U, G, hdt, i - 1, j, a0, a1);
-            evolved_pair<0>(U, G, hdt, i, j, b0, b1);
-            hllcf<0>(G.g, G.g1, a1, b0, out);
-        } else {
-            evolved_pair<1>(U, G, hdt, i, j - 1, a0, a1);
-            evolved_pair<1>(U, G, hdt, i, j, b0, b1);
-            hllcf<1>(G.g, G.g1, a1, b0, out);
-        }
+        float out[4];
+        plain_face_flux(U, G, hdt, f, out);
         for (int v = 0; v < 4; ++v) F[(size_t)v * nf + f] = out[v];
     }
 }
@@ -199,11 +211,52 @@ __global__ void prims_kernel(const float* __restrict__ U, int n, float g1, float
     }
 }
 
-__device__ __forceinline__ float4 prim_at(const float4* __restrict__ W, int n, int i, int j) {
-    return W[(size_t)mir(j, n) * n + mir(i, n)];
+constexpr int kFeatNT = 256;
+
+// two FP32 values rounded to BF16 (lo in the low half)
+__device__ __forceinline__ uint32_t pack2(float lo, float hi) {
+    __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<uint32_t*>(&v);
 }
 
-constexpr int kFeatNT = 256;
+// face f's 64 features, rounded to BF16 and packed in pairs (normal offset outer, tangential
+// offset inner; per cell rho, u_n, u_t, p), its correction scale (rho_ref, c_ref) and whether it
+// is an x face.  The scaled values are products with the reciprocals of rho_ref, c_ref and
+// p_ref (one division each per face), and the stencil's mirrored columns and rows are formed
+// once per face.
+__device__ __forceinline__ void face_features(const float4* __restrict__ W, const Grid& G, int f, uint32_t* pk,
+                                              float& rr, float& cref, bool& xface) {
+    int dir, i, j;
+    face_of(f, G.n, dir, i, j);
+    xface = dir == 0;
+    const int n = G.n;
+    // lower cell (il, jl); stencil cell (a, b), a along the normal and b along the face, both
+    // -1..2, is column il + a, row jl + b on an x face and column il + b, row jl + a on a y face
+    const int il = xface ? i - 1 : i, jl = xface ? j : j - 1;
+    int col[4], row[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        col[k] = mir(il + k - 1, n);
+        row[k] = mir(jl + k - 1, n);
+    }
+    const float4 wl = W[(size_t)row[1] * n + col[1]];
+    const float4 wr = xface ? W[(size_t)row[1] * n + col[2]] : W[(size_t)row[2] * n + col[1]];
+    rr = 0.5f * (wl.x + wr.x);
+    const float pr = 0.5f * (wl.w + wr.w);
+    cref = sqrtf(fmaxf(G.g * pr / rr, 1e-12f));
+    const float irr = 1.0f / rr, ipr = 1.0f / pr, ic = 1.0f / cref;
+    int k = 0;
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+            const int r = xface ? row[b] : row[a], c = xface ? col[a] : col[b];
+            const float4 w = W[(size_t)r * n + c];
+            const float un = xface ? w.y : w.z, ut = xface ? w.z : w.y;
+            pk[k++] = pack2(w.x * irr - 1.0f, un * ic);
+            pk[k++] = pack2(ut * ic, w.w * ipr - 1.0f);
+        }
+}
 
 // features (BF16 [nf][64]) and the correction scale of every face.  Each thread forms one
 // face's 64 features in registers; a CTA's 256 faces (32 KB) go out through shared memory as
@@ -218,30 +271,11 @@ __global__ void __launch_bounds__(kFeatNT) features_kernel(const float4* __restr
         const int f = base + threadIdx.x;
         uint32_t pk[32] = {};
         if (f < nf) {
-            int dir, i, j;
-            face_of(f, G.n, dir, i, j);
-            // lower cell (il, jl), normal unit (ni, nj), tangent (ti, tj)
-            const int il = dir == 0 ? i - 1 : i, jl = dir == 0 ? j : j - 1;
-            const int ni = dir == 0, nj = dir == 1, ti = dir == 1, tj = dir == 0;
-            const float4 wl = prim_at(W, G.n, il, jl), wr = prim_at(W, G.n, il + ni, jl + nj);
-            const float rr = 0.5f * (wl.x + wr.x), pr = 0.5f * (wl.w + wr.w);
-            const float cref = sqrtf(fmaxf(G.g * pr / rr, 1e-12f));
+            float rr, cref;
+            bool xface;
+            face_features(W, G, f, pk, rr, cref, xface);
             scale[2 * (size_t)f] = rr;
             scale[2 * (size_t)f + 1] = cref;
-            int k = 0;
-#pragma unroll
-            for (int a = -1; a <= 2; ++a)
-#pragma unroll
-                for (int b = -1; b <= 2; ++b) {
-                    const float4 w = prim_at(W, G.n, il + a * ni + b * ti, jl + a * nj + b * tj);
-                    const float un = dir == 0 ? w.y : w.z, ut = dir == 0 ? w.z : w.y;
-                    const __nv_bfloat16 x0 = __float2bfloat16_rn(w.x / rr - 1.0f);
-                    const __nv_bfloat16 x1 = __float2bfloat16_rn(un / cref);
-                    const __nv_bfloat16 x2 = __float2bfloat16_rn(ut / cref);
-                    const __nv_bfloat16 x3 = __float2bfloat16_rn(w.w / pr - 1.0f);
-                    pk[k++] = (uint32_t)__bfloat16_as_ushort(x0) | ((uint32_t)__bfloat16_as_ushort(x1) << 16);
-                    pk[k++] = (uint32_t)__bfloat16_as_ushort(x2) | ((uint32_t)__bfloat16_as_ushort(x3) << 16);
-                }
         }
         // chunk q (16 bytes) of face t sits at t * 8 + (q ^ (t & 7)): conflict-free both ways
 #pragma unroll
@@ -260,29 +294,57 @@ __global__ void __launch_bounds__(kFeatNT) features_kernel(const float4* __restr
 }
 
 // ---------------------------------------------------------------------------------
-// MLP forward on the 5th-generation tensor cores: tcgen05.mma, BF16 x BF16 -> FP32 in TMEM
+// MLP on the 5th-generation tensor cores: tcgen05.mma, BF16 x BF16 -> FP32 in TMEM
 // ---------------------------------------------------------------------------------
-// A CTA of 128 threads takes 128 faces per tile, one face per thread and per TMEM lane.
+// A CTA of 256 threads is two independent groups of 128 (warps 0-3 and 4-7) that share the
+// weights in shared memory.  A group takes 128 faces per tile, one face per thread and per TMEM
+// lane, with its own A operand, TMEM accumulator (64 columns), mbarrier, named barrier and MMA
+// issuing thread: every layer is 5 MMAs of M 128, K 16.  Decoupled, the groups of the CTAs on
+// an SM overlap one another's feature loads, MMAs and epilogues.
 // Operands sit in shared memory in the canonical K-major layout without swizzle: 8 x 8 BF16
 // core matrices of 128 contiguous bytes, core matrices adjacent along K 128 B apart (the
-// descriptor's leading-dimension offset), 8-row groups 1024 B apart (its stride offset).
-// Each layer is 4 MMAs of K = 16 issued by one thread and committed to an mbarrier; the
-// 64 FP32 accumulator columns are read back with tcgen05.ld, biased, passed through GELU,
-// rounded to BF16 and stored as the next layer's A operand.  The output layer runs with
-// N = 16 (rows 4..15 of its weight tile are zero).
-constexpr int kTcRows = 128;       // faces per tile = threads per CTA = TMEM lanes
-constexpr int kTcTiles = 2;        // tiles in flight per CTA: one's MMA overlaps the other's epilogue
-constexpr int kTcCols = 64 * kTcTiles;   // TMEM columns held by a CTA (one accumulator per tile)
-constexpr uint32_t kTcWaitLimit = 1u << 22;
+// descriptor's leading-dimension offset), 8-row groups 1280 B apart (its stride offset).
+// K runs to 80: columns 0..63 hold the layer's inputs, column 64 and 65 of every A row are 1
+// and the same columns of the weight rows hold the bias split into two BF16 parts (hi, and
+// the remainder lo), so the MMA adds the bias with FP32 accumulation; columns 66..79 are 0.
+// Each layer's MMAs are issued by one thread and committed to an mbarrier; the FP32
+// accumulators are read back with tcgen05.ld, passed through GELU in packed FP32x2 arithmetic,
+// rounded to BF16 and stored as the next layer's A operand -- stored doubled, 2 GELU(z) =
+// z + z tanh(.), with the next layer's weights halved: both scalings are exact, so the products
+// equal those of GELU(z) and the unscaled weights.  The output layer runs with N = 16 (rows
+// 4..15 of its weight tile are zero).
+constexpr int kTcRows = 128;       // rows of an MMA tile = TMEM lanes
+constexpr int kTcThreads = 256;    // threads per CTA: two groups of kTcRows
+constexpr int kTcCols = 128;       // TMEM columns held by a CTA (two 64-column accumulators)
+constexpr int kTcK = 80;           // operand K: 64 inputs, the bias pair, zero padding
+constexpr int kTcKSteps = kTcK / 16;
+constexpr uint32_t kTcWaitLimit = 1u << 16;   // polls of at most kTcSleepNs each
+constexpr uint32_t kTcSleepNs = 20000;
 
-__device__ __forceinline__ uint32_t canon_off(int r, int k) {   // bytes; K = 64 BF16 per row
-    return (uint32_t)((r >> 3) * 1024 + (k >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2);
+__device__ __forceinline__ uint32_t canon_off(int r, int k) {   // bytes; K = 80 BF16 per row
+    return (uint32_t)((r >> 3) * (kTcK * 16) + (k >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2);
 }
-// shared-memory matrix descriptor: start >> 4, leading offset 128 B, stride offset 1024 B,
+// shared-memory matrix descriptor: start >> 4, leading offset 128 B, stride offset 1280 B,
 // descriptor version 1, no swizzle
 __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr) {
     return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)(128u >> 4) << 16) |
-           ((uint64_t)(1024u >> 4) << 32) | (1ull << 46);
+           ((uint64_t)((kTcK * 16) >> 4) << 32) | (1ull << 46);
+}
+// bounded mbarrier wait that lets the waiting warps sleep: each poll suspends the thread until
+// the phase completes or kTcSleepNs pass, so the wait costs few issue slots; gives up after
+// `limit` polls
+__device__ __forceinline__ bool mbar_wait_sleep(uint64_t* bar, uint32_t parity, uint32_t limit) {
+    for (uint32_t i = 0; i < limit; ++i) {
+        uint32_t ok;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n"
+            " selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(ok)
+            : "r"(smem_u32(bar)), "r"(parity), "r"(kTcSleepNs)
+            : "memory");
+        if (ok) return true;
+    }
+    return false;
 }
 // kind::f16 instruction descriptor: D FP32, A and B BF16, both K-major, M = 128, N = n
 __host__ __device__ constexpr uint32_t idesc_bf16(int n) {
@@ -323,61 +385,136 @@ __device__ __forceinline__ void tc_ld16(uint32_t taddr, float* v) {
     for (int k = 0; k < 16; ++k) v[k] = __uint_as_float(r[k]);
 }
 
-__device__ __forceinline__ uint32_t pack2(float lo, float hi) {
-    __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
-    return *reinterpret_cast<uint32_t*>(&v);
+// 32 consecutive accumulator columns of this thread's TMEM lane, as tc_ld16
+__device__ __forceinline__ void tc_ld32(uint32_t taddr, float* v) {
+    uint32_t r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;"
+                 : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7]), "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]), "+r"(r[12]), "+r"(r[13]), "+r"(r[14]), "+r"(r[15]), "+r"(r[16]), "+r"(r[17]), "+r"(r[18]), "+r"(r[19]), "+r"(r[20]), "+r"(r[21]), "+r"(r[22]), "+r"(r[23]), "+r"(r[24]), "+r"(r[25]), "+r"(r[26]), "+r"(r[27]), "+r"(r[28]), "+r"(r[29]), "+r"(r[30]), "+r"(r[31])
+                 :
+                 : "memory");
+#pragma unroll
+    for (int k = 0; k < 32; ++k) v[k] = __uint_as_float(r[k]);
 }
 
-// 8 BF16 values into row r, columns k0..k0+7, of a canonical operand tile
-__device__ __forceinline__ void put8(unsigned char* tile, int r, int k0, const float* h) {
-    uint4 q;
-    q.x = pack2(h[0], h[1]);
-    q.y = pack2(h[2], h[3]);
-    q.z = pack2(h[4], h[5]);
-    q.w = pack2(h[6], h[7]);
-    *reinterpret_cast<uint4*>(tile + canon_off(r, k0)) = q;
-}
 
 struct __align__(1024) TcSmem {
-    unsigned char a[kTcTiles][kTcRows * 64 * 2];   // activations of each tile (A operands)
-    unsigned char w1[64 * 64 * 2], w2[64 * 64 * 2], w3[16 * 64 * 2];
-    float b1[64], b2[64], b3[4];
-    uint64_t bar[kTcTiles];
+    unsigned char a[2][kTcRows * kTcK * 2];   // each group's activations (its A operand)
+    unsigned char w1[64 * kTcK * 2], w2[64 * kTcK * 2], w3[16 * kTcK * 2];
+    uint64_t bar[2];                          // each group's MMA completion
     uint32_t taddr;
 };
 
-// Y[nf][4] = MLP(X).  When Z1/Z2 are given (training), the hidden pre-activations are saved.
-// A CTA takes its tiles two at a time (tiles blockIdx.x + k gridDim.x, k = 2i and 2i + 1), each
-// with its own operand buffer, TMEM accumulator (64 columns) and mbarrier, and alternates between
-// them: while the tensor cores run one tile's layer, the CTA's threads run the other tile's
-// epilogue.  A bounded wait that gives up sets *err, waits (bounded) for the CTA's MMAs in
-// flight, frees the TMEM columns and returns.
-__global__ void __launch_bounds__(kTcRows)
-mlp_forward_kernel(const __nv_bfloat16* __restrict__ X, int nf, const __nv_bfloat16* __restrict__ Wb,
-                   const float* __restrict__ P, float* __restrict__ Y, float* __restrict__ Z1,
-                   float* __restrict__ Z2, int* __restrict__ err) {
-    extern __shared__ unsigned char smem_raw[];
-    TcSmem& S = *reinterpret_cast<TcSmem*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-    const int tid = threadIdx.x, warp = tid >> 5;
-    // weights into the canonical layout (W3 padded to 16 rows), biases
-    for (int c = tid; c < 64 * 8; c += kTcRows) {
-        const int n = c >> 3, kb = c & 7;
-        *reinterpret_cast<uint4*>(S.w1 + canon_off(n, kb * 8)) =
-            *reinterpret_cast<const uint4*>(Wb + (size_t)n * NIN + kb * 8);
-        *reinterpret_cast<uint4*>(S.w2 + canon_off(n, kb * 8)) =
-            *reinterpret_cast<const uint4*>(Wb + H * NIN + (size_t)n * H + kb * 8);
+// this thread's group (0 or 1) and its index in the group
+__device__ __forceinline__ int grp() { return threadIdx.x >> 7; }
+__device__ __forceinline__ int grp_tid() { return threadIdx.x & (kTcRows - 1); }
+// the group's named barrier (ids 1 and 2, as immediates; 0 is the CTA's)
+__device__ __forceinline__ void grp_sync() {
+    if (grp() == 0) asm volatile("bar.sync 1, 128;" ::: "memory");
+    else asm volatile("bar.sync 2, 128;" ::: "memory");
+}
+__device__ __forceinline__ bool grp_any(bool v) {
+    uint32_t r;
+    if (grp() == 0)
+        asm volatile("{\n .reg .pred p, q;\n setp.ne.u32 p, %1, 0;\n bar.red.or.pred q, 1, 128, p;\n selp.u32 %0, 1, 0, q;\n}\n"
+                     : "=r"(r) : "r"((uint32_t)v) : "memory");
+    else
+        asm volatile("{\n .reg .pred p, q;\n setp.ne.u32 p, %1, 0;\n bar.red.or.pred q, 2, 128, p;\n selp.u32 %0, 1, 0, q;\n}\n"
+                     : "=r"(r) : "r"((uint32_t)v) : "memory");
+    return r != 0;
+}
+
+// packed FP32x2 arithmetic (one instruction for two lanes' worth of work)
+__device__ __forceinline__ uint64_t f2(float lo, float hi) {
+    uint64_t r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+__device__ __forceinline__ float2 f2_split(uint64_t v) {
+    float2 r;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(v));
+    return r;
+}
+__device__ __forceinline__ uint64_t f2_add(uint64_t a, uint64_t b) {
+    uint64_t r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ uint64_t f2_mul(uint64_t a, uint64_t b) {
+    uint64_t r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ uint64_t f2_fma(uint64_t a, uint64_t b, uint64_t c) {
+    uint64_t r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+    return r;
+}
+// two BF16 values packed (lo in the low half) from their bit patterns
+__device__ __forceinline__ uint32_t bf16_pair(__nv_bfloat16 lo, __nv_bfloat16 hi) {
+    return (uint32_t)__bfloat16_as_ushort(lo) | ((uint32_t)__bfloat16_as_ushort(hi) << 16);
+}
+// 8 BF16 weights from global memory, halved (exact) when `half`
+__device__ __forceinline__ uint4 w_chunk(const __nv_bfloat16* __restrict__ w, bool half) {
+    uint4 q = *reinterpret_cast<const uint4*>(w);
+    if (half) {
+        uint32_t* u = &q.x;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const __nv_bfloat162 v = *reinterpret_cast<const __nv_bfloat162*>(&u[k]);
+            u[k] = bf16_pair(__float2bfloat16_rn(0.5f * __low2float(v)), __float2bfloat16_rn(0.5f * __high2float(v)));
+        }
     }
-    for (int c = tid; c < 16 * 8; c += kTcRows) {
-        const int n = c >> 3, kb = c & 7;
-        uint4 q = make_uint4(0u, 0u, 0u, 0u);
-        if (n < NOUT) q = *reinterpret_cast<const uint4*>(Wb + H * NIN + H * H + (size_t)n * H + kb * 8);
+    return q;
+}
+// the bias b as its BF16 part and the BF16 rounding of the remainder, in K columns 64 and 65
+__device__ __forceinline__ uint4 bias_chunk(float b) {
+    const __nv_bfloat16 hi = __float2bfloat16_rn(b);
+    const __nv_bfloat16 lo = __float2bfloat16_rn(b - __bfloat162float(hi));
+    return make_uint4(bf16_pair(hi, lo), 0u, 0u, 0u);
+}
+
+// The pieces of one CTA's MLP work.  Weights into the canonical layout (W2 and W3 halved, W3
+// padded to 16 rows) with the bias pairs, the constant K columns 64..79 of the A operands, the
+// mbarrier and the CTA's TMEM columns; returns with the CTA synchronised.
+__device__ __forceinline__ void mlp_setup(TcSmem& S, const __nv_bfloat16* __restrict__ Wb,
+                                          const float* __restrict__ P) {
+    const int tid = threadIdx.x;
+    const uint4 zero = make_uint4(0u, 0u, 0u, 0u);
+    for (int c = tid; c < 64 * 10; c += kTcThreads) {
+        const int n = c / 10, kb = c % 10;
+        uint4 q1 = zero, q2 = zero;
+        if (kb < 8) {
+            q1 = w_chunk(Wb + (size_t)n * NIN + kb * 8, false);
+            q2 = w_chunk(Wb + H * NIN + (size_t)n * H + kb * 8, true);
+        } else if (kb == 8) {
+            q1 = bias_chunk(P[OFF_B1 + n]);
+            q2 = bias_chunk(P[OFF_B2 + n]);
+        }
+        *reinterpret_cast<uint4*>(S.w1 + canon_off(n, kb * 8)) = q1;
+        *reinterpret_cast<uint4*>(S.w2 + canon_off(n, kb * 8)) = q2;
+    }
+    for (int c = tid; c < 16 * 10; c += kTcThreads) {
+        const int n = c / 10, kb = c % 10;
+        uint4 q = zero;
+        if (n < NOUT && kb < 8) q = w_chunk(Wb + H * NIN + H * H + (size_t)n * H + kb * 8, true);
+        else if (n < NOUT && kb == 8) q = bias_chunk(P[OFF_B3 + n]);
         *reinterpret_cast<uint4*>(S.w3 + canon_off(n, kb * 8)) = q;
     }
-    for (int k = tid; k < H; k += kTcRows) { S.b1[k] = P[OFF_B1 + k]; S.b2[k] = P[OFF_B2 + k]; }
-    if (tid < NOUT) S.b3[tid] = P[OFF_B3 + tid];
-    if (tid == 0)
-        for (int k = 0; k < kTcTiles; ++k) mbar_init(&S.bar[k], 1);
-    if (warp == 0) {
+    {   // A columns 64..79 of this thread's row: (1, 1, 0, ..., 0)
+        const uint32_t one2 = bf16_pair(__float2bfloat16_rn(1.0f), __float2bfloat16_rn(1.0f));
+        unsigned char* A = S.a[tid >> 7];
+        *reinterpret_cast<uint4*>(A + canon_off(tid & (kTcRows - 1), 64)) = make_uint4(one2, 0u, 0u, 0u);
+        *reinterpret_cast<uint4*>(A + canon_off(tid & (kTcRows - 1), 72)) = zero;
+    }
+    if (tid == 0) {
+        mbar_init(&S.bar[0], 1);
+        mbar_init(&S.bar[1], 1);
+    }
+    if ((tid >> 5) == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&S.taddr)),
                      "r"(kTcCols)
                      : "memory");
@@ -387,112 +524,204 @@ mlp_forward_kernel(const __nv_bfloat16* __restrict__ X, int nf, const __nv_bfloa
     tc_before_sync();
     __syncthreads();
     tc_after_sync();
-    const uint32_t tm = S.taddr;
-    const uint32_t tm_row = tm + ((uint32_t)(warp * 32) << 16);   // this warp's lane quarter
-    const uint32_t sw1 = smem_u32(S.w1), sw2 = smem_u32(S.w2), sw3 = smem_u32(S.w3);
-    uint32_t phase[kTcTiles] = {0u, 0u};
-    int pending[kTcTiles] = {0, 0};   // MMA groups committed and not yet waited for
-    bool failed = false;
-    const int ntiles = (nf + kTcRows - 1) / kTcRows;
+}
 
-    // one layer's 4 MMAs of tile k (thread 0), committed to the tile's mbarrier
-    auto issue = [&](int k, int layer) {
-        if (tid == 0) {
-            tc_after_sync();
-            const uint32_t wb = layer == 0 ? sw1 : (layer == 1 ? sw2 : sw3);
-            const uint32_t id = idesc_bf16(layer == 2 ? 16 : 64);
-            const uint32_t sa = smem_u32(S.a[k]);
-#pragma unroll
-            for (int kk = 0; kk < 4; ++kk)
-                tc_mma(tm + (uint32_t)(k * 64), smem_desc(sa + kk * 256), smem_desc(wb + kk * 256), id, kk);
-            tc_commit(&S.bar[k]);
-        }
-        ++pending[k];
-    };
-    // the writes of the tiles' operands are visible to the tensor cores before the next issue
-    auto publish = [&]() {
-        async_smem_fence();
-        tc_before_sync();
-        __syncthreads();
-    };
-
-    for (int t0 = blockIdx.x; t0 < ntiles && !failed; t0 += kTcTiles * gridDim.x) {
-        int face[kTcTiles];
-        bool valid[kTcTiles];
-        // features -> A; a tile past the last is computed on zeros and not stored
-#pragma unroll
-        for (int k = 0; k < kTcTiles; ++k) {
-            const int t = t0 + k * gridDim.x;
-            face[k] = t * kTcRows + tid;
-            valid[k] = t < ntiles && face[k] < nf;
-            const uint4* x = reinterpret_cast<const uint4*>(X + (size_t)(valid[k] ? face[k] : 0) * NIN);
-#pragma unroll
-            for (int kb = 0; kb < 8; ++kb)
-                *reinterpret_cast<uint4*>(S.a[k] + canon_off(tid, kb * 8)) = valid[k] ? x[kb] : make_uint4(0u, 0u, 0u, 0u);
-        }
-        publish();
-        for (int k = 0; k < kTcTiles; ++k) issue(k, 0);
-#pragma unroll 1
-        for (int layer = 0; layer < 3 && !failed; ++layer) {
-#pragma unroll 1
-            for (int k = 0; k < kTcTiles; ++k) {
-                const bool ok = mbar_wait_bounded(&S.bar[k], phase[k], kTcWaitLimit);
-                if (__syncthreads_or(!ok)) {
-                    failed = true;
-                    break;
-                }
-                phase[k] ^= 1u;
-                --pending[k];
-                tc_after_sync();
-                const uint32_t tcol = tm_row + (uint32_t)(k * 64);
-                if (layer < 2) {
-                    const float* b = layer == 0 ? S.b1 : S.b2;
-                    float* Zs = layer == 0 ? Z1 : Z2;
-#pragma unroll 1
-                    for (int q = 0; q < 4; ++q) {
-                        float z[16];
-                        tc_ld16(tcol + q * 16, z);
-                        float h[16];
-#pragma unroll
-                        for (int j = 0; j < 16; ++j) {
-                            z[j] += b[q * 16 + j];
-                            h[j] = gelu(z[j]);
-                        }
-                        if (Zs && valid[k]) {
-                            float4* zo = reinterpret_cast<float4*>(Zs + (size_t)face[k] * H + q * 16);
-#pragma unroll
-                            for (int j = 0; j < 4; ++j)
-                                zo[j] = make_float4(z[4 * j], z[4 * j + 1], z[4 * j + 2], z[4 * j + 3]);
-                        }
-                        put8(S.a[k], tid, q * 16, h);
-                        put8(S.a[k], tid, q * 16 + 8, h + 8);
-                    }
-                    publish();
-                    issue(k, layer + 1);
-                } else {
-                    float y[16];
-                    tc_ld16(tcol, y);
-                    if (valid[k])
-                        *reinterpret_cast<float4*>(Y + (size_t)face[k] * 4) =
-                            make_float4(y[0] + S.b3[0], y[1] + S.b3[1], y[2] + S.b3[2], y[3] + S.b3[3]);
-                }
-            }
-        }
-    }
-    if (failed && tid == 0) {
-        atomicExch(err, 1);
-        for (int k = 0; k < kTcTiles; ++k)   // let the MMAs in flight land
-            for (; pending[k] > 0; --pending[k]) {
-                mbar_wait_bounded(&S.bar[k], phase[k], kTcWaitLimit);
-                phase[k] ^= 1u;
-            }
-    }
+__device__ __forceinline__ void mlp_teardown(TcSmem& S) {
     tc_before_sync();
     __syncthreads();
-    if (warp == 0) {
+    if ((threadIdx.x >> 5) == 0) {
         tc_after_sync();
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tm), "r"(kTcCols) : "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(S.taddr), "r"(kTcCols) : "memory");
     }
+}
+
+// this thread's row of the tile's A operands (16-byte chunk q of 8 along K)
+__device__ __forceinline__ uint4* a_chunk(TcSmem& S, int q) {
+    return reinterpret_cast<uint4*>(S.a[threadIdx.x >> 7] + canon_off(threadIdx.x & (kTcRows - 1), q * 8));
+}
+// this thread's TMEM lane and accumulator: lane quarter warp mod 4, half warp / 4
+__device__ __forceinline__ uint32_t lane_addr(const TcSmem& S) {
+    const uint32_t w = threadIdx.x >> 5;
+    return S.taddr + ((uint32_t)((w & 3) * 32) << 16) + (w >> 2) * 64;
+}
+
+// the group's operand made visible to the tensor cores, then one layer's MMAs (K = 5 x 16)
+// issued by the group's first thread and committed to the group's mbarrier
+__device__ __forceinline__ void mlp_issue(TcSmem& S, int layer) {
+    async_smem_fence();
+    tc_before_sync();
+    grp_sync();
+    if (grp_tid() == 0) {
+        tc_after_sync();
+        const int g = grp();
+        const uint32_t wb = smem_u32(layer == 0 ? S.w1 : (layer == 1 ? S.w2 : S.w3));
+        const uint32_t id = idesc_bf16(layer == 2 ? 16 : 64);
+        const uint32_t sa = smem_u32(S.a[g]);
+#pragma unroll
+        for (int kk = 0; kk < kTcKSteps; ++kk)
+            tc_mma(S.taddr + g * 64, smem_desc(sa + kk * 256), smem_desc(wb + kk * 256), id, kk);
+        tc_commit(&S.bar[g]);
+    }
+}
+
+// waits for the group's layer.  false, in every thread of the group, when the bounded wait gave
+// up: *err is set and the group's issuing thread has waited (bounded) for its MMAs in flight, so
+// the TMEM can be freed.
+__device__ __forceinline__ bool mlp_wait(TcSmem& S, uint32_t& phase, int* err) {
+    uint64_t* bar = &S.bar[grp()];
+    const bool ok = mbar_wait_sleep(bar, phase, kTcWaitLimit);
+    phase ^= 1u;
+    if (grp_any(!ok)) {
+        if (grp_tid() == 0) {
+            atomicExch(err, 1);
+            mbar_wait_sleep(bar, phase ^ 1u, kTcWaitLimit);
+        }
+        return false;
+    }
+    tc_after_sync();
+    return true;
+}
+
+// GELU doubled (tanh form) of a pair: 2 GELU(z) = z + z t, t = tanh(z (k + 0.044715 k z^2)),
+// k = sqrt(2/pi)
+__device__ __forceinline__ uint64_t gelu2x(uint64_t z) {
+    const float k = 0.7978845608028654f, c = 0.7978845608028654f * 0.044715f;
+    const float2 u = f2_split(f2_mul(z, f2_fma(f2_mul(z, z), f2(c, c), f2(k, k))));
+    return f2_fma(z, f2(tanh_fast(u.x), tanh_fast(u.y)), z);
+}
+
+// a hidden layer's epilogue: this thread's accumulator row (its face, bias included) through
+// GELU, doubled, into the next A operand as BF16; the pre-activations to Zs[face] when given
+__device__ __forceinline__ void mlp_hidden(TcSmem& S, uint32_t tl, float* __restrict__ Zs, int face, bool valid) {
+#pragma unroll 1
+    for (int q = 0; q < 2; ++q) {
+        float z[32];
+        tc_ld32(tl + q * 32, z);
+        uint32_t hb[16];
+#pragma unroll
+        for (int k = 0; k < 16; ++k) {
+            const float2 g = f2_split(gelu2x(f2(z[2 * k], z[2 * k + 1])));
+            hb[k] = pack2(g.x, g.y);
+        }
+        if (Zs && valid) {
+            float4* zo = reinterpret_cast<float4*>(Zs + (size_t)face * H + q * 32);
+#pragma unroll
+            for (int k = 0; k < 8; ++k) zo[k] = make_float4(z[4 * k], z[4 * k + 1], z[4 * k + 2], z[4 * k + 3]);
+        }
+#pragma unroll
+        for (int c = 0; c < 4; ++c) *a_chunk(S, q * 4 + c) = make_uint4(hb[4 * c], hb[4 * c + 1], hb[4 * c + 2], hb[4 * c + 3]);
+    }
+}
+
+// the output layer's 4 values of this thread's face (biases included)
+__device__ __forceinline__ void mlp_out(uint32_t tl, float* o) {
+    float y[16];
+    tc_ld16(tl, y);
+#pragma unroll
+    for (int k = 0; k < NOUT; ++k) o[k] = y[k];
+}
+
+// Y[nf][4] = MLP(X), 128-face tiles per group.  When Z1/Z2 are given (training), the hidden
+// pre-activations are saved.
+// A bounded wait that gives up sets *err, waits (bounded) for the CTA's MMAs in flight,
+// frees the TMEM columns and returns.
+__global__ void __launch_bounds__(kTcThreads, 3)
+mlp_forward_kernel(const __nv_bfloat16* __restrict__ X, int nf, const __nv_bfloat16* __restrict__ Wb,
+                   const float* __restrict__ P, float* __restrict__ Y, float* __restrict__ Z1,
+                   float* __restrict__ Z2, int* __restrict__ err) {
+    extern __shared__ unsigned char smem_raw[];
+    TcSmem& S = *reinterpret_cast<TcSmem*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    mlp_setup(S, Wb, P);
+    const uint32_t tl = lane_addr(S);
+    uint32_t phase = 0;
+    bool failed = false;
+
+    for (int base = (blockIdx.x * 2 + grp()) * kTcRows; base < nf && !failed; base += gridDim.x * 2 * kTcRows) {
+        const int face = base + grp_tid();
+        const bool valid = face < nf;
+        {   // features -> A
+            const uint4* x = reinterpret_cast<const uint4*>(X + (size_t)(valid ? face : 0) * NIN);
+#pragma unroll
+            for (int q = 0; q < 8; ++q) *a_chunk(S, q) = valid ? x[q] : make_uint4(0u, 0u, 0u, 0u);
+        }
+#pragma unroll
+        for (int layer = 0; layer < 3; ++layer) {
+            mlp_issue(S, layer);
+            if (!mlp_wait(S, phase, err)) {
+                failed = true;
+                break;
+            }
+            if (layer < 2) {
+                mlp_hidden(S, tl, layer == 0 ? Z1 : Z2, face, valid);
+            } else {
+                float o[NOUT];
+                mlp_out(tl, o);
+                if (valid) *reinterpret_cast<float4*>(Y + (size_t)face * 4) = make_float4(o[0], o[1], o[2], o[3]);
+            }
+        }
+    }
+    mlp_teardown(S);
+}
+
+// The inference path of a learned step in one kernel, per 128-face tile of a group: the features of every
+// face formed straight into the MLP's first operand, the three layers on the tensor cores, and
+// (FLUX) the plain MUSCL-Hancock HLLC flux computed on the CUDA cores while the first layer
+// runs.  Out go the correction dF [4][nf] (the correction kernel's formula), the guard's face
+// mask set to 1 and (FLUX) the plain flux F [4][nf].  The results equal those of features +
+// mlp_forward + correction (+ plain_flux) bit for bit: the same device functions.  Failure
+// handling as mlp_forward_kernel's.
+template <bool FLUX>
+__global__ void __launch_bounds__(kTcThreads, 3)
+face_kernel(const float* __restrict__ U, const float4* __restrict__ W, Grid G, float dt,
+            const __nv_bfloat16* __restrict__ Wb, const float* __restrict__ P, float* __restrict__ F,
+            float* __restrict__ dF, unsigned char* __restrict__ ok, int* __restrict__ err) {
+    extern __shared__ unsigned char smem_raw[];
+    TcSmem& S = *reinterpret_cast<TcSmem*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    const int nf = 2 * (G.n + 1) * G.n;
+    const float hdt = 0.5f * dt / G.dx;
+    mlp_setup(S, Wb, P);
+    const uint32_t tl = lane_addr(S);
+    uint32_t phase = 0;
+
+    for (int base = (blockIdx.x * 2 + grp()) * kTcRows; base < nf; base += gridDim.x * 2 * kTcRows) {
+        const int f = base + grp_tid();
+        const bool valid = f < nf;
+        float rr = 0.0f, cref = 0.0f;
+        bool xface = false;
+        {
+            uint32_t pk[32] = {};
+            if (valid) face_features(W, G, f, pk, rr, cref, xface);
+#pragma unroll
+            for (int q = 0; q < 8; ++q) *a_chunk(S, q) = make_uint4(pk[4 * q], pk[4 * q + 1], pk[4 * q + 2], pk[4 * q + 3]);
+        }
+        mlp_issue(S, 0);
+        if (valid) {
+            if (FLUX) {   // the plain flux while the tensor cores run the first layer
+                float fl[4];
+                plain_face_flux(U, G, hdt, f, fl);
+#pragma unroll
+                for (int v = 0; v < 4; ++v) F[(size_t)v * nf + f] = fl[v];
+            }
+            ok[f] = 1;
+        }
+        if (!mlp_wait(S, phase, err)) break;
+        mlp_hidden(S, tl, nullptr, f, valid);
+        mlp_issue(S, 1);
+        if (!mlp_wait(S, phase, err)) break;
+        mlp_hidden(S, tl, nullptr, f, valid);
+        mlp_issue(S, 2);
+        if (!mlp_wait(S, phase, err)) break;
+        float o[NOUT];
+        mlp_out(tl, o);
+        if (valid) {
+            const float m = rr * cref;
+            dF[f] = m * o[0];
+            dF[(size_t)nf + f] = m * cref * (xface ? o[1] : o[2]);
+            dF[2 * (size_t)nf + f] = m * cref * (xface ? o[2] : o[1]);
+            dF[3 * (size_t)nf + f] = m * cref * cref * o[3];
+        }
+    }
+    mlp_teardown(S);
 }
 
 size_t mlp_forward_smem() { return sizeof(TcSmem) + 1024; }
@@ -723,8 +952,16 @@ __global__ void update_kernel(const float* __restrict__ U, const float* __restri
         const float s = fmaxf(fabsf(w.u), fabsf(w.v)) + cs;
         if (s > m) m = s;
     }
+    // the CTA's maximum, then one atomic per CTA (non-negative floats order as their bit patterns)
+    __shared__ float wmax[32];
     for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-    if ((threadIdx.x & 31) == 0 && m > 0.0f) atomicMax(reinterpret_cast<int*>(maxs), __float_as_int(m));
+    if ((threadIdx.x & 31) == 0) wmax[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        m = threadIdx.x < (blockDim.x >> 5) ? wmax[threadIdx.x] : 0.0f;
+        for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if (threadIdx.x == 0 && m > 0.0f) atomicMax(reinterpret_cast<int*>(maxs), __float_as_int(m));
+    }
 }
 
 // dL/dY for L = (1/N) sum_cells sum_v w_v (U^{n+1}_v - T_v)^2, U^{n+1} with every correction
@@ -785,6 +1022,9 @@ struct hf_lc {
     double dx = 0, gamma = 1.4, cfl = 0.8, bound = 0.5;
     int guard_mode = 0;        // 0: change bound, 1: local-extremum bounds
     int train_guard = 0;       // training applies the guard as inference does
+    int fused = 1;             // inference: 1 features + MLP + correction in face_kernel, 2 with the
+                               // plain flux too, 0 the separate kernels
+    int face_ctas_per_sm = 0;  // face_kernel CTAs per SM (0: as many as fit)
     cudaStream_t stream = nullptr;
     float *U[2] = {nullptr, nullptr}, *F = nullptr, *dF = nullptr, *scale = nullptr, *Y = nullptr;
     float *Z1 = nullptr, *Z2 = nullptr, *dY = nullptr, *T = nullptr, *wv = nullptr;
@@ -837,26 +1077,35 @@ hf::lc::Grid grid(const hf_lc* L) {
 int nfaces(const hf_lc* L) { return 2 * (L->n + 1) * L->n; }
 int blocks_for(long long n, int t) { long long b = (n + t - 1) / t; return (int)(b > 4096 ? 4096 : (b < 1 ? 1 : b)); }
 
-// CTAs of the MLP forward: 4 per SM.  Each loads the weights once and then walks its tiles;
-// measured on the 512^2 learned step, 2 / 3 / 4 / 5 / 6 CTAs per SM gave 1175 / 1238 / 1257 /
-// 1243 / 987 Mcell-updates/s (shared memory would allow 6).
-int forward_grid_cap() {
-    static int cap = 0;
-    if (cap == 0) {
-        int sms = 0, dev = 0;
-        if (cudaGetDevice(&dev) != cudaSuccess ||
-            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1)
-            return 4 * 152;
-        cap = 4 * sms;
+// Persistent CTAs of the MLP kernels (256 threads, two 128-face tiles at a time): per_sm per SM (0: as
+// many as fit by registers, shared memory and TMEM), never more than the tiles.  The fit is
+// formed from the kernel's attributes: registers are allocated per warp in units of 256 from
+// each SM sub-partition's 16,384; each CTA holds its dynamic shared memory plus 1 KB the
+// hardware reserves; 4 CTAs x 128 TMEM columns fill an SM's 512.
+int mlp_grid(const void* kernel, int nf, int per_sm) {
+    int sms = 0, dev = 0, smem_sm = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        sms < 1)
+        sms = 152;
+    if (cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev) != cudaSuccess || smem_sm < 1)
+        smem_sm = 233472;
+    cudaFuncAttributes fa{};
+    int fit = 1;
+    if (cudaFuncGetAttributes(&fa, kernel) == cudaSuccess && fa.numRegs > 0) {
+        const int warp_regs = ((fa.numRegs * 32 + 255) / 256) * 256;
+        const int by_regs = 4 * (16384 / warp_regs) / (hf::lc::kTcThreads / 32);
+        const int by_smem = smem_sm / (int)(hf::lc::mlp_forward_smem() + fa.sharedSizeBytes + 1024);
+        fit = by_regs < by_smem ? by_regs : by_smem;
+        fit = fit > 4 ? 4 : (fit < 1 ? 1 : fit);
     }
-    return cap;
+    const int per = per_sm > 0 && per_sm < fit ? per_sm : fit;
+    const int tiles = (nf + hf::lc::kTcThreads - 1) / hf::lc::kTcThreads;
+    return tiles < per * sms ? tiles : per * sms;
 }
 
 void launch_forward(hf_lc* L, int nf, bool save_acts) {
-    const int tiles = (nf + hf::lc::kTcRows - 1) / hf::lc::kTcRows;
-    const int cap = forward_grid_cap();
-    const int grid = tiles < cap ? tiles : cap;
-    hf::lc::mlp_forward_kernel<<<grid, hf::lc::kTcRows, hf::lc::mlp_forward_smem(), L->stream>>>(
+    const int g = mlp_grid((const void*)hf::lc::mlp_forward_kernel, nf, 0);
+    hf::lc::mlp_forward_kernel<<<g, hf::lc::kTcThreads, hf::lc::mlp_forward_smem(), L->stream>>>(
         L->X, nf, L->Wb, L->P, L->Y, save_acts ? L->Z1 : nullptr, save_acts ? L->Z2 : nullptr, L->derr);
 }
 
@@ -876,9 +1125,28 @@ void launch_features(hf_lc* L) {
     features_kernel<<<blocks_for(nf, hf::lc::kFeatNT), hf::lc::kFeatNT, 0, L->stream>>>(L->Wp, G, L->X, L->scale);
 }
 
-int fluxes(hf_lc* L, float dt, bool use_mlp, bool save_acts) {
+// plain fluxes F, and (use_mlp) the corrections dF for state U[cur].  Inference (no saved
+// activations) with the fused kernel also sets the guard's face mask; returns through *mask_set
+// whether it did.
+int fluxes(hf_lc* L, float dt, bool use_mlp, bool save_acts, bool* mask_set = nullptr) {
     hf::lc::Grid G = grid(L);
     const int nf = nfaces(L);
+    if (mask_set) *mask_set = false;
+    if (use_mlp && !save_acts && L->fused) {
+        if (L->fused == 1)
+            plain_flux_kernel<<<blocks_for(nf, 256), 256, 0, L->stream>>>(L->U[L->cur], G, dt, L->F);
+        prims_kernel<<<blocks_for(L->n * L->n, 256), 256, 0, L->stream>>>(L->U[L->cur], L->n, G.g1, L->Wp);
+        const size_t sm = hf::lc::mlp_forward_smem();
+        if (L->fused == 2)
+            face_kernel<true><<<mlp_grid((const void*)face_kernel<true>, nf, L->face_ctas_per_sm), hf::lc::kTcThreads, sm,
+                                L->stream>>>(L->U[L->cur], L->Wp, G, dt, L->Wb, L->P, L->F, L->dF, L->ok, L->derr);
+        else
+            face_kernel<false><<<mlp_grid((const void*)face_kernel<false>, nf, L->face_ctas_per_sm), hf::lc::kTcThreads,
+                                 sm, L->stream>>>(L->U[L->cur], L->Wp, G, dt, L->Wb, L->P, L->F, L->dF, L->ok, L->derr);
+        LCK(cudaGetLastError());
+        if (mask_set) *mask_set = true;
+        return HF_OK;
+    }
     plain_flux_kernel<<<blocks_for(nf, 256), 256, 0, L->stream>>>(L->U[L->cur], G, dt, L->F);
     if (use_mlp) {
         launch_features(L);
@@ -907,9 +1175,15 @@ int hf_lc_create(int n, double dx, double gamma, double cfl, int limiter, hf_lc*
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return lfail(L, HF_ERR_NO_DEVICE, "no CUDA device");
     L->n = n; L->dx = dx; L->gamma = gamma; L->cfl = cfl; L->lim = limiter;
     LCK(cudaStreamCreateWithFlags(&L->stream, cudaStreamNonBlocking));
-    // the MLP kernel's two operand buffers take it past the 48 KB default
+    LCK(cudaFuncSetAttribute(hf::lc::face_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)hf::lc::mlp_forward_smem()));
+    LCK(cudaFuncSetAttribute(hf::lc::face_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)hf::lc::mlp_forward_smem()));
     LCK(cudaFuncSetAttribute(hf::lc::mlp_forward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)hf::lc::mlp_forward_smem()));
+    for (const void* k : {(const void*)hf::lc::face_kernel<false>, (const void*)hf::lc::face_kernel<true>,
+                          (const void*)hf::lc::mlp_forward_kernel})
+        LCK(cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
     const size_t cells = (size_t)n * n, nf = nfaces(L);
     int r;
     if ((r = alloc(L, &L->U[0], 4 * cells)) || (r = alloc(L, &L->U[1], 4 * cells)) || (r = alloc(L, &L->F, 4 * nf)) ||
@@ -987,13 +1261,14 @@ int hf_lc_step(hf_lc* L, double dt, int use_mlp, int64_t* rejected_cells) {
     hf::TraceRange trace_("hf_lc_step");
     if (!L || dt <= 0) return HF_ERR_ARG;
     hf::lc::Grid G = grid(L);
-    int r = fluxes(L, (float)dt, use_mlp != 0, false);
+    bool mask_set = false;
+    int r = fluxes(L, (float)dt, use_mlp != 0, false, &mask_set);
     if (r) return r;
     const float rr = (float)(dt / L->dx);
     const int nf = nfaces(L);
     LCK(cudaMemsetAsync(L->maxs, 0, 4, L->stream));
     if (use_mlp) {
-        LCK(cudaMemsetAsync(L->ok, 1, nf, L->stream));
+        if (!mask_set) LCK(cudaMemsetAsync(L->ok, 1, nf, L->stream));
         LCK(cudaMemsetAsync(L->rejected, 0, 8, L->stream));
         guard_kernel<<<blocks_for((long long)L->n * L->n, 256), 256, 0, L->stream>>>(
             L->U[L->cur], L->F, L->dF, G, rr, (float)L->bound, L->guard_mode, L->ok, L->rejected);
@@ -1053,6 +1328,12 @@ int hf_lc_set_bound(hf_lc* L, double bound) { if (!L || bound <= 0) return HF_ER
 int hf_lc_set_train_guard(hf_lc* L, int on) {
     if (!L) return HF_ERR_ARG;
     L->train_guard = on ? 1 : 0;
+    return HF_OK;
+}
+int hf_lc_set_fused(hf_lc* L, int fused, int ctas_per_sm) {
+    if (!L || fused < 0 || fused > 2 || ctas_per_sm < 0 || ctas_per_sm > 4) return HF_ERR_ARG;
+    L->fused = fused;
+    L->face_ctas_per_sm = ctas_per_sm;
     return HF_OK;
 }
 int hf_lc_set_guard_mode(hf_lc* L, int mode) {

@@ -87,6 +87,12 @@ class LearnedSolver:
         """training steps apply the guard as inference does"""
         self._c(lib().hf_lc_set_train_guard(self._h, int(on)))
 
+    def set_fused(self, mode: int, ctas_per_sm: int = 0):
+        """how inference steps run: 1 (default) features + MLP + corrections in one kernel, 2 the
+        plain fluxes in it too, 0 separate kernels -- the same results bit for bit; ctas_per_sm
+        sets the fused kernel's launch shape (0: as many as fit)"""
+        self._c(lib().hf_lc_set_fused(self._h, int(mode), int(ctas_per_sm)))
+
     def set_guard_mode(self, mode: int):
         """0: change bound (set_bound); 1: local-extremum (flux-corrected transport) bounds"""
         self._c(lib().hf_lc_set_guard_mode(self._h, mode))
@@ -107,7 +113,12 @@ class LearnedSolver:
         self._c(lib().hf_lc_cfl_dt(self._h, C.byref(d)))
         return d.value
 
-    def step(self, dt: float, use_mlp: bool) -> int:
+    def step(self, dt: float, use_mlp: bool, count_rejected: bool = True):
+        """one step; returns the cells whose corrections the guard rejected (a wait for the
+        step), or None with count_rejected False (the step is only enqueued)"""
+        if not count_rejected:
+            self._c(lib().hf_lc_step(self._h, dt, int(use_mlp), None))
+            return None
         r = C.c_int64()
         self._c(lib().hf_lc_step(self._h, dt, int(use_mlp), C.byref(r)))
         return r.value

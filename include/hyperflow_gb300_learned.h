@@ -43,6 +43,12 @@ int hf_lc_set_guard_mode(hf_lc* L, int mode);
 /* on != 0: training steps apply the guard as inference does (rejected faces take the plain
  * flux and pass no gradient); default off */
 int hf_lc_set_train_guard(hf_lc* L, int on);
+/* How an inference step runs.  fused 1 (default): the features, the MLP and the corrections
+ * in one kernel per 256-face tile (face_kernel), the plain fluxes in their own kernel; 2: the
+ * plain fluxes inside face_kernel as well; 0: separate kernels (plain flux, features, MLP
+ * forward, correction).  All three give the same results bit for bit.  ctas_per_sm (0..4, 0 = as
+ * many as fit) sets face_kernel's launch shape. */
+int hf_lc_set_fused(hf_lc* L, int fused, int ctas_per_sm);
 
 int hf_lc_set_state(hf_lc* L, const float* U);
 int hf_lc_get_state(hf_lc* L, float* U);

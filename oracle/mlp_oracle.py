@@ -98,10 +98,10 @@ def features(U, gamma: float):
     """The MLP's inputs for every face, restating hf_learned.cu's feature kernel in float32
     (same operations, same order, IEEE float32 rounding): faces x first ([n][n+1], face i of
     row j between cells i-1 and i), then y; per face the 4x4 primitive stencil (normal offsets
-    -1..2 outer, tangential -1..2 inner; cells mirrored past the edges) as rho/rho_ref - 1,
-    u_n/c_ref, u_t/c_ref, p/p_ref - 1 with rho_ref, p_ref the two face cells' means and
-    c_ref = sqrt(max(gamma p_ref / rho_ref, 1e-12)).  Returns (BF16 bits [nf][64], scale
-    [nf][2] = rho_ref, c_ref)."""
+    -1..2 outer, tangential -1..2 inner; cells mirrored past the edges) as rho (1/rho_ref) - 1,
+    u_n (1/c_ref), u_t (1/c_ref), p (1/p_ref) - 1 with rho_ref, p_ref the two face cells' means,
+    c_ref = sqrt(max(gamma p_ref / rho_ref, 1e-12)) and each reciprocal a rounded float32
+    division.  Returns (BF16 bits [nf][64], scale [nf][2] = rho_ref, c_ref)."""
     U = np.asarray(U, np.float32)
     n = U.shape[1]
     g = np.float32(gamma)
@@ -134,13 +134,15 @@ def features(U, gamma: float):
             rr = np.float32(0.5) * (at(r, jl, il) + at(r, jl + nj, il + ni))
             pr = np.float32(0.5) * (at(p, jl, il) + at(p, jl + nj, il + ni))
             cref = np.sqrt(np.maximum(g * pr / rr, np.float32(1e-12)))
+            one = np.float32(1.0)
+            irr, ipr, ic = one / rr, one / pr, one / cref
             cols = []
             for a in (-1, 0, 1, 2):
                 for b in (-1, 0, 1, 2):
                     ci, cj = il + a * ni + b * ti, jl + a * nj + b * tj
                     wr, wu, wv, wp = at(r, cj, ci), at(u, cj, ci), at(v, cj, ci), at(p, cj, ci)
                     un, ut = (wu, wv) if d == 0 else (wv, wu)
-                    cols += [wr / rr - np.float32(1.0), un / cref, ut / cref, wp / pr - np.float32(1.0)]
+                    cols += [wr * irr - one, un * ic, ut * ic, wp * ipr - one]
         out_x.append(np.stack(cols, axis=1))
         out_s.append(np.stack([rr, cref], axis=1))
     x = np.concatenate(out_x).astype(np.float32)

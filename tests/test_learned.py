@@ -57,8 +57,8 @@ def test_mlp_forward_on_tensor_cores_matches_oracle():
     from hyperflow_gb300.learned import LearnedSolver
     rng = np.random.default_rng(4)
     ls = LearnedSolver(300, 1 / 300)   # room for 180,600 faces
-    # partial tiles, a full grid's faces, and more 128-face tiles than the kernel has CTAs (4 per
-    # SM), so that CTAs run two tiles at a time, the second of a pair partial or absent
+    # partial tiles, a full grid's faces, and more 256-face tiles than the kernel has CTAs (at
+    # most 4 per SM), so that CTAs walk several tiles, the last one partial
     for nf in (1000, 17, 2 * 65 * 64, 160_000 + 77):
         p, x = _rand_case(rng, nf)
         ls.set_params(p)
@@ -151,6 +151,40 @@ def test_guard_keeps_positivity_and_rejects():
     rho = U[0]
     pres = 0.4 * (U[3] - 0.5 * (U[1] ** 2 + U[2] ** 2) / rho)
     assert rejected > 0 and (rho > 0).all() and (pres > 0).all()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n,mode,ctas", [(37, 0, 0), (128, 0, 2), (128, 1, 1), (300, 0, 0), (300, 1, 3)])
+def test_fused_face_kernel_equals_the_separate_kernels(n, mode, ctas):
+    """An inference step with the features, MLP and corrections in one kernel per 256-face tile
+    (and with the plain flux in it too) against the separate kernels (plain flux, features, MLP
+    forward, correction): states and rejection counts equal bit for bit over steps of a
+    shock-bubble flow with corrections large enough that the guard rejects some, in both guard
+    modes (n = 37: a partial last tile; n = 300 at 1 CTA per SM: more tiles than CTAs)."""
+    from oracle import mlp_oracle as M
+    from hyperflow_gb300 import CartSolver, cases
+    from hyperflow_gb300.learned import LearnedSolver, init_params
+    s = CartSolver(cases.shock_bubble_case(n))
+    s.run(10)
+    U0 = s.state(0)[:, 2:-2, 2:-2].astype(np.float32)
+    s.close()
+    p = init_params(3, out_scale=0.05)
+    p[M.OFF_B3:] = [0.05, -0.03, 0.04, -0.2]
+    runs = []
+    for fused in (0, 1, 2):
+        ls = LearnedSolver(n, 1.0 / n)
+        ls.set_params(p)
+        ls.set_guard_mode(mode)
+        ls.set_fused(fused, ctas)
+        ls.set_state(U0)
+        rej = [ls.step(ls.cfl_dt(), use_mlp=True) for _ in range(8)]
+        runs.append((ls.state(), rej))
+        ls.close()
+    Ua, ra = runs[0]
+    assert sum(ra) > 0 and sum(ra) < 8 * n * n, ra
+    for Ub, rb in runs[1:]:
+        assert ra == rb
+        np.testing.assert_array_equal(Ua.view(np.uint32), Ub.view(np.uint32))
 
 
 @pytest.mark.gpu
