@@ -219,16 +219,14 @@ __device__ __forceinline__ uint32_t pack2(float lo, float hi) {
     return *reinterpret_cast<uint32_t*>(&v);
 }
 
-// face f's 64 features, rounded to BF16 and packed in pairs (normal offset outer, tangential
-// offset inner; per cell rho, u_n, u_t, p), its correction scale (rho_ref, c_ref) and whether it
-// is an x face.  The scaled values are products with the reciprocals of rho_ref, c_ref and
+// the 64 features of face (dir, i, j) (face_of's indices), rounded to BF16 and packed in pairs
+// (normal offset outer, tangential offset inner; per cell rho, u_n, u_t, p), and its correction
+// scale (rho_ref, c_ref).  The scaled values are products with the reciprocals of rho_ref, c_ref and
 // p_ref (one division each per face), and the stencil's mirrored columns and rows are formed
 // once per face.
-__device__ __forceinline__ void face_features(const float4* __restrict__ W, const Grid& G, int f, uint32_t* pk,
-                                              float& rr, float& cref, bool& xface) {
-    int dir, i, j;
-    face_of(f, G.n, dir, i, j);
-    xface = dir == 0;
+__device__ __forceinline__ void face_features(const float4* __restrict__ W, const Grid& G, int dir, int i, int j,
+                                              uint32_t* pk, float& rr, float& cref) {
+    const bool xface = dir == 0;
     const int n = G.n;
     // lower cell (il, jl); stencil cell (a, b), a along the normal and b along the face, both
     // -1..2, is column il + a, row jl + b on an x face and column il + b, row jl + a on a y face
@@ -272,8 +270,9 @@ __global__ void __launch_bounds__(kFeatNT) features_kernel(const float4* __restr
         uint32_t pk[32] = {};
         if (f < nf) {
             float rr, cref;
-            bool xface;
-            face_features(W, G, f, pk, rr, cref, xface);
+            int dir, i, j;
+            face_of(f, G.n, dir, i, j);
+            face_features(W, G, dir, i, j, pk, rr, cref);
             scale[2 * (size_t)f] = rr;
             scale[2 * (size_t)f + 1] = cref;
         }
@@ -590,26 +589,48 @@ __device__ __forceinline__ uint64_t gelu2x(uint64_t z) {
     return f2_fma(z, f2(tanh_fast(u.x), tanh_fast(u.y)), z);
 }
 
+// 16 accumulator columns of this thread's TMEM lane into r, without waiting: tc_wait16(r)
+// must come before r is read (several loads may be in flight; the wait covers them all)
+__device__ __forceinline__ void tc_ld16_issue(uint32_t taddr, uint32_t* r) {
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+                 : "r"(taddr));
+}
+__device__ __forceinline__ void tc_wait16(uint32_t* r) {
+    asm volatile("tcgen05.wait::ld.sync.aligned;"
+                 : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7]), "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]), "+r"(r[12]), "+r"(r[13]), "+r"(r[14]), "+r"(r[15])
+                 :
+                 : "memory");
+}
+
 // a hidden layer's epilogue: this thread's accumulator row (its face, bias included) through
-// GELU, doubled, into the next A operand as BF16; the pre-activations to Zs[face] when given
+// GELU, doubled, into the next A operand as BF16; the pre-activations to Zs[face] when given.
+// The row is read in four 16-column pieces, the next one loading while this one is processed.
 __device__ __forceinline__ void mlp_hidden(TcSmem& S, uint32_t tl, float* __restrict__ Zs, int face, bool valid) {
-#pragma unroll 1
-    for (int q = 0; q < 2; ++q) {
-        float z[32];
-        tc_ld32(tl + q * 32, z);
-        uint32_t hb[16];
+    uint32_t ra[16], rb[16];
+    tc_ld16_issue(tl, ra);
+    tc_wait16(ra);
 #pragma unroll
-        for (int k = 0; k < 16; ++k) {
-            const float2 g = f2_split(gelu2x(f2(z[2 * k], z[2 * k + 1])));
+    for (int q = 0; q < 4; ++q) {
+        uint32_t* cur = (q & 1) ? rb : ra;
+        uint32_t* nxt = (q & 1) ? ra : rb;
+        if (q < 3) tc_ld16_issue(tl + (q + 1) * 16, nxt);
+        uint32_t hb[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const float2 g = f2_split(gelu2x(f2(__uint_as_float(cur[2 * k]), __uint_as_float(cur[2 * k + 1]))));
             hb[k] = pack2(g.x, g.y);
         }
         if (Zs && valid) {
-            float4* zo = reinterpret_cast<float4*>(Zs + (size_t)face * H + q * 32);
+            float4* zo = reinterpret_cast<float4*>(Zs + (size_t)face * H + q * 16);
 #pragma unroll
-            for (int k = 0; k < 8; ++k) zo[k] = make_float4(z[4 * k], z[4 * k + 1], z[4 * k + 2], z[4 * k + 3]);
+            for (int k = 0; k < 4; ++k)
+                zo[k] = make_float4(__uint_as_float(cur[4 * k]), __uint_as_float(cur[4 * k + 1]),
+                                    __uint_as_float(cur[4 * k + 2]), __uint_as_float(cur[4 * k + 3]));
         }
-#pragma unroll
-        for (int c = 0; c < 4; ++c) *a_chunk(S, q * 4 + c) = make_uint4(hb[4 * c], hb[4 * c + 1], hb[4 * c + 2], hb[4 * c + 3]);
+        *a_chunk(S, 2 * q) = make_uint4(hb[0], hb[1], hb[2], hb[3]);
+        *a_chunk(S, 2 * q + 1) = make_uint4(hb[4], hb[5], hb[6], hb[7]);
+        if (q < 3) tc_wait16(nxt);
     }
 }
 
@@ -667,16 +688,22 @@ mlp_forward_kernel(const __nv_bfloat16* __restrict__ X, int nf, const __nv_bfloa
 // face formed straight into the MLP's first operand, the three layers on the tensor cores, and
 // (FLUX) the plain MUSCL-Hancock HLLC flux computed on the CUDA cores while the first layer
 // runs.  Out go the correction dF [4][nf] (the correction kernel's formula), the guard's face
-// mask set to 1 and (FLUX) the plain flux F [4][nf].  The results equal those of features +
+// mask set to 1, the step's rejection count and maximum wave speed zeroed, and (FLUX) the plain
+// flux F [4][nf].  The results equal those of features +
 // mlp_forward + correction (+ plain_flux) bit for bit: the same device functions.  Failure
 // handling as mlp_forward_kernel's.
 template <bool FLUX>
 __global__ void __launch_bounds__(kTcThreads, 3)
 face_kernel(const float* __restrict__ U, const float4* __restrict__ W, Grid G, float dt,
             const __nv_bfloat16* __restrict__ Wb, const float* __restrict__ P, float* __restrict__ F,
-            float* __restrict__ dF, unsigned char* __restrict__ ok, int* __restrict__ err) {
+            float* __restrict__ dF, unsigned char* __restrict__ ok, unsigned long long* __restrict__ rejected,
+            float* __restrict__ maxs, int* __restrict__ err) {
     extern __shared__ unsigned char smem_raw[];
     TcSmem& S = *reinterpret_cast<TcSmem*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    if (blockIdx.x == 0 && threadIdx.x == 0) {   // the step's counters, read by the guard and the update
+        *rejected = 0ull;
+        *maxs = 0.0f;
+    }
     const int nf = 2 * (G.n + 1) * G.n;
     const float hdt = 0.5f * dt / G.dx;
     mlp_setup(S, Wb, P);
@@ -686,11 +713,13 @@ face_kernel(const float* __restrict__ U, const float4* __restrict__ W, Grid G, f
     for (int base = (blockIdx.x * 2 + grp()) * kTcRows; base < nf; base += gridDim.x * 2 * kTcRows) {
         const int f = base + grp_tid();
         const bool valid = f < nf;
+        int dir = 0, i = 0, j = 0;
+        if (valid) face_of(f, G.n, dir, i, j);
+        const bool xface = dir == 0;
         float rr = 0.0f, cref = 0.0f;
-        bool xface = false;
         {
             uint32_t pk[32] = {};
-            if (valid) face_features(W, G, f, pk, rr, cref, xface);
+            if (valid) face_features(W, G, dir, i, j, pk, rr, cref);
 #pragma unroll
             for (int q = 0; q < 8; ++q) *a_chunk(S, q) = make_uint4(pk[4 * q], pk[4 * q + 1], pk[4 * q + 2], pk[4 * q + 3]);
         }
@@ -910,16 +939,18 @@ __device__ __forceinline__ bool guard_bad(const float* __restrict__ U, const flo
     return mode == 1 ? cell_bad_local(U, F, G, r, i, j, un) : cell_bad(G.g1, un, up, u0, bound);
 }
 
-// pass 1: mark faces whose correction is rejected (any adjacent cell violates)
+// pass 1: mark faces whose correction is rejected (any adjacent cell violates); Uc (optional)
+// keeps every cell's update with all its corrections for pass 2
 __global__ void guard_kernel(const float* __restrict__ U, const float* __restrict__ F, const float* __restrict__ dF,
                              Grid G, float r, float bound, int mode, unsigned char* __restrict__ ok,
-                             unsigned long long* __restrict__ rejected) {
+                             unsigned long long* __restrict__ rejected, float4* __restrict__ Uc) {
     const int n = G.n;
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n * n; c += gridDim.x * blockDim.x) {
         const int i = c % n, j = c / n;
         float un[4], up[4], u0[4];
         cell_update(U, F, dF, nullptr, n, r, i, j, un);
         cell_update(U, F, nullptr, nullptr, n, r, i, j, up);
+        if (Uc) Uc[c] = make_float4(un[0], un[1], un[2], un[3]);
         for (int v = 0; v < 4; ++v) u0[v] = U[(size_t)v * n * n + (size_t)j * n + i];
         if (guard_bad(U, F, G, r, i, j, un, up, u0, bound, mode)) {
             ok[xf(n, i, j)] = 0; ok[xf(n, i + 1, j)] = 0; ok[yf(n, i, j)] = 0; ok[yf(n, i, j + 1)] = 0;
@@ -929,25 +960,34 @@ __global__ void guard_kernel(const float* __restrict__ U, const float* __restric
 }
 
 // pass 2: the update (corrections where accepted); a cell still violating takes its plain update
+// Wn (optional): the primitives of the new state, as prims_kernel forms them, for the next step's
+// features.  Uc (optional, with dF and ok): pass 1's fully corrected updates -- a cell whose four
+// faces all kept their corrections takes its own (the same arithmetic as recomputing it; the
+// guard passed it, or a face would have been rejected), the others are recomputed.
 __global__ void update_kernel(const float* __restrict__ U, const float* __restrict__ F, const float* __restrict__ dF,
                               const unsigned char* __restrict__ ok, Grid G, float r, float bound, int mode,
-                              float* __restrict__ Un, float* __restrict__ maxs) {
+                              float* __restrict__ Un, float* __restrict__ maxs, float4* __restrict__ Wn,
+                              const float4* __restrict__ Uc) {
     const int n = G.n;
     float m = 0.0f;
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n * n; c += gridDim.x * blockDim.x) {
         const int i = c % n, j = c / n;
         float un[4], up[4], u0[4];
-        cell_update(U, F, nullptr, nullptr, n, r, i, j, up);
-        if (dF) {
+        if (Uc && ok[xf(n, i, j)] && ok[xf(n, i + 1, j)] && ok[yf(n, i, j)] && ok[yf(n, i, j + 1)]) {
+            const float4 q = Uc[c];
+            un[0] = q.x; un[1] = q.y; un[2] = q.z; un[3] = q.w;
+        } else if (dF) {
+            cell_update(U, F, nullptr, nullptr, n, r, i, j, up);
             cell_update(U, F, dF, ok, n, r, i, j, un);
             for (int v = 0; v < 4; ++v) u0[v] = U[(size_t)v * n * n + (size_t)j * n + i];
             if (ok && guard_bad(U, F, G, r, i, j, un, up, u0, bound, mode))
                 for (int v = 0; v < 4; ++v) un[v] = up[v];
         } else {
-            for (int v = 0; v < 4; ++v) un[v] = up[v];
+            cell_update(U, F, nullptr, nullptr, n, r, i, j, un);
         }
         for (int v = 0; v < 4; ++v) Un[(size_t)v * n * n + (size_t)j * n + i] = un[v];
         PrimF w = prim(G.g1, un);
+        if (Wn) Wn[(size_t)j * n + i] = make_float4(w.r, w.u, w.v, w.p);
         const float cs = sqrtf(G.g * w.p / w.r);
         const float s = fmaxf(fabsf(w.u), fabsf(w.v)) + cs;
         if (s > m) m = s;
@@ -1026,10 +1066,14 @@ struct hf_lc {
                                // plain flux too, 0 the separate kernels
     int face_ctas_per_sm = 0;  // face_kernel CTAs per SM (0: as many as fit)
     cudaStream_t stream = nullptr;
+    cudaStream_t side = nullptr;           // the plain fluxes, beside the fused face kernel
+    cudaEvent_t fork = nullptr, join = nullptr;
     float *U[2] = {nullptr, nullptr}, *F = nullptr, *dF = nullptr, *scale = nullptr, *Y = nullptr;
     float *Z1 = nullptr, *Z2 = nullptr, *dY = nullptr, *T = nullptr, *wv = nullptr;
     __nv_bfloat16 *X = nullptr, *Wb = nullptr;
     float4* Wp = nullptr;      // per-cell primitives (rho, u, v, p) for the feature stencils
+    bool wp_valid = false;     // Wp holds the primitives of U[cur] (written by the last step)
+    float4* Uc = nullptr;      // the guard pass's fully corrected cell updates
     float *P = nullptr, *grad = nullptr, *m1 = nullptr, *m2 = nullptr, *maxs = nullptr;
     unsigned char* ok = nullptr;
     unsigned long long* rejected = nullptr;
@@ -1122,27 +1166,41 @@ void launch_features(hf_lc* L) {
     hf::lc::Grid G = grid(L);
     const int nf = nfaces(L);
     prims_kernel<<<blocks_for(L->n * L->n, 256), 256, 0, L->stream>>>(L->U[L->cur], L->n, G.g1, L->Wp);
+    L->wp_valid = true;
     features_kernel<<<blocks_for(nf, hf::lc::kFeatNT), hf::lc::kFeatNT, 0, L->stream>>>(L->Wp, G, L->X, L->scale);
 }
 
 // plain fluxes F, and (use_mlp) the corrections dF for state U[cur].  Inference (no saved
-// activations) with the fused kernel also sets the guard's face mask; returns through *mask_set
-// whether it did.
+// activations) with the fused kernel also sets the guard's face mask and zeroes the step's
+// counters; returns through *mask_set whether it did.
 int fluxes(hf_lc* L, float dt, bool use_mlp, bool save_acts, bool* mask_set = nullptr) {
     hf::lc::Grid G = grid(L);
     const int nf = nfaces(L);
     if (mask_set) *mask_set = false;
     if (use_mlp && !save_acts && L->fused) {
-        if (L->fused == 1)
-            plain_flux_kernel<<<blocks_for(nf, 256), 256, 0, L->stream>>>(L->U[L->cur], G, dt, L->F);
-        prims_kernel<<<blocks_for(L->n * L->n, 256), 256, 0, L->stream>>>(L->U[L->cur], L->n, G.g1, L->Wp);
+        if (!L->wp_valid)   // else the previous step's update wrote them
+            prims_kernel<<<blocks_for(L->n * L->n, 256), 256, 0, L->stream>>>(L->U[L->cur], L->n, G.g1, L->Wp);
+        L->wp_valid = true;
         const size_t sm = hf::lc::mlp_forward_smem();
-        if (L->fused == 2)
-            face_kernel<true><<<mlp_grid((const void*)face_kernel<true>, nf, L->face_ctas_per_sm), hf::lc::kTcThreads, sm,
-                                L->stream>>>(L->U[L->cur], L->Wp, G, dt, L->Wb, L->P, L->F, L->dF, L->ok, L->derr);
-        else
-            face_kernel<false><<<mlp_grid((const void*)face_kernel<false>, nf, L->face_ctas_per_sm), hf::lc::kTcThreads,
-                                 sm, L->stream>>>(L->U[L->cur], L->Wp, G, dt, L->Wb, L->P, L->F, L->dF, L->ok, L->derr);
+        const int units = nf;
+        if (L->fused == 2) {
+            face_kernel<true><<<mlp_grid((const void*)face_kernel<true>, units, L->face_ctas_per_sm),
+                                hf::lc::kTcThreads, sm, L->stream>>>(L->U[L->cur], L->Wp, G, dt, L->Wb, L->P, L->F,
+                                                                     L->dF, L->ok, L->rejected, L->maxs, L->derr);
+        } else {
+            // the plain fluxes on the side stream, running beside the face kernel (independent
+            // work: the face kernel is latency-bound, the flux kernel arithmetic-bound); the face
+            // kernel at 2 CTAs per SM by default leaves the flux kernel room on every SM
+            LCK(cudaEventRecord(L->fork, L->stream));
+            face_kernel<false><<<mlp_grid((const void*)face_kernel<false>, units,
+                                          L->face_ctas_per_sm > 0 ? L->face_ctas_per_sm : 2),
+                                 hf::lc::kTcThreads, sm, L->stream>>>(L->U[L->cur], L->Wp, G, dt, L->Wb, L->P, L->F,
+                                                                      L->dF, L->ok, L->rejected, L->maxs, L->derr);
+            LCK(cudaStreamWaitEvent(L->side, L->fork, 0));
+            plain_flux_kernel<<<blocks_for(nf, 256), 256, 0, L->side>>>(L->U[L->cur], G, dt, L->F);
+            LCK(cudaEventRecord(L->join, L->side));
+            LCK(cudaStreamWaitEvent(L->stream, L->join, 0));
+        }
         LCK(cudaGetLastError());
         if (mask_set) *mask_set = true;
         return HF_OK;
@@ -1175,6 +1233,9 @@ int hf_lc_create(int n, double dx, double gamma, double cfl, int limiter, hf_lc*
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return lfail(L, HF_ERR_NO_DEVICE, "no CUDA device");
     L->n = n; L->dx = dx; L->gamma = gamma; L->cfl = cfl; L->lim = limiter;
     LCK(cudaStreamCreateWithFlags(&L->stream, cudaStreamNonBlocking));
+    LCK(cudaStreamCreateWithFlags(&L->side, cudaStreamNonBlocking));
+    LCK(cudaEventCreateWithFlags(&L->fork, cudaEventDisableTiming));
+    LCK(cudaEventCreateWithFlags(&L->join, cudaEventDisableTiming));
     LCK(cudaFuncSetAttribute(hf::lc::face_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)hf::lc::mlp_forward_smem()));
     LCK(cudaFuncSetAttribute(hf::lc::face_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1194,7 +1255,7 @@ int hf_lc_create(int n, double dx, double gamma, double cfl, int limiter, hf_lc*
         (r = alloc(L, &L->grad, (size_t)NPARAM)) || (r = alloc(L, &L->m1, (size_t)NPARAM)) ||
         (r = alloc(L, &L->m2, (size_t)NPARAM)) || (r = alloc(L, &L->maxs, 4)) || (r = alloc(L, &L->ok, nf)) ||
         (r = alloc(L, &L->rejected, 1)) || (r = alloc(L, &L->loss, 1)) || (r = alloc(L, &L->derr, 1)) ||
-        (r = alloc(L, &L->Wp, cells)))
+        (r = alloc(L, &L->Wp, cells)) || (r = alloc(L, &L->Uc, cells)))
         return r;
     return HF_OK;
 }
@@ -1202,7 +1263,11 @@ int hf_lc_create(int n, double dx, double gamma, double cfl, int limiter, hf_lc*
 void hf_lc_destroy(hf_lc* L) {
     if (!L) return;
     if (L->stream) cudaStreamSynchronize(L->stream);
+    if (L->side) cudaStreamSynchronize(L->side);
     for (void* p : L->allocs) cudaFree(p);
+    if (L->fork) cudaEventDestroy(L->fork);
+    if (L->join) cudaEventDestroy(L->join);
+    if (L->side) cudaStreamDestroy(L->side);
     if (L->stream) cudaStreamDestroy(L->stream);
     delete L;
 }
@@ -1232,6 +1297,7 @@ int hf_lc_set_state(hf_lc* L, const float* U) {
     if (!L || !U) return HF_ERR_ARG;
     LCK(cudaStreamSynchronize(L->stream));
     LCK(cudaMemcpy(L->U[L->cur], U, (size_t)4 * L->n * L->n * sizeof(float), cudaMemcpyHostToDevice));
+    L->wp_valid = false;
     return HF_OK;
 }
 
@@ -1249,7 +1315,7 @@ int hf_lc_cfl_dt(hf_lc* L, double* dt) {
     LCK(cudaMemsetAsync(L->maxs, 0, 4, L->stream));
     LCK(cudaMemsetAsync(L->F, 0, (size_t)4 * nfaces(L) * sizeof(float), L->stream));
     update_kernel<<<blocks_for((long long)L->n * L->n, 256), 256, 0, L->stream>>>(
-        L->U[L->cur], L->F, nullptr, nullptr, G, 0.0f, 0.0f, 0, L->U[L->cur ^ 1], L->maxs);
+        L->U[L->cur], L->F, nullptr, nullptr, G, 0.0f, 0.0f, 0, L->U[L->cur ^ 1], L->maxs, nullptr, nullptr);
     LCK(cudaGetLastError());
     LCK(cudaStreamSynchronize(L->stream));
     *dt = L->cfl * L->dx / max_speed(L);
@@ -1266,18 +1332,26 @@ int hf_lc_step(hf_lc* L, double dt, int use_mlp, int64_t* rejected_cells) {
     if (r) return r;
     const float rr = (float)(dt / L->dx);
     const int nf = nfaces(L);
-    LCK(cudaMemsetAsync(L->maxs, 0, 4, L->stream));
-    if (use_mlp) {
-        if (!mask_set) LCK(cudaMemsetAsync(L->ok, 1, nf, L->stream));
-        LCK(cudaMemsetAsync(L->rejected, 0, 8, L->stream));
-        guard_kernel<<<blocks_for((long long)L->n * L->n, 256), 256, 0, L->stream>>>(
-            L->U[L->cur], L->F, L->dF, G, rr, (float)L->bound, L->guard_mode, L->ok, L->rejected);
+    if (!mask_set) {   // else the fused kernel set the mask and zeroed the counters
+        LCK(cudaMemsetAsync(L->maxs, 0, 4, L->stream));
+        if (use_mlp) {
+            LCK(cudaMemsetAsync(L->ok, 1, nf, L->stream));
+            LCK(cudaMemsetAsync(L->rejected, 0, 8, L->stream));
+        }
     }
+    if (use_mlp)
+        guard_kernel<<<blocks_for((long long)L->n * L->n, 256), 256, 0, L->stream>>>(
+            L->U[L->cur], L->F, L->dF, G, rr, (float)L->bound, L->guard_mode, L->ok, L->rejected,
+            L->fused ? L->Uc : nullptr);
+    // an MLP step also leaves the primitives of the new state for the next one's features; with
+    // the fused kernels the update takes the guard pass's corrected states where no face was
+    // rejected (the separate kernels recompute them all: the same values)
     update_kernel<<<blocks_for((long long)L->n * L->n, 256), 256, 0, L->stream>>>(
         L->U[L->cur], L->F, use_mlp ? L->dF : nullptr, use_mlp ? L->ok : nullptr, G, rr, (float)L->bound,
-        L->guard_mode, L->U[L->cur ^ 1], L->maxs);
+        L->guard_mode, L->U[L->cur ^ 1], L->maxs, use_mlp ? L->Wp : nullptr, use_mlp && L->fused ? L->Uc : nullptr);
     LCK(cudaGetLastError());
     L->cur ^= 1;
+    L->wp_valid = use_mlp != 0;
     L->t += dt;
     L->steps += 1;
     if (rejected_cells) {
@@ -1351,7 +1425,10 @@ int hf_lc_train_step(hf_lc* L, const float* U0, const float* T, const float* w, 
     const size_t bytes = (size_t)4 * L->n * L->n * sizeof(float);
     const int nf = nfaces(L);
     hf::lc::Grid G = grid(L);
-    if (U0) LCK(cudaMemcpyAsync(L->U[L->cur], U0, bytes, cudaMemcpyHostToDevice, L->stream));
+    if (U0) {
+        LCK(cudaMemcpyAsync(L->U[L->cur], U0, bytes, cudaMemcpyHostToDevice, L->stream));
+        L->wp_valid = false;
+    }
     LCK(cudaMemcpyAsync(L->T, T, bytes, cudaMemcpyHostToDevice, L->stream));
     LCK(cudaMemcpyAsync(L->wv, w, 4 * sizeof(float), cudaMemcpyHostToDevice, L->stream));
     int r = fluxes(L, (float)dt, true, true);
@@ -1361,12 +1438,13 @@ int hf_lc_train_step(hf_lc* L, const float* U0, const float* T, const float* w, 
         LCK(cudaMemsetAsync(L->ok, 1, nf, L->stream));
         LCK(cudaMemsetAsync(L->rejected, 0, 8, L->stream));
         guard_kernel<<<blocks_for((long long)L->n * L->n, 256), 256, 0, L->stream>>>(
-            L->U[L->cur], L->F, L->dF, G, rr, (float)L->bound, L->guard_mode, L->ok, L->rejected);
+            L->U[L->cur], L->F, L->dF, G, rr, (float)L->bound, L->guard_mode, L->ok, L->rejected, nullptr);
         update_kernel<<<blocks_for((long long)L->n * L->n, 256), 256, 0, L->stream>>>(
-            L->U[L->cur], L->F, L->dF, L->ok, G, rr, (float)L->bound, L->guard_mode, L->U[L->cur ^ 1], L->maxs);
+            L->U[L->cur], L->F, L->dF, L->ok, G, rr, (float)L->bound, L->guard_mode, L->U[L->cur ^ 1], L->maxs,
+            nullptr, nullptr);
     } else {
         update_kernel<<<blocks_for((long long)L->n * L->n, 256), 256, 0, L->stream>>>(
-            L->U[L->cur], L->F, L->dF, nullptr, G, rr, 0.0f, 0, L->U[L->cur ^ 1], L->maxs);
+            L->U[L->cur], L->F, L->dF, nullptr, G, rr, 0.0f, 0, L->U[L->cur ^ 1], L->maxs, nullptr, nullptr);
     }
     LCK(cudaMemsetAsync(L->loss, 0, 8, L->stream));
     loss_grad_kernel<<<blocks_for(nf, 256), 256, 0, L->stream>>>(L->U[L->cur ^ 1], L->T, L->scale, L->n, rr, L->wv,
