@@ -441,6 +441,12 @@ def bench_uns(args):
     s.close()
 
 
+def state_note(args, t_start: float) -> str:
+    if args.pre_steps > 0:
+        return f"developed flow: timed from t = {t_start:.4g}, after {args.pre_steps} untimed steps"
+    return "from the initial condition (first steps of the run)"
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -462,6 +468,12 @@ def main():
                     help="scheme of the square workload")
     ap.add_argument("--per-block-launches", action="store_true",
                     help="ffs/square workloads: one stencil launch per block instead of the all-blocks launch")
+    ap.add_argument("--pre-steps", type=int, default=0,
+                    help="ffs/square workloads: untimed steps before the warm-up, so that the timed steps see a "
+                         "developed flow instead of the initial condition")
+    ap.add_argument("--developed-steps", type=int, default=10000,
+                    help="ffs workload, full run: after the main measurement, advance this many untimed steps "
+                         "and time --steps more on the developed flow (0: skip)")
     ap.add_argument("--quick", action="store_true",
                     help="device-resident timing only (no graph pass, e2e or CPU baseline)")
     args = ap.parse_args()
@@ -509,6 +521,10 @@ def main():
     stream = torch.cuda.ExternalStream(s.stream())
 
     # ---- device-resident timed region ----
+    if args.pre_steps > 0:
+        s.run(args.pre_steps, graph=True)
+        s.sync()
+    t_start = s.time()[0]
     s.run(args.warmup, graph=False)
     s.sync()
     s.profile(True)          # events around every step's stencil launches (same stream)
@@ -532,7 +548,8 @@ def main():
         if rank == 0:
             print(json.dumps({"metric": "Mcell-updates/s", "value": value, "unit": "Mcell-updates/s",
                               "steps": args.steps, "ms_per_step": t_max / args.steps,
-                              "config": {"workload": workload_name(args), "cells": cells},
+                              "config": {"workload": workload_name(args), "cells": cells,
+                                         "state": state_note(args, t_start)},
                               "stencil_ms_per_step": stencil_ms / args.steps,
                               "blocks_rerun": reruns}), flush=True)
         s.close()
@@ -570,6 +587,26 @@ def main():
     barrier()
     e2e_s = time.perf_counter() - t0
     e2e_value = ws * cells * e2e_steps / e2e_s / 1e6
+
+    # ---- the same steps on a developed flow: the bow shock, reflections and subsonic regions put
+    # HLLC star states on many more faces than the uniform inflow the run starts from ----
+    developed = None
+    if args.workload == "ffs" and args.developed_steps > 0:
+        s.run(args.developed_steps, graph=True)
+        s.sync()
+        t_dev = s.time()[0]
+        s.run(args.warmup, graph=False)
+        barrier()
+        d0 = torch.cuda.Event(enable_timing=True)
+        d1 = torch.cuda.Event(enable_timing=True)
+        d0.record(stream)
+        s.run(args.steps, graph=False)
+        d1.record(stream)
+        torch.cuda.synchronize()
+        s.sync()
+        dms = d0.elapsed_time(d1)
+        developed = {"value": cells * args.steps / (dms / 1e3) / 1e6, "unit": "Mcell-updates/s",
+                     "ms_per_step": dms / args.steps, "t_start": t_dev, "untimed_steps": args.developed_steps}
 
     # ---- roofline of the stencil kernel ----
     hbm, peak_kind = peaks()
@@ -629,6 +666,7 @@ def main():
             "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (the case's own initial condition: uniform Mach 3 inflow)",
             "config": {"workload": workload_name(args), "cells": cells, "blocks": nb, "limiter": args.limiter,
+                       "state": state_note(args, t_start),
                        "cfl": 0.8, "l2": "state 2 x 151 MB buffers > 129 MB L2, no flush needed",
                        "parallelism": "replicas" if ws > 1 else "single GPU"},
             "roofline": roof,
@@ -638,6 +676,7 @@ def main():
                     "d2h_bytes_per_step": h2d, "steps": e2e_steps,
                     "path": "kernels read and write pinned host buffers" if direct else "copies"},
             "gpu_launches": launches_per_step * args.steps,
+            "developed": developed,
             "clocks": clk.summary(),
             "graph_value": graph_value,
             "hllc_zero_flux_fallbacks": hllc_fallbacks,
