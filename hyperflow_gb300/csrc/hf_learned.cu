@@ -51,20 +51,17 @@ __device__ __forceinline__ float tanh_fast(float x) {
     asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
     return y;
 }
-// GELU, tanh form: 0.5 z (1 + tanh(k (z + 0.044715 z^3))), k = sqrt(2/pi), formed as h + h t
-// with h = z / 2 and t = tanh(z (k + 0.044715 k z^2)) -- half of what the MLP kernels' packed
-// gelu2x computes, exactly, so the backward's recomputed activations equal the forward's
-__device__ __forceinline__ float gelu(float z) {
+// GELU, tanh form: 0.5 z (1 + tanh(k (z + 0.044715 z^3))), k = sqrt(2/pi), formed as h + h t with
+// h = z / 2 and t = tanh(z (k + 0.044715 k z^2)) -- half of what the MLP kernels' packed gelu2x
+// computes, exactly, so the backward's recomputed activations equal the forward's -- and its
+// derivative 0.5 (1 + t) + 0.5 z (1 - t^2) k (1 + 3 0.044715 z^2) from the same tanh
+__device__ __forceinline__ void gelu_both(float z, float& h, float& g) {
     const float k = 0.7978845608028654f, c = 0.7978845608028654f * 0.044715f;
-    const float t = tanh_fast(z * fmaf(z * z, c, k));
-    const float h = z * 0.5f;
-    return fmaf(h, t, h);
-}
-__device__ __forceinline__ float gelu_grad(float z) {
-    const float k = 0.7978845608028654f;
-    const float u = k * (z + 0.044715f * z * z * z);
-    const float t = tanh_fast(u);
-    return 0.5f * (1.0f + t) + 0.5f * z * (1.0f - t * t) * k * (1.0f + 3.0f * 0.044715f * z * z);
+    const float z2 = z * z;
+    const float t = tanh_fast(z * fmaf(z2, c, k));
+    const float hz = z * 0.5f;
+    h = fmaf(hz, t, hz);
+    g = fmaf(hz * fmaf(-t, t, 1.0f), fmaf(3.0f * c, z2, k), fmaf(0.5f, t, 0.5f));
 }
 
 __device__ __forceinline__ int mir(int x, int n) {
@@ -756,85 +753,276 @@ face_kernel(const float* __restrict__ U, const float4* __restrict__ W, Grid G, f
 size_t mlp_forward_smem() { return sizeof(TcSmem) + 1024; }
 
 // ---------------------------------------------------------------------------------
-// MLP backward (FP32 on the CUDA cores, the forward's BF16 weights and activations)
+// MLP backward on the tensor cores (BF16 operands, FP32 accumulation in TMEM)
 // ---------------------------------------------------------------------------------
-constexpr int kBwdFaces = 16;   // 38 KB of static shared memory per CTA
-__global__ void __launch_bounds__(256)
-mlp_backward_kernel(const __nv_bfloat16* __restrict__ X, int nf, const __nv_bfloat16* __restrict__ Wb,
-                    const float* __restrict__ Z1, const float* __restrict__ Z2,
-                    const float* __restrict__ dY, float* __restrict__ grad) {
-    __shared__ float sW2[H * H], sW3[NOUT * H];
-    __shared__ float sx[kBwdFaces][NIN], sh1[kBwdFaces][H], sh2[kBwdFaces][H];
-    __shared__ float sdz1[kBwdFaces][H], sdz2[kBwdFaces][H], sdy[kBwdFaces][NOUT];
-    for (int k = threadIdx.x; k < H * H; k += blockDim.x) sW2[k] = __bfloat162float(Wb[H * NIN + k]);
-    for (int k = threadIdx.x; k < NOUT * H; k += blockDim.x) sW3[k] = __bfloat162float(Wb[H * NIN + H * H + k]);
-    // per-thread gradient accumulators: thread owns 16 entries of each weight matrix
-    float gW1[16], gW2[16], gb1 = 0.f, gb2 = 0.f, gW3 = 0.f, gb3 = 0.f;
-    for (int q = 0; q < 16; ++q) gW1[q] = gW2[q] = 0.f;
-    const int tid = threadIdx.x;
-    __syncthreads();
-    for (int base = blockIdx.x * kBwdFaces; base < nf; base += gridDim.x * kBwdFaces) {
-        // stage inputs, activations (as the forward rounded them) and output gradients
-        for (int k = tid; k < kBwdFaces * H; k += 256) {
-            const int f = k / H, c = k % H, r = base + f;
-            const bool ok = r < nf;
-            sx[f][c] = ok ? __bfloat162float(X[(size_t)r * NIN + c]) : 0.f;
-            const float z1 = ok ? Z1[(size_t)r * H + c] : 0.f, z2 = ok ? Z2[(size_t)r * H + c] : 0.f;
-            sh1[f][c] = __bfloat162float(__float2bfloat16_rn(gelu(z1)));
-            sh2[f][c] = __bfloat162float(__float2bfloat16_rn(gelu(z2)));
-            sdz1[f][c] = gelu_grad(z1);     // temporarily the derivative factors
-            sdz2[f][c] = gelu_grad(z2);
-        }
-        for (int k = tid; k < kBwdFaces * NOUT; k += 256) {
-            const int f = k / NOUT, o = k % NOUT, r = base + f;
-            sdy[f][o] = r < nf ? dY[(size_t)r * NOUT + o] : 0.f;
-        }
-        __syncthreads();
-        // dz2 = (dY W3) * gelu'(z2)
-        for (int k = tid; k < kBwdFaces * H; k += 256) {
-            const int f = k / H, c = k % H;
-            float s = 0.f;
-            for (int o = 0; o < NOUT; ++o) s += sdy[f][o] * sW3[o * H + c];
-            sdz2[f][c] *= s;
-        }
-        __syncthreads();
-        // dz1 = (dz2 W2) * gelu'(z1)
-        for (int k = tid; k < kBwdFaces * H; k += 256) {
-            const int f = k / H, c = k % H;
-            float s = 0.f;
-            for (int o = 0; o < H; ++o) s += sdz2[f][o] * sW2[o * H + c];
-            sdz1[f][c] *= s;
-        }
-        __syncthreads();
-        // weight gradients: thread tid owns rows (tid / 4), columns (tid % 4) * 16 .. + 15
-        const int row = tid >> 2, c0 = (tid & 3) * 16;
-        for (int f = 0; f < kBwdFaces; ++f) {
-            const float d1 = sdz1[f][row], d2 = sdz2[f][row];
-            for (int q = 0; q < 16; ++q) {
-                gW1[q] += d1 * sx[f][c0 + q];
-                gW2[q] += d2 * sh1[f][c0 + q];
-            }
-        }
-        if ((tid & 3) == 0)
-            for (int f = 0; f < kBwdFaces; ++f) { gb1 += sdz1[f][row]; gb2 += sdz2[f][row]; }
-        // W3 (4 x 64) and b3: threads 0..255 own one W3 entry each
-        {
-            const int o = tid / H, c = tid % H;
-            for (int f = 0; f < kBwdFaces; ++f) gW3 += sdy[f][o] * sh2[f][c];
-            if (tid < NOUT)
-                for (int f = 0; f < kBwdFaces; ++f) gb3 += sdy[f][tid];
-        }
-        __syncthreads();
-    }
-    const int row = tid >> 2, c0 = (tid & 3) * 16;
-    for (int q = 0; q < 16; ++q) {
-        atomicAdd(&grad[OFF_W1 + row * NIN + c0 + q], gW1[q]);
-        atomicAdd(&grad[OFF_W2 + row * H + c0 + q], gW2[q]);
-    }
-    if ((tid & 3) == 0) { atomicAdd(&grad[OFF_B1 + row], gb1); atomicAdd(&grad[OFF_B2 + row], gb2); }
-    atomicAdd(&grad[OFF_W3 + tid], gW3);
-    if (tid < NOUT) atomicAdd(&grad[OFF_B3 + tid], gb3);
+// Per tile of 128 faces (one per TMEM lane; four threads per face, 16 of the 64 units each) of a
+// 512-thread CTA:
+//   the tile's saved rows (pre-activations z1, z2, inputs x, output gradients dY) arrive in
+//     shared memory by coalesced 16-byte asynchronous copies into rows padded by 16 bytes, so
+//     that a thread reading its own face's row meets no bank conflict; the next tile's are
+//     issued as soon as this one's are consumed, so the copies overlap the MMAs;
+//   dz2 = (dY W3) * gelu'(z2) on the CUDA cores (K = 4);
+//   dz1 = (dz2 W2) * gelu'(z1): one MMA, M 128 faces, N 64, K 64; A = dz2 read in place from the
+//     weight-gradient operand below (its bytes are a K-major view of the faces' dz2 rows), B =
+//     W2 transposed into K-major rows at setup;
+//   the weight gradients in one MMA per tile, accumulated in TMEM over all the CTA's tiles:
+//     M 128 = [dz1 | dz2] units, N 144 = [x | h1 | 1 | 0 ...], K 128 = the tile's faces, both
+//     operands MN-major (a face's values contiguous): D[0:64][0:64] = sum dz1^T x = dW1,
+//     D[64:128][64:128] = sum dz2^T h1 = dW2, D[:][128] = sum dz = db1, db2; the off-diagonal
+//     blocks are not used;
+//   dW3 = sum dY^T h2 and db3 on the CUDA cores from shared memory while that MMA runs.
+// The activations h1, h2 are the forward's (BF16(gelu(z)) from the saved pre-activations).
+// MN-major canonical layout without swizzle: core matrices of 8 K-rows x 8 contiguous M/N
+// elements (128 B), K-adjacent core matrices 128 B apart (the descriptor's leading offset),
+// M/N-adjacent ones 2048 B apart (its stride offset), so a face's 8 consecutive values are one
+// 16-byte store.  Bounded waits as the forward kernel's.
+constexpr int kBwTile = 128;                 // faces per tile = threads per CTA = the MMA's K
+constexpr int kBwN = 144;                    // N of the weight-gradient MMA
+constexpr int kBwColD1 = 192;                // TMEM column of the dz1 accumulator (64 columns)
+constexpr int kBwCols = 256;                 // TMEM columns held by a CTA
+
+__device__ __forceinline__ uint32_t mn_off(int r, int k) {   // bytes; K = 128 faces
+    return (uint32_t)((r >> 3) * (kBwTile * 16) + (k >> 3) * 128 + (k & 7) * 16 + (r & 7) * 2);
 }
+__device__ __forceinline__ uint32_t k64_off(int r, int k) {  // bytes; K-major, K = 64
+    return (uint32_t)((r >> 3) * 1024 + (k >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2);
+}
+__device__ __forceinline__ uint64_t smem_desc_lbo_sbo(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+    return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)(lbo >> 4) << 16) | ((uint64_t)(sbo >> 4) << 32) |
+           (1ull << 46);
+}
+// kind::f16 instruction descriptor, both operands MN-major
+__host__ __device__ constexpr uint32_t idesc_bf16_mn(int m, int n) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | (1u << 15) | (1u << 16) | ((uint32_t)(n >> 3) << 17) |
+           ((uint32_t)(m >> 4) << 24);
+}
+constexpr int kBwParts = 4;                          // threads per face: each takes 16 of the 64 units
+constexpr int kBwThreads = kBwTile * kBwParts;       // 512
+constexpr int kBwU = H / kBwParts;                   // 16 units per thread
+
+struct __align__(1024) BwSmem {
+    unsigned char aw[128 * kBwTile * 2];    // [dz1 | dz2] per face, MN-major (32 KB)
+    unsigned char bw[kBwN * kBwTile * 2];   // [x | h1 | 1 | 0] per face, MN-major (36 KB)
+    unsigned char w2t[64 * 64 * 2];         // W2 transposed, K-major (8 KB)
+    float z1[kBwTile][H + 4], z2[kBwTile][H + 4];   // the tile's saved rows, padded (68 KB)
+    __nv_bfloat16 x[kBwTile][NIN + 8];              // (18 KB)
+    float dyr[kBwTile][NOUT];                       // (2 KB)
+    __nv_bfloat16 h2[kBwTile][H + 8];               // the tile's h2 and dY for dW3 (18 KB + 2 KB)
+    float dy[kBwTile][NOUT];
+    float w3[NOUT][H];
+    uint64_t bar;
+    uint32_t taddr;
+};
+
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
+__global__ void __launch_bounds__(kBwThreads, 1)
+mlp_backward_kernel(const __nv_bfloat16* __restrict__ X, int nf, const __nv_bfloat16* __restrict__ Wb,
+                    const float* __restrict__ Z1, const float* __restrict__ Z2, const float* __restrict__ dY,
+                    float* __restrict__ grad, int* __restrict__ err) {
+    extern __shared__ unsigned char smem_raw[];
+    BwSmem& S = *reinterpret_cast<BwSmem*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    const int tid = threadIdx.x;
+    const int l = tid & (kBwTile - 1), part = tid / kBwTile, u0 = part * kBwU;   // face row, its units
+    // W2 transposed: B row c, K column o = W2[o][c]; W3 as FP32; the constant rows of bw
+    for (int e = tid; e < H * H; e += kBwThreads) {
+        const int o = e / H, c = e % H;
+        *reinterpret_cast<__nv_bfloat16*>(S.w2t + k64_off(c, o)) = Wb[H * NIN + e];
+    }
+    for (int e = tid; e < NOUT * H; e += kBwThreads) S.w3[e / H][e % H] = __bfloat162float(Wb[H * NIN + H * H + e]);
+    if (part < 2) {
+        const uint32_t one = (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(1.0f));
+        const int r = 128 + part * 8;
+        *reinterpret_cast<uint4*>(S.bw + mn_off(r, l)) = make_uint4(r == 128 ? one : 0u, 0u, 0u, 0u);
+    }
+    if (tid == 0) mbar_init(&S.bar, 1);
+    if ((tid >> 5) == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&S.taddr)),
+                     "r"(kBwCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    async_smem_fence();
+    tc_before_sync();
+    __syncthreads();
+    tc_after_sync();
+    const uint32_t tm = S.taddr;
+    const uint32_t lane = tm + ((uint32_t)(((tid >> 5) & 3) * 32) << 16);   // lane quarter of row l
+    uint32_t phase = 0;
+    bool failed = false, first = true, ld_inflight = false;   // ld_inflight: a tile's copies issued, not waited for
+    float g3 = 0.0f, gb3 = 0.0f;   // dW3 entry (tid mod 256) over half the faces; db3
+
+    // the saved rows of the tile at base into the padded rows: coalesced 16-byte asynchronous
+    // copies by all threads, one commit group (waited for before the rows are read)
+    auto load_tile = [&](int base) {
+        const int nv = nf - base < kBwTile ? nf - base : kBwTile;
+        for (int c = tid; c < nv * (H / 4); c += kBwThreads) {
+            const int r = c / (H / 4), k = (c % (H / 4)) * 4;
+            cp_async16(&S.z1[r][k], Z1 + (size_t)(base + r) * H + k);
+            cp_async16(&S.z2[r][k], Z2 + (size_t)(base + r) * H + k);
+        }
+        for (int c = tid; c < nv * (NIN / 8); c += kBwThreads) {
+            const int r = c / (NIN / 8), k = (c % (NIN / 8)) * 8;
+            cp_async16(&S.x[r][k], X + (size_t)(base + r) * NIN + k);
+        }
+        for (int c = tid; c < nv; c += kBwThreads) cp_async16(S.dyr[c], dY + (size_t)(base + c) * NOUT);
+        cp_async_commit();
+    };
+    // publish the operands, issue MMAs (thread 0), wait; false when the bounded wait gave up
+    auto run_mma = [&](int which) -> bool {
+        async_smem_fence();
+        tc_before_sync();
+        __syncthreads();
+        if (tid == 0) {
+            tc_after_sync();
+            if (which == 0) {   // dz1 pre-activations: dz2 (K-major view of aw's rows 64..127) x W2^T
+                const uint32_t sa = smem_u32(S.aw) + 8 * (kBwTile * 16), sb = smem_u32(S.w2t);
+#pragma unroll
+                for (int kk = 0; kk < 4; ++kk)
+                    tc_mma(tm + kBwColD1, smem_desc_lbo_sbo(sa + kk * 2 * (kBwTile * 16), kBwTile * 16, 128),
+                           smem_desc_lbo_sbo(sb + kk * 256, 128, 1024), idesc_bf16(64), kk);
+            } else {            // weight gradients, K = the tile's 128 faces
+                const uint32_t sa = smem_u32(S.aw), sb = smem_u32(S.bw);
+#pragma unroll
+                for (int kk = 0; kk < kBwTile / 16; ++kk)
+                    tc_mma(tm, smem_desc_lbo_sbo(sa + kk * 256, 128, kBwTile * 16),
+                           smem_desc_lbo_sbo(sb + kk * 256, 128, kBwTile * 16), idesc_bf16_mn(128, kBwN),
+                           (first && kk == 0) ? 0 : 1);
+            }
+            tc_commit(&S.bar);
+        }
+        const bool ok = mbar_wait_sleep(&S.bar, phase, kTcWaitLimit);
+        phase ^= 1u;
+        if (__syncthreads_or(!ok)) {
+            if (tid == 0) {
+                atomicExch(err, 1);
+                mbar_wait_sleep(&S.bar, phase ^ 1u, kTcWaitLimit);
+            }
+            return false;
+        }
+        tc_after_sync();
+        return true;
+    };
+
+    int base = blockIdx.x * kBwTile;
+    if (base < nf) {
+        load_tile(base);
+        ld_inflight = true;
+    }
+    for (; base < nf && !failed; base += gridDim.x * kBwTile) {
+        const bool valid = base + l < nf;
+        cp_async_wait_all();
+        __syncthreads();
+        ld_inflight = false;
+        float dy[NOUT] = {0.0f, 0.0f, 0.0f, 0.0f};
+        if (valid) {
+            const float4 d = *reinterpret_cast<const float4*>(S.dyr[l]);
+            dy[0] = d.x; dy[1] = d.y; dy[2] = d.z; dy[3] = d.w;
+        }
+        if (part == 0)
+#pragma unroll
+            for (int k = 0; k < NOUT; ++k) S.dy[l][k] = dy[k];
+        // this thread's 16 units: x, h1 into bw; dz2 into aw; h2 into its tile; gelu'(z1) kept
+        float g1[kBwU];
+#pragma unroll
+        for (int q = 0; q < kBwU / 8; ++q) {
+            const int ub = u0 + q * 8;
+            uint4 xq = make_uint4(0u, 0u, 0u, 0u);
+            float z1v[8] = {}, z2v[8] = {};
+            if (valid) {
+                xq = *reinterpret_cast<const uint4*>(&S.x[l][ub]);
+                const float4 a = *reinterpret_cast<const float4*>(&S.z1[l][ub]);
+                const float4 b = *reinterpret_cast<const float4*>(&S.z1[l][ub + 4]);
+                const float4 c = *reinterpret_cast<const float4*>(&S.z2[l][ub]);
+                const float4 d = *reinterpret_cast<const float4*>(&S.z2[l][ub + 4]);
+                z1v[0] = a.x; z1v[1] = a.y; z1v[2] = a.z; z1v[3] = a.w; z1v[4] = b.x; z1v[5] = b.y; z1v[6] = b.z; z1v[7] = b.w;
+                z2v[0] = c.x; z2v[1] = c.y; z2v[2] = c.z; z2v[3] = c.w; z2v[4] = d.x; z2v[5] = d.y; z2v[6] = d.z; z2v[7] = d.w;
+            }
+            uint32_t h1p[4], h2p[4], dzp[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                float dz[2], h1[2], h2[2];
+#pragma unroll
+                for (int u = 0; u < 2; ++u) {
+                    const int o = ub + 2 * k + u;
+                    const float z1 = z1v[2 * k + u], z2 = z2v[2 * k + u];
+                    float s = 0.0f;
+#pragma unroll
+                    for (int m = 0; m < NOUT; ++m) s = fmaf(dy[m], S.w3[m][o], s);
+                    float hh1, gg1, hh2, gg2;
+                    gelu_both(z1, hh1, gg1);
+                    gelu_both(z2, hh2, gg2);
+                    dz[u] = valid ? gg2 * s : 0.0f;
+                    h1[u] = valid ? hh1 : 0.0f;
+                    h2[u] = valid ? hh2 : 0.0f;
+                    g1[q * 8 + 2 * k + u] = valid ? gg1 : 0.0f;
+                }
+                h1p[k] = pack2(h1[0], h1[1]);
+                h2p[k] = pack2(h2[0], h2[1]);
+                dzp[k] = pack2(dz[0], dz[1]);
+            }
+            *reinterpret_cast<uint4*>(S.bw + mn_off(ub, l)) = xq;
+            *reinterpret_cast<uint4*>(S.bw + mn_off(64 + ub, l)) = make_uint4(h1p[0], h1p[1], h1p[2], h1p[3]);
+            *reinterpret_cast<uint4*>(S.aw + mn_off(64 + ub, l)) = make_uint4(dzp[0], dzp[1], dzp[2], dzp[3]);
+            *reinterpret_cast<uint4*>(&S.h2[l][ub]) = make_uint4(h2p[0], h2p[1], h2p[2], h2p[3]);
+        }
+        __syncthreads();   // the saved rows are consumed: the next tile's copies may land
+        if (base + gridDim.x * kBwTile < nf) {
+            load_tile(base + gridDim.x * kBwTile);
+            ld_inflight = true;
+        }
+        if (!run_mma(0)) { failed = true; break; }
+        {   // dz1 = (dz2 W2) * gelu'(z1) for this thread's 16 units, into aw's first 64 rows
+            float d[16];
+            tc_ld16(lane + kBwColD1 + u0, d);
+            uint32_t p[8];
+#pragma unroll
+            for (int k = 0; k < 8; ++k) p[k] = pack2(d[2 * k] * g1[2 * k], d[2 * k + 1] * g1[2 * k + 1]);
+            *reinterpret_cast<uint4*>(S.aw + mn_off(u0, l)) = make_uint4(p[0], p[1], p[2], p[3]);
+            *reinterpret_cast<uint4*>(S.aw + mn_off(u0 + 8, l)) = make_uint4(p[4], p[5], p[6], p[7]);
+        }
+        if (!run_mma(1)) { failed = true; break; }
+        first = false;
+        {   // dW3 entry tid mod 256 over this thread's half of the faces; db3
+            const int e = tid & 255, o = e / H, c = e % H, g0 = (tid >> 8) * (kBwTile / 2);
+            for (int g = g0; g < g0 + kBwTile / 2; ++g) g3 = fmaf(S.dy[g][o], __bfloat162float(S.h2[g][c]), g3);
+            if (tid < NOUT)
+                for (int g = 0; g < kBwTile; ++g) gb3 += S.dy[g][tid];
+        }
+        __syncthreads();
+    }
+    if (ld_inflight) cp_async_wait_all();   // copies still in flight land before the shared memory is given up
+    if (!failed && !first) {
+        // row l of the accumulated D, this thread's 16 columns of its block
+        const bool l1 = l < 64;
+        const int row = l1 ? l : l - 64;
+        float d[16];
+        tc_ld16(lane + (l1 ? 0 : 64) + u0, d);
+        float* gw = grad + (l1 ? OFF_W1 + row * NIN : OFF_W2 + row * H) + u0;
+#pragma unroll
+        for (int k = 0; k < 16; ++k) atomicAdd(gw + k, d[k]);
+        if (part == 0) {   // warp-uniform, as the collective tcgen05.ld requires
+            tc_ld16(lane + 128, d);
+            atomicAdd(grad + (l1 ? OFF_B1 : OFF_B2) + row, d[0]);
+        }
+    }
+    if (!first) {
+        atomicAdd(&grad[OFF_W3 + (tid & 255)], g3);
+        if (tid < NOUT) atomicAdd(&grad[OFF_B3 + tid], gb3);
+    }
+    tc_before_sync();
+    __syncthreads();
+    if ((tid >> 5) == 0) {
+        tc_after_sync();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tm), "r"(kBwCols) : "memory");
+    }
+}
+
+size_t mlp_backward_smem() { return sizeof(BwSmem) + 1024; }
 
 // Adam on the FP32 master parameters; refreshes the BF16 weight copy
 __global__ void adam_kernel(float* __restrict__ P, const float* __restrict__ G, float* __restrict__ m,
@@ -1153,6 +1341,17 @@ void launch_forward(hf_lc* L, int nf, bool save_acts) {
         L->X, nf, L->Wb, L->P, L->Y, save_acts ? L->Z1 : nullptr, save_acts ? L->Z2 : nullptr, L->derr);
 }
 
+// the MLP backward: one persistent CTA per SM at most (its shared memory allows one)
+void launch_backward(hf_lc* L, int nf) {
+    int sms = 0, dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        sms < 1)
+        sms = 152;
+    const int tiles = (nf + hf::lc::kBwTile - 1) / hf::lc::kBwTile;
+    hf::lc::mlp_backward_kernel<<<tiles < sms ? tiles : sms, hf::lc::kBwThreads, hf::lc::mlp_backward_smem(), L->stream>>>(
+        L->X, nf, L->Wb, L->Z1, L->Z2, L->dY, L->grad, L->derr);
+}
+
 // the device error word: a bounded wait in a kernel gave up
 int check_derr(hf_lc* L) {
     int e = 0;
@@ -1242,6 +1441,8 @@ int hf_lc_create(int n, double dx, double gamma, double cfl, int limiter, hf_lc*
                              (int)hf::lc::mlp_forward_smem()));
     LCK(cudaFuncSetAttribute(hf::lc::mlp_forward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)hf::lc::mlp_forward_smem()));
+    LCK(cudaFuncSetAttribute(hf::lc::mlp_backward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)hf::lc::mlp_backward_smem()));
     for (const void* k : {(const void*)hf::lc::face_kernel<false>, (const void*)hf::lc::face_kernel<true>,
                           (const void*)hf::lc::mlp_forward_kernel})
         LCK(cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
@@ -1450,8 +1651,7 @@ int hf_lc_train_step(hf_lc* L, const float* U0, const float* T, const float* w, 
     loss_grad_kernel<<<blocks_for(nf, 256), 256, 0, L->stream>>>(L->U[L->cur ^ 1], L->T, L->scale, L->n, rr, L->wv,
                                                                   L->train_guard ? L->ok : nullptr, L->dY, L->loss);
     LCK(cudaMemsetAsync(L->grad, 0, NPARAM * sizeof(float), L->stream));
-    mlp_backward_kernel<<<blocks_for(nf, kBwdFaces) > 1024 ? 1024 : blocks_for(nf, kBwdFaces), 256, 0, L->stream>>>(
-        L->X, nf, L->Wb, L->Z1, L->Z2, L->dY, L->grad);
+    launch_backward(L, nf);
     L->adam_t += 1;
     const float b1 = 0.9f, b2 = 0.999f;
     const float c1 = 1.f - powf(b1, (float)L->adam_t), c2 = 1.f - powf(b2, (float)L->adam_t);
@@ -1493,8 +1693,7 @@ int hf_lc_mlp_backward(hf_lc* L, const uint16_t* x_bf16, const float* dy, int nf
     launch_forward(L, nf, true);
     LCK(cudaMemcpyAsync(L->dY, dy, (size_t)nf * 4 * sizeof(float), cudaMemcpyHostToDevice, L->stream));
     LCK(cudaMemsetAsync(L->grad, 0, NPARAM * sizeof(float), L->stream));
-    mlp_backward_kernel<<<blocks_for(nf, kBwdFaces) > 1024 ? 1024 : blocks_for(nf, kBwdFaces), 256, 0, L->stream>>>(
-        L->X, nf, L->Wb, L->Z1, L->Z2, L->dY, L->grad);
+    launch_backward(L, nf);
     LCK(cudaGetLastError());
     LCK(cudaStreamSynchronize(L->stream));
     LCK(cudaMemcpy(grad, L->grad, NPARAM * sizeof(float), cudaMemcpyDeviceToHost));
