@@ -20,8 +20,9 @@
 //     corrections on all its faces (they fall back to the plain flux); a cell still violating
 //     after that takes its plain update.
 // Training: one-step loss L = mean_cells sum_v w_v (U^{n+1}_v - T_v)^2 against the filtered
-// fine solution T; dL/dF flows only through the linear conservative update.  Backward and
-// Adam are hand-written FP32 kernels (weight gradients on the CUDA cores).
+// fine solution T; dL/dF flows only through the linear conservative update.  The backward runs
+// its products on the tensor cores (weight gradients accumulated in TMEM), Adam on the CUDA
+// cores.
 #include <cmath>
 #include <cstdio>
 #include <cstring>
