@@ -21,6 +21,7 @@ Other workloads (`--workload`, one JSON line each, not the headline):
     uns       the ~1M-triangle channel, edge-based (or --uns-per-side) fluxes
     quad256   the 256^2 Godunov problem as a batch of one (the whole run one launch)
     learned   the 512^2 learned coarse step (FP32 + the tcgen05 MLP on every face)
+    learned-train  a 512^2 training iteration of the learned solver (tcgen05 forward and backward)
 """
 from __future__ import annotations
 
@@ -441,6 +442,40 @@ def bench_uns(args):
     s.close()
 
 
+def bench_learned_train(args):
+    """Training iterations of the learned coarse solver at 512^2: forward with the activations
+    saved (tcgen05), loss and its gradient, the backward (tcgen05 weight gradients), Adam --
+    each on a state of the 512^2 quadrant Riemann problem against a slightly perturbed target,
+    the iteration's loss read back (a wait per iteration, as training does)."""
+    import numpy as np
+    import torch
+    from hyperflow_gb300 import CartSolver, cases
+    from hyperflow_gb300.learned import LearnedSolver, init_params
+    n = 512
+    s = CartSolver(cases.quadrant_case(n, scheme="MUSCLHancock", limiter="MinBee", cfl=cases.CFL_2D))
+    U0 = s.state(0)[:, 2:-2, 2:-2].astype(np.float32)
+    s.close()
+    ls = LearnedSolver(n, 1.0 / n, cfl=cases.CFL_2D)
+    ls.set_params(init_params(0))
+    w = np.ones(4, np.float32)
+    T = U0 * np.float32(1.001)
+    ls.set_state(U0)
+    dt = ls.cfl_dt()
+    for _ in range(args.warmup):
+        ls.train_step(U0, T, w, dt, 1e-4)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        ls.train_step(None, T, w, dt, 1e-4)
+    torch.cuda.synchronize()
+    ms = (time.perf_counter() - t0) * 1e3 / args.steps
+    print(json.dumps({
+        "metric": "ms per training iteration", "value": ms, "unit": "ms", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "higher_is_better": False, "dtype": "fp32 + bf16 MLP",
+        "data": "synthetic (the 512^2 quadrant Riemann problem, target scaled by 1.001)",
+        "config": {"workload": "learned_training_iteration_512x512", "faces": 2 * n * (n + 1)}}), flush=True)
+
+
 def state_note(args, t_start: float) -> str:
     if args.pre_steps > 0:
         return f"developed flow: timed from t = {t_start:.4g}, after {args.pre_steps} untimed steps"
@@ -455,7 +490,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--limiter", default="MinBee", choices=["MinBee", "VanLeer"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="CPU-baseline sample budget")
-    ap.add_argument("--workload", default="ffs", choices=["ffs", "square", "batch", "uns", "quad256", "learned"],
+    ap.add_argument("--workload", default="ffs",
+                    choices=["ffs", "square", "batch", "uns", "quad256", "learned", "learned-train"],
                     help="ffs: the 3-block forward-facing step (default); square: one n x n block; "
                          "batch: 512 batched Riemann problems; uns: the 1M-triangle channel")
     ap.add_argument("--instances", type=int, default=512, help="batch workload: number of instances")
@@ -479,7 +515,7 @@ def main():
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
-    if args.workload in ("batch", "uns", "quad256", "learned"):
+    if args.workload in ("batch", "uns", "quad256", "learned", "learned-train"):
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "unavailable":
                               "the reference arm is timed on the forward-facing step and square workloads"}))
@@ -487,7 +523,8 @@ def main():
         import numpy as np  # noqa: F401
         import torch
         torch.cuda.set_device(0)
-        {"batch": bench_batch, "uns": bench_uns, "quad256": bench_quad256, "learned": bench_learned}[args.workload](args)
+        {"batch": bench_batch, "uns": bench_uns, "quad256": bench_quad256, "learned": bench_learned,
+         "learned-train": bench_learned_train}[args.workload](args)
         return
 
     from hyperflow_gb300 import cases
