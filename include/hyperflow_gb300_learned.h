@@ -58,7 +58,8 @@ int hf_lc_get_time(hf_lc* L, double* t);
 /* CFL dt of the current state: cfl * dx / max(max(|u|,|v|) + c) */
 int hf_lc_cfl_dt(hf_lc* L, double* dt);
 /* one step with dt; use_mlp != 0 applies the guarded correction; rejected_cells (optional)
- * counts cells whose faces' corrections were rejected */
+ * counts cells whose faces' corrections were rejected -- given, the call waits for the step and
+ * reports a device error; null, the step is only enqueued on the solver's stream */
 int hf_lc_step(hf_lc* L, double dt, int use_mlp, int64_t* rejected_cells);
 /* steps with the CFL dt until t_end (dt clamped to reach it) */
 int hf_lc_run_to(hf_lc* L, double t_end, int use_mlp, int64_t* steps, int64_t* rejected_cells);
