@@ -1254,6 +1254,8 @@ struct hf_lc {
     int fused = 1;             // inference: 1 features + MLP + correction in face_kernel, 2 with the
                                // plain flux too, 0 the separate kernels
     int face_ctas_per_sm = 0;  // face_kernel CTAs per SM (0: as many as fit)
+    int sms = 152;             // the device's SMs, and how many CTAs of each MLP kernel fit on one
+    int fit_fwd = 1, fit_face[2] = {1, 1};
     cudaStream_t stream = nullptr;
     cudaStream_t side = nullptr;           // the plain fluxes, beside the fused face kernel
     cudaEvent_t fork = nullptr, join = nullptr;
@@ -1311,16 +1313,14 @@ int nfaces(const hf_lc* L) { return 2 * (L->n + 1) * L->n; }
 int blocks_for(long long n, int t) { long long b = (n + t - 1) / t; return (int)(b > 4096 ? 4096 : (b < 1 ? 1 : b)); }
 
 // Persistent CTAs of the MLP kernels (256 threads, two 128-face tiles at a time): per_sm per SM (0: as
-// many as fit by registers, shared memory and TMEM), never more than the tiles.  The fit is
-// formed from the kernel's attributes: registers are allocated per warp in units of 256 from
+// many as fit by registers, shared memory and TMEM), never more than the tiles.  The fit (formed
+// once per context) comes from the kernel's attributes: registers are allocated per warp in units of 256 from
 // each SM sub-partition's 16,384; each CTA holds its dynamic shared memory plus 1 KB the
 // hardware reserves; 4 CTAs x 128 TMEM columns fill an SM's 512.
-int mlp_grid(const void* kernel, int nf, int per_sm) {
-    int sms = 0, dev = 0, smem_sm = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
-        sms < 1)
-        sms = 152;
-    if (cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev) != cudaSuccess || smem_sm < 1)
+int mlp_fit(const void* kernel) {
+    int dev = 0, smem_sm = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev) != cudaSuccess || smem_sm < 1)
         smem_sm = 233472;
     cudaFuncAttributes fa{};
     int fit = 1;
@@ -1331,23 +1331,24 @@ int mlp_grid(const void* kernel, int nf, int per_sm) {
         fit = by_regs < by_smem ? by_regs : by_smem;
         fit = fit > 4 ? 4 : (fit < 1 ? 1 : fit);
     }
+    return fit;
+}
+// the grid for nf faces with fit CTAs per SM at most (per_sm, when set and lower, instead)
+int mlp_grid(const hf_lc* L, int fit, int nf, int per_sm) {
     const int per = per_sm > 0 && per_sm < fit ? per_sm : fit;
     const int tiles = (nf + hf::lc::kTcThreads - 1) / hf::lc::kTcThreads;
-    return tiles < per * sms ? tiles : per * sms;
+    return tiles < per * L->sms ? tiles : per * L->sms;
 }
 
 void launch_forward(hf_lc* L, int nf, bool save_acts) {
-    const int g = mlp_grid((const void*)hf::lc::mlp_forward_kernel, nf, 0);
+    const int g = mlp_grid(L, L->fit_fwd, nf, 0);
     hf::lc::mlp_forward_kernel<<<g, hf::lc::kTcThreads, hf::lc::mlp_forward_smem(), L->stream>>>(
         L->X, nf, L->Wb, L->P, L->Y, save_acts ? L->Z1 : nullptr, save_acts ? L->Z2 : nullptr, L->derr);
 }
 
 // the MLP backward: one persistent CTA per SM at most (its shared memory allows one)
 void launch_backward(hf_lc* L, int nf) {
-    int sms = 0, dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
-        sms < 1)
-        sms = 152;
+    const int sms = L->sms;
     const int tiles = (nf + hf::lc::kBwTile - 1) / hf::lc::kBwTile;
     hf::lc::mlp_backward_kernel<<<tiles < sms ? tiles : sms, hf::lc::kBwThreads, hf::lc::mlp_backward_smem(), L->stream>>>(
         L->X, nf, L->Wb, L->Z1, L->Z2, L->dY, L->grad, L->derr);
@@ -1384,7 +1385,7 @@ int fluxes(hf_lc* L, float dt, bool use_mlp, bool save_acts, bool* mask_set = nu
         const size_t sm = hf::lc::mlp_forward_smem();
         const int units = nf;
         if (L->fused == 2) {
-            face_kernel<true><<<mlp_grid((const void*)face_kernel<true>, units, L->face_ctas_per_sm),
+            face_kernel<true><<<mlp_grid(L, L->fit_face[1], units, L->face_ctas_per_sm),
                                 hf::lc::kTcThreads, sm, L->stream>>>(L->U[L->cur], L->Wp, G, dt, L->Wb, L->P, L->F,
                                                                      L->dF, L->ok, L->rejected, L->maxs, L->derr);
         } else {
@@ -1392,7 +1393,7 @@ int fluxes(hf_lc* L, float dt, bool use_mlp, bool save_acts, bool* mask_set = nu
             // work: the face kernel is latency-bound, the flux kernel arithmetic-bound); the face
             // kernel at 2 CTAs per SM by default leaves the flux kernel room on every SM
             LCK(cudaEventRecord(L->fork, L->stream));
-            face_kernel<false><<<mlp_grid((const void*)face_kernel<false>, units,
+            face_kernel<false><<<mlp_grid(L, L->fit_face[0], units,
                                           L->face_ctas_per_sm > 0 ? L->face_ctas_per_sm : 2),
                                  hf::lc::kTcThreads, sm, L->stream>>>(L->U[L->cur], L->Wp, G, dt, L->Wb, L->P, L->F,
                                                                       L->dF, L->ok, L->rejected, L->maxs, L->derr);
@@ -1447,6 +1448,15 @@ int hf_lc_create(int n, double dx, double gamma, double cfl, int limiter, hf_lc*
     for (const void* k : {(const void*)hf::lc::face_kernel<false>, (const void*)hf::lc::face_kernel<true>,
                           (const void*)hf::lc::mlp_forward_kernel})
         LCK(cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+    {
+        int dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&L->sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || L->sms < 1)
+            L->sms = 152;
+        L->fit_fwd = mlp_fit((const void*)hf::lc::mlp_forward_kernel);
+        L->fit_face[0] = mlp_fit((const void*)hf::lc::face_kernel<false>);
+        L->fit_face[1] = mlp_fit((const void*)hf::lc::face_kernel<true>);
+    }
     const size_t cells = (size_t)n * n, nf = nfaces(L);
     int r;
     if ((r = alloc(L, &L->U[0], 4 * cells)) || (r = alloc(L, &L->U[1], 4 * cells)) || (r = alloc(L, &L->F, 4 * nf)) ||
