@@ -713,6 +713,8 @@ def main():
                     "d2h_bytes_per_step": h2d, "steps": e2e_steps,
                     "path": "kernels read and write pinned host buffers" if direct else "copies"},
             "gpu_launches": launches_per_step * args.steps,
+            "stencil_ms_per_step": stencil_ms / args.steps,
+            "non_stencil_ms_per_step": t_max / args.steps - stencil_ms / args.steps,
             "developed": developed,
             "clocks": clk.summary(),
             "graph_value": graph_value,
