@@ -241,3 +241,28 @@ def test_batch_manifest_cell_counts_are_checked_before_any_device_work():
         if h:
             L.hf_batch_destroy(h)
         assert st == 3 and "square" in msg, (nx, ny, st, msg)
+
+
+def test_learned_solver_host_checks():
+    """hf_lc_create refuses bad sizes before any device work; without a GPU it reports the missing
+    device and still hands back a context whose setters check their arguments on the host: the
+    inference path (0 separate kernels, 1 fused, 2 fused with the plain flux) and the fused
+    kernel's CTAs per SM (0..4), the guard mode and bound."""
+    import torch
+    from hyperflow_gb300._lib import lib
+    L = lib()
+    h = C.c_void_p()
+    assert L.hf_lc_create(3, 0.1, 1.4, 0.4, 0, C.byref(h)) == 1
+    h = C.c_void_p()
+    st = L.hf_lc_create(64, 1 / 64, 1.4, 0.4, 0, C.byref(h))
+    assert st == (0 if torch.cuda.is_available() else 7) and h.value
+    try:
+        for mode, ctas in ((3, 0), (-1, 0), (1, 5), (1, -1)):
+            assert L.hf_lc_set_fused(h, mode, ctas) == 1
+        for mode, ctas in ((0, 0), (1, 4), (2, 1)):
+            assert L.hf_lc_set_fused(h, mode, ctas) == 0
+        assert L.hf_lc_set_guard_mode(h, 2) == 1 and L.hf_lc_set_guard_mode(h, 1) == 0
+        assert L.hf_lc_set_bound(h, 0.0) == 1 and L.hf_lc_set_bound(h, 2.0) == 0
+        assert L.hf_lc_set_fused(None, 1, 0) == 1
+    finally:
+        L.hf_lc_destroy(h)
