@@ -298,3 +298,48 @@ def test_learned_solver_lowers_the_end_time_error_in_both_families():
         ratios[name] = learned["l1_rho"] / res["fp32_plain"]["l1_rho"]
     assert all(r < 0.97 for r in ratios.values()), ratios
     assert np.mean(list(ratios.values())) < 0.9, ratios
+
+
+def test_feature_oracle_equals_a_per_face_restatement():
+    """The oracle's vectorised features (what the GPU features are pinned to, bit for bit) against
+    a face-by-face float32 restatement of the same definition on a small random state: the 4x4
+    stencil with mirrored cells past the edges, x faces first, scaled by the reciprocals of the
+    face's reference density, sound speed and pressure, rounded to BF16."""
+    from oracle import mlp_oracle as M
+    rng = np.random.default_rng(11)
+    n, g = 5, np.float32(1.4)
+    U = np.empty((4, n, n), np.float32)
+    U[0] = rng.uniform(0.5, 2.0, (n, n))
+    U[1] = U[0] * rng.uniform(-0.5, 0.5, (n, n))
+    U[2] = U[0] * rng.uniform(-0.5, 0.5, (n, n))
+    U[3] = rng.uniform(2.0, 4.0, (n, n))
+    x, sc = M.features(U, 1.4)
+
+    def prim(j, i):
+        def m(k):
+            k = -1 - k if k < 0 else (2 * n - 1 - k if k >= n else k)
+            return min(max(k, 0), n - 1)
+        c = U[:, m(j), m(i)]
+        r = c[0]
+        u, v = c[1] / r, c[2] / r
+        p = np.float32(1.4 - 1.0) * (c[3] - np.float32(0.5) * r * (u * u + v * v))   # gamma - 1 in double, as the kernels
+        return r, u, v, p
+
+    one = np.float32(1.0)
+    faces = [(0, i, j) for j in range(n) for i in range(n + 1)] + [(1, i, j) for j in range(n + 1) for i in range(n)]
+    assert len(faces) == x.shape[0] == 2 * n * (n + 1)
+    for f, (d, i, j) in enumerate(faces):
+        il, jl = (i - 1, j) if d == 0 else (i, j - 1)
+        ni, nj, ti, tj = (1, 0, 0, 1) if d == 0 else (0, 1, 1, 0)
+        rl, _, _, pl = prim(jl, il)
+        rh, _, _, ph = prim(jl + nj, il + ni)
+        rr, pr = np.float32(0.5) * (rl + rh), np.float32(0.5) * (pl + ph)
+        cref = np.sqrt(np.maximum(g * pr / rr, np.float32(1e-12)))
+        assert sc[f, 0] == rr and sc[f, 1] == cref
+        row = []
+        for a in (-1, 0, 1, 2):
+            for b in (-1, 0, 1, 2):
+                r, u, v, p = prim(jl + a * nj + b * tj, il + a * ni + b * ti)
+                un, ut = (u, v) if d == 0 else (v, u)
+                row += [r * (one / rr) - one, un * (one / cref), ut * (one / cref), p * (one / pr) - one]
+        np.testing.assert_array_equal(x[f], M.bf16_bits(np.array(row, np.float32)))
