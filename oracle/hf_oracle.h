@@ -4,7 +4,7 @@
  * src/fvm_2d_cart and src/fvm_2d_uns), written to reproduce the reference's
  * floating-point results bit for bit: same operations, same evaluation order, no
  * FMA contraction (built with -ffp-contract=off).  Only tests/, __graft_entry__.smoke()
- * and bench.py's CPU-baseline leg may load it, and only as the checker or as the timed
+ * and bench.py's CPU-baseline leg may load it, and only to check results or as the timed
  * CPU baseline.  The product never calls it.
  *
  * Parity of this restatement is pinned against the reference itself: the reference's

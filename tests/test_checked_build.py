@@ -1,4 +1,4 @@
-"""The bounds-checked build (-DHF_CHECKS; compute-sanitizer is not available on this machine):
+"""The bounds-checked build (-DHF_CHECKS; it stands in for compute-sanitizer's memory checks):
 every global index that depends on a block's geometry or on mesh data -- ghost fill sources and
 destinations, ghost and interior CFL reads, stencil and host-buffer stores, unstructured pair,
 neighbour and edge indices -- is range-checked, and a violation sets the context's error word
