@@ -1246,6 +1246,8 @@ struct hf_lc {
     float4* Wp = nullptr;      // per-cell primitives (rho, u, v, p) for the feature stencils
     bool wp_valid = false;     // Wp holds the primitives of U[cur] (written by the last step)
     float4* Uc = nullptr;      // the guard pass's fully corrected cell updates
+    bool maxs_valid = false;   // maxs holds the maximum wave speed of U[cur] (the last step's update
+                               // or CFL pass formed it)
     float *P = nullptr, *grad = nullptr, *m1 = nullptr, *m2 = nullptr, *maxs = nullptr;
     unsigned char* ok = nullptr;
     unsigned long long* rejected = nullptr;
@@ -1491,6 +1493,7 @@ int hf_lc_set_state(hf_lc* L, const float* U) {
     LCK(cudaStreamSynchronize(L->stream));
     LCK(cudaMemcpy(L->U[L->cur], U, (size_t)4 * L->n * L->n * sizeof(float), cudaMemcpyHostToDevice));
     L->wp_valid = false;
+    L->maxs_valid = false;
     return HF_OK;
 }
 
@@ -1501,15 +1504,25 @@ int hf_lc_get_state(hf_lc* L, float* U) {
     return HF_OK;
 }
 
-int hf_lc_cfl_dt(hf_lc* L, double* dt) {
-    if (!L || !dt) return HF_ERR_ARG;
-    // max wave speed of the current state (an update with zero fluxes writes U unchanged)
+// the maximum wave speed of the current state into maxs, unless the last step's update left it
+// (the same cells through the same code: the same value)
+static int enqueue_max_speed(hf_lc* L) {
+    if (L->maxs_valid) return HF_OK;
+    // an update with zero fluxes writes U unchanged and forms its maximum
     hf::lc::Grid G = grid(L);
     LCK(cudaMemsetAsync(L->maxs, 0, 4, L->stream));
     LCK(cudaMemsetAsync(L->F, 0, (size_t)4 * nfaces(L) * sizeof(float), L->stream));
     update_kernel<<<blocks_for((long long)L->n * L->n, 256), 256, 0, L->stream>>>(
         L->U[L->cur], L->F, nullptr, nullptr, G, 0.0f, 0.0f, 0, L->U[L->cur ^ 1], L->maxs, nullptr, nullptr);
     LCK(cudaGetLastError());
+    L->maxs_valid = true;
+    return HF_OK;
+}
+
+int hf_lc_cfl_dt(hf_lc* L, double* dt) {
+    if (!L || !dt) return HF_ERR_ARG;
+    int r = enqueue_max_speed(L);
+    if (r) return r;
     LCK(cudaStreamSynchronize(L->stream));
     *dt = L->cfl * L->dx / max_speed(L);
     return HF_OK;
@@ -1545,6 +1558,7 @@ int hf_lc_step(hf_lc* L, double dt, int use_mlp, int64_t* rejected_cells) {
     LCK(cudaGetLastError());
     L->cur ^= 1;
     L->wp_valid = use_mlp != 0;
+    L->maxs_valid = true;   // the update formed the new state's maximum wave speed
     L->t += dt;
     L->steps += 1;
     if (rejected_cells) {
@@ -1561,22 +1575,34 @@ int hf_lc_step(hf_lc* L, double dt, int use_mlp, int64_t* rejected_cells) {
 int hf_lc_run_to(hf_lc* L, double t_end, int use_mlp, int64_t* steps, int64_t* rejected_cells) {
     hf::TraceRange trace_("hf_lc_run_to");
     if (!L) return HF_ERR_ARG;
+    // one wait per step: the step's wave-speed maximum (the next dt) and rejection count are read
+    // together; the device error word once at the end
     int64_t k = 0, rej = 0;
+    int r = enqueue_max_speed(L);
+    if (r) return r;
     while (L->t < t_end) {
-        double dt;
-        int r = hf_lc_cfl_dt(L, &dt);
-        if (r) return r;
+        float m = 0.0f;
+        unsigned long long rc = 0;
+        LCK(cudaMemcpyAsync(&m, L->maxs, sizeof m, cudaMemcpyDeviceToHost, L->stream));
+        if (use_mlp && k > 0) LCK(cudaMemcpyAsync(&rc, L->rejected, sizeof rc, cudaMemcpyDeviceToHost, L->stream));
+        LCK(cudaStreamSynchronize(L->stream));
+        rej += (int64_t)rc;
+        double dt = L->cfl * L->dx / (double)m;
         // the reference's TimeStep uses 0.2 x CFL for its first 10 calls; a MUSCL-Hancock
         // step makes two (step and predictor), so the first 5 steps are reduced
         if (L->steps < 5) dt *= 0.2;
         if (!(dt > 0.0) || !std::isfinite(dt))
             return lfail(L, HF_ERR_DEVICE, "coarse run stopped advancing (non-positive or non-finite dt)");
         if (L->t + dt > t_end) dt = t_end - L->t;
-        int64_t rc = 0;
-        r = hf_lc_step(L, dt, use_mlp, use_mlp ? &rc : nullptr);
+        r = hf_lc_step(L, dt, use_mlp, nullptr);
         if (r) return r;
-        rej += rc;
         ++k;
+    }
+    if (use_mlp && k > 0) {
+        unsigned long long rc = 0;
+        LCK(cudaMemcpyAsync(&rc, L->rejected, sizeof rc, cudaMemcpyDeviceToHost, L->stream));
+        LCK(cudaStreamSynchronize(L->stream));
+        rej += (int64_t)rc;
     }
     LCK(cudaStreamSynchronize(L->stream));
     if (steps) *steps = k;
@@ -1615,6 +1641,7 @@ int hf_lc_set_guard_mode(hf_lc* L, int mode) {
 int hf_lc_train_step(hf_lc* L, const float* U0, const float* T, const float* w, double dt, double lr,
                      double* loss) {
     if (!L || !T || !w || dt <= 0) return HF_ERR_ARG;
+    L->maxs_valid = false;   // the training update forms the maximum of its prediction, not of U[cur]
     const size_t bytes = (size_t)4 * L->n * L->n * sizeof(float);
     const int nf = nfaces(L);
     hf::lc::Grid G = grid(L);

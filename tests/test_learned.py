@@ -343,3 +343,44 @@ def test_feature_oracle_equals_a_per_face_restatement():
                 un, ut = (u, v) if d == 0 else (v, u)
                 row += [r * (one / rr) - one, un * (one / cref), ut * (one / cref), p * (one / pr) - one]
         np.testing.assert_array_equal(x[f], M.bf16_bits(np.array(row, np.float32)))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("use_mlp", [False, True])
+def test_run_to_equals_a_loop_with_fresh_cfl_passes(use_mlp):
+    """hf_lc_run_to waits once per step and takes each dt from the wave-speed maximum the previous
+    step's update left; a loop that re-uploads the state before every step makes each dt come
+    from a fresh CFL pass instead.  Same step count, rejection count and state, bit for bit."""
+    from oracle import mlp_oracle as M
+    from hyperflow_gb300 import CartSolver, cases
+    from hyperflow_gb300.learned import LearnedSolver, init_params
+    n, t_end = 64, 0.02
+    s = CartSolver(cases.shock_bubble_case(n))
+    s.run(5)
+    U0 = s.state(0)[:, 2:-2, 2:-2].astype(np.float32)
+    s.close()
+    p = init_params(3, out_scale=0.05)
+    p[M.OFF_B3:] = [0.05, -0.03, 0.04, -0.2]
+    a = LearnedSolver(n, 1.0 / n)
+    a.set_params(p)
+    a.set_state(U0)
+    ka, ra = a.run_to(t_end, use_mlp)
+    b = LearnedSolver(n, 1.0 / n)
+    b.set_params(p)
+    b.set_state(U0)
+    kb = rb = 0
+    t = 0.0
+    while t < t_end:
+        b.set_state(b.state(), t)          # forgets the cached maximum
+        dt = b.cfl_dt()
+        if kb < 5:
+            dt *= 0.2
+        if t + dt > t_end:
+            dt = t_end - t
+        rb += b.step(dt, use_mlp)
+        t += dt
+        kb += 1
+    assert ka == kb and ka > 10 and ra == rb and (ra > 0) == use_mlp
+    np.testing.assert_array_equal(a.state().view(np.uint32), b.state().view(np.uint32))
+    a.close()
+    b.close()
